@@ -1,0 +1,402 @@
+"""Benchmark: PSF+gradient evaluations per second on one GB300.
+
+Workload (the polychromatic split-precision configuration): 512 x 512 pupil
+of a 1 m circular aperture with a 10 cm central obscuration and four 1 cm
+spider vanes, 21 Noll Zernikes (j = 4..24) with N(0, 30 nm) coefficients,
+64 wavelengths uniform on 0.8-1.2 um with Dirichlet(1) weights, MFT to
+512 x 512 at 4x oversampling of a 0.02"/px detector, then a 4 x 4 sum
+downsample to 128 x 128. One step = one PSF evaluation plus the gradient of
+sum(R * image) (R a seeded N(0, 1) 128 x 128 array) with respect to the 21
+coefficients, through the public API (AngularOpticalSystem.propagate,
+LayeredDetector, torch autograd -> the hand-written reverse kernels).
+
+Every step touches ~1 GB of device memory (cached DFT matrices plus the
+per-wavelength fields), far more than the 129 MB L2, so no explicit L2 flush
+is made between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--variant split_bf16|fp32]
+  python bench.py --impl reference   # the CPU restatement of the same step
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+N_PUPIL = 512
+N_FOCAL = 512
+OVERSAMPLE = 4
+PSF_PIXEL_SCALE = 0.02  # arcsec per detector pixel
+N_WAVELENGTHS = 64
+NOLLS = list(range(4, 25))
+SEED = 2
+METRIC = "PSF+grad evals/sec"
+
+
+def config_dict(extra=None):
+    d = {"workload": "polychromatic PSF + coefficient gradient: 512^2 pupil (D=1 m, 10% "
+                     "obscuration, 4 x 1 cm spiders), 21 Zernikes N(0,30nm), 64 lambda "
+                     "0.8-1.2 um Dirichlet(1), MFT 512^2 at 4x oversampling, 4x4 sum "
+                     "downsample to 128^2, grad of sum(R*image) w.r.t. coefficients",
+         "pupil": N_PUPIL, "focal": N_FOCAL, "wavelengths": N_WAVELENGTHS,
+         "zernikes": len(NOLLS), "detector": 128,
+         "l2": "inputs larger than L2 (~1 GB of device state touched per step), no flush"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def make_inputs(seed=SEED):
+    """Seeded synthetic inputs (NumPy PCG64), shared by every implementation."""
+    rng = np.random.default_rng(seed)
+    coeffs = rng.normal(0, 30e-9, len(NOLLS))
+    wls = np.linspace(0.8e-6, 1.2e-6, N_WAVELENGTHS)
+    weights = rng.dirichlet(np.ones(N_WAVELENGTHS))
+    R = rng.normal(size=(128, 128))
+    return coeffs, wls, weights, R
+
+
+# ----------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# CPU arm: the oracle's complex64 restatement of dLux's op order
+# ----------------------------------------------------------------------------
+def cpu_step_sample(n_lambda_sample=2):
+    """Times one PSF+grad evaluation on the host for a sample of the wavelengths."""
+    from oracle import dlux_oracle as O
+
+    coeffs, wls, weights, R = make_inputs()
+    T, B = O.circular_aperture(N_PUPIL, 1.0, oversample=5, secondary_diameter=0.1,
+                               spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                               zernike_nolls=NOLLS)
+    ps_out = float(O.arcsec2rad(PSF_PIXEL_SCALE / OVERSAMPLE))
+    idx = np.linspace(0, N_WAVELENGTHS - 1, n_lambda_sample).astype(int)
+    Bf = B.astype(np.float32)
+    t0 = time.perf_counter()
+    opd = np.tensordot(Bf, coeffs.astype(np.float32), axes=(0, 0))
+    Teff = (T / np.sqrt((T ** 2).sum())).astype(np.float32)
+    psf = O.poly_psf(T, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out, precision="c64")
+    img = O.downsample(psf, OVERSAMPLE, mean=False)
+    G = np.kron(R.astype(np.float32), np.ones((OVERSAMPLE, OVERSAMPLE), np.float32))
+    g = O.poly_psf_grad(Teff, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out, G,
+                        precision="c64")
+    gc = np.tensordot(Bf, g["g_opd"], axes=((1, 2), (0, 1)))
+    dt = time.perf_counter() - t0
+    assert np.isfinite(img).all() and np.isfinite(gc).all()
+    return dt * (N_WAVELENGTHS / n_lambda_sample), n_lambda_sample
+
+
+def cpu_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        info = threadpool_info()
+        return max([i.get("num_threads", 1) for i in info] + [1])
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the CPU restatement timed on the host cores."""
+    if rank != 0:
+        return 0
+    times = []
+    nsample = 2
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_step_sample(nsample)
+    for _ in range(args.steps):
+        t, nsample = cpu_step_sample(nsample)
+        times.append(t)
+    t = statistics.median(times)
+    value = 1.0 / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+        "data": "synthetic (seeded PCG64)", "config": config_dict(),
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cpu_threads(),
+                         "kind": "port",
+                         "sample": f"{nsample} of {N_WAVELENGTHS} wavelengths per step at full "
+                                   f"512^2 pupil / 512^2 focal size, time scaled by "
+                                   f"{N_WAVELENGTHS // nsample}; NumPy complex64 restatement of "
+                                   "dLux's op order (dLux/JAX is not installable here)"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def build_workload(variant):
+    import torch
+    import dlux_gb300 as dl
+    import dlux_gb300.utils as dlu
+
+    dl.set_variant(variant)
+    coeffs, wls, weights, R = make_inputs()
+    T, B = dlu.circular_aperture(N_PUPIL, 1.0, oversample=5, secondary_diameter=0.1,
+                                 spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                                 zernike_nolls=NOLLS)
+    c = torch.as_tensor(coeffs, dtype=torch.float32, device="cuda")
+    optics = dl.AngularOpticalSystem(N_PUPIL, 1.0, [dl.TransmissiveLayer(T, normalise=True),
+                                                    dl.BasisLayer(B, c)],
+                                     N_FOCAL // OVERSAMPLE, PSF_PIXEL_SCALE, OVERSAMPLE)
+    detector = dl.LayeredDetector([dl.Downsample(OVERSAMPLE)])
+    w = torch.as_tensor(weights, dtype=torch.float32, device="cuda")
+    Rt = torch.as_tensor(R, dtype=torch.float32, device="cuda")
+    return optics, detector, wls, w, Rt, coeffs
+
+
+def step(optics, detector, wls, w, R, c):
+    """One PSF + gradient evaluation through the public API."""
+    import dlux_gb300 as dl
+
+    c = c.detach().requires_grad_(True)
+    sys_ = optics.set("layers.BasisLayer.coefficients", c)
+    psf = sys_.propagate(wls, weights=w, return_psf=True)
+    img = detector.model(psf)
+    loss = (img * R).sum()
+    loss.backward()
+    return loss, c.grad, img
+
+
+def time_gpu(args, variant, rank, world, measure_roofline=True):
+    import torch
+    import dlux_gb300._lib as L
+
+    optics, detector, wls, w, R, coeffs = build_workload(variant)
+    c = torch.as_tensor(coeffs, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        step(optics, detector, wls, w, R, c)
+    torch.cuda.synchronize()
+    lib = L.load()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = lib.dlx_launch_count()
+    if measure_roofline:
+        L.check(lib.dlx_gemm_timing_begin())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        step(optics, detector, wls, w, R, c)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = lib.dlx_launch_count() - launches0
+    gemm = None
+    if measure_roofline:
+        import ctypes
+        tot = ctypes.c_double(0)
+        cnt = ctypes.c_int(0)
+        fl = ctypes.c_double(0)
+        L.check(lib.dlx_gemm_timing_end(ctypes.byref(tot), ctypes.byref(cnt), ctypes.byref(fl)))
+        gemm = {"total_ms": tot.value, "launches": cnt.value, "flops": fl.value}
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"ms_total": ms, "launches": launches, "gemm": gemm, "clocks": clk,
+            "objects": (optics, detector, wls, w, R, coeffs)}
+
+
+def time_e2e(args, objs, world):
+    """Same step with the coefficients copied from pinned host memory and the
+    loss, gradient and image read back every step."""
+    import torch
+
+    optics, detector, wls, w, R, coeffs = objs
+    host_c = torch.as_tensor(coeffs, dtype=torch.float32).pin_memory()
+    out_img = torch.empty((128, 128), dtype=torch.float32).pin_memory()
+    out_g = torch.empty((len(NOLLS),), dtype=torch.float32).pin_memory()
+    out_l = torch.empty((), dtype=torch.float32).pin_memory()
+    c = torch.empty((len(NOLLS),), dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        c.copy_(host_c, non_blocking=True)
+        step(optics, detector, wls, w, R, c)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        c.copy_(host_c, non_blocking=True)
+        loss, g, img = step(optics, detector, wls, w, R, c)
+        out_l.copy_(loss.detach(), non_blocking=True)
+        out_g.copy_(g, non_blocking=True)
+        out_img.copy_(img.detach(), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    dt = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([dt], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    h2d = host_c.numel() * 4
+    d2h = 4 + out_g.numel() * 4 + out_img.numel() * 4
+    return dt, h2d, d2h
+
+
+def load_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return p.get("hbm_gbs", 6800.0), p.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--variant", default="split_bf16", choices=["split_bf16", "fp32"])
+    ap.add_argument("--no-fp32-compare", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+
+    res = time_gpu(args, args.variant, rank, world)
+    ms_step = res["ms_total"] / args.steps
+    value = world * args.steps / (res["ms_total"] / 1e3)
+    e2e_dt, h2d, d2h = time_e2e(args, res["objects"], world)
+    e2e_value = world * args.steps / e2e_dt
+
+    fp32 = None
+    if not args.no_fp32_compare and args.variant == "split_bf16":
+        r2 = time_gpu(args, "fp32", rank, world, measure_roofline=False)
+        fp32 = {"value": world * args.steps / (r2["ms_total"] / 1e3),
+                "ms_per_step": r2["ms_total"] / args.steps}
+
+    hbm, tflops, src = load_peaks()
+    g = res["gemm"]
+    roofline = None
+    if g and g["launches"]:
+        avg_ms = g["total_ms"] / g["launches"]
+        flops_launch = g["flops"] / g["launches"]
+        achieved = flops_launch / (avg_ms * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": tflops, "unit": "TFLOP/s",
+                    "frac": achieved / tflops, "traffic": None,
+                    "peak_source": f"{src} bf16 dense (burst)",
+                    "kernel": "tc_cgemm_kernel" if args.variant == "split_bf16" else
+                              "cgemm_fp32_kernel",
+                    "algorithmic_flops_per_launch": flops_launch,
+                    "avg_launch_ms": avg_ms,
+                    "frac_of_split_ceiling": achieved / (tflops / 3.0),
+                    "gemm_share_of_step": g["total_ms"] / res["ms_total"]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t, ns = cpu_step_sample(2)
+        cpu = {"value": 1.0 / t, "unit": "evals/s", "cores": cpu_threads(), "kind": "port",
+               "sample": f"{ns} of {N_WAVELENGTHS} wavelengths at full size, time scaled by "
+                         f"{N_WAVELENGTHS // ns}; NumPy complex64 restatement of dLux's op "
+                         "order"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
+            "data": "synthetic (seeded PCG64)",
+            "config": config_dict({"variant": args.variant,
+                                   "parallelism": f"replicas x{world}"}),
+            "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": res["launches"],
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": res["clocks"],
+            "fp32_form": fp32,
+            "speedup_vs_fp32": (value / fp32["value"]) if fp32 else None,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,172 @@
+"""torch.autograd.Function wrappers over the C ABI.
+
+Each Function's forward and backward call the library's kernels; the
+backward passes are the hand-written adjoints (the polychromatic PSF
+backward recomputes every focal field rather than storing it).
+"""
+
+from __future__ import annotations
+
+import torch
+
+from . import kernels
+
+
+class BasisEval(torch.autograd.Function):
+    """opd = base + sum_k c_k B_k (dLux utils/math.py:177-196)."""
+
+    @staticmethod
+    def forward(ctx, basis, coeffs, base):
+        ctx.save_for_backward(basis)
+        ctx.coeff_shape = tuple(coeffs.shape)
+        ctx.has_base = base is not None
+        return kernels.basis_eval(basis.detach(), coeffs.detach(),
+                                  None if base is None else base.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        (basis,) = ctx.saved_tensors
+        g = g.contiguous()
+        g_c = kernels.basis_grad(basis, g, ctx.coeff_shape) if ctx.needs_input_grad[1] else None
+        g_base = g if (ctx.has_base and ctx.needs_input_grad[2]) else None
+        return None, g_c, g_base
+
+
+def eval_basis(basis, coeffs, base=None):
+    return BasisEval.apply(basis, coeffs, base)
+
+
+class PolyPSF(torch.autograd.Function):
+    """sum_l |MFT_l(sqrt(w_l) A exp(i (2 pi (opd + tilt)/lambda_l + phase)))|^2.
+
+    A = amp * sqrt(1 / sum amp^2) when ``normalise`` (TransmissiveLayer with
+    normalise=True, wavefronts.py:397-424), else amp. amp/opd/phase may be None.
+    """
+
+    @staticmethod
+    def forward(ctx, plan, normalise, amp, opd, phase, weights, tilt):
+        amp_scale = kernels.amp_norm(amp.detach()) if (normalise and amp is not None) else None
+        t = (float(tilt[0]), float(tilt[1]))
+        ctx.plan, ctx.normalise, ctx.tilt = plan, normalise, t
+        ctx.save_for_backward(amp, opd, phase, weights, amp_scale)
+        return plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t)
+
+    @staticmethod
+    def backward(ctx, g_psf):
+        amp, opd, phase, weights, amp_scale = ctx.saved_tensors
+        plan = ctx.plan
+        want = []
+        if ctx.needs_input_grad[2] and amp is not None:
+            want.append("amp")
+        if (ctx.needs_input_grad[3] and opd is not None) or ctx.needs_input_grad[6]:
+            want.append("opd")
+        if ctx.needs_input_grad[4] and phase is not None:
+            want.append("phase")
+        if ctx.needs_input_grad[5]:
+            want.append("w")
+        if not want:
+            return (None,) * 7
+        gr = plan.grad(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(),
+                       g_psf.contiguous(), ctx.tilt, tuple(want))
+        g_amp = gr["amp"]
+        if g_amp is not None and ctx.normalise:
+            g_amp = kernels.amp_norm_backward(amp.detach(), g_amp)
+        g_tilt = None
+        if ctx.needs_input_grad[6]:
+            # d/d(theta_x, theta_y) of opd + theta_x X + theta_y Y: project on the pixel grid
+            g_tilt = kernels.basis_grad(plan.tilt_basis(), gr["opd"], (2,)).to(torch.float64)
+        g_opd = gr["opd"] if (ctx.needs_input_grad[3] and opd is not None) else None
+        return None, None, g_amp, g_opd, gr["phase"], gr["w"], g_tilt
+
+
+def _d(t):
+    return None if t is None else t.detach().contiguous()
+
+
+def poly_psf(plan, amp, opd, phase, weights, normalise=False, tilt=None):
+    """Fused polychromatic PSF; ``tilt`` is a float64 tensor [2] (radians), may require grad."""
+    if tilt is None:
+        tilt = torch.zeros(2, dtype=torch.float64)
+    tilt = torch.as_tensor(tilt, dtype=torch.float64)
+    return PolyPSF.apply(plan, bool(normalise), amp, opd, phase, weights, tilt)
+
+
+class LinearTransform(torch.autograd.Function):
+    """A cached MFT or FFT plan applied to complex64 fields; backward is the adjoint."""
+
+    @staticmethod
+    def forward(ctx, plan, field):
+        ctx.plan = plan
+        return plan.forward(field.detach())
+
+    @staticmethod
+    def backward(ctx, g):
+        return None, ctx.plan.adjoint(g.contiguous())
+
+
+def apply_plan(plan, field):
+    return LinearTransform.apply(plan, field)
+
+
+class DownsampleFlat(torch.autograd.Function):
+    """k x k block sum times a pixel response (array_ops.py:124-162, detector_layers.py:100-131)."""
+
+    @staticmethod
+    def forward(ctx, psf, flat, k, mean):
+        ctx.k, ctx.mean = k, mean
+        ctx.save_for_backward(psf, flat)
+        return kernels.downsample(psf.detach().contiguous(), k, mean,
+                                  None if flat is None else flat.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        psf, flat = ctx.saved_tensors
+        want_flat = flat is not None and ctx.needs_input_grad[1]
+        g_in, g_flat = kernels.downsample_backward(
+            psf.detach().contiguous(), g.contiguous(), ctx.k, ctx.mean,
+            None if flat is None else flat.detach().contiguous(), want_flat)
+        return (g_in if ctx.needs_input_grad[0] else None), g_flat, None, None
+
+
+def downsample(psf, k, mean=False, flat=None):
+    return DownsampleFlat.apply(psf, flat, int(k), bool(mean))
+
+
+class PhasorMul(torch.autograd.Function):
+    """field * amp * exp(i (2 pi opd / lambda_b + phase)) for a batch of wavelengths.
+
+    The forward runs the phasor kernel. The backward (used only by the
+    layer-by-layer path, not by the fused system path) is written with torch
+    complex elementwise operations.
+    """
+
+    @staticmethod
+    def forward(ctx, wavelengths, pixel_scale, field, amp, opd, phase):
+        n = field.shape[-1]
+        out = kernels.phasor(wavelengths, n, pixel_scale, field=field.detach().contiguous(),
+                             amp=_d(amp), opd=_d(opd), phase=_d(phase))
+        ctx.wavelengths = wavelengths
+        ctx.save_for_backward(field, amp, opd, phase)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        field, amp, opd, phase = ctx.saved_tensors
+        wl = torch.as_tensor(ctx.wavelengths, dtype=torch.float64, device=g.device).reshape(-1, 1, 1)
+        k = (2 * torch.pi / wl).to(torch.float32)
+        ph = torch.zeros((), device=g.device)
+        if opd is not None:
+            ph = ph + k * opd
+        if phase is not None:
+            ph = ph + phase
+        u = torch.polar(torch.ones_like(ph), ph) if torch.is_tensor(ph) and ph.dim() else \
+            torch.ones((), dtype=torch.complex64, device=g.device)
+        a = amp if amp is not None else torch.ones((), device=g.device)
+        fac = a * u
+        g_field = g * fac.conj() if ctx.needs_input_grad[2] else None
+        inner = (field * u).conj() * g  # d/d(real amp)
+        g_amp = inner.real.sum(0) if (amp is not None and ctx.needs_input_grad[3]) else None
+        dphi = ((field * fac).conj() * g).imag
+        g_opd = (k * dphi).sum(0) if (opd is not None and ctx.needs_input_grad[4]) else None
+        g_phase = dphi.sum(0) if (phase is not None and ctx.needs_input_grad[5]) else None
+        return None, None, g_field, g_amp, g_opd, g_phase

@@ -1,0 +1,36 @@
+"""Coordinate specification (dLux coordinates.py:74-157)."""
+
+from __future__ import annotations
+
+import torch
+
+from .base import Base
+
+__all__ = ["CoordSpec"]
+
+
+class CoordSpec(Base):
+    """Sampling of one axis: n pixels of size d centred on c."""
+
+    def __init__(self, n=None, d=None, c=0.0):
+        self.n = n
+        self.d = None if d is None else float(d)
+        self.c = None if c is None else float(c)
+
+    @property
+    def xs(self):
+        if self.d is None:
+            raise ValueError("d must be specified to calculate coordinates.")
+        return self.c + (torch.arange(self.n, dtype=torch.float64) - (self.n - 1) / 2) * self.d
+
+    @property
+    def fov(self):
+        if self.d is None:
+            raise ValueError("d must be specified to calculate FOV.")
+        return self.n * self.d
+
+    @property
+    def extent(self):
+        if self.d is None:
+            raise ValueError("d must be specified to calculate extent.")
+        return self.c - (self.n / 2) * self.d, self.c + (self.n / 2) * self.d

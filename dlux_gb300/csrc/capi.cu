@@ -1,0 +1,838 @@
+// capi.cu -- the extern "C" entry points declared in include/dluxgb.h, the
+// plan objects that own cached DFT matrices and intermediate buffers, and the
+// orchestration of the two-step MFT:
+//
+//   forward   D1[u][y] = sum_x AxT[u][x] E[y][x]          (contract x)
+//             F[v][u]  = alpha * sum_y AyT[v][y] D1[u][y]  (contract y)
+//   adjoint   Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
+//             Ebar[y][x] = alpha * sum_v conj(Ay[y][v]) Xt[x][v]
+//
+// where Ax[x][u] is dLux's transfer_matrix (utils/propagation.py:67-127) and
+// AxT its transpose. Every GEMM is "D = A * B^T" with both operands
+// K-contiguous, so all stores are row-major and coalesced.
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace dlx {
+
+static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void set_error(const std::string& msg) { g_err = msg; }
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+int check_cuda(cudaError_t e, const char* what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  return DLX_ERR_CUDA;
+}
+
+namespace {
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// dLux transfer_matrix axis (utils/propagation.py:67-127), FP64.
+DftAxis mft_axis(double wl, int n_in, double ps_in, int n_out, double ps_out, double shift,
+                 double focal, bool inverse) {
+  DftAxis a{};
+  const double fringe = wl / (ps_in * n_in);
+  double s_out = ps_out / fringe;
+  if (focal > 0) s_out /= focal;
+  a.a_in = 1.0 / n_in;
+  a.b_in = -(0.5 * (n_in - 1) + shift) / n_in;
+  a.a_out = s_out;
+  a.b_out = -(0.5 * (n_out - 1) + shift) * s_out;
+  a.sigma = inverse ? 1.0 : -1.0;
+  a.scale = 1.0;
+  return a;
+}
+
+// nfringes / (N_in N_out) (utils/propagation.py:130-175, 246-254), FP64.
+double mft_alpha(double wl, int n_in, double ps_in, int n_out, double ps_out, double focal) {
+  double out_size = n_out * ps_out;
+  if (focal > 0) out_size /= focal;
+  const double nfringes = out_size / (wl / (n_in * ps_in));
+  return nfringes / ((double)n_in * (double)n_out);
+}
+
+// fft_spec (utils/fourier.py:14-45): output pixel scale and centre.
+void fft_spec(int n, double ps, double wl, double focal, double* d, double* c) {
+  double d_out = wl / (n * ps);
+  if (focal > 0) d_out *= focal;
+  *d = d_out;
+  *c = (n % 2 != 0) ? 0.0 : -0.5 * d_out;
+}
+
+// One axis of the padded centred FFT (utils/propagation.py:8-64) with the
+// propagate_FFT ramps (wavefronts.py:683-712, utils/fourier.py:48-78).
+DftAxis fft_axis(const dlx_fft_desc& d, double wl) {
+  DftAxis a{};
+  const int N = d.n_in, P = d.n_in * d.pad;
+  const int npad = (N * (d.pad - 1)) / 2;
+  const int c = P / 2;
+  a.a_in = 1.0;
+  a.b_in = (double)(npad - c);
+  a.a_out = 1.0 / P;
+  a.b_out = -(double)c / P;
+  a.sigma = d.inverse ? 1.0 : -1.0;
+  a.scale = 1.0;
+  if (d.apply_ramps) {
+    const double f = d.focal_length > 0 ? d.focal_length : 0.0;
+    const double alpha = f > 0 ? wl * f : wl;
+    const double sign = d.inverse ? -1.0 : 1.0;
+    double d_fft, c_fft;
+    fft_spec(P, d.pixel_scale_in, wl, f, &d_fft, &c_fft);
+    const double shift_in = c_fft - d.center_out;
+    a.g_in = sign * shift_in * d.pixel_scale_in / alpha;
+    a.d_in = sign * shift_in / alpha * (d.center_in - 0.5 * (N - 1) * d.pixel_scale_in);
+    double d2, shift_out;
+    fft_spec(P, d_fft, wl, f, &d2, &shift_out);
+    a.g_out = sign * shift_out * d_fft / alpha;
+    a.d_out = sign * shift_out / alpha * (d.center_out - 0.5 * (P - 1) * d_fft);
+  }
+  return a;
+}
+
+// Device buffer owned by a plan.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int alloc(size_t n) {
+    if (n == 0) return DLX_OK;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      cudaGetLastError();
+      return fail(DLX_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(n) +
+                                     " bytes failed: " + cudaGetErrorString(e));
+    }
+    bytes = n;
+    return DLX_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// Cached transfer matrices of a batch of two-step transforms.
+struct TwoStep {
+  int batch = 0, n_in = 0, n_out = 0, variant = 0;
+  bool shared_xy = true;
+  // c64 matrices (FP32 form) or split matrices (tensor-core form).
+  DevBuf atx, aty, anx, any;   // T layout [b][n_out][n_in], N layout [b][n_in][n_out]
+  DevBuf alpha;                // float [b]
+  DevBuf inv_lambda, kvec;     // double [b]
+  std::vector<double> wl;
+
+  size_t elem_bytes() const { return variant == DLX_VARIANT_SPLIT_BF16 ? 8 : 8; }
+  size_t mat_bytes() const { return (size_t)batch * n_in * n_out * elem_bytes(); }
+
+  int build(const std::vector<DftAxis>& ax_x, const std::vector<DftAxis>& ax_y,
+            const std::vector<float>& alphas) {
+    shared_xy = std::memcmp(ax_x.data(), ax_y.data(), sizeof(DftAxis) * batch) == 0;
+    DevBuf axes;
+    DLX_TRY(axes.alloc(sizeof(DftAxis) * batch * 2));
+    int st = DLX_OK;
+    do {
+      cudaError_t e = cudaMemcpy(axes.p, ax_x.data(), sizeof(DftAxis) * batch,
+                                 cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(axes.as<DftAxis>() + batch, ax_y.data(), sizeof(DftAxis) * batch,
+                       cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(axes)"); break; }
+      if ((st = atx.alloc(mat_bytes())) != DLX_OK) break;
+      if ((st = anx.alloc(mat_bytes())) != DLX_OK) break;
+      if (!shared_xy) {
+        if ((st = aty.alloc(mat_bytes())) != DLX_OK) break;
+        if ((st = any.alloc(mat_bytes())) != DLX_OK) break;
+      }
+      const bool split = variant == DLX_VARIANT_SPLIT_BF16;
+      auto gen = [&](DevBuf& buf, const DftAxis* ax, bool t_layout) {
+        const int rows = t_layout ? n_out : n_in, cols = t_layout ? n_in : n_out;
+        return launch_dft_gen(ax, batch, rows, cols, t_layout, split ? nullptr : buf.as<float2>(),
+                              (long long)rows * cols, split ? buf.as<__nv_bfloat16>() : nullptr,
+                              0);
+      };
+      if ((st = gen(atx, axes.as<DftAxis>(), true)) != DLX_OK) break;
+      if ((st = gen(anx, axes.as<DftAxis>(), false)) != DLX_OK) break;
+      if (!shared_xy) {
+        if ((st = gen(aty, axes.as<DftAxis>() + batch, true)) != DLX_OK) break;
+        if ((st = gen(any, axes.as<DftAxis>() + batch, false)) != DLX_OK) break;
+      }
+      if ((st = alpha.alloc(sizeof(float) * batch)) != DLX_OK) break;
+      e = cudaMemcpy(alpha.p, alphas.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(alpha)"); break; }
+      std::vector<double> il(batch), kv(batch);
+      for (int b = 0; b < batch; ++b) {
+        il[b] = 1.0 / wl[b];
+        kv[b] = 2.0 * M_PI / wl[b];
+      }
+      if ((st = inv_lambda.alloc(sizeof(double) * batch)) != DLX_OK) break;
+      if ((st = kvec.alloc(sizeof(double) * batch)) != DLX_OK) break;
+      e = cudaMemcpy(inv_lambda.p, il.data(), sizeof(double) * batch, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(kvec.p, kv.data(), sizeof(double) * batch, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(lambda)"); break; }
+      e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) { st = check_cuda(e, "transfer-matrix generation"); break; }
+    } while (0);
+    axes.release();
+    return st;
+  }
+  const void* ATy() const { return shared_xy ? atx.p : aty.p; }
+  const void* ANy() const { return shared_xy ? anx.p : any.p; }
+  void release() {
+    atx.release(); aty.release(); anx.release(); any.release();
+    alpha.release(); inv_lambda.release(); kvec.release();
+  }
+  size_t footprint() const {
+    return atx.bytes + aty.bytes + anx.bytes + any.bytes + alpha.bytes + inv_lambda.bytes +
+           kvec.bytes;
+  }
+};
+
+int validate_variant(int variant) {
+  if (variant == DLX_VARIANT_FP32) return DLX_OK;
+  if (variant == DLX_VARIANT_SPLIT_BF16) {
+    if (!tc_supported())
+      return fail(DLX_ERR_UNSUPPORTED,
+                  "the split-BF16 tensor-core form needs an sm_103a (GB300) device");
+    return DLX_OK;
+  }
+  return fail(DLX_ERR_ARG, "variant must be DLX_VARIANT_FP32 or DLX_VARIANT_SPLIT_BF16");
+}
+
+int check_split_shape(int variant, int n_in, int n_out) {
+  if (variant == DLX_VARIANT_SPLIT_BF16 && (n_in % 8 != 0 || n_out % 8 != 0))
+    return fail(DLX_ERR_SHAPE,
+                "the split-BF16 form needs input and output sides that are multiples of 8 "
+                "(TMA row pitch); use DLX_VARIANT_FP32 for other sizes");
+  return DLX_OK;
+}
+
+// Optional CUDA-event timing of every GEMM launch (dlx_gemm_timing_*), used
+// to measure the dominant kernel inside a timed region on its own stream.
+struct GemmTiming {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+  double flops = 0.0;  // algorithmic complex-GEMM flops of the recorded launches
+};
+GemmTiming g_timing;
+
+int run_gemm(int variant, const GemmArgs& g, cudaStream_t s) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (g_timing.on) {
+    DLX_TRY_CUDA(cudaEventCreate(&a));
+    DLX_TRY_CUDA(cudaEventCreate(&b));
+    DLX_TRY_CUDA(cudaEventRecord(a, s));
+  }
+  int st = variant == DLX_VARIANT_SPLIT_BF16 ? launch_gemm_tc(g, s) : launch_gemm_fp32(g, s);
+  if (g_timing.on) {
+    DLX_TRY_CUDA(cudaEventRecord(b, s));
+    g_timing.ev.emplace_back(a, b);
+    g_timing.flops += 8.0 * g.batch * (double)g.M * g.N * g.K;
+  }
+  return st;
+}
+
+GemmArgs gemm_c64(int batch, int M, int N, int K, const void* A, bool conj_a, const void* B,
+                  const EpiArgs& epi) {
+  GemmArgs g{};
+  g.batch = batch; g.M = M; g.N = N; g.K = K;
+  g.A = reinterpret_cast<const float2*>(A);
+  g.a_bs = (long long)M * K;
+  g.B = reinterpret_cast<const float2*>(B);
+  g.b_bs = (long long)N * K;
+  g.conj_a = conj_a;
+  g.a_batch_div = 1;
+  g.epi = epi;
+  return g;
+}
+
+GemmArgs gemm_split(int batch, int M, int N, int K, const void* A, bool conj_a, const void* B,
+                    const EpiArgs& epi) {
+  GemmArgs g{};
+  g.batch = batch; g.M = M; g.N = N; g.K = K;
+  g.As = reinterpret_cast<const __nv_bfloat16*>(A);
+  g.Bs = reinterpret_cast<const __nv_bfloat16*>(B);
+  g.conj_a = conj_a;
+  g.a_batch_div = 1;
+  g.epi = epi;
+  return g;
+}
+
+GemmArgs gemm_for(int variant, int batch, int M, int N, int K, const void* A, bool conj_a,
+                  const void* B, const EpiArgs& epi) {
+  return variant == DLX_VARIANT_SPLIT_BF16 ? gemm_split(batch, M, N, K, A, conj_a, B, epi)
+                                           : gemm_c64(batch, M, N, K, A, conj_a, B, epi);
+}
+
+EpiArgs epi_store(int variant, void* out, const float* alpha) {
+  EpiArgs e{};
+  e.alpha = alpha;
+  if (variant == DLX_VARIANT_SPLIT_BF16) {
+    e.kind = EPI_SPLIT;
+    e.out_split = reinterpret_cast<__nv_bfloat16*>(out);
+  } else {
+    e.kind = EPI_C64;
+    e.out_c64 = reinterpret_cast<float2*>(out);
+  }
+  return e;
+}
+
+EpiArgs epi_c64(void* out, const float* alpha) {
+  EpiArgs e{};
+  e.kind = EPI_C64;
+  e.alpha = alpha;
+  e.out_c64 = reinterpret_cast<float2*>(out);
+  return e;
+}
+
+}  // namespace
+}  // namespace dlx
+
+using namespace dlx;
+
+// ---------------------------------------------------------------------------
+// Generic two-step transform plan (MFT and FFT share it).
+// ---------------------------------------------------------------------------
+struct TwoStepPlan {
+  TwoStep ts;
+  DevBuf in_split;   // [b][4][n_in][n_in]   (split form: converted input)
+  DevBuf mid;        // [b][n_out][n_in] (forward) / [b][n_in][n_out] (adjoint) intermediate
+  DevBuf gout_split; // [b][4][n_out][n_out] (split form: converted cotangent)
+
+  int alloc_buffers() {
+    const size_t b = ts.batch, ni = ts.n_in, no = ts.n_out;
+    DLX_TRY(mid.alloc(b * ni * no * 8));
+    if (ts.variant == DLX_VARIANT_SPLIT_BF16) {
+      DLX_TRY(in_split.alloc(b * ni * ni * 8));
+      DLX_TRY(gout_split.alloc(b * no * no * 8));
+    }
+    return DLX_OK;
+  }
+  int forward(const void* in, void* out, cudaStream_t s) {
+    const int B = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    const void* field = in;
+    if (v == DLX_VARIANT_SPLIT_BF16) {
+      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(in), (long long)N * N,
+                                          B, in_split.as<__nv_bfloat16>(), s));
+      field = in_split.p;
+    }
+    // D1[u][y] = sum_x AxT[u][x] E[y][x]
+    DLX_TRY(run_gemm(v, gemm_for(v, B, M, N, N, ts.atx.p, false, field,
+                                 epi_store(v, mid.p, nullptr)), s));
+    // F[v][u] = alpha sum_y AyT[v][y] D1[u][y]
+    DLX_TRY(run_gemm(v, gemm_for(v, B, M, M, N, ts.ATy(), false, mid.p,
+                                 epi_c64(out, ts.alpha.as<float>())), s));
+    return DLX_OK;
+  }
+  int adjoint(const void* gout, void* gin, cudaStream_t s) {
+    const int B = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    const void* g = gout;
+    if (v == DLX_VARIANT_SPLIT_BF16) {
+      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(gout),
+                                          (long long)M * M, B, gout_split.as<__nv_bfloat16>(),
+                                          s));
+      g = gout_split.p;
+    }
+    // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
+    DLX_TRY(run_gemm(v, gemm_for(v, B, N, M, M, ts.anx.p, true, g,
+                                 epi_store(v, mid.p, nullptr)), s));
+    // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v]
+    DLX_TRY(run_gemm(v, gemm_for(v, B, N, N, M, ts.ANy(), true, mid.p,
+                                 epi_c64(gin, ts.alpha.as<float>())), s));
+    return DLX_OK;
+  }
+  void release() {
+    ts.release();
+    in_split.release();
+    mid.release();
+    gout_split.release();
+  }
+};
+
+struct dlx_mft_plan_s {
+  TwoStepPlan p;
+};
+struct dlx_fft_plan_s {
+  TwoStepPlan p;
+};
+
+extern "C" {
+
+const char* dlx_last_error(void) { return g_err.c_str(); }
+int dlx_version(void) { return 100; }
+long long dlx_launch_count(void) { return g_launches.load(); }
+
+int dlx_gemm_timing_begin(void) {
+  for (auto& p : g_timing.ev) {
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+  g_timing.ev.clear();
+  g_timing.flops = 0.0;
+  g_timing.on = true;
+  return DLX_OK;
+}
+
+int dlx_gemm_timing_end(double* total_ms, int* launches, double* flops) {
+  g_timing.on = false;
+  double t = 0.0;
+  int st = DLX_OK;
+  for (auto& p : g_timing.ev) {
+    float ms = 0.f;
+    cudaError_t e = cudaEventSynchronize(p.second);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, p.first, p.second);
+    if (e != cudaSuccess && st == DLX_OK) st = check_cuda(e, "gemm timing");
+    t += ms;
+    cudaEventDestroy(p.first);
+    cudaEventDestroy(p.second);
+  }
+  if (total_ms) *total_ms = t;
+  if (launches) *launches = (int)g_timing.ev.size();
+  if (flops) *flops = g_timing.flops;
+  g_timing.ev.clear();
+  g_timing.flops = 0.0;
+  return st;
+}
+
+int dlx_transfer_matrix(const double* wavelengths_host, int batch, int n_in,
+                        double pixel_scale_in, int n_out, double pixel_scale_out, double shift,
+                        double focal_length, int inverse, int transpose, void* out_c64,
+                        void* stream) {
+  if (batch < 0 || n_in <= 0 || n_out <= 0)
+    return fail(DLX_ERR_SHAPE, "transfer_matrix: batch >= 0, n_in > 0 and n_out > 0 required");
+  if (batch == 0) return DLX_OK;
+  if (!wavelengths_host || !out_c64) return fail(DLX_ERR_ARG, "transfer_matrix: null pointer");
+  cudaStream_t s = as_stream(stream);
+  std::vector<DftAxis> ax(batch);
+  for (int b = 0; b < batch; ++b) {
+    if (!(wavelengths_host[b] > 0))
+      return fail(DLX_ERR_ARG, "transfer_matrix: wavelengths must be positive");
+    ax[b] = mft_axis(wavelengths_host[b], n_in, pixel_scale_in, n_out, pixel_scale_out, shift,
+                     focal_length, inverse != 0);
+  }
+  DftAxis* dev = nullptr;
+  DLX_TRY_CUDA(cudaMallocAsync((void**)&dev, sizeof(DftAxis) * batch, s));
+  cudaError_t e = cudaMemcpyAsync(dev, ax.data(), sizeof(DftAxis) * batch,
+                                  cudaMemcpyHostToDevice, s);
+  int st = (e == cudaSuccess) ? DLX_OK : check_cuda(e, "cudaMemcpyAsync(axes)");
+  if (st == DLX_OK) {
+    const bool t = transpose != 0;
+    st = launch_dft_gen(dev, batch, t ? n_out : n_in, t ? n_in : n_out, t,
+                        reinterpret_cast<float2*>(out_c64), (long long)n_in * n_out, nullptr, s);
+  }
+  // The host vector must outlive the copy: wait for it before returning.
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaFreeAsync(dev, s);
+  if (st == DLX_OK && e2 != cudaSuccess) st = check_cuda(e2, "transfer_matrix");
+  return st;
+}
+
+// ---- MFT plan ---------------------------------------------------------------
+int dlx_mft_plan_create(const dlx_mft_desc* d, const double* wl, dlx_mft_plan* plan) {
+  if (!d || !wl || !plan) return fail(DLX_ERR_ARG, "mft_plan_create: null pointer");
+  *plan = nullptr;
+  if (d->batch <= 0 || d->n_in <= 0 || d->n_out <= 0)
+    return fail(DLX_ERR_SHAPE, "mft_plan_create: batch, n_in and n_out must be positive");
+  if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
+    return fail(DLX_ERR_ARG, "mft_plan_create: pixel scales must be positive");
+  DLX_TRY(validate_variant(d->variant));
+  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
+  auto* p = new (std::nothrow) dlx_mft_plan_s();
+  if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+  TwoStep& ts = p->p.ts;
+  ts.batch = d->batch; ts.n_in = d->n_in; ts.n_out = d->n_out; ts.variant = d->variant;
+  ts.wl.assign(wl, wl + d->batch);
+  std::vector<DftAxis> ax(d->batch), ay(d->batch);
+  std::vector<float> alphas(d->batch);
+  for (int b = 0; b < d->batch; ++b) {
+    if (!(wl[b] > 0)) {
+      delete p;
+      return fail(DLX_ERR_ARG, "mft_plan_create: wavelengths must be positive");
+    }
+    ax[b] = mft_axis(wl[b], d->n_in, d->pixel_scale_in, d->n_out, d->pixel_scale_out, d->shift_x,
+                     d->focal_length, d->inverse != 0);
+    ay[b] = mft_axis(wl[b], d->n_in, d->pixel_scale_in, d->n_out, d->pixel_scale_out, d->shift_y,
+                     d->focal_length, d->inverse != 0);
+    alphas[b] = (float)mft_alpha(wl[b], d->n_in, d->pixel_scale_in, d->n_out, d->pixel_scale_out,
+                                 d->focal_length);
+  }
+  int st = ts.build(ax, ay, alphas);
+  if (st == DLX_OK) st = p->p.alloc_buffers();
+  if (st != DLX_OK) {
+    p->p.release();
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return DLX_OK;
+}
+
+int dlx_mft_plan_destroy(dlx_mft_plan plan) {
+  if (!plan) return DLX_OK;
+  cudaDeviceSynchronize();
+  plan->p.release();
+  delete plan;
+  return DLX_OK;
+}
+
+int dlx_mft_forward(dlx_mft_plan plan, const void* in, void* out, void* stream) {
+  if (!plan || !in || !out) return fail(DLX_ERR_ARG, "mft_forward: null pointer");
+  return plan->p.forward(in, out, as_stream(stream));
+}
+
+int dlx_mft_adjoint(dlx_mft_plan plan, const void* gout, void* gin, void* stream) {
+  if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "mft_adjoint: null pointer");
+  return plan->p.adjoint(gout, gin, as_stream(stream));
+}
+
+// ---- FFT plan ---------------------------------------------------------------
+int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* plan) {
+  if (!d || !wl || !plan) return fail(DLX_ERR_ARG, "fft_plan_create: null pointer");
+  *plan = nullptr;
+  if (d->batch <= 0 || d->n_in <= 0 || d->pad <= 0)
+    return fail(DLX_ERR_SHAPE, "fft_plan_create: batch, n_in and pad must be positive");
+  if (!(d->pixel_scale_in > 0)) return fail(DLX_ERR_ARG, "fft_plan_create: pixel scale <= 0");
+  DLX_TRY(validate_variant(d->variant));
+  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_in * d->pad));
+  auto* p = new (std::nothrow) dlx_fft_plan_s();
+  if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+  TwoStep& ts = p->p.ts;
+  ts.batch = d->batch; ts.n_in = d->n_in; ts.n_out = d->n_in * d->pad; ts.variant = d->variant;
+  ts.wl.assign(wl, wl + d->batch);
+  std::vector<DftAxis> ax(d->batch);
+  std::vector<float> alphas(d->batch, 1.0f / (float)(d->n_in * d->pad));
+  for (int b = 0; b < d->batch; ++b) {
+    if (!(wl[b] > 0)) {
+      delete p;
+      return fail(DLX_ERR_ARG, "fft_plan_create: wavelengths must be positive");
+    }
+    ax[b] = fft_axis(*d, wl[b]);
+  }
+  int st = ts.build(ax, ax, alphas);
+  if (st == DLX_OK) st = p->p.alloc_buffers();
+  if (st != DLX_OK) {
+    p->p.release();
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return DLX_OK;
+}
+
+int dlx_fft_plan_destroy(dlx_fft_plan plan) {
+  if (!plan) return DLX_OK;
+  cudaDeviceSynchronize();
+  plan->p.release();
+  delete plan;
+  return DLX_OK;
+}
+
+int dlx_fft_forward(dlx_fft_plan plan, const void* in, void* out, void* stream) {
+  if (!plan || !in || !out) return fail(DLX_ERR_ARG, "fft_forward: null pointer");
+  return plan->p.forward(in, out, as_stream(stream));
+}
+
+int dlx_fft_adjoint(dlx_fft_plan plan, const void* gout, void* gin, void* stream) {
+  if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "fft_adjoint: null pointer");
+  return plan->p.adjoint(gout, gin, as_stream(stream));
+}
+
+// ---- elementwise entry points ----------------------------------------------
+int dlx_phasor(const void* in, const float* amp, const float* opd, const float* phase,
+               const float* amp_scale, const float* weights, double const_scale,
+               const double* wavelengths_host, int batch, int n, double pixel_scale,
+               double tilt_x, double tilt_y, void* out, void* stream) {
+  if (batch < 0 || n < 0) return fail(DLX_ERR_SHAPE, "phasor: negative size");
+  if (batch == 0 || n == 0) return DLX_OK;
+  if (!out || !wavelengths_host) return fail(DLX_ERR_ARG, "phasor: null pointer");
+  cudaStream_t s = as_stream(stream);
+  for (int b0 = 0; b0 < batch; b0 += kMaxBatchArg) {
+    const int nb = (batch - b0) < kMaxBatchArg ? (batch - b0) : kMaxBatchArg;
+    BatchD il;
+    for (int i = 0; i < kMaxBatchArg; ++i) il.v[i] = 0.0;
+    for (int i = 0; i < nb; ++i) {
+      const double w = wavelengths_host[b0 + i];
+      if (!(w > 0)) return fail(DLX_ERR_ARG, "phasor: wavelengths must be positive");
+      il.v[i] = 1.0 / w;
+    }
+    const long long off = (long long)b0 * n * n;
+    PhasorArgs a{};
+    a.in = in ? reinterpret_cast<const float2*>(in) + off : nullptr;
+    a.amp = amp; a.opd = opd; a.phase = phase; a.amp_scale = amp_scale;
+    a.weights = weights ? weights + b0 : nullptr;
+    a.inv_lambda_dev = nullptr;
+    a.const_scale = const_scale;
+    a.batch = nb; a.n = n;
+    a.pixel_scale = pixel_scale; a.tilt_x = tilt_x; a.tilt_y = tilt_y;
+    a.out_c64 = reinterpret_cast<float2*>(out) + off;
+    a.out_split = nullptr;
+    DLX_TRY(launch_phasor(a, &il, s));
+  }
+  return DLX_OK;
+}
+
+int dlx_power_scale(const void* in, int batch, int n, double value, float* out_scale,
+                    void* stream) {
+  if (batch < 0 || n < 0) return fail(DLX_ERR_SHAPE, "power_scale: negative size");
+  if (!in || !out_scale) return fail(DLX_ERR_ARG, "power_scale: null pointer");
+  return launch_power_scale(reinterpret_cast<const float2*>(in), batch, (long long)n * n, value,
+                            out_scale, as_stream(stream));
+}
+
+static int with_partials(size_t count, cudaStream_t s, double** ws) {
+  DLX_TRY_CUDA(cudaMallocAsync((void**)ws, sizeof(double) * (count > 0 ? count : 1), s));
+  return DLX_OK;
+}
+
+int dlx_amp_norm(const float* amp, int n, double value, float* out_scale, void* stream) {
+  if (n <= 0) return fail(DLX_ERR_SHAPE, "amp_norm: n must be positive");
+  if (!amp || !out_scale) return fail(DLX_ERR_ARG, "amp_norm: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const int nparts = 128;
+  double* ws = nullptr;
+  DLX_TRY(with_partials(nparts, s, &ws));
+  int st = launch_amp_norm(amp, (long long)n * n, value, out_scale, ws, nparts, s);
+  cudaFreeAsync(ws, s);
+  return st;
+}
+
+int dlx_amp_norm_backward(const float* amp, const float* g_eff, int n, double value,
+                          float* g_amp, void* stream) {
+  if (n <= 0) return fail(DLX_ERR_SHAPE, "amp_norm_backward: n must be positive");
+  if (!amp || !g_eff || !g_amp) return fail(DLX_ERR_ARG, "amp_norm_backward: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const int nparts = 128;
+  double* ws = nullptr;
+  DLX_TRY(with_partials(2 * nparts, s, &ws));
+  int st = launch_amp_norm_backward(amp, g_eff, (long long)n * n, value, g_amp, ws, nparts, s);
+  cudaFreeAsync(ws, s);
+  return st;
+}
+
+int dlx_basis_eval(const float* basis, const float* coeffs, const float* base, int nterms,
+                   long long npix, float* out, void* stream) {
+  if (nterms < 0 || npix < 0) return fail(DLX_ERR_SHAPE, "basis_eval: negative size");
+  if (!out || (nterms > 0 && (!basis || !coeffs)))
+    return fail(DLX_ERR_ARG, "basis_eval: null pointer");
+  return launch_basis_eval(basis, coeffs, base, nterms, npix, out, as_stream(stream));
+}
+
+int dlx_basis_grad(const float* basis, const float* g, int nterms, long long npix,
+                   float* g_coeffs, void* stream) {
+  if (nterms < 0 || npix < 0) return fail(DLX_ERR_SHAPE, "basis_grad: negative size");
+  if (nterms == 0) return DLX_OK;
+  if (!basis || !g || !g_coeffs) return fail(DLX_ERR_ARG, "basis_grad: null pointer");
+  cudaStream_t s = as_stream(stream);
+  const int nparts = 64;
+  double* ws = nullptr;
+  DLX_TRY(with_partials((size_t)nparts * nterms, s, &ws));
+  int st = launch_basis_grad(basis, g, nterms, npix, g_coeffs, ws, nparts, s);
+  cudaFreeAsync(ws, s);
+  return st;
+}
+
+int dlx_psf_sum(const void* in, int batch, long long npix, float* psf, void* stream) {
+  if (batch < 0 || npix < 0) return fail(DLX_ERR_SHAPE, "psf_sum: negative size");
+  if (!in || !psf) return fail(DLX_ERR_ARG, "psf_sum: null pointer");
+  return launch_psf_sum(reinterpret_cast<const float2*>(in), batch, npix, psf,
+                        as_stream(stream));
+}
+
+int dlx_downsample(const float* in, int n_in, int k, int mean, const float* flat, float* out,
+                   void* stream) {
+  if (k <= 0) return fail(DLX_ERR_ARG, "downsample: kernel size must be greater than 0");
+  if (n_in % k != 0)
+    return fail(DLX_ERR_SHAPE, "downsample: input size " + std::to_string(n_in) +
+                                   " is not divisible by " + std::to_string(k));
+  if (!in || !out) return fail(DLX_ERR_ARG, "downsample: null pointer");
+  return launch_downsample(in, n_in, k, mean, flat, out, as_stream(stream));
+}
+
+int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k, int mean,
+                            const float* flat, float* g_in, float* g_flat, void* stream) {
+  if (k <= 0) return fail(DLX_ERR_ARG, "downsample: kernel size must be greater than 0");
+  if (n_in % k != 0) return fail(DLX_ERR_SHAPE, "downsample: size not divisible");
+  if (!g_out || (g_flat && !in)) return fail(DLX_ERR_ARG, "downsample_backward: null pointer");
+  return launch_downsample_backward(in, g_out, n_in, k, mean, flat, g_in, g_flat,
+                                    as_stream(stream));
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Fused polychromatic PSF plan.
+// ---------------------------------------------------------------------------
+struct dlx_poly_plan_s {
+  TwoStep ts;
+  double pixel_scale_in = 0;
+  DevBuf field;      // E: [L][N][N] c64 or [L][4][N][N] split
+  DevBuf mid;        // D1 [L][M][N] / Xt [L][N][M]
+  DevBuf fbar;       // [L][M][M] c64 or split
+  DevBuf planes;     // intensity [L][M][M] f32, or pre/pim [2][L][N][N] f32
+  DevBuf partial;    // double reduction partials
+  int nparts = 64;
+
+  size_t footprint() const {
+    return ts.footprint() + field.bytes + mid.bytes + fbar.bytes + planes.bytes + partial.bytes;
+  }
+  void release() {
+    ts.release(); field.release(); mid.release(); fbar.release(); planes.release();
+    partial.release();
+  }
+  int build_field(const float* amp, const float* amp_scale, const float* opd,
+                  const float* phase, const float* weights, double tx, double ty,
+                  cudaStream_t s) {
+    PhasorArgs a{};
+    a.amp = amp; a.amp_scale = amp_scale; a.opd = opd; a.phase = phase; a.weights = weights;
+    a.inv_lambda_dev = ts.inv_lambda.as<double>();
+    a.const_scale = 1.0;
+    a.batch = ts.batch; a.n = ts.n_in;
+    a.pixel_scale = pixel_scale_in; a.tilt_x = tx; a.tilt_y = ty;
+    if (ts.variant == DLX_VARIANT_SPLIT_BF16) a.out_split = field.as<__nv_bfloat16>();
+    else a.out_c64 = field.as<float2>();
+    return launch_phasor(a, nullptr, s);
+  }
+};
+
+extern "C" {
+
+int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan* plan) {
+  if (!d || !wl || !plan) return fail(DLX_ERR_ARG, "poly_plan_create: null pointer");
+  *plan = nullptr;
+  if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0)
+    return fail(DLX_ERR_SHAPE, "poly_plan_create: sizes must be positive");
+  if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
+    return fail(DLX_ERR_ARG, "poly_plan_create: pixel scales must be positive");
+  DLX_TRY(validate_variant(d->variant));
+  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
+  auto* p = new (std::nothrow) dlx_poly_plan_s();
+  if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+  const int L = d->n_wavelengths, N = d->n_in, M = d->n_out;
+  TwoStep& ts = p->ts;
+  ts.batch = L; ts.n_in = N; ts.n_out = M; ts.variant = d->variant;
+  ts.wl.assign(wl, wl + L);
+  p->pixel_scale_in = d->pixel_scale_in;
+  std::vector<DftAxis> ax(L);
+  std::vector<float> alphas(L);
+  for (int b = 0; b < L; ++b) {
+    if (!(wl[b] > 0)) {
+      delete p;
+      return fail(DLX_ERR_ARG, "poly_plan_create: wavelengths must be positive");
+    }
+    ax[b] = mft_axis(wl[b], N, d->pixel_scale_in, M, d->pixel_scale_out, 0.0, d->focal_length,
+                     false);
+    alphas[b] = (float)mft_alpha(wl[b], N, d->pixel_scale_in, M, d->pixel_scale_out,
+                                 d->focal_length);
+  }
+  int st = ts.build(ax, ax, alphas);
+  const size_t l = L, n = N, m = M;
+  if (st == DLX_OK) st = p->field.alloc(l * n * n * 8);
+  if (st == DLX_OK) st = p->mid.alloc(l * n * m * 8);
+  if (st == DLX_OK) st = p->fbar.alloc(l * m * m * 8);
+  if (st == DLX_OK) {
+    const size_t a = l * m * m * 4, b = 2 * l * n * n * 4;
+    st = p->planes.alloc(a > b ? a : b);
+  }
+  if (st == DLX_OK) st = p->partial.alloc(sizeof(double) * (size_t)p->nparts * (L + 2));
+  if (st != DLX_OK) {
+    p->release();
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return DLX_OK;
+}
+
+int dlx_poly_plan_destroy(dlx_poly_plan plan) {
+  if (!plan) return DLX_OK;
+  cudaDeviceSynchronize();
+  plan->release();
+  delete plan;
+  return DLX_OK;
+}
+
+int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes) {
+  if (!plan || !bytes) return fail(DLX_ERR_ARG, "poly_plan_footprint: null pointer");
+  *bytes = plan->footprint();
+  return DLX_OK;
+}
+
+int dlx_poly_psf(dlx_poly_plan plan, const float* amp, const float* amp_scale, const float* opd,
+                 const float* phase, const float* weights, double tilt_x, double tilt_y,
+                 float* psf_out, void* stream) {
+  if (!plan || !psf_out) return fail(DLX_ERR_ARG, "poly_psf: null pointer");
+  cudaStream_t s = as_stream(stream);
+  dlx_poly_plan_s& p = *plan;
+  const int L = p.ts.batch, N = p.ts.n_in, M = p.ts.n_out, v = p.ts.variant;
+  DLX_TRY(p.build_field(amp, amp_scale, opd, phase, weights, tilt_x, tilt_y, s));
+  DLX_TRY(run_gemm(v, gemm_for(v, L, M, N, N, p.ts.atx.p, false, p.field.p,
+                               epi_store(v, p.mid.p, nullptr)), s));
+  EpiArgs e{};
+  e.kind = EPI_INTENSITY;
+  e.alpha = p.ts.alpha.as<float>();
+  e.out_f32 = p.planes.as<float>();
+  DLX_TRY(run_gemm(v, gemm_for(v, L, M, M, N, p.ts.ATy(), false, p.mid.p, e), s));
+  return launch_plane_sum(p.planes.as<float>(), L, (long long)M * M, psf_out, s);
+}
+
+int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_scale,
+                      const float* opd, const float* phase, const float* weights, double tilt_x,
+                      double tilt_y, const float* g_psf, float* g_amp, float* g_opd,
+                      float* g_phase, float* g_w, void* stream) {
+  if (!plan || !g_psf) return fail(DLX_ERR_ARG, "poly_psf_grad: null pointer");
+  cudaStream_t s = as_stream(stream);
+  dlx_poly_plan_s& p = *plan;
+  const int L = p.ts.batch, N = p.ts.n_in, M = p.ts.n_out, v = p.ts.variant;
+  // Recompute the forward fields (nothing is stored between the passes).
+  DLX_TRY(p.build_field(amp, amp_scale, opd, phase, weights, tilt_x, tilt_y, s));
+  DLX_TRY(run_gemm(v, gemm_for(v, L, M, N, N, p.ts.atx.p, false, p.field.p,
+                               epi_store(v, p.mid.p, nullptr)), s));
+  // Fbar[v][u] = 2 alpha G[v][u] D[v][u]
+  EpiArgs eg{};
+  eg.kind = EPI_GRADF;
+  eg.alpha = p.ts.alpha.as<float>();
+  eg.G = g_psf;
+  if (v == DLX_VARIANT_SPLIT_BF16) eg.out_split = p.fbar.as<__nv_bfloat16>();
+  else eg.out_c64 = p.fbar.as<float2>();
+  DLX_TRY(run_gemm(v, gemm_for(v, L, M, M, N, p.ts.ATy(), false, p.mid.p, eg), s));
+  // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
+  DLX_TRY(run_gemm(v, gemm_for(v, L, N, M, M, p.ts.anx.p, true, p.fbar.p,
+                               epi_store(v, p.mid.p, nullptr)), s));
+  // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v] -> pupil-gradient planes
+  float* pre = p.planes.as<float>();
+  float* pim = pre + (size_t)L * N * N;
+  EpiArgs ep{};
+  ep.kind = EPI_PUPIL;
+  ep.alpha = p.ts.alpha.as<float>();
+  ep.out_f32 = pre;
+  ep.out_f32b = pim;
+  ep.amp = amp; ep.amp_scale = amp_scale; ep.opd = opd; ep.phase = phase; ep.weights = weights;
+  ep.inv_lambda = p.ts.inv_lambda.as<double>();
+  ep.pixel_scale = p.pixel_scale_in; ep.tilt_x = tilt_x; ep.tilt_y = tilt_y;
+  DLX_TRY(run_gemm(v, gemm_for(v, L, N, N, M, p.ts.ANy(), true, p.mid.p, ep), s));
+  PupilReduceArgs r{};
+  r.pre = pre; r.pim = pim; r.amp = amp; r.amp_scale = amp_scale; r.weights = weights;
+  r.k_dev = p.ts.kvec.as<double>();
+  r.batch = L; r.npix = (long long)N * N;
+  r.g_amp = g_amp; r.g_opd = g_opd; r.g_phase = g_phase;
+  r.g_w = weights ? g_w : nullptr;
+  r.partial_ws = p.partial.as<double>();
+  r.nparts = p.nparts;
+  return launch_pupil_reduce(r, s);
+}
+
+}  // extern "C"

@@ -1,0 +1,498 @@
+// elementwise.cu -- DFT-matrix generation, phasor build, reductions, basis
+// contraction and detector kernels. All of these are HBM- or latency-bound;
+// each is written for coalesced access with one pixel per thread and a
+// wavelength loop inside the thread where the inputs are shared across the
+// batch.
+#include "kernels.h"
+
+#include <math_constants.h>
+
+namespace dlx {
+
+// ---------------------------------------------------------------------------
+// DFT / transfer-matrix generation (dLux utils/propagation.py:67-127 for the
+// MFT, utils/propagation.py:8-64 + utils/fourier.py:48-78 for the FFT).
+// ---------------------------------------------------------------------------
+__global__ void dft_gen_kernel(const DftAxis* __restrict__ axes, int rows, int cols,
+                               bool rows_are_out, float2* __restrict__ out_c64,
+                               long long out_bs, __nv_bfloat16* __restrict__ out_split) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y * blockDim.y + threadIdx.y;
+  const int b = blockIdx.z;
+  if (r >= rows || c >= cols) return;
+  const DftAxis ax = axes[b];
+  const int i_in = rows_are_out ? c : r;
+  const int j_out = rows_are_out ? r : c;
+  const double x = ax.a_in * (double)i_in + ax.b_in;
+  const double u = ax.a_out * (double)j_out + ax.b_out;
+  const double t = ax.sigma * x * u + (ax.g_in * (double)i_in + ax.d_in) +
+                   (ax.g_out * (double)j_out + ax.d_out);
+  float2 v = cis_cycles(t);
+  v.x *= (float)ax.scale;
+  v.y *= (float)ax.scale;
+  const long long idx = (long long)r * cols + c;
+  if (out_c64) out_c64[(long long)b * out_bs + idx] = v;
+  if (out_split) {
+    const long long plane = (long long)rows * cols;
+    __nv_bfloat16* base = out_split + (long long)b * 4 * plane + idx;
+    __nv_bfloat16 h, l;
+    split_bf16(v.x, h, l);
+    base[0] = h;
+    base[plane] = l;
+    split_bf16(v.y, h, l);
+    base[2 * plane] = h;
+    base[3 * plane] = l;
+  }
+}
+
+int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool rows_are_out,
+                   float2* out_c64, long long out_batch_stride, __nv_bfloat16* out_split,
+                   cudaStream_t s) {
+  if (batch <= 0 || rows <= 0 || cols <= 0) return DLX_OK;
+  dim3 block(32, 8);
+  dim3 grid(ceil_div(cols, 32), ceil_div(rows, 8), batch);
+  dft_gen_kernel<<<grid, block, 0, s>>>(axes_dev, rows, cols, rows_are_out, out_c64,
+                                        out_batch_stride, out_split);
+  DLX_LAUNCH_CHECK("dft_gen_kernel");
+  return DLX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Phasor build (wavefronts.py:70-122, :332-395; optical_layers.py:181-186,
+// 319-327; optics.py:77-96; optical_systems.py:213-215).
+// One thread per pixel; the wavelength loop reuses amp/opd/phase.
+// ---------------------------------------------------------------------------
+__global__ void phasor_kernel(PhasorArgs a, BatchD inv_lambda_arg) {
+  const long long npix = (long long)a.n * a.n;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  const int y = (int)(p / a.n);
+  const int x = (int)(p - (long long)y * a.n);
+  const double half = 0.5 * (a.n - 1);
+  const double X = ((double)x - half) * a.pixel_scale;
+  const double Y = ((double)y - half) * a.pixel_scale;
+  const double path = (a.opd ? (double)a.opd[p] : 0.0) + a.tilt_x * X + a.tilt_y * Y;
+  const double ph_cyc = a.phase ? (double)a.phase[p] * (0.5 / CUDART_PI) : 0.0;
+  float amp = a.amp ? a.amp[p] : 1.0f;
+  if (a.amp_scale) amp *= *a.amp_scale;
+  amp *= (float)a.const_scale;
+  for (int b = 0; b < a.batch; ++b) {
+    const double il = a.inv_lambda_dev ? a.inv_lambda_dev[b] : inv_lambda_arg.v[b];
+    float2 u = cis_cycles(path * il + ph_cyc);
+    float sc = amp;
+    if (a.weights) sc *= sqrtf(a.weights[b]);
+    float2 v = make_float2(u.x * sc, u.y * sc);
+    const long long o = (long long)b * npix + p;
+    if (a.in) v = cmul(a.in[o], v);
+    if (a.out_c64) a.out_c64[o] = v;
+    if (a.out_split) {
+      __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p;
+      __nv_bfloat16 h, l;
+      split_bf16(v.x, h, l);
+      base[0] = h;
+      base[npix] = l;
+      split_bf16(v.y, h, l);
+      base[2 * npix] = h;
+      base[3 * npix] = l;
+    }
+  }
+}
+
+int launch_phasor(const PhasorArgs& a, const BatchD* inv_lambda_arg, cudaStream_t s) {
+  const long long npix = (long long)a.n * a.n;
+  if (npix == 0 || a.batch == 0) return DLX_OK;
+  BatchD dummy;
+  if (!inv_lambda_arg) {
+    for (int i = 0; i < kMaxBatchArg; ++i) dummy.v[i] = 0.0;
+    inv_lambda_arg = &dummy;
+  }
+  phasor_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(a, *inv_lambda_arg);
+  DLX_LAUNCH_CHECK("phasor_kernel");
+  return DLX_OK;
+}
+
+// c64 [b][plane] -> split [b][4][plane]: the batch is folded into the
+// element count because the split planes of batch b start at 4 * b * plane.
+__global__ void c64_to_split_kernel(const float2* __restrict__ in, long long plane, int batch,
+                                    __nv_bfloat16* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= plane) return;
+  for (int b = 0; b < batch; ++b) {
+    __nv_bfloat16* base = out + (long long)b * 4 * plane;
+    float2 v = in[(long long)b * plane + p];
+    __nv_bfloat16 h, l;
+    split_bf16(v.x, h, l);
+    base[p] = h;
+    base[plane + p] = l;
+    split_bf16(v.y, h, l);
+    base[2 * plane + p] = h;
+    base[3 * plane + p] = l;
+  }
+}
+
+int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
+                                __nv_bfloat16* out_split, cudaStream_t s) {
+  if (plane == 0 || batch == 0) return DLX_OK;
+  c64_to_split_kernel<<<ceil_div(plane, 256), 256, 0, s>>>(in, plane, batch, out_split);
+  DLX_LAUNCH_CHECK("c64_to_split_kernel");
+  return DLX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Block-level double reduction helper (fixed order -> deterministic).
+// ---------------------------------------------------------------------------
+template <int BLOCK>
+__device__ __forceinline__ double block_sum(double v, double* smem) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = (lane < BLOCK / 32) ? smem[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;  // valid in thread 0
+}
+
+// psf[p] = sum_b |in[b][p]|^2 (wavefronts.py:279 summed as optical_systems.py:223)
+__global__ void psf_sum_kernel(const float2* __restrict__ in, int batch, long long npix,
+                               float* __restrict__ psf) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  float acc = 0.f;
+  for (int b = 0; b < batch; ++b) {
+    float2 v = in[(long long)b * npix + p];
+    acc += v.x * v.x + v.y * v.y;
+  }
+  psf[p] = acc;
+}
+
+int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cudaStream_t s) {
+  if (npix == 0) return DLX_OK;
+  psf_sum_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(in, batch, npix, psf);
+  DLX_LAUNCH_CHECK("psf_sum_kernel");
+  return DLX_OK;
+}
+
+__global__ void plane_sum_kernel(const float* __restrict__ planes, int batch, long long npix,
+                                 float* __restrict__ out) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  float acc = 0.f;
+  for (int b = 0; b < batch; ++b) acc += planes[(long long)b * npix + p];
+  out[p] = acc;
+}
+
+int launch_plane_sum(const float* planes, int batch, long long npix, float* out, cudaStream_t s) {
+  if (npix == 0) return DLX_OK;
+  plane_sum_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(planes, batch, npix, out);
+  DLX_LAUNCH_CHECK("plane_sum_kernel");
+  return DLX_OK;
+}
+
+// out[b] = sqrt(value / sum_p |in[b][p]|^2): one block per batch element.
+__global__ void power_scale_kernel(const float2* __restrict__ in, long long npix, double value,
+                                   float* __restrict__ out) {
+  __shared__ double smem[32];
+  const int b = blockIdx.x;
+  const float2* src = in + (long long)b * npix;
+  double acc = 0.0;
+  for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
+    float2 v = src[p];
+    acc += (double)v.x * v.x + (double)v.y * v.y;
+  }
+  double t = block_sum<1024>(acc, smem);
+  if (threadIdx.x == 0) out[b] = (float)sqrt(value / t);
+}
+
+int launch_power_scale(const float2* in, int batch, long long npix, double value, float* out,
+                       cudaStream_t s) {
+  if (batch == 0) return DLX_OK;
+  power_scale_kernel<<<batch, 1024, 0, s>>>(in, npix, value, out);
+  DLX_LAUNCH_CHECK("power_scale_kernel");
+  return DLX_OK;
+}
+
+// Two-level deterministic sum of amp^2 (partials then one block).
+__global__ void sumsq_partial_kernel(const float* __restrict__ x, long long npix, int nparts,
+                                     double* __restrict__ partial) {
+  __shared__ double smem[32];
+  const long long chunk = (npix + nparts - 1) / nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(npix, lo + chunk);
+  double acc = 0.0;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    double v = x[p];
+    acc += v * v;
+  }
+  double t = block_sum<256>(acc, smem);
+  if (threadIdx.x == 0) partial[blockIdx.x] = t;
+}
+
+__global__ void norm_finish_kernel(const double* __restrict__ partial, int nparts, double value,
+                                   float* __restrict__ out_scale) {
+  __shared__ double smem[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partial[i];
+  double t = block_sum<256>(acc, smem);
+  if (threadIdx.x == 0) out_scale[0] = (float)sqrt(value / t);
+}
+
+int launch_amp_norm(const float* amp, long long npix, double value, float* out_scale,
+                    double* partial_ws, int nparts, cudaStream_t s) {
+  sumsq_partial_kernel<<<nparts, 256, 0, s>>>(amp, npix, nparts, partial_ws);
+  DLX_LAUNCH_CHECK("sumsq_partial_kernel");
+  norm_finish_kernel<<<1, 256, 0, s>>>(partial_ws, nparts, value, out_scale);
+  DLX_LAUNCH_CHECK("norm_finish_kernel");
+  return DLX_OK;
+}
+
+// Reverse of a_eff = a * n, n = sqrt(value / S), S = sum a^2:
+// g_a[j] = n g_eff[j] - a_j n^3 / value * sum_i a_i g_eff[i].
+__global__ void dot_sumsq_partial_kernel(const float* __restrict__ a, const float* __restrict__ g,
+                                         long long npix, int nparts,
+                                         double* __restrict__ partial) {
+  __shared__ double smem[32];
+  const long long chunk = (npix + nparts - 1) / nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(npix, lo + chunk);
+  double s2 = 0.0, sg = 0.0;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    double v = a[p];
+    s2 += v * v;
+    sg += v * (double)g[p];
+  }
+  double t2 = block_sum<256>(s2, smem);
+  double tg = block_sum<256>(sg, smem);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = t2;
+    partial[2 * blockIdx.x + 1] = tg;
+  }
+}
+
+__global__ void amp_norm_bwd_kernel(const float* __restrict__ a, const float* __restrict__ g,
+                                    long long npix, double value,
+                                    const double* __restrict__ partial, int nparts,
+                                    float* __restrict__ g_a) {
+  // Every block re-reduces the (few) partials in the same fixed order.
+  __shared__ double sh[2];
+  if (threadIdx.x == 0) {
+    double s2 = 0.0, sg = 0.0;
+    for (int i = 0; i < nparts; ++i) {
+      s2 += partial[2 * i];
+      sg += partial[2 * i + 1];
+    }
+    sh[0] = s2;
+    sh[1] = sg;
+  }
+  __syncthreads();
+  const double S = sh[0], D = sh[1];
+  const double n = sqrt(value / S);
+  const double c = n * n * n / value * D;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  g_a[p] = (float)(n * (double)g[p] - (double)a[p] * c);
+}
+
+int launch_amp_norm_backward(const float* amp, const float* g_eff, long long npix, double value,
+                             float* g_amp, double* partial_ws, int nparts, cudaStream_t s) {
+  dot_sumsq_partial_kernel<<<nparts, 256, 0, s>>>(amp, g_eff, npix, nparts, partial_ws);
+  DLX_LAUNCH_CHECK("dot_sumsq_partial_kernel");
+  amp_norm_bwd_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(amp, g_eff, npix, value, partial_ws,
+                                                          nparts, g_amp);
+  DLX_LAUNCH_CHECK("amp_norm_bwd_kernel");
+  return DLX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Basis contraction (utils/math.py:177-196) and its reverse.
+// ---------------------------------------------------------------------------
+__global__ void basis_eval_kernel(const float* __restrict__ basis,
+                                  const float* __restrict__ coeffs,
+                                  const float* __restrict__ base, int nterms, long long npix,
+                                  float* __restrict__ out) {
+  extern __shared__ float sc[];
+  for (int k = threadIdx.x; k < nterms; k += blockDim.x) sc[k] = coeffs[k];
+  __syncthreads();
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npix) return;
+  float acc = base ? base[p] : 0.f;
+  for (int k = 0; k < nterms; ++k) acc = fmaf(sc[k], __ldg(basis + (long long)k * npix + p), acc);
+  out[p] = acc;
+}
+
+int launch_basis_eval(const float* basis, const float* coeffs, const float* base, int nterms,
+                      long long npix, float* out, cudaStream_t s) {
+  if (npix == 0) return DLX_OK;
+  basis_eval_kernel<<<ceil_div(npix, 256), 256, sizeof(float) * (nterms > 0 ? nterms : 1), s>>>(
+      basis, coeffs, base, nterms, npix, out);
+  DLX_LAUNCH_CHECK("basis_eval_kernel");
+  return DLX_OK;
+}
+
+__global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
+                                          const float* __restrict__ g, long long npix,
+                                          int nparts, double* __restrict__ partial) {
+  __shared__ double smem[32];
+  const int k = blockIdx.y;
+  const long long chunk = (npix + nparts - 1) / nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(npix, lo + chunk);
+  const float* row = basis + (long long)k * npix;
+  double acc = 0.0;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x)
+    acc += (double)__ldg(row + p) * (double)__ldg(g + p);
+  double t = block_sum<256>(acc, smem);
+  if (threadIdx.x == 0) partial[(long long)k * nparts + blockIdx.x] = t;
+}
+
+__global__ void basis_grad_finish_kernel(const double* __restrict__ partial, int nparts,
+                                         float* __restrict__ g_coeffs) {
+  __shared__ double smem[32];
+  const int k = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partial[(long long)k * nparts + i];
+  double t = block_sum<256>(acc, smem);
+  if (threadIdx.x == 0) g_coeffs[k] = (float)t;
+}
+
+int launch_basis_grad(const float* basis, const float* g, int nterms, long long npix,
+                      float* g_coeffs, double* partial_ws, int nparts, cudaStream_t s) {
+  if (nterms == 0) return DLX_OK;
+  dim3 grid(nparts, nterms);
+  basis_grad_partial_kernel<<<grid, 256, 0, s>>>(basis, g, npix, nparts, partial_ws);
+  DLX_LAUNCH_CHECK("basis_grad_partial_kernel");
+  basis_grad_finish_kernel<<<nterms, 256, 0, s>>>(partial_ws, nparts, g_coeffs);
+  DLX_LAUNCH_CHECK("basis_grad_finish_kernel");
+  return DLX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Detector: k x k block sum (utils/array_ops.py:124-162) x pixel response
+// (layers/detector_layers.py:100-131), and the reverse.
+// ---------------------------------------------------------------------------
+__global__ void downsample_kernel(const float* __restrict__ in, int n_in, int k, int mean,
+                                  const float* __restrict__ flat, float* __restrict__ out) {
+  const int n_out = n_in / k;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y * blockDim.y + threadIdx.y;
+  if (a >= n_out || c >= n_out) return;
+  float acc = 0.f;
+  for (int i = 0; i < k; ++i) {
+    const float* row = in + (long long)(a * k + i) * n_in + (long long)c * k;
+    float r = 0.f;
+    for (int j = 0; j < k; ++j) r += row[j];
+    acc += r;
+  }
+  if (mean) acc /= (float)(k * k);
+  if (flat) acc *= flat[(long long)a * n_out + c];
+  out[(long long)a * n_out + c] = acc;
+}
+
+int launch_downsample(const float* in, int n_in, int k, int mean, const float* flat, float* out,
+                      cudaStream_t s) {
+  const int n_out = n_in / k;
+  if (n_out == 0) return DLX_OK;
+  dim3 block(32, 8);
+  dim3 grid(ceil_div(n_out, 32), ceil_div(n_out, 8));
+  downsample_kernel<<<grid, block, 0, s>>>(in, n_in, k, mean, flat, out);
+  DLX_LAUNCH_CHECK("downsample_kernel");
+  return DLX_OK;
+}
+
+__global__ void downsample_bwd_kernel(const float* __restrict__ g_out, int n_in, int k, int mean,
+                                      const float* __restrict__ flat, float* __restrict__ g_in) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= n_in || y >= n_in) return;
+  const int n_out = n_in / k;
+  const long long o = (long long)(y / k) * n_out + (x / k);
+  float v = g_out[o];
+  if (flat) v *= flat[o];
+  if (mean) v /= (float)(k * k);
+  g_in[(long long)y * n_in + x] = v;
+}
+
+int launch_downsample_backward(const float* in, const float* g_out, int n_in, int k, int mean,
+                               const float* flat, float* g_in, float* g_flat, cudaStream_t s) {
+  const int n_out = n_in / k;
+  if (g_in) {
+    dim3 block(32, 8);
+    dim3 grid(ceil_div(n_in, 32), ceil_div(n_in, 8));
+    downsample_bwd_kernel<<<grid, block, 0, s>>>(g_out, n_in, k, mean, flat, g_in);
+    DLX_LAUNCH_CHECK("downsample_bwd_kernel");
+  }
+  if (g_flat) {
+    // g_flat = g_out * downsample(in): reuse the forward kernel with flat = g_out.
+    DLX_TRY(launch_downsample(in, n_in, k, mean, g_out, g_flat, s));
+  }
+  (void)n_out;
+  return DLX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Reduction of per-wavelength pupil-gradient planes (reverse of the phasor).
+// ---------------------------------------------------------------------------
+__global__ void pupil_reduce_pix_kernel(PupilReduceArgs a) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  float sre = 0.f, sim = 0.f, sk = 0.f;
+  for (int b = 0; b < a.batch; ++b) {
+    const long long o = (long long)b * a.npix + p;
+    const float re = a.pre[o], im = a.pim[o];
+    sre += re;
+    sim += im;
+    sk += (float)a.k_dev[b] * im;
+  }
+  if (a.g_amp) a.g_amp[p] = sre;
+  if (a.g_phase) a.g_phase[p] = sim;
+  if (a.g_opd) a.g_opd[p] = sk;
+}
+
+__global__ void pupil_reduce_w_partial_kernel(PupilReduceArgs a) {
+  __shared__ double smem[32];
+  const int b = blockIdx.y;
+  const long long chunk = (a.npix + a.nparts - 1) / a.nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(a.npix, lo + chunk);
+  const float* pre = a.pre + (long long)b * a.npix;
+  double acc = 0.0;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x)
+    acc += (double)pre[p] * (a.amp ? (double)a.amp[p] : 1.0);
+  double t = block_sum<256>(acc, smem);
+  if (a.amp_scale) t *= (double)*a.amp_scale;
+  if (threadIdx.x == 0) a.partial_ws[(long long)b * a.nparts + blockIdx.x] = t;
+}
+
+__global__ void pupil_reduce_w_finish_kernel(PupilReduceArgs a) {
+  __shared__ double smem[32];
+  const int b = blockIdx.x;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < a.nparts; i += blockDim.x)
+    acc += a.partial_ws[(long long)b * a.nparts + i];
+  double t = block_sum<256>(acc, smem);
+  // d/dw of sqrt(w): pre already carries sqrt(w_b); sum amp*pre = Re<E, Ebar>/1.
+  if (threadIdx.x == 0) a.g_w[b] = (float)(t / (2.0 * (double)a.weights[b]));
+}
+
+int launch_pupil_reduce(const PupilReduceArgs& a, cudaStream_t s) {
+  if (a.npix == 0) return DLX_OK;
+  if (a.g_amp || a.g_phase || a.g_opd) {
+    pupil_reduce_pix_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("pupil_reduce_pix_kernel");
+  }
+  if (a.g_w) {
+    dim3 grid(a.nparts, a.batch);
+    pupil_reduce_w_partial_kernel<<<grid, 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("pupil_reduce_w_partial_kernel");
+    pupil_reduce_w_finish_kernel<<<a.batch, 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("pupil_reduce_w_finish_kernel");
+  }
+  return DLX_OK;
+}
+
+}  // namespace dlx

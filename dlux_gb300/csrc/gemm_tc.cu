@@ -1,0 +1,595 @@
+// gemm_tc.cu -- split-precision complex GEMM on the 5th-generation tensor cores.
+//
+//   D[b][m][n] = sum_k opA(A[b][m][k]) * B[b][n][k]
+//
+// Every real operand is stored as two bf16 planes, hi = rn(x) and
+// lo = rn(x - hi) (layout [b][4][rows][K]: re_hi, re_lo, im_hi, im_lo), and
+// every real product is formed as hi*hi + hi*lo + lo*hi with FP32
+// accumulation in tensor memory (the lo*lo term, ~2^-16 relative, is
+// dropped). The complex product needs four real products, so one complex
+// K-step issues 12 tcgen05.mma instructions; the minus sign of Im*Im (and the
+// conjugate of A) is applied with the instruction descriptor's negate-A bit.
+//
+// CTA tile: 128 complex rows of A x 256 complex rows of B. TMEM holds the
+// real and imaginary accumulators (2 x 256 fp32 columns = all 512 columns).
+// K is staged 32 elements at a time (64-byte rows, 64B swizzle) by TMA in a
+// 2-stage mbarrier pipeline (96 KB per stage). Warp roles: warp 0 issues TMA,
+// warp 1 issues MMA (one thread each), warps 2-5 drain TMEM through the
+// shared epilogues. The kernel is persistent over (batch, m-tile, n-tile)
+// work items. Every mbarrier wait is bounded by a wall-clock limit; on
+// expiry the CTA records DLX_ERR_TIMEOUT in a device status word, drains its
+// own in-flight copies and MMAs, frees TMEM and exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "epilogue.cuh"
+
+namespace dlx {
+namespace {
+
+constexpr int TC_BM = 128;
+constexpr int TC_BN = 256;
+constexpr int TC_BK = 32;
+constexpr int TC_STAGES = 2;
+constexpr int A_PLANE_BYTES = TC_BM * TC_BK * 2;                         // 8 KB
+constexpr int B_PLANE_BYTES = TC_BN * TC_BK * 2;                         // 16 KB
+constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;       // 96 KB
+constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int TC_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
+
+// ------------------------------- PTX wrappers -------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait. Returns false if another role aborted or the limit expired
+// (then the abort flag and the device status word are set).
+__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                       int* status, bool honour_abort = true) {
+  const unsigned long long t0 = globaltimer();
+  for (uint32_t it = 0;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 63u) == 63u) {
+      if (honour_abort && *abort_flag) return false;
+      if (globaltimer() - t0 > kTimeoutNs) {
+        *abort_flag = 1;
+        if (status) atomicExch(status, DLX_ERR_TIMEOUT);
+        return false;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(slot)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
+                                        uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 32 lanes x 32 consecutive 32-bit TMEM columns -> 32 registers per thread.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* out) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) out[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tmem_ld_wait() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 64B swizzle, 64-byte rows, 8-row
+// core groups 512 bytes apart.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;   // stride byte offset
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)4 << 61;            // SWIZZLE_64B
+  return d;
+}
+
+// Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major,
+// M = 128, N = 256, optional negation of A.
+__host__ __device__ constexpr uint32_t make_idesc(bool neg_a) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((neg_a ? 1u : 0u) << 13) |
+         ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
+
+// --------------------------- vectorised epilogue ----------------------------
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
+  return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
+}
+
+// Writes 32 consecutive complex values of one row as four split planes.
+__device__ __forceinline__ void store_split32(__nv_bfloat16* base_b, long long plane,
+                                              long long row, const float* re, const float* im) {
+  uint32_t rh[16], rl[16], ih[16], il[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    __nv_bfloat16 h0, l0, h1, l1;
+    split_bf16(re[2 * j], h0, l0);
+    split_bf16(re[2 * j + 1], h1, l1);
+    rh[j] = pack_bf16(h0, h1);
+    rl[j] = pack_bf16(l0, l1);
+    split_bf16(im[2 * j], h0, l0);
+    split_bf16(im[2 * j + 1], h1, l1);
+    ih[j] = pack_bf16(h0, h1);
+    il[j] = pack_bf16(l0, l1);
+  }
+  uint4* p0 = reinterpret_cast<uint4*>(base_b + row);
+  uint4* p1 = reinterpret_cast<uint4*>(base_b + plane + row);
+  uint4* p2 = reinterpret_cast<uint4*>(base_b + 2 * plane + row);
+  uint4* p3 = reinterpret_cast<uint4*>(base_b + 3 * plane + row);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    p0[q] = make_uint4(rh[4 * q], rh[4 * q + 1], rh[4 * q + 2], rh[4 * q + 3]);
+    p1[q] = make_uint4(rl[4 * q], rl[4 * q + 1], rl[4 * q + 2], rl[4 * q + 3]);
+    p2[q] = make_uint4(ih[4 * q], ih[4 * q + 1], ih[4 * q + 2], ih[4 * q + 3]);
+    p3[q] = make_uint4(il[4 * q], il[4 * q + 1], il[4 * q + 2], il[4 * q + 3]);
+  }
+}
+
+__device__ __forceinline__ void epi_chunk32(const EpiArgs& e, int b, int m, int n0, int M, int N,
+                                            float* re, float* im) {
+  if (n0 + 32 > N) {
+    for (int j = 0; j < 32; ++j)
+      if (n0 + j < N) epi_apply(e, b, m, n0 + j, M, N, make_float2(re[j], im[j]));
+    return;
+  }
+  const float a = e.alpha ? e.alpha[b] : 1.0f;
+  const long long plane = (long long)M * N;
+  const long long row = (long long)m * N + n0;
+  switch (e.kind) {
+    case EPI_C64: {
+      float4* o = reinterpret_cast<float4*>(e.out_c64 + (long long)b * plane + row);
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        o[j] = make_float4(a * re[2 * j], a * im[2 * j], a * re[2 * j + 1], a * im[2 * j + 1]);
+      break;
+    }
+    case EPI_SPLIT: {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        re[j] *= a;
+        im[j] *= a;
+      }
+      store_split32(e.out_split + (long long)b * 4 * plane, plane, row, re, im);
+      break;
+    }
+    case EPI_INTENSITY: {
+      const float a2 = a * a;
+      float4* o = reinterpret_cast<float4*>(e.out_f32 + (long long)b * plane + row);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float4 v;
+        v.x = a2 * (re[4 * j] * re[4 * j] + im[4 * j] * im[4 * j]);
+        v.y = a2 * (re[4 * j + 1] * re[4 * j + 1] + im[4 * j + 1] * im[4 * j + 1]);
+        v.z = a2 * (re[4 * j + 2] * re[4 * j + 2] + im[4 * j + 2] * im[4 * j + 2]);
+        v.w = a2 * (re[4 * j + 3] * re[4 * j + 3] + im[4 * j + 3] * im[4 * j + 3]);
+        o[j] = v;
+      }
+      break;
+    }
+    case EPI_GRADF: {
+      const float4* gp = reinterpret_cast<const float4*>(e.G + row);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float4 g = __ldg(gp + j);
+        const float gg[4] = {g.x, g.y, g.z, g.w};
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const float s = 2.0f * a * gg[t];
+          re[4 * j + t] *= s;
+          im[4 * j + t] *= s;
+        }
+      }
+      if (e.out_split) {
+        store_split32(e.out_split + (long long)b * 4 * plane, plane, row, re, im);
+      } else {
+        float4* o = reinterpret_cast<float4*>(e.out_c64 + (long long)b * plane + row);
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          o[j] = make_float4(re[2 * j], im[2 * j], re[2 * j + 1], im[2 * j + 1]);
+      }
+      break;
+    }
+    default: {
+      for (int j = 0; j < 32; ++j) epi_apply(e, b, m, n0 + j, M, N, make_float2(re[j], im[j]));
+      break;
+    }
+  }
+}
+
+// --------------------------------- kernel -----------------------------------
+struct TcParams {
+  int batch, M, N, K;
+  int a_batch_div;
+  int mt, nt, total;
+  int conj_a;
+  int* status;
+  EpiArgs epi;
+};
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_cgemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                    const __grid_constant__ CUtensorMap tmB, const TcParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TC_STAGES * STAGE_BYTES);
+  uint64_t* empty = full + TC_STAGES;
+  uint64_t* tfull = empty + TC_STAGES;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* mdone = tempty + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nkb = (p.K + TC_BK - 1) / TC_BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 4);
+    mbar_init(mdone, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+    prefetch_tmap(&tmA);
+    prefetch_tmap(&tmB);
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------------ TMA producer ------------------------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t ph = 0;
+      uint32_t issued_mask = 0, issued_ph = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+        const int b = w / (p.mt * p.nt);
+        const int r = w - b * p.mt * p.nt;
+        const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
+        const int ab = b / p.a_batch_div;
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&empty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+          mbar_expect_tx(&full[stage], STAGE_BYTES);
+          uint8_t* base = smem + stage * STAGE_BYTES;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            tma_load_3d(base + q * A_PLANE_BYTES, &tmA, &full[stage], kb * TC_BK, mt * TC_BM,
+                        ab * 4 + q);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            tma_load_3d(base + 4 * A_PLANE_BYTES + q * B_PLANE_BYTES, &tmB, &full[stage],
+                        kb * TC_BK, nt * TC_BN, b * 4 + q);
+          issued_mask |= 1u << stage;
+          issued_ph = (issued_ph & ~(1u << stage)) | (ph << stage);
+          if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
+        }
+      }
+      if (!ok) {
+        // Drain every copy this thread issued before the CTA can exit.
+        for (int s = 0; s < TC_STAGES; ++s)
+          if (issued_mask & (1u << s))
+            mbar_wait(&full[s], (issued_ph >> s) & 1u, abort_flag, p.status, false);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------- MMA issuer -------------------------------
+    if (lane == 0) {
+      const uint32_t id_pos = make_idesc(false);
+      const uint32_t id_neg = make_idesc(true);
+      // Sign of the Ai * Bi term in Re and of the Ai * Br term in Im.
+      const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
+      const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
+      const uint32_t d_re = tmem, d_im = tmem + TC_BN;
+      int stage = 0;
+      uint32_t ph = 0, acc_ph = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&full[stage], ph, abort_flag, p.status)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t sa = smem_u32(smem + stage * STAGE_BYTES);
+          const uint32_t sb = sa + 4 * A_PLANE_BYTES;
+#pragma unroll
+          for (int j = 0; j < TC_BK / 16; ++j) {
+            const uint32_t ko = j * 32;  // 16 bf16 = 32 bytes along K
+            const uint64_t arh = make_desc(sa + 0 * A_PLANE_BYTES + ko);
+            const uint64_t arl = make_desc(sa + 1 * A_PLANE_BYTES + ko);
+            const uint64_t aih = make_desc(sa + 2 * A_PLANE_BYTES + ko);
+            const uint64_t ail = make_desc(sa + 3 * A_PLANE_BYTES + ko);
+            const uint64_t brh = make_desc(sb + 0 * B_PLANE_BYTES + ko);
+            const uint64_t brl = make_desc(sb + 1 * B_PLANE_BYTES + ko);
+            const uint64_t bih = make_desc(sb + 2 * B_PLANE_BYTES + ko);
+            const uint64_t bil = make_desc(sb + 3 * B_PLANE_BYTES + ko);
+            const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+            // Re += Ar Br -/+ Ai Bi
+            mma_bf16(d_re, arh, brh, id_pos, acc);
+            mma_bf16(d_re, arh, brl, id_pos, 1u);
+            mma_bf16(d_re, arl, brh, id_pos, 1u);
+            mma_bf16(d_re, aih, bih, id_rii, 1u);
+            mma_bf16(d_re, aih, bil, id_rii, 1u);
+            mma_bf16(d_re, ail, bih, id_rii, 1u);
+            // Im += Ar Bi +/- Ai Br
+            mma_bf16(d_im, arh, bih, id_pos, acc);
+            mma_bf16(d_im, arh, bil, id_pos, 1u);
+            mma_bf16(d_im, arl, bih, id_pos, 1u);
+            mma_bf16(d_im, aih, brh, id_iir, 1u);
+            mma_bf16(d_im, aih, brl, id_iir, 1u);
+            mma_bf16(d_im, ail, brh, id_iir, 1u);
+          }
+          mma_commit(&empty[stage]);
+          if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
+        }
+        if (!ok) break;
+        mma_commit(tfull);
+        acc_ph ^= 1u;
+      }
+      // Wait for every MMA this thread issued before TMEM is released.
+      mma_commit(mdone);
+      mbar_wait(mdone, 0, abort_flag, p.status, false);
+    }
+  } else {
+    // -------------------------------- epilogue --------------------------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;
+    uint32_t acc_ph = 0;
+    for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
+      if (!mbar_wait(tfull, acc_ph, abort_flag, p.status)) break;
+      tc_fence_after();
+      const int b = w / (p.mt * p.nt);
+      const int r = w - b * p.mt * p.nt;
+      const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
+      const int m = mt * TC_BM + row;
+      const int nbase = nt * TC_BN;
+      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int c = 0; c < TC_BN / 32; ++c) {
+        if (nbase + c * 32 >= p.N) break;  // warp-uniform
+        float re[32], im[32];
+        tmem_ld32(lane_addr + c * 32, re);
+        tmem_ld32(lane_addr + TC_BN + c * 32, im);
+        tmem_ld_wait();
+        if (m < p.M) epi_chunk32(p.epi, b, m, nbase + c * 32, p.M, p.N, re, im);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty);
+      acc_ph ^= 1u;
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    __syncwarp();
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// ------------------------------- host side ----------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+int g_num_sms = 0;
+int g_cc = 0;
+int* g_status = nullptr;
+std::once_flag g_once;
+int g_init_status = DLX_OK;
+
+void init_once() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    g_init_status = fail(DLX_ERR_CUDA, "cudaGetDevice failed");
+    return;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+    g_init_status = fail(DLX_ERR_CUDA, "cudaGetDeviceProperties failed");
+    return;
+  }
+  g_num_sms = prop.multiProcessorCount;
+  g_cc = prop.major * 10 + prop.minor;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                       &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    g_init_status = fail(DLX_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    return;
+  }
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  if (cudaMalloc(&g_status, sizeof(int)) != cudaSuccess ||
+      cudaMemset(g_status, 0, sizeof(int)) != cudaSuccess) {
+    g_init_status = fail(DLX_ERR_NOMEM, "status word allocation failed");
+    return;
+  }
+  if (cudaFuncSetAttribute(tc_cgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           SMEM_BYTES) != cudaSuccess) {
+    g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tc_cgemm_kernel) failed");
+    return;
+  }
+}
+
+int encode_split(CUtensorMap* map, const __nv_bfloat16* base, int rows, int K, int nbatch,
+                 int box_rows) {
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)nbatch * 4};
+  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
+  cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(base),
+                        dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(DLX_ERR_ARG, "cuTensorMapEncodeTiled failed (code " + std::to_string((int)r) +
+                                 ") for a split operand of " + std::to_string(rows) + " x " +
+                                 std::to_string(K));
+  return DLX_OK;
+}
+
+}  // namespace
+
+bool tc_supported() {
+  std::call_once(g_once, init_once);
+  return g_init_status == DLX_OK && g_cc == 103;
+}
+
+int* tc_status_word() {
+  std::call_once(g_once, init_once);
+  return g_status;
+}
+
+int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
+  std::call_once(g_once, init_once);
+  if (g_init_status != DLX_OK) return g_init_status;
+  if (g.batch <= 0 || g.M <= 0 || g.N <= 0) return DLX_OK;
+  if (g.K % 8 != 0 || g.N % 8 != 0)
+    return fail(DLX_ERR_SHAPE, "split-BF16 GEMM needs K and N to be multiples of 8");
+  if (!g.As || !g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
+  const int div = g.a_batch_div > 0 ? g.a_batch_div : 1;
+  const int nA = (g.batch + div - 1) / div;
+  CUtensorMap ta, tb;
+  DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, TC_BM));
+  DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, g.batch, TC_BN));
+  TcParams p{};
+  p.batch = g.batch; p.M = g.M; p.N = g.N; p.K = g.K;
+  p.a_batch_div = div;
+  p.mt = (g.M + TC_BM - 1) / TC_BM;
+  p.nt = (g.N + TC_BN - 1) / TC_BN;
+  p.total = g.batch * p.mt * p.nt;
+  p.conj_a = g.conj_a ? 1 : 0;
+  p.status = g_status;
+  p.epi = g.epi;
+  const int grid = p.total < g_num_sms ? p.total : g_num_sms;
+  tc_cgemm_kernel<<<grid, TC_THREADS, SMEM_BYTES, s>>>(ta, tb, p);
+  DLX_LAUNCH_CHECK("tc_cgemm_kernel");
+  return DLX_OK;
+}
+
+}  // namespace dlx
+
+extern "C" int dlx_device_status(void* stream, int* status) {
+  using namespace dlx;
+  if (!status) return fail(DLX_ERR_ARG, "device_status: null pointer");
+  int* word = tc_status_word();
+  *status = DLX_OK;
+  if (!word) return DLX_OK;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  DLX_TRY_CUDA(cudaStreamSynchronize(s));
+  int v = 0;
+  DLX_TRY_CUDA(cudaMemcpy(&v, word, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v != 0) {
+    DLX_TRY_CUDA(cudaMemset(word, 0, sizeof(int)));
+    *status = v;
+  }
+  return DLX_OK;
+}

@@ -1,0 +1,121 @@
+// kernels.h -- host launchers shared between the translation units.
+#pragma once
+
+#include "common.cuh"
+
+namespace dlx {
+
+// Per-batch double scalars passed by value (chunks of up to kMaxBatchArg).
+constexpr int kMaxBatchArg = 256;
+struct BatchD {
+  double v[kMaxBatchArg];
+};
+
+// --- elementwise.cu --------------------------------------------------------
+int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool rows_are_out,
+                   float2* out_c64, long long out_batch_stride, __nv_bfloat16* out_split,
+                   cudaStream_t s);
+
+struct PhasorArgs {
+  const float2* in;        // nullable [b][n][n]
+  const float* amp;        // nullable [n][n]
+  const float* opd;        // nullable [n][n]
+  const float* phase;      // nullable [n][n]
+  const float* amp_scale;  // nullable device scalar
+  const float* weights;    // nullable [b]
+  const double* inv_lambda_dev;  // [b] (device) or nullptr -> use inv_lambda_arg
+  double const_scale;
+  int batch, n;
+  double pixel_scale, tilt_x, tilt_y;
+  float2* out_c64;             // one of the two outputs
+  __nv_bfloat16* out_split;    // [b][4][n][n]
+};
+int launch_phasor(const PhasorArgs& a, const BatchD* inv_lambda_arg, cudaStream_t s);
+
+int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
+                                __nv_bfloat16* out_split, cudaStream_t s);
+int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cudaStream_t s);
+int launch_plane_sum(const float* planes, int batch, long long npix, float* out, cudaStream_t s);
+int launch_power_scale(const float2* in, int batch, long long npix, double value, float* out,
+                       cudaStream_t s);
+int launch_amp_norm(const float* amp, long long npix, double value, float* out_scale,
+                    double* partial_ws, int nparts, cudaStream_t s);
+int launch_amp_norm_backward(const float* amp, const float* g_eff, long long npix, double value,
+                             float* g_amp, double* partial_ws, int nparts, cudaStream_t s);
+int launch_basis_eval(const float* basis, const float* coeffs, const float* base, int nterms,
+                      long long npix, float* out, cudaStream_t s);
+int launch_basis_grad(const float* basis, const float* g, int nterms, long long npix,
+                      float* g_coeffs, double* partial_ws, int nparts, cudaStream_t s);
+int launch_downsample(const float* in, int n_in, int k, int mean, const float* flat, float* out,
+                      cudaStream_t s);
+int launch_downsample_backward(const float* in, const float* g_out, int n_in, int k, int mean,
+                               const float* flat, float* g_in, float* g_flat, cudaStream_t s);
+
+// Reduction of the per-wavelength pupil-gradient planes:
+// g_amp = sum_b pre[b], g_phase = sum_b pim[b], g_opd = sum_b k_b pim[b],
+// g_w[b] = sum_p amp[p] pre[b][p] / (2 w_b) (two-level, deterministic).
+struct PupilReduceArgs {
+  const float* pre;
+  const float* pim;
+  const float* amp;       // nullable (1)
+  const float* amp_scale; // nullable device scalar multiplying amp
+  const float* weights;   // [b]
+  const double* k_dev;    // [b] 2 pi / lambda_b
+  int batch;
+  long long npix;
+  float* g_amp;
+  float* g_opd;
+  float* g_phase;
+  float* g_w;
+  double* partial_ws;     // >= batch * nparts doubles
+  int nparts;
+};
+int launch_pupil_reduce(const PupilReduceArgs& a, cudaStream_t s);
+
+// --- gemm_fp32.cu / gemm_tc.cu ---------------------------------------------
+// Complex GEMM D[b][m][n] = sum_k opA(A[b][m][k]) * B[b][n][k], opA = conj if conj_a.
+// Epilogue kinds shared by both arithmetic forms.
+enum EpiKind {
+  EPI_C64 = 0,       // out_c64[b][m][n] = alpha_b * D
+  EPI_SPLIT = 1,     // out_split[b][4][m][n] = split(alpha_b * D)   (tensor-core form only)
+  EPI_INTENSITY = 2, // out_f32[b][m][n] = alpha_b^2 |D|^2
+  EPI_GRADF = 3,     // out[b][m][n] = 2 alpha_b G[m][n] D    (c64 or split)
+  EPI_PUPIL = 4,     // pupil-gradient planes from D = Ebar_unscaled[b][y=m][x=n]
+};
+
+struct EpiArgs {
+  int kind;
+  const float* alpha;        // [b] device
+  float2* out_c64;
+  __nv_bfloat16* out_split;
+  float* out_f32;            // intensity planes, or pre planes for EPI_PUPIL
+  float* out_f32b;           // pim planes for EPI_PUPIL
+  const float* G;            // [m][n] for EPI_GRADF
+  // EPI_PUPIL recompute of the unit phasor
+  const float* amp;          // nullable
+  const float* amp_scale;    // nullable device scalar multiplying amp
+  const float* opd;          // nullable
+  const float* phase;        // nullable
+  const float* weights;      // [b] nullable (1)
+  const double* inv_lambda;  // [b]
+  double pixel_scale, tilt_x, tilt_y;
+};
+
+struct GemmArgs {
+  int batch, M, N, K;
+  const float2* A;          // c64 form
+  long long a_bs;           // batch stride in elements (0: shared)
+  const float2* B;
+  long long b_bs;
+  const __nv_bfloat16* As;  // split form [b][4][M][K]
+  const __nv_bfloat16* Bs;  // split form [b][4][N][K]
+  int a_batch_div;          // A batch index = b / a_batch_div (split form)
+  bool conj_a;
+  EpiArgs epi;
+};
+
+int launch_gemm_fp32(const GemmArgs& g, cudaStream_t s);
+int launch_gemm_tc(const GemmArgs& g, cudaStream_t s);
+bool tc_supported();
+
+}  // namespace dlx

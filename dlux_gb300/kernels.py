@@ -1,0 +1,398 @@
+"""Tensor-level wrappers of the C ABI: one function or plan class per entry point.
+
+All inputs and outputs are CUDA tensors (float32, complex64). Work is enqueued
+on torch's current stream. Shapes follow dLux: square fields, axis 0 = y.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes
+import math
+import threading
+
+import torch
+
+from . import _lib
+from ._lib import call, ptr, stream_ptr
+
+_variant_lock = threading.Lock()
+_default_variant = None
+
+
+def tensor_core_available() -> bool:
+    """True when the split-BF16 tcgen05 form can run on the current device."""
+    if not torch.cuda.is_available():
+        return False
+    major, minor = torch.cuda.get_device_capability()
+    return (major, minor) == (10, 3)
+
+
+def set_variant(name: str | None) -> None:
+    """Select the MFT arithmetic form: "split_bf16", "fp32", or None (automatic)."""
+    global _default_variant
+    if name not in (None, "split_bf16", "fp32"):
+        raise ValueError("variant must be 'split_bf16', 'fp32' or None")
+    with _variant_lock:
+        _default_variant = name
+
+
+def get_variant() -> str | None:
+    return _default_variant
+
+
+def resolve_variant(n_in: int, n_out: int, variant: str | None = None) -> int:
+    """Integer variant for a transform of the given sides.
+
+    Automatic choice: the split-BF16 tensor-core form on sm_103a when both sides
+    are multiples of 8 (the TMA row-pitch rule), the FP32 form otherwise.
+    """
+    v = variant if variant is not None else _default_variant
+    if v == "fp32":
+        return _lib.VARIANT_FP32
+    if v == "split_bf16":
+        return _lib.VARIANT_SPLIT_BF16
+    if tensor_core_available() and n_in % 8 == 0 and n_out % 8 == 0:
+        return _lib.VARIANT_SPLIT_BF16
+    return _lib.VARIANT_FP32
+
+
+def _stream():
+    return stream_ptr()
+
+
+def _f32(x, device=None):
+    dev = device or _lib.require_cuda()
+    return torch.as_tensor(x, dtype=torch.float32, device=dev).contiguous()
+
+
+def _c64(x, device=None):
+    dev = device or _lib.require_cuda()
+    return torch.as_tensor(x, dtype=torch.complex64, device=dev).contiguous()
+
+
+# ---------------------------------------------------------------------------
+# a1: transfer matrix
+# ---------------------------------------------------------------------------
+def transfer_matrix(wavelengths, npixels_in, pixel_scale_in, npixels_out, pixel_scale_out,
+                    shift=0.0, focal_length=None, inverse=False, transpose=False):
+    """[B, N_in, N_out] complex64 DFT matrices (dLux utils/propagation.py:67-127)."""
+    dev = _lib.require_cuda()
+    wl = [float(w) for w in torch.as_tensor(wavelengths, dtype=torch.float64).reshape(-1)]
+    shape = (len(wl), npixels_out, npixels_in) if transpose else (len(wl), npixels_in, npixels_out)
+    out = torch.empty(shape, dtype=torch.complex64, device=dev)
+    call("dlx_transfer_matrix", _lib.dbl_array(wl), len(wl), int(npixels_in),
+         float(pixel_scale_in), int(npixels_out), float(pixel_scale_out), float(shift),
+         float(focal_length) if focal_length is not None else 0.0, int(bool(inverse)),
+         int(bool(transpose)), ptr(out), _stream())
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Plan caches
+# ---------------------------------------------------------------------------
+class _PlanCache:
+    """Small LRU of device plans keyed by their full description."""
+
+    def __init__(self, capacity: int):
+        self.capacity = capacity
+        self._d = collections.OrderedDict()
+        self._lock = threading.Lock()
+
+    def get(self, key, factory):
+        with self._lock:
+            if key in self._d:
+                self._d.move_to_end(key)
+                return self._d[key]
+        plan = factory()
+        with self._lock:
+            self._d[key] = plan
+            self._d.move_to_end(key)
+            while len(self._d) > self.capacity:
+                _, old = self._d.popitem(last=False)
+                old.close()
+        return plan
+
+    def clear(self):
+        with self._lock:
+            items = list(self._d.values())
+            self._d.clear()
+        for p in items:
+            p.close()
+
+
+class _Plan:
+    _destroy = None
+
+    def __init__(self):
+        self.handle = ctypes.c_void_p()
+
+    def close(self):
+        if self.handle and self.handle.value:
+            try:
+                torch.cuda.current_stream().synchronize()
+            except Exception:  # pragma: no cover - interpreter shutdown
+                pass
+            getattr(_lib.load(), self._destroy)(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MFTPlan(_Plan):
+    """Batched MFT with cached DFT matrices (dLux utils/propagation.py:178-256)."""
+
+    _destroy = "dlx_mft_plan_destroy"
+
+    def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                 focal_length=None, shift=(0.0, 0.0), inverse=False, variant=None):
+        super().__init__()
+        _lib.require_cuda()
+        self.wavelengths = tuple(float(w) for w in wavelengths)
+        self.n_in, self.n_out = int(n_in), int(n_out)
+        self.variant = resolve_variant(self.n_in, self.n_out, variant)
+        d = _lib.MftDesc(len(self.wavelengths), self.n_in, self.n_out, float(pixel_scale_in),
+                         float(pixel_scale_out),
+                         float(focal_length) if focal_length is not None else 0.0,
+                         float(shift[0]), float(shift[1]), int(bool(inverse)), self.variant)
+        call("dlx_mft_plan_create", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
+             ctypes.byref(self.handle))
+
+    def forward(self, phasor):
+        b = len(self.wavelengths)
+        x = phasor.reshape(b, self.n_in, self.n_in).contiguous()
+        out = torch.empty((b, self.n_out, self.n_out), dtype=torch.complex64, device=x.device)
+        call("dlx_mft_forward", self.handle, ptr(x), ptr(out), _stream())
+        return out
+
+    def adjoint(self, gout):
+        b = len(self.wavelengths)
+        g = gout.reshape(b, self.n_out, self.n_out).contiguous()
+        out = torch.empty((b, self.n_in, self.n_in), dtype=torch.complex64, device=g.device)
+        call("dlx_mft_adjoint", self.handle, ptr(g), ptr(out), _stream())
+        return out
+
+
+class FFTPlan(_Plan):
+    """Padded centred FFT as a DFT-GEMM pair (dLux utils/propagation.py:8-64)."""
+
+    _destroy = "dlx_fft_plan_destroy"
+
+    def __init__(self, wavelengths, n_in, pixel_scale_in, pad=2, focal_length=None,
+                 inverse=False, ramps=None, variant=None):
+        super().__init__()
+        _lib.require_cuda()
+        self.wavelengths = tuple(float(w) for w in wavelengths)
+        self.n_in, self.pad = int(n_in), int(pad)
+        self.n_out = self.n_in * self.pad
+        self.variant = resolve_variant(self.n_in, self.n_out, variant)
+        apply, c_in, c_out = (0, 0.0, 0.0) if ramps is None else (1, float(ramps[0]),
+                                                                 float(ramps[1]))
+        d = _lib.FftDesc(len(self.wavelengths), self.n_in, self.pad, float(pixel_scale_in),
+                         float(focal_length) if focal_length is not None else 0.0,
+                         int(bool(inverse)), apply, c_in, c_out, self.variant)
+        call("dlx_fft_plan_create", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
+             ctypes.byref(self.handle))
+
+    def forward(self, phasor):
+        b = len(self.wavelengths)
+        x = phasor.reshape(b, self.n_in, self.n_in).contiguous()
+        out = torch.empty((b, self.n_out, self.n_out), dtype=torch.complex64, device=x.device)
+        call("dlx_fft_forward", self.handle, ptr(x), ptr(out), _stream())
+        return out
+
+    def adjoint(self, gout):
+        b = len(self.wavelengths)
+        g = gout.reshape(b, self.n_out, self.n_out).contiguous()
+        out = torch.empty((b, self.n_in, self.n_in), dtype=torch.complex64, device=g.device)
+        call("dlx_fft_adjoint", self.handle, ptr(g), ptr(out), _stream())
+        return out
+
+
+class PolyPlan(_Plan):
+    """Fused polychromatic PSF and its gradient (OpticalSystem.propagate)."""
+
+    _destroy = "dlx_poly_plan_destroy"
+
+    def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                 focal_length=None, variant=None):
+        super().__init__()
+        _lib.require_cuda()
+        self.wavelengths = tuple(float(w) for w in wavelengths)
+        self.n_in, self.n_out = int(n_in), int(n_out)
+        self.pixel_scale_in = float(pixel_scale_in)
+        self.variant = resolve_variant(self.n_in, self.n_out, variant)
+        d = _lib.PolyDesc(len(self.wavelengths), self.n_in, self.n_out, float(pixel_scale_in),
+                          float(pixel_scale_out),
+                          float(focal_length) if focal_length is not None else 0.0,
+                          self.variant)
+        call("dlx_poly_plan_create", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
+             ctypes.byref(self.handle))
+
+    @property
+    def footprint(self) -> int:
+        n = ctypes.c_size_t(0)
+        call("dlx_poly_plan_footprint", self.handle, ctypes.byref(n))
+        return int(n.value)
+
+    def tilt_basis(self):
+        """[2, N, N] pupil coordinates (X, Y) in metres, cached on the device."""
+        tb = getattr(self, "_tilt_basis", None)
+        if tb is None:
+            n = self.n_in
+            xs = (torch.arange(n, dtype=torch.float64) - (n - 1) / 2) * self.pixel_scale_in
+            yy, xx = torch.meshgrid(xs, xs, indexing="ij")
+            tb = torch.stack([xx, yy]).to(device="cuda", dtype=torch.float32).contiguous()
+            self._tilt_basis = tb
+        return tb
+
+    def psf(self, amp, amp_scale, opd, phase, weights, tilt=(0.0, 0.0), out=None):
+        dev = weights.device
+        if out is None:
+            out = torch.empty((self.n_out, self.n_out), dtype=torch.float32, device=dev)
+        call("dlx_poly_psf", self.handle, ptr(amp), ptr(amp_scale), ptr(opd), ptr(phase),
+             ptr(weights), float(tilt[0]), float(tilt[1]), ptr(out), _stream())
+        return out
+
+    def grad(self, amp, amp_scale, opd, phase, weights, g_psf, tilt=(0.0, 0.0),
+             want=("amp", "opd", "phase", "w")):
+        dev = g_psf.device
+        n = self.n_in
+        g_amp = torch.empty((n, n), dtype=torch.float32, device=dev) if "amp" in want else None
+        g_opd = torch.empty((n, n), dtype=torch.float32, device=dev) if "opd" in want else None
+        g_ph = torch.empty((n, n), dtype=torch.float32, device=dev) if "phase" in want else None
+        g_w = (torch.empty((len(self.wavelengths),), dtype=torch.float32, device=dev)
+               if "w" in want else None)
+        call("dlx_poly_psf_grad", self.handle, ptr(amp), ptr(amp_scale), ptr(opd), ptr(phase),
+             ptr(weights), float(tilt[0]), float(tilt[1]), ptr(g_psf.contiguous()), ptr(g_amp),
+             ptr(g_opd), ptr(g_ph), ptr(g_w), _stream())
+        return {"amp": g_amp, "opd": g_opd, "phase": g_ph, "w": g_w}
+
+
+mft_plans = _PlanCache(16)
+fft_plans = _PlanCache(8)
+poly_plans = _PlanCache(8)
+
+
+def get_mft_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,
+                 shift=(0.0, 0.0), inverse=False, variant=None):
+    wl = tuple(float(w) for w in wavelengths)
+    v = resolve_variant(n_in, n_out, variant)
+    key = (wl, int(n_in), float(pixel_scale_in), int(n_out), float(pixel_scale_out),
+           None if focal_length is None else float(focal_length),
+           (float(shift[0]), float(shift[1])), bool(inverse), v)
+    return mft_plans.get(key, lambda: MFTPlan(wl, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                                              focal_length, shift, inverse,
+                                              "fp32" if v == 0 else "split_bf16"))
+
+
+def get_fft_plan(wavelengths, n_in, pixel_scale_in, pad=2, focal_length=None, inverse=False,
+                 ramps=None, variant=None):
+    wl = tuple(float(w) for w in wavelengths)
+    v = resolve_variant(n_in, n_in * pad, variant)
+    key = (wl, int(n_in), float(pixel_scale_in), int(pad),
+           None if focal_length is None else float(focal_length), bool(inverse),
+           None if ramps is None else (float(ramps[0]), float(ramps[1])), v)
+    return fft_plans.get(key, lambda: FFTPlan(wl, n_in, pixel_scale_in, pad, focal_length,
+                                              inverse, ramps,
+                                              "fp32" if v == 0 else "split_bf16"))
+
+
+def get_poly_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,
+                  variant=None):
+    wl = tuple(float(w) for w in wavelengths)
+    v = resolve_variant(n_in, n_out, variant)
+    key = (wl, int(n_in), float(pixel_scale_in), int(n_out), float(pixel_scale_out),
+           None if focal_length is None else float(focal_length), v)
+    return poly_plans.get(key, lambda: PolyPlan(wl, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                                                focal_length,
+                                                "fp32" if v == 0 else "split_bf16"))
+
+
+# ---------------------------------------------------------------------------
+# Elementwise and reductions
+# ---------------------------------------------------------------------------
+def phasor(wavelengths, n, pixel_scale, field=None, amp=None, opd=None, phase=None,
+           amp_scale=None, weights=None, const_scale=1.0, tilt=(0.0, 0.0), out=None):
+    """field * amp * exp(i (2 pi (opd + tilt . xy) / lambda + phase)) for every wavelength."""
+    dev = _lib.require_cuda()
+    wl = [float(w) for w in torch.as_tensor(wavelengths, dtype=torch.float64).reshape(-1)]
+    b = len(wl)
+    if out is None:
+        out = torch.empty((b, n, n), dtype=torch.complex64, device=dev)
+    call("dlx_phasor", ptr(field), ptr(amp), ptr(opd), ptr(phase), ptr(amp_scale), ptr(weights),
+         float(const_scale), _lib.dbl_array(wl), b, int(n), float(pixel_scale), float(tilt[0]),
+         float(tilt[1]), ptr(out), _stream())
+    return out
+
+
+def power_scale(field, value=1.0):
+    """sqrt(value / sum |E|^2) per batch element (Wavefront.normalise, mode "power")."""
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    out = torch.empty((f.shape[0],), dtype=torch.float32, device=f.device)
+    call("dlx_power_scale", ptr(f), f.shape[0], f.shape[-1], float(value), ptr(out), _stream())
+    return out
+
+
+def amp_norm(amp, value=1.0):
+    out = torch.empty((), dtype=torch.float32, device=amp.device)
+    call("dlx_amp_norm", ptr(amp.contiguous()), amp.shape[-1], float(value), ptr(out), _stream())
+    return out
+
+
+def amp_norm_backward(amp, g_eff, value=1.0):
+    out = torch.empty_like(amp)
+    call("dlx_amp_norm_backward", ptr(amp.contiguous()), ptr(g_eff.contiguous()), amp.shape[-1],
+         float(value), ptr(out), _stream())
+    return out
+
+
+def basis_eval(basis, coeffs, base=None):
+    """sum_k coeffs[k] basis[k] (+ base) over flattened coefficient dims (utils/math.py:177-196)."""
+    k = coeffs.numel()
+    spatial = basis.shape[coeffs.dim():]
+    npix = int(math.prod(spatial))
+    out = torch.empty(spatial, dtype=torch.float32, device=basis.device)
+    call("dlx_basis_eval", ptr(basis.contiguous()), ptr(coeffs.contiguous().float()),
+         ptr(base), k, npix, ptr(out), _stream())
+    return out
+
+
+def basis_grad(basis, g, coeff_shape):
+    k = int(math.prod(coeff_shape))
+    out = torch.empty(coeff_shape, dtype=torch.float32, device=basis.device)
+    call("dlx_basis_grad", ptr(basis.contiguous()), ptr(g.contiguous()), k, g.numel(), ptr(out),
+         _stream())
+    return out
+
+
+def psf_sum(field):
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    out = torch.empty(f.shape[-2:], dtype=torch.float32, device=f.device)
+    call("dlx_psf_sum", ptr(f), f.shape[0], f.shape[-1] * f.shape[-2], ptr(out), _stream())
+    return out
+
+
+def downsample(psf, k, mean=False, flat=None):
+    n = psf.shape[-1]
+    if psf.shape[-2] != n:
+        raise ValueError(f"Input array has shape {tuple(psf.shape)}, which is not square")
+    if n % k != 0:
+        raise ValueError(f"Input array has {n} pixels, which is not divisible by {k}")
+    out = torch.empty((n // k, n // k), dtype=torch.float32, device=psf.device)
+    call("dlx_downsample", ptr(psf.contiguous()), n, int(k), int(bool(mean)), ptr(flat), ptr(out),
+         _stream())
+    return out
+
+
+def downsample_backward(psf, g_out, k, mean=False, flat=None, want_flat=False):
+    n = psf.shape[-1]
+    g_in = torch.empty((n, n), dtype=torch.float32, device=g_out.device)
+    g_flat = torch.empty_like(g_out) if want_flat else None
+    call("dlx_downsample_backward", ptr(psf.contiguous()), ptr(g_out.contiguous()), n, int(k),
+         int(bool(mean)), ptr(flat), ptr(g_in), ptr(g_flat), _stream())
+    return g_in, g_flat

@@ -1,0 +1,8 @@
+"""dLux-compatible layer namespace (``dlux_gb300.layers`` mirrors ``dLux.layers``)."""
+
+from .optical_layers import (BaseLayer, OpticalLayer, TransmissiveLayer,  # noqa: F401
+                             AberratedLayer, BasisLayer, Tilt, Normalise)
+from .optics import Optic, BasisOptic  # noqa: F401
+from .propagators import MFT, FFT  # noqa: F401
+from .detector_layers import (DetectorLayer, ApplyPixelResponse, Downsample,  # noqa: F401
+                              AddConstant, ApplySaturation)

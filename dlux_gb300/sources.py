@@ -1,0 +1,109 @@
+"""Point sources (dLux sources.py:132-411)."""
+
+from __future__ import annotations
+
+import torch
+
+from . import spectra
+from .base import Base
+from .psfs import PSF
+
+__all__ = ["BaseSource", "Source", "PointSource", "PointSources"]
+
+
+def _validate_return_mode(return_wf, return_psf):
+    if return_wf and return_psf:
+        raise ValueError("Cannot return both Wavefront and PSF objects. Choose one: set "
+                         "return_wf=True for Wavefront, or return_psf=True for PSF object.")
+
+
+def _dev():
+    return torch.device("cuda") if torch.cuda.is_available() else torch.device("cpu")
+
+
+class BaseSource(Base):
+    pass
+
+
+class Source(BaseSource):
+    def __init__(self, wavelengths=None, weights=None, spectrum=None):
+        if spectrum is not None:
+            if not isinstance(spectrum, spectra.BaseSpectrum):
+                raise TypeError(f"spectrum must be a dLux BaseSpectrum instance from "
+                                f"dLux.spectra, got {type(spectrum).__name__}.")
+            self.spectrum = spectrum
+        else:
+            self.spectrum = spectra.Spectrum(wavelengths, weights)
+
+    def __getattr__(self, key):
+        spec = self.__dict__.get("spectrum")
+        if spec is not None and hasattr(spec, key):
+            return getattr(spec, key)
+        raise AttributeError(f"{type(self).__name__} has no attribute {key!r}")
+
+    def normalise(self):
+        return self.set("spectrum", self.spectrum.normalise())
+
+
+class PointSource(Source):
+    """Polychromatic point source at an angular position (sources.py:132-327)."""
+
+    def __init__(self, wavelengths=None, position=(0.0, 0.0), flux=1.0, weights=None,
+                 spectrum=None):
+        pos = position if isinstance(position, torch.Tensor) else torch.as_tensor(
+            position, dtype=torch.float64)
+        if tuple(pos.shape) != (2,):
+            raise ValueError(f"position must be a 1d array of shape (2,), got shape "
+                             f"{tuple(pos.shape)}. Pass position=[x, y] where x, y are on-sky "
+                             "angles in radians.")
+        self.position = pos
+        self.flux = flux if isinstance(flux, torch.Tensor) else torch.as_tensor(
+            float(flux), dtype=torch.float32, device=_dev())
+        super().__init__(wavelengths=wavelengths, weights=weights, spectrum=spectrum)
+
+    def model(self, optics, return_wf=False, return_psf=False):
+        _validate_return_mode(return_wf, return_psf)
+        src = self.normalise()
+        weights = src.spectrum.weights * src.flux.to(src.spectrum.weights.device)
+        return optics.propagate(src.spectrum.wavelengths, src.position, weights, return_wf,
+                                return_psf)
+
+
+class PointSources(Source):
+    """Many point sources sharing one spectrum (sources.py:330-411)."""
+
+    def __init__(self, wavelengths=None, position=((0.0, 0.0),), flux=None, weights=None,
+                 spectrum=None):
+        super().__init__(spectrum=spectrum, wavelengths=wavelengths, weights=weights)
+        pos = position if isinstance(position, torch.Tensor) else torch.as_tensor(
+            position, dtype=torch.float64)
+        if pos.dim() != 2:
+            raise ValueError("position must be a 2d array.")
+        self.position = pos
+        if flux is None:
+            self.flux = torch.ones(len(pos), dtype=torch.float32, device=_dev())
+        else:
+            f = flux if isinstance(flux, torch.Tensor) else torch.as_tensor(
+                flux, dtype=torch.float32, device=_dev())
+            if f.dim() != 1:
+                raise ValueError("flux must be a 1d array.")
+            if len(f) != len(pos):
+                raise ValueError("Length of flux must be equal to length of positions.")
+            self.flux = f
+
+    def model(self, optics, return_wf=False, return_psf=False):
+        _validate_return_mode(return_wf, return_psf)
+        src = self.normalise()
+        w = src.spectrum.weights
+        weights = w[None, :] * src.flux.to(w.device)[:, None]
+        if return_wf:
+            wfs = [optics.propagate(src.spectrum.wavelengths, p, wt, return_wf=True)
+                   for p, wt in zip(src.position, weights)]
+            return wfs[0].set(phasor=torch.stack([wf.phasor for wf in wfs]))
+        psf = None
+        for p, wt in zip(src.position, weights):
+            one = optics.propagate(src.spectrum.wavelengths, p, wt)
+            psf = one if psf is None else psf + one
+        if return_psf:
+            return PSF(psf, optics._psf_pixel_scale())
+        return psf

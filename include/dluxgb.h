@@ -1,0 +1,226 @@
+/*
+ * dluxgb.h -- C ABI of the GB300-native dLux diffraction hot path.
+ *
+ * Every entry point takes plain pointers to caller-owned device memory,
+ * explicit sizes and a cudaStream_t (passed as void*; NULL is the legacy
+ * default stream), enqueues its work on that stream and returns an int status
+ * (DLX_OK or one of the DLX_ERR_* codes below). dlx_last_error() returns a
+ * thread-local message for the most recent failure on the calling thread.
+ *
+ * Complex arrays are interleaved complex64 (float re, float im), row-major,
+ * axis 0 = y and axis 1 = x, the same layout as a numpy/torch complex64 array.
+ * Real arrays are float32, row-major.
+ *
+ * Citations are to dLux v0.16.0 (paths relative to the dLux project root).
+ */
+#ifndef DLUXGB_H
+#define DLUXGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DLX_OK 0
+#define DLX_ERR_ARG 1         /* invalid argument value (dLux raises ValueError) */
+#define DLX_ERR_SHAPE 2       /* inconsistent sizes (dLux raises ValueError) */
+#define DLX_ERR_NOMEM 3       /* device allocation failed */
+#define DLX_ERR_CUDA 4        /* a CUDA runtime call failed */
+#define DLX_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+#define DLX_ERR_UNSUPPORTED 6 /* device or configuration not supported */
+
+/* ---- MFT arithmetic forms ---------------------------------------------- */
+#define DLX_VARIANT_FP32 0       /* FP32 complex GEMM on the CUDA cores */
+#define DLX_VARIANT_SPLIT_BF16 1 /* BF16 hi/lo three-product tcgen05 GEMM, FP32 accumulation */
+
+/* Thread-local message of the last failing call ("" if none). */
+const char* dlx_last_error(void);
+/* ABI version (major * 10000 + minor * 100 + patch). */
+int dlx_version(void);
+/* Synchronises `stream`, then reports (and clears) the device status word that
+ * the tensor-core kernels set when a bounded wait expires: *status is DLX_OK
+ * or DLX_ERR_TIMEOUT. No dLux counterpart (dLux has no device-side waits). */
+int dlx_device_status(void* stream, int* status);
+/* Number of kernel launches the library has issued in this process. */
+long long dlx_launch_count(void);
+/* Brackets every complex-GEMM launch with CUDA events on its own stream until
+ * dlx_gemm_timing_end, which waits for them and returns the summed kernel time
+ * (ms), the number of launches and their algorithmic flops (8 M N K per
+ * complex GEMM). Measurement aid for the roofline; not thread-safe. */
+int dlx_gemm_timing_begin(void);
+int dlx_gemm_timing_end(double* total_ms, int* launches, double* flops);
+
+/* ---- a1: transfer matrix ------------------------------------------------
+ * Replaces dLux utils/propagation.py:67-127 (transfer_matrix), batched over
+ * wavelengths. out[b] is the [n_in][n_out] matrix
+ *   exp(-+2 pi i in_vec (x) out_vec)
+ * (or its [n_out][n_in] transpose when transpose != 0), with the phase
+ * argument formed and range-reduced in FP64 on the device.
+ * focal_length <= 0 means angular (dLux focal_length=None).
+ */
+int dlx_transfer_matrix(const double* wavelengths_host, int batch, int n_in,
+                        double pixel_scale_in, int n_out, double pixel_scale_out,
+                        double shift, double focal_length, int inverse,
+                        int transpose, void* out_c64, void* stream);
+
+/* ---- a2/a3: batched MFT plan -------------------------------------------
+ * Replaces dLux utils/propagation.py:178-256 (MFT) and its normalisation
+ * utils/propagation.py:130-175,246-254, vmapped over a batch of wavelengths
+ * (optical_systems.py:213-216). The plan caches the DFT matrices of every
+ * wavelength on the device and owns its intermediate buffers.
+ */
+typedef struct dlx_mft_plan_s* dlx_mft_plan;
+typedef struct {
+  int batch;              /* number of fields (one wavelength each) */
+  int n_in;               /* input side N */
+  int n_out;              /* output side M */
+  double pixel_scale_in;  /* input pixel scale (m/pixel) */
+  double pixel_scale_out; /* output pixel scale (rad/pixel, or m/pixel with focal_length) */
+  double focal_length;    /* <= 0: angular propagation */
+  double shift_x;         /* output-plane shift in output pixels (dLux pixel=True) */
+  double shift_y;
+  int inverse;            /* dLux inverse=True */
+  int variant;            /* DLX_VARIANT_* */
+} dlx_mft_desc;
+
+int dlx_mft_plan_create(const dlx_mft_desc* desc, const double* wavelengths_host,
+                        dlx_mft_plan* plan);
+int dlx_mft_plan_destroy(dlx_mft_plan plan);
+/* out[b] = MFT(in[b]) : in [batch][n_in][n_in] c64 -> out [batch][n_out][n_out] c64. */
+int dlx_mft_forward(dlx_mft_plan plan, const void* in_c64, void* out_c64, void* stream);
+/* Adjoint (vector-Jacobian product) of dlx_mft_forward: gin = MFT^H(gout). */
+int dlx_mft_adjoint(dlx_mft_plan plan, const void* gout_c64, void* gin_c64, void* stream);
+
+/* ---- a4: FFT propagation -------------------------------------------------
+ * Replaces dLux utils/propagation.py:8-64 (FFT) together with the optional
+ * input/output phase ramps of wavefronts.py:654-727 (propagate_FFT) and
+ * utils/fourier.py:48-78. The padded centred FFT is evaluated as a DFT-GEMM
+ * pair (exact DFT, no radix restriction). ramp_shift_in/out are the ramp
+ * shifts in output units (0 and 0 give dLux's spec_out=None behaviour).
+ */
+typedef struct dlx_fft_plan_s* dlx_fft_plan;
+typedef struct {
+  int batch;
+  int n_in;               /* input side N */
+  int pad;                /* output side is n_in * pad */
+  double pixel_scale_in;
+  double focal_length;    /* <= 0: angular */
+  int inverse;
+  int apply_ramps;        /* 0: no ramps (spec_out None); 1: ramps from centers below */
+  double center_in;       /* input grid centre (m) */
+  double center_out;      /* requested output centre (CoordSpec.c) */
+  int variant;
+} dlx_fft_desc;
+int dlx_fft_plan_create(const dlx_fft_desc* desc, const double* wavelengths_host,
+                        dlx_fft_plan* plan);
+int dlx_fft_plan_destroy(dlx_fft_plan plan);
+int dlx_fft_forward(dlx_fft_plan plan, const void* in_c64, void* out_c64, void* stream);
+int dlx_fft_adjoint(dlx_fft_plan plan, const void* gout_c64, void* gin_c64, void* stream);
+
+/* ---- a5-a11: phasor build ----------------------------------------------
+ * Replaces the elementwise wavefront updates of wavefronts.py:70-122
+ * (1/N^2 initial field), :332-368 (add_phase / add_opd), :370-395 (tilt),
+ * layers/optical_layers.py:181-186 and layers/optics.py:77-96 (transmission),
+ * fused into one pass:
+ *   out[b][y][x] = (in ? in[b][y][x] : 1) * scale_b * amp[y][x]
+ *                  * exp(i (2 pi (opd[y][x] + tx*X + ty*Y) / lambda_b + phase[y][x]))
+ * scale_b = (amp_scale ? *amp_scale : 1) * (weights ? sqrt(weights[b]) : 1) * const_scale.
+ * X, Y are the wavefront pixel centres (pixel_scale, centre 0). amp, opd,
+ * phase, in, amp_scale and weights may be NULL. The phase is reduced in
+ * cycles in FP64 before sincos. in/out may alias.
+ */
+int dlx_phasor(const void* in_c64, const float* amp, const float* opd, const float* phase,
+               const float* amp_scale, const float* weights, double const_scale,
+               const double* wavelengths_host, int batch, int n, double pixel_scale,
+               double tilt_x, double tilt_y, void* out_c64, void* stream);
+
+/* ---- a8: power and normalisation ----------------------------------------
+ * Wavefront.normalise (wavefronts.py:397-424), mode "power":
+ * out_scale[b] = sqrt(value / sum |in[b]|^2). Deterministic two-level reduction.
+ */
+int dlx_power_scale(const void* in_c64, int batch, int n, double value,
+                    float* out_scale, void* stream);
+/* Same for a real amplitude: out_scale = sqrt(value / sum amp^2). */
+int dlx_amp_norm(const float* amp, int n, double value, float* out_scale, void* stream);
+/* Reverse of a_eff = amp * sqrt(value / sum amp^2): g_amp from g_eff. */
+int dlx_amp_norm_backward(const float* amp, const float* g_eff, int n, double value,
+                          float* g_amp, void* stream);
+
+/* ---- a9 / a21: basis contraction and its reverse ------------------------
+ * eval_basis (utils/math.py:177-196): out[p] = base[p] + sum_k coeffs[k] basis[k][p].
+ * coeffs is a device pointer; base may be NULL.
+ */
+int dlx_basis_eval(const float* basis, const float* coeffs, const float* base,
+                   int nterms, long long npix, float* out, void* stream);
+/* g_coeffs[k] = sum_p basis[k][p] g[p] (deterministic, fixed order). */
+int dlx_basis_grad(const float* basis, const float* g, int nterms, long long npix,
+                   float* g_coeffs, void* stream);
+
+/* ---- a16/a13: intensity ------------------------------------------------
+ * Wavefront.psf (wavefronts.py:269-279) summed over the batch
+ * (optical_systems.py:222-223): psf[p] = sum_b |in[b][p]|^2.
+ */
+int dlx_psf_sum(const void* in_c64, int batch, long long npix, float* psf, void* stream);
+
+/* ---- a17/a18: detector ---------------------------------------------------
+ * downsample(mean=False) (utils/array_ops.py:124-162, psfs.py:74-91) fused
+ * with ApplyPixelResponse (layers/detector_layers.py:100-131):
+ * out[a][c] = (flat ? flat[a][c] : 1) * sum_{i,j<k} in[a k + i][c k + j].
+ * k = 1 gives the pixel response alone. mean != 0 divides by k*k.
+ */
+int dlx_downsample(const float* in, int n_in, int k, int mean, const float* flat,
+                   float* out, void* stream);
+/* Reverse: g_in[y][x] = g_out[y/k][x/k] * flat(...) (/k^2 if mean);
+ * g_flat[a][c] = g_out[a][c] * downsample(in) (g_flat may be NULL). */
+int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k, int mean,
+                            const float* flat, float* g_in, float* g_flat, void* stream);
+
+/* ---- fused polychromatic PSF plan ----------------------------------------
+ * The whole of OpticalSystem.propagate (optical_systems.py:147-223) for a
+ * layered system whose layers reduce to a wavelength-independent amplitude,
+ * OPD and phase (Transmissive/Basis/Aberrated/Optic/BasisOptic/Tilt/
+ * Normalise layers) followed by AngularOpticalSystem.to_focus
+ * (optical_systems.py:659-680) or CartesianOpticalSystem.to_focus
+ * (:754-775):
+ *   psf = sum_l |MFT_l( sqrt(w_l) amp exp(i (2 pi (opd + tilt)/lambda_l + phase)) )|^2
+ * and its reverse-mode gradient, which recomputes every focal field instead
+ * of storing it.
+ */
+typedef struct dlx_poly_plan_s* dlx_poly_plan;
+typedef struct {
+  int n_wavelengths;      /* L */
+  int n_in;               /* pupil side N */
+  int n_out;              /* focal side M (psf_npixels * oversample) */
+  double pixel_scale_in;  /* diameter / N */
+  double pixel_scale_out; /* rad/pixel (angular) or m/pixel */
+  double focal_length;    /* <= 0: angular */
+  int variant;            /* DLX_VARIANT_* */
+} dlx_poly_desc;
+
+int dlx_poly_plan_create(const dlx_poly_desc* desc, const double* wavelengths_host,
+                         dlx_poly_plan* plan);
+int dlx_poly_plan_destroy(dlx_poly_plan plan);
+/* Device bytes the plan holds (cached DFT matrices plus intermediates). */
+int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
+/* psf_out [M][M] = polychromatic PSF. amp, amp_scale (device scalar that
+ * multiplies amp, e.g. from dlx_amp_norm), opd, phase and weights ([L]) are
+ * device pointers and may be NULL (1, 1, 0, 0, 1). tilt is the source offset
+ * in radians (initialise_wavefront, optical_systems.py:363-389). */
+int dlx_poly_psf(dlx_poly_plan plan, const float* amp, const float* amp_scale, const float* opd,
+                 const float* phase, const float* weights, double tilt_x, double tilt_y,
+                 float* psf_out, void* stream);
+/* Gradient of <g_psf, psf> w.r.t. the effective amplitude (amp * amp_scale),
+ * opd, phase ([N][N]) and weights ([L]). Any output pointer may be NULL (not
+ * computed). The focal fields are recomputed, not stored. */
+int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_scale,
+                      const float* opd, const float* phase, const float* weights, double tilt_x,
+                      double tilt_y, const float* g_psf, float* g_amp, float* g_opd,
+                      float* g_phase, float* g_w, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DLUXGB_H */
