@@ -323,7 +323,11 @@ def main():
     ap.add_argument("--variant", default="split_bf16", choices=["split_bf16", "fp32"])
     ap.add_argument("--no-fp32-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
+                    help="wavelength count (64 is the benchmark workload; smaller values "
+                         "make the bounded cases used for profiling captures)")
     args = ap.parse_args()
+    globals()["N_WAVELENGTHS"] = int(args.wavelengths)
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -48,6 +48,7 @@ class PolyPSF(torch.autograd.Function):
         amp_scale = kernels.amp_norm(amp.detach()) if (normalise and amp is not None) else None
         t = (float(tilt[0]), float(tilt[1]))
         ctx.plan, ctx.normalise, ctx.tilt = plan, normalise, t
+        ctx.tilt_device = tilt.device
         ctx.save_for_backward(amp, opd, phase, weights, amp_scale)
         return plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t)
 
@@ -74,7 +75,8 @@ class PolyPSF(torch.autograd.Function):
         g_tilt = None
         if ctx.needs_input_grad[6]:
             # d/d(theta_x, theta_y) of opd + theta_x X + theta_y Y: project on the pixel grid
-            g_tilt = kernels.basis_grad(plan.tilt_basis(), gr["opd"], (2,)).to(torch.float64)
+            g_tilt = kernels.basis_grad(plan.tilt_basis(), gr["opd"], (2,)).to(
+                device=ctx.tilt_device, dtype=torch.float64)
         g_opd = gr["opd"] if (ctx.needs_input_grad[3] and opd is not None) else None
         return None, None, g_amp, g_opd, gr["phase"], gr["w"], g_tilt
 

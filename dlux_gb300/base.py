@@ -61,7 +61,9 @@ class Base:
             obj = _get_child(obj, p)
         return obj
 
-    def set(self, paths, values=None, **kwargs):
+    def set(self, paths=None, values=None, **kwargs):
+        if paths is None and not kwargs:
+            raise TypeError("set() needs a path and a value, or keyword updates")
         if kwargs:
             obj = self
             for k, v in kwargs.items():

@@ -61,6 +61,10 @@ def _stream():
     return stream_ptr()
 
 
+def _contig(t):
+    return None if t is None else t.contiguous()
+
+
 def _f32(x, device=None):
     dev = device or _lib.require_cuda()
     return torch.as_tensor(x, dtype=torch.float32, device=dev).contiguous()
@@ -251,6 +255,7 @@ class PolyPlan(_Plan):
         return tb
 
     def psf(self, amp, amp_scale, opd, phase, weights, tilt=(0.0, 0.0), out=None):
+        amp, amp_scale, opd, phase, weights = map(_contig, (amp, amp_scale, opd, phase, weights))
         dev = weights.device
         if out is None:
             out = torch.empty((self.n_out, self.n_out), dtype=torch.float32, device=dev)
@@ -260,6 +265,7 @@ class PolyPlan(_Plan):
 
     def grad(self, amp, amp_scale, opd, phase, weights, g_psf, tilt=(0.0, 0.0),
              want=("amp", "opd", "phase", "w")):
+        amp, amp_scale, opd, phase, weights = map(_contig, (amp, amp_scale, opd, phase, weights))
         dev = g_psf.device
         n = self.n_in
         g_amp = torch.empty((n, n), dtype=torch.float32, device=dev) if "amp" in want else None

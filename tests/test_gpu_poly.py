@@ -38,7 +38,7 @@ def make_case(n, m, nz, L, seed, spiders=False):
 
 
 def to_dev(x, dtype=torch.float32):
-    return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda")
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device="cuda")
 
 
 @pytest.mark.parametrize("variant", VARIANTS)

@@ -1,0 +1,214 @@
+"""The oracle pinned against dLux's own known-answer and structural tests, plus
+physics known answers derived from the mathematics (CPU only)."""
+
+import numpy as np
+import pytest
+
+from oracle import dlux_oracle as O
+from oracle import split_emulator as S
+
+
+# ---- dLux tests/utils/test_zernike.py:24-52 ---------------------------------
+def test_noll_known_indices():
+    expected = {1: (0, 0), 2: (1, 1), 3: (1, -1), 4: (2, 0), 5: (2, -2), 6: (2, 2),
+                7: (3, -1), 8: (3, 1), 9: (3, -3), 10: (3, 3)}
+    for j, nm in expected.items():
+        assert O.noll_indices(j) == nm
+
+
+@pytest.mark.parametrize("diameter", [2.0, 1.5])
+def test_zernike_fast_matches_zernike(diameter):
+    """dLux tests/utils/test_zernike.py:120-129."""
+    coords = O.pixel_coords(16, 2.0)
+    n, m = O.noll_indices(5)
+    c, k = O.zernike_factors(5)
+    a = O.zernike_fast(n, m, c, k, coords, diameter)
+    b = O.zernike(5, coords, diameter)
+    assert np.allclose(a, b)
+    assert not np.isnan(a).any()
+
+
+def test_zernike_orthonormal_on_unit_disk():
+    """Noll normalisation: <Z_i, Z_j> = delta_ij (area-weighted mean over the disk)."""
+    coords = O.pixel_coords(512, 2.0)
+    Z = O.zernike_basis(range(1, 12), coords, 2.0)
+    mask = np.hypot(coords[0], coords[1]) <= 1.0
+    G = np.einsum("ipq,jpq->ij", Z * mask, Z * mask) / mask.sum()
+    assert np.allclose(G, np.eye(11), atol=2e-2)
+
+
+# ---- dLux tests/utils/test_propagation.py:58-176 ----------------------------
+@pytest.mark.parametrize("inverse", [True, False])
+def test_fft_output_shape(inverse):
+    out, _ = O.fft_prop(np.ones((32, 32)), 1.0, 0.1, 2.0, pad=2, inverse=inverse)
+    assert out.shape == (64, 64)
+
+
+def test_fft_round_trip_no_padding():
+    ph = np.ones((32, 32), complex)
+    fwd, _ = O.fft_prop(ph, 1.0, 0.1, None, 1, False)
+    back, _ = O.fft_prop(fwd, 1.0, 0.1, None, 1, True)
+    assert np.allclose(back, ph, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("fl,inverse,pixel", [(2.0, True, True), (2.0, False, True),
+                                              (2.0, True, False), (2.0, False, False),
+                                              (None, True, True), (None, False, True),
+                                              (None, True, False), (None, False, False)])
+def test_mft_shape_and_finite(fl, inverse, pixel):
+    out = O.mft(np.ones((32, 32), complex), 1.0, 0.1, 16, 0.05, fl, (1.0, -2.0), pixel, inverse)
+    assert out.shape == (16, 16) and np.isfinite(out).all()
+
+
+def test_mft_shift_units_consistent():
+    ph = np.ones((32, 32), complex)
+    a = O.mft(ph, 1.0, 0.1, 16, 0.05, 2.0, np.array([1.0, -2.0]), True)
+    b = O.mft(ph, 1.0, 0.1, 16, 0.05, 2.0, np.array([1.0, -2.0]) * 0.05, False)
+    assert np.allclose(a, b, rtol=1e-6, atol=1e-6)
+
+
+# ---- dLux tests/utils/test_fourier.py:58-105 --------------------------------
+def test_fft_spec_offsets():
+    d, c = O.fft_spec(16, 0.1, 1.0)
+    assert np.isfinite(d) and c != 0.0
+    d, c = O.fft_spec(15, 0.1, 1.0)
+    assert c == 0.0
+    assert np.isclose(O.fft_spec(16, 0.1, 1.0, 2.0)[0], O.fft_spec(16, 0.1, 1.0)[0] * 2.0)
+
+
+def test_fft_ramp_conjugacy():
+    xs = np.linspace(-0.5, 0.5, 16) * 0.1
+    f = O.fft_phase_ramp(xs, 1.0, 0.3)
+    i = O.fft_phase_ramp(xs, 1.0, 0.3, inverse=True)
+    assert f.shape == (16, 16) and np.allclose(f, np.conj(i))
+    assert not np.allclose(f, O.fft_phase_ramp(xs, 1.0, 0.3, focal_length=2.0))
+
+
+# ---- dLux tests/utils/test_math.py:87-94, test_array_ops.py:95-127 ----------
+def test_eval_basis_is_tensordot():
+    c = np.arange(6.0).reshape(2, 3)
+    B = np.arange(2 * 3 * 4 * 5 * 6.0).reshape(2, 3, 4, 5, 6)
+    out = O.eval_basis(B, c)
+    assert out.shape == (4, 5, 6)
+    assert np.allclose(out, np.tensordot(B, c, ((0, 1), (0, 1))))
+    with pytest.raises(ValueError):
+        O.eval_basis(np.ones((2, 3, 4)), np.ones((3, 2)))
+
+
+@pytest.mark.parametrize("shape,n", [((10, 9), 2), ((10, 10), 3)])
+def test_downsample_invalid(shape, n):
+    with pytest.raises(ValueError):
+        O.downsample(np.ones(shape), n)
+
+
+@pytest.mark.parametrize("size,n", [(10, 2), (9, 3), (10, 5), (15, 3)])
+def test_downsample_shapes(size, n):
+    for mean in (True, False):
+        assert O.downsample(np.ones((size, size)), n, mean).shape == (size // n, size // n)
+
+
+def test_downsample_is_block_sum():
+    a = np.random.default_rng(0).normal(size=(12, 12))
+    ref = a.reshape(4, 3, 4, 3).sum((1, 3))
+    assert np.allclose(O.downsample(a, 3, mean=False), ref)
+
+
+# ---- physics known answers ---------------------------------------------------
+def test_mft_equals_fft_at_matched_sampling():
+    """An MFT sampled at the FFT's native grid equals the centred padded FFT."""
+    rng = np.random.default_rng(1)
+    n, pad, wl, ps = 32, 2, 1e-6, 1 / 32
+    E = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    fft_out, d_out = O.fft_prop(E, wl, ps, None, pad)
+    # The padded FFT's input and output grids are centred on index n/2 and P/2;
+    # the MFT's on (n-1)/2 and (M-1)/2, so a +1/2-pixel shift aligns both. With
+    # M = P the normalisations nfringes / (N M) and 1 / P coincide.
+    mft_out = O.mft(E, wl, ps, n * pad, d_out, None, (0.5, 0.5), True)
+    assert np.allclose(mft_out, fft_out, rtol=1e-9, atol=1e-12 * np.abs(fft_out).max())
+
+
+def test_parseval_full_band_mft():
+    """An MFT covering exactly the full band at Nyquist conserves power up to its scale."""
+    rng = np.random.default_rng(2)
+    n, wl, ps = 32, 1e-6, 1 / 32
+    E = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    d = wl / (n * ps)  # one fringe per pixel: the DFT of size n
+    F = O.mft(E, wl, ps, n, d)
+    s = O.calc_nfringes(wl, n, ps, n, d) / (n * n)
+    assert np.isclose((np.abs(F) ** 2).sum(), s ** 2 * n * n * (np.abs(E) ** 2).sum())
+
+
+def test_zero_opd_psf_is_centro_symmetric():
+    T = O.circular_aperture(64, 1.0, oversample=3, secondary_diameter=0.1)
+    psf = O.poly_psf(T, np.zeros_like(T), [1e-6], [1.0], 1.0, 32, float(O.arcsec2rad(0.05)))
+    assert np.allclose(psf, psf[::-1, ::-1], rtol=1e-9, atol=1e-12 * psf.max())
+    assert np.unravel_index(psf.argmax(), psf.shape) in [(15, 15), (15, 16), (16, 15), (16, 16)]
+
+
+def test_mft_adjoint_identity():
+    rng = np.random.default_rng(3)
+    n, m, wl, ps, po = 24, 16, 1e-6, 1 / 24, float(O.arcsec2rad(0.05))
+    x = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    y = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+    A = O.transfer_matrix(wl, n, ps, m, po)
+    s = O.calc_nfringes(wl, n, ps, m, po) / (n * m)
+    fx = s * (A.T @ x @ A)
+    ahy = s * (A.conj() @ y @ A.conj().T)
+    assert np.isclose(np.vdot(y, fx), np.vdot(ahy, x))
+
+
+def test_gradient_oracle_matches_central_differences():
+    rng = np.random.default_rng(0)
+    n, m = 32, 16
+    T, B = O.circular_aperture(n, 1.0, oversample=3, secondary_diameter=0.1,
+                               zernike_nolls=list(range(4, 8)))
+    opd = O.eval_basis(B, rng.normal(0, 80e-9, 4))
+    wls, w = np.array([0.9e-6, 1.1e-6]), np.array([0.3, 0.7])
+    ps = float(O.arcsec2rad(0.05))
+    G = rng.normal(size=(m, m))
+    ph = rng.normal(0, 0.2, (n, n))
+    tilt = (0.1e-6, -0.05e-6)
+    Teff = T / np.sqrt((T ** 2).sum())
+
+    def L(a=Teff, o=opd, p=ph, ww=w):
+        # the oracle's forward includes the 1/N^2 initial field; cancel it
+        return (G * O.poly_psf(a * n ** 2, o, wls, ww, 1.0, m, ps, phase=p, offset=tilt,
+                               normalise=False)).sum()
+
+    g = O.poly_psf_grad(Teff, opd, wls, w, 1.0, m, ps, G, phase=ph, offset=tilt)
+    for (i, j) in [(10, 20), (5, 16), (25, 9)]:
+        d = np.zeros((n, n))
+        d[i, j] = 1e-12
+        assert np.isclose((L(o=opd + d) - L(o=opd - d)) / 2e-12, g["g_opd"][i, j], rtol=1e-5)
+        d[i, j] = 1e-6
+        assert np.isclose((L(p=ph + d) - L(p=ph - d)) / 2e-6, g["g_phase"][i, j], rtol=1e-5)
+        assert np.isclose((L(a=Teff + d) - L(a=Teff - d)) / 2e-6, g["g_amp"][i, j], rtol=1e-5)
+    for k in range(2):
+        d = np.zeros(2)
+        d[k] = 1e-6
+        assert np.isclose((L(ww=w + d) - L(ww=w - d)) / 2e-6, g["g_w"][k], rtol=1e-5)
+
+
+def test_c64_mimic_close_to_f64():
+    T, B = O.circular_aperture(128, 1.0, oversample=3, secondary_diameter=0.1,
+                               zernike_nolls=list(range(4, 14)))
+    opd = O.eval_basis(B, np.random.default_rng(4).normal(0, 50e-9, 10))
+    ps = float(O.arcsec2rad(0.02))
+    a = O.poly_psf(T, opd, [1e-6], [1.0], 1.0, 64, ps)
+    b = O.poly_psf(T, opd, [1e-6], [1.0], 1.0, 64, ps, precision="c64")
+    assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-5
+
+
+def test_split_emulator_meets_1e5():
+    """BF16 hi/lo three-product MFT error (emulated) at a config-2-like field."""
+    T, B = O.circular_aperture(128, 1.0, oversample=3, secondary_diameter=0.1,
+                               spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                               zernike_nolls=list(range(4, 25)))
+    opd = O.eval_basis(B, np.random.default_rng(5).normal(0, 30e-9, 21))
+    ps = float(O.arcsec2rad(0.01))
+    F, E = O.poly_psf_fields(T, opd, [1e-6], [1.0], 1.0, 128, ps)
+    A = O.transfer_matrix(1e-6, 128, 1 / 128, 128, ps)
+    s = O.calc_nfringes(1e-6, 128, 1 / 128, 128, ps) / (128 * 128)
+    Fs = S.split_mft(E[0].astype(np.complex64), A.astype(np.complex64), A.astype(np.complex64), s)
+    P, P64 = np.abs(Fs.astype(complex)) ** 2, np.abs(F[0]) ** 2
+    assert np.linalg.norm(P - P64) / np.linalg.norm(P64) < 1e-5
