@@ -133,6 +133,7 @@ struct TwoStep {
   DevBuf atx, aty, anx, any;   // T layout [b][n_out][n_in], N layout [b][n_in][n_out]
   DevBuf alpha;                // float [b]
   DevBuf inv_lambda, kvec;     // double [b]
+  DevBuf inv_lambda_ff;        // float2 [b]: 1/lambda as a (hi, lo) pair
   std::vector<double> wl;
 
   size_t elem_bytes() const { return variant == DLX_VARIANT_SPLIT_BF16 ? 8 : 8; }
@@ -178,9 +179,18 @@ struct TwoStep {
         il[b] = 1.0 / wl[b];
         kv[b] = 2.0 * M_PI / wl[b];
       }
+      std::vector<float2> ilff(batch);
+      for (int b = 0; b < batch; ++b) {
+        const FF f = ff_from_double(il[b]);
+        ilff[b] = make_float2(f.hi, f.lo);
+      }
       if ((st = inv_lambda.alloc(sizeof(double) * batch)) != DLX_OK) break;
+      if ((st = inv_lambda_ff.alloc(sizeof(float2) * batch)) != DLX_OK) break;
       if ((st = kvec.alloc(sizeof(double) * batch)) != DLX_OK) break;
       e = cudaMemcpy(inv_lambda.p, il.data(), sizeof(double) * batch, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(inv_lambda_ff.p, ilff.data(), sizeof(float2) * batch,
+                       cudaMemcpyHostToDevice);
       if (e == cudaSuccess)
         e = cudaMemcpy(kvec.p, kv.data(), sizeof(double) * batch, cudaMemcpyHostToDevice);
       if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(lambda)"); break; }
@@ -194,10 +204,11 @@ struct TwoStep {
   const void* ANy() const { return shared_xy ? anx.p : any.p; }
   void release() {
     atx.release(); aty.release(); anx.release(); any.release();
-    alpha.release(); inv_lambda.release(); kvec.release();
+    alpha.release(); inv_lambda.release(); kvec.release(); inv_lambda_ff.release();
   }
   size_t footprint() const {
     return atx.bytes + aty.bytes + anx.bytes + any.bytes + alpha.bytes + inv_lambda.bytes +
+           inv_lambda_ff.bytes +
            kvec.bytes;
   }
 };
@@ -562,19 +573,20 @@ int dlx_phasor(const void* in, const float* amp, const float* opd, const float* 
   cudaStream_t s = as_stream(stream);
   for (int b0 = 0; b0 < batch; b0 += kMaxBatchArg) {
     const int nb = (batch - b0) < kMaxBatchArg ? (batch - b0) : kMaxBatchArg;
-    BatchD il;
-    for (int i = 0; i < kMaxBatchArg; ++i) il.v[i] = 0.0;
+    BatchFF il;
+    for (int i = 0; i < kMaxBatchArg; ++i) il.v[i] = make_float2(0.f, 0.f);
     for (int i = 0; i < nb; ++i) {
       const double w = wavelengths_host[b0 + i];
       if (!(w > 0)) return fail(DLX_ERR_ARG, "phasor: wavelengths must be positive");
-      il.v[i] = 1.0 / w;
+      const FF f = ff_from_double(1.0 / w);
+      il.v[i] = make_float2(f.hi, f.lo);
     }
     const long long off = (long long)b0 * n * n;
     PhasorArgs a{};
     a.in = in ? reinterpret_cast<const float2*>(in) + off : nullptr;
     a.amp = amp; a.opd = opd; a.phase = phase; a.amp_scale = amp_scale;
     a.weights = weights ? weights + b0 : nullptr;
-    a.inv_lambda_dev = nullptr;
+    a.inv_lambda_ff = nullptr;
     a.const_scale = const_scale;
     a.batch = nb; a.n = n;
     a.pixel_scale = pixel_scale; a.tilt_x = tilt_x; a.tilt_y = tilt_y;
@@ -698,7 +710,7 @@ struct dlx_poly_plan_s {
                   cudaStream_t s) {
     PhasorArgs a{};
     a.amp = amp; a.amp_scale = amp_scale; a.opd = opd; a.phase = phase; a.weights = weights;
-    a.inv_lambda_dev = ts.inv_lambda.as<double>();
+    a.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
     a.const_scale = 1.0;
     a.batch = ts.batch; a.n = ts.n_in;
     a.pixel_scale = pixel_scale_in; a.tilt_x = tx; a.tilt_y = ty;
@@ -821,7 +833,7 @@ int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_sca
   ep.out_f32 = pre;
   ep.out_f32b = pim;
   ep.amp = amp; ep.amp_scale = amp_scale; ep.opd = opd; ep.phase = phase; ep.weights = weights;
-  ep.inv_lambda = p.ts.inv_lambda.as<double>();
+  ep.inv_lambda_ff = p.ts.inv_lambda_ff.as<float2>();
   ep.pixel_scale = p.pixel_scale_in; ep.tilt_x = tilt_x; ep.tilt_y = tilt_y;
   DLX_TRY(run_gemm(v, gemm_for(v, L, N, N, M, p.ts.ANy(), true, p.mid.p, ep), s));
   PupilReduceArgs r{};

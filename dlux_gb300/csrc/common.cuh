@@ -62,6 +62,37 @@ __device__ __forceinline__ float2 cis_cycles(double t) {
   return make_float2(c, s);
 }
 
+// Per-(pixel, wavelength) phase in cycles, reduced with FP64 accuracy using
+// FP32 instructions only (GB300's FP64 rate is ~1/64 of its FP32 rate, and
+// this runs once per pixel per wavelength). The path length and the inverse
+// wavelength arrive as unevaluated float pairs (hi + lo, |lo| <= ulp(hi)/2)
+// formed once in FP64; Dekker's error-free product hi*hi = p + e (one FMA)
+// gives the leading term exactly, p - rint(p) is exact for |p| < 2^22, and
+// the remaining terms are below 2^-24 of |p|. The result has the absolute
+// error of an FP64 reduction followed by rounding to FP32 (~3e-8 cycles).
+struct FF {
+  float hi, lo;
+};
+
+__host__ __device__ __forceinline__ FF ff_from_double(double v) {
+  FF r;
+  r.hi = (float)v;
+  r.lo = (float)(v - (double)r.hi);
+  return r;
+}
+
+__device__ __forceinline__ float2 cis_ff(FF path, FF inv_lambda, FF phase_cycles) {
+  const float p = path.hi * inv_lambda.hi;
+  const float e = fmaf(path.hi, inv_lambda.hi, -p);  // exact residual of the product
+  const float small = e + fmaf(path.hi, inv_lambda.lo, path.lo * inv_lambda.hi);
+  float r = (p - rintf(p)) + phase_cycles.hi;
+  r = r + (small + phase_cycles.lo);
+  r = r - rintf(r);
+  float s, c;
+  sincospif(2.0f * r, &s, &c);
+  return make_float2(c, s);
+}
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -62,23 +62,24 @@ int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool 
 // 319-327; optics.py:77-96; optical_systems.py:213-215).
 // One thread per pixel; the wavelength loop reuses amp/opd/phase.
 // ---------------------------------------------------------------------------
-__global__ void phasor_kernel(PhasorArgs a, BatchD inv_lambda_arg) {
+__global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
   const long long npix = (long long)a.n * a.n;
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
   const int y = (int)(p / a.n);
   const int x = (int)(p - (long long)y * a.n);
+  // Per pixel, once: optical path (m) and phase (cycles) in FP64, kept as float pairs.
   const double half = 0.5 * (a.n - 1);
   const double X = ((double)x - half) * a.pixel_scale;
   const double Y = ((double)y - half) * a.pixel_scale;
-  const double path = (a.opd ? (double)a.opd[p] : 0.0) + a.tilt_x * X + a.tilt_y * Y;
-  const double ph_cyc = a.phase ? (double)a.phase[p] * (0.5 / CUDART_PI) : 0.0;
+  const FF path = ff_from_double((a.opd ? (double)a.opd[p] : 0.0) + a.tilt_x * X + a.tilt_y * Y);
+  const FF ph_cyc = ff_from_double(a.phase ? (double)a.phase[p] * (0.5 / CUDART_PI) : 0.0);
   float amp = a.amp ? a.amp[p] : 1.0f;
   if (a.amp_scale) amp *= *a.amp_scale;
   amp *= (float)a.const_scale;
   for (int b = 0; b < a.batch; ++b) {
-    const double il = a.inv_lambda_dev ? a.inv_lambda_dev[b] : inv_lambda_arg.v[b];
-    float2 u = cis_cycles(path * il + ph_cyc);
+    const float2 il2 = a.inv_lambda_ff ? a.inv_lambda_ff[b] : inv_lambda_arg.v[b];
+    float2 u = cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
     float sc = amp;
     if (a.weights) sc *= sqrtf(a.weights[b]);
     float2 v = make_float2(u.x * sc, u.y * sc);
@@ -98,12 +99,12 @@ __global__ void phasor_kernel(PhasorArgs a, BatchD inv_lambda_arg) {
   }
 }
 
-int launch_phasor(const PhasorArgs& a, const BatchD* inv_lambda_arg, cudaStream_t s) {
+int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream_t s) {
   const long long npix = (long long)a.n * a.n;
   if (npix == 0 || a.batch == 0) return DLX_OK;
-  BatchD dummy;
+  BatchFF dummy;
   if (!inv_lambda_arg) {
-    for (int i = 0; i < kMaxBatchArg; ++i) dummy.v[i] = 0.0;
+    for (int i = 0; i < kMaxBatchArg; ++i) dummy.v[i] = make_float2(0.f, 0.f);
     inv_lambda_arg = &dummy;
   }
   phasor_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(a, *inv_lambda_arg);

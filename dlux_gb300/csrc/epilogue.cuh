@@ -24,12 +24,14 @@ __device__ __forceinline__ void store_split(__nv_bfloat16* base_b, long long pla
 // (recomputed in the reverse pass instead of stored).
 __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int b, int y, int x, int n,
                                                     long long p) {
+  // Same arithmetic as the phasor kernel so that forward and reverse agree.
   const double half = 0.5 * (n - 1);
   const double X = ((double)x - half) * e.pixel_scale;
   const double Y = ((double)y - half) * e.pixel_scale;
-  const double path = (e.opd ? (double)e.opd[p] : 0.0) + e.tilt_x * X + e.tilt_y * Y;
-  const double ph = e.phase ? (double)e.phase[p] * (0.5 / CUDART_PI) : 0.0;
-  return cis_cycles(path * e.inv_lambda[b] + ph);
+  const FF path = ff_from_double((e.opd ? (double)e.opd[p] : 0.0) + e.tilt_x * X + e.tilt_y * Y);
+  const FF ph = ff_from_double(e.phase ? (double)e.phase[p] * (0.5 / CUDART_PI) : 0.0);
+  const float2 il = e.inv_lambda_ff[b];
+  return cis_ff(path, FF{il.x, il.y}, ph);
 }
 
 __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n, int M, int N,

@@ -10,10 +10,20 @@
 // K-step issues 12 tcgen05.mma instructions; the minus sign of Im*Im (and the
 // conjugate of A) is applied with the instruction descriptor's negate-A bit.
 //
-// CTA tile: 128 complex rows of A x 256 complex rows of B. TMEM holds the
-// real and imaginary accumulators (2 x 256 fp32 columns = all 512 columns).
-// K is staged 32 elements at a time (64-byte rows, 64B swizzle) by TMA in a
-// 2-stage mbarrier pipeline (96 KB per stage). Warp roles: warp 0 issues TMA,
+// Accuracy: each MMA rounds its running FP32 accumulator, so an accumulator
+// that absorbs many MMAs of a coherent sum (the bright core of a PSF) drifts
+// by about one ulp of the running sum per MMA. The hi*hi products therefore
+// go to a "main" accumulator (2 MMAs per complex K-step) and the ~2^-8
+// smaller hi*lo + lo*hi cross products to a separate "cross" accumulator (4
+// per K-step), whose rounding is 2^-8 smaller; the epilogue adds the two in
+// FP32. This keeps the polychromatic PSF within 1e-5 (relative L2) of the FP64
+// oracle at 512 x 512 x 512.
+//
+// CTA tile: 128 complex rows of A x 128 complex rows of B. TMEM holds main and
+// cross accumulators for the real and imaginary parts (4 x 128 fp32 columns =
+// all 512 columns). K is staged 32 elements at a time (64-byte rows, 64B
+// swizzle) by TMA in a 3-stage mbarrier pipeline (64 KB per stage). Warp
+// roles: warp 0 issues TMA,
 // warp 1 issues MMA (one thread each), warps 2-5 drain TMEM through the
 // shared epilogues. The kernel is persistent over (batch, m-tile, n-tile)
 // work items. Every mbarrier wait is bounded by a wall-clock limit; on
@@ -30,12 +40,12 @@ namespace dlx {
 namespace {
 
 constexpr int TC_BM = 128;
-constexpr int TC_BN = 256;
+constexpr int TC_BN = 128;
 constexpr int TC_BK = 32;
-constexpr int TC_STAGES = 2;
+constexpr int TC_STAGES = 3;
 constexpr int A_PLANE_BYTES = TC_BM * TC_BK * 2;                         // 8 KB
-constexpr int B_PLANE_BYTES = TC_BN * TC_BK * 2;                         // 16 KB
-constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;       // 96 KB
+constexpr int B_PLANE_BYTES = TC_BN * TC_BK * 2;                         // 8 KB
+constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;       // 64 KB
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int TC_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 512;
@@ -388,7 +398,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // Sign of the Ai * Bi term in Re and of the Ai * Br term in Im.
       const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
       const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
-      const uint32_t d_re = tmem, d_im = tmem + TC_BN;
+      // main (hi*hi) and cross (hi*lo + lo*hi) accumulators, real and imaginary
+      const uint32_t m_re = tmem, m_im = tmem + TC_BN;
+      const uint32_t c_re = tmem + 2 * TC_BN, c_im = tmem + 3 * TC_BN;
       int stage = 0;
       uint32_t ph = 0, acc_ph = 0;
       bool ok = true;
@@ -413,19 +425,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint64_t bil = make_desc(sb + 3 * B_PLANE_BYTES + ko);
             const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
             // Re += Ar Br -/+ Ai Bi
-            mma_bf16(d_re, arh, brh, id_pos, acc);
-            mma_bf16(d_re, arh, brl, id_pos, 1u);
-            mma_bf16(d_re, arl, brh, id_pos, 1u);
-            mma_bf16(d_re, aih, bih, id_rii, 1u);
-            mma_bf16(d_re, aih, bil, id_rii, 1u);
-            mma_bf16(d_re, ail, bih, id_rii, 1u);
+            mma_bf16(m_re, arh, brh, id_pos, acc);
+            mma_bf16(m_re, aih, bih, id_rii, 1u);
+            mma_bf16(c_re, arh, brl, id_pos, acc);
+            mma_bf16(c_re, arl, brh, id_pos, 1u);
+            mma_bf16(c_re, aih, bil, id_rii, 1u);
+            mma_bf16(c_re, ail, bih, id_rii, 1u);
             // Im += Ar Bi +/- Ai Br
-            mma_bf16(d_im, arh, bih, id_pos, acc);
-            mma_bf16(d_im, arh, bil, id_pos, 1u);
-            mma_bf16(d_im, arl, bih, id_pos, 1u);
-            mma_bf16(d_im, aih, brh, id_iir, 1u);
-            mma_bf16(d_im, aih, brl, id_iir, 1u);
-            mma_bf16(d_im, ail, brh, id_iir, 1u);
+            mma_bf16(m_im, arh, bih, id_pos, acc);
+            mma_bf16(m_im, aih, brh, id_iir, 1u);
+            mma_bf16(c_im, arh, bil, id_pos, acc);
+            mma_bf16(c_im, arl, bih, id_pos, 1u);
+            mma_bf16(c_im, aih, brl, id_iir, 1u);
+            mma_bf16(c_im, ail, brh, id_iir, 1u);
           }
           mma_commit(&empty[stage]);
           if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
@@ -455,10 +467,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll 1
       for (int c = 0; c < TC_BN / 32; ++c) {
         if (nbase + c * 32 >= p.N) break;  // warp-uniform
-        float re[32], im[32];
+        float re[32], im[32], cre[32], cim[32];
         tmem_ld32(lane_addr + c * 32, re);
         tmem_ld32(lane_addr + TC_BN + c * 32, im);
+        tmem_ld32(lane_addr + 2 * TC_BN + c * 32, cre);
+        tmem_ld32(lane_addr + 3 * TC_BN + c * 32, cim);
         tmem_ld_wait();
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+          re[t] += cre[t];
+          im[t] += cim[t];
+        }
         if (m < p.M) epi_chunk32(p.epi, b, m, nbase + c * 32, p.M, p.N, re, im);
       }
       tc_fence_before();

@@ -10,6 +10,10 @@ constexpr int kMaxBatchArg = 256;
 struct BatchD {
   double v[kMaxBatchArg];
 };
+// Per-batch (hi, lo) float pairs, e.g. 1 / lambda for the FP32 phase reduction.
+struct BatchFF {
+  float2 v[kMaxBatchArg];
+};
 
 // --- elementwise.cu --------------------------------------------------------
 int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool rows_are_out,
@@ -23,14 +27,14 @@ struct PhasorArgs {
   const float* phase;      // nullable [n][n]
   const float* amp_scale;  // nullable device scalar
   const float* weights;    // nullable [b]
-  const double* inv_lambda_dev;  // [b] (device) or nullptr -> use inv_lambda_arg
+  const float2* inv_lambda_ff;   // [b] (hi, lo) of 1/lambda (device), or nullptr -> by value
   double const_scale;
   int batch, n;
   double pixel_scale, tilt_x, tilt_y;
   float2* out_c64;             // one of the two outputs
   __nv_bfloat16* out_split;    // [b][4][n][n]
 };
-int launch_phasor(const PhasorArgs& a, const BatchD* inv_lambda_arg, cudaStream_t s);
+int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream_t s);
 
 int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
                                 __nv_bfloat16* out_split, cudaStream_t s);
@@ -97,7 +101,7 @@ struct EpiArgs {
   const float* opd;          // nullable
   const float* phase;        // nullable
   const float* weights;      // [b] nullable (1)
-  const double* inv_lambda;  // [b]
+  const float2* inv_lambda_ff;  // [b] (hi, lo) of 1/lambda
   double pixel_scale, tilt_x, tilt_y;
 };
 
