@@ -74,6 +74,8 @@ _SIGNATURES = {
     "dlx_mft_plan_destroy": (_c_int, [_c_vp]),
     "dlx_mft_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_mft_adjoint": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "dlx_mft_forward_noalloc": (_c_int, [_c_vp, _c_int, _c_int, _c_dbl, _c_int, _c_dbl, _c_vp,
+                                         _c_dbl, _c_dbl, _c_dbl, _c_int, _c_vp, _c_vp]),
     "dlx_fft_plan_create": (_c_int, [ctypes.POINTER(FftDesc), _c_vp, ctypes.POINTER(_c_vp)]),
     "dlx_fft_plan_destroy": (_c_int, [_c_vp]),
     "dlx_fft_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),

@@ -94,6 +94,23 @@ int dlx_mft_forward(dlx_mft_plan plan, const void* in_c64, void* out_c64, void* 
 /* Adjoint (vector-Jacobian product) of dlx_mft_forward: gin = MFT^H(gout). */
 int dlx_mft_adjoint(dlx_mft_plan plan, const void* gout_c64, void* gin_c64, void* stream);
 
+/* The batched MFT of dlx_mft_forward (FP32 form) for callers that may not
+ * allocate device memory -- e.g. a JAX/XLA custom call, where XLA has already
+ * preallocated most of the GPU for its own pool, or a loop that forbids
+ * allocation after start-up. No counterpart in the reference (dLux allocates
+ * through XLA). Needs no plan: the DFT matrices and the intermediate field
+ * live in a fixed 8 MiB device array inside the library, so
+ * 3 * n_in * n_out * 8 bytes must fit (n_in = n_out = 512 does); larger sizes
+ * return DLX_ERR_SHAPE. The caller passes input [batch][n_in][n_in] and
+ * output [batch][n_out][n_out] complex64 device buffers. All calls share the
+ * array: calls that can overlap on the GPU (unordered streams) race. The first
+ * call on a device looks the array up (cudaGetSymbolAddress); make it before
+ * any stream capture. */
+int dlx_mft_forward_noalloc(const void* in_c64, int batch, int n_in, double pixel_scale_in,
+                            int n_out, double pixel_scale_out, const double* wavelengths_host,
+                            double focal_length, double shift_x, double shift_y, int inverse,
+                            void* out_c64, void* stream);
+
 /* ---- a4: FFT propagation -------------------------------------------------
  * Replaces dLux utils/propagation.py:8-64 (FFT) together with the optional
  * input/output phase ramps of wavefronts.py:654-727 (propagate_FFT) and
