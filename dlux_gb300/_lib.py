@@ -60,6 +60,16 @@ class PolyDesc(ctypes.Structure):
     ]
 
 
+class PolyObject(ctypes.Structure):
+    """dlx_poly_object: one request or source of a batched PSF evaluation."""
+    _fields_ = [
+        ("amp", _c_vp), ("amp_scale", _c_vp), ("opd", _c_vp), ("phase", _c_vp),
+        ("weights", _c_vp), ("tilt_x", _c_dbl), ("tilt_y", _c_dbl), ("psf", _c_vp),
+        ("g_psf", _c_vp), ("g_amp", _c_vp), ("g_opd", _c_vp), ("g_phase", _c_vp),
+        ("g_w", _c_vp), ("g_tilt", _c_vp),
+    ]
+
+
 _SIGNATURES = {
     "dlx_last_error": (ctypes.c_char_p, []),
     "dlx_version": (_c_int, []),
@@ -92,6 +102,11 @@ _SIGNATURES = {
     "dlx_downsample_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp,
                                          _c_vp, _c_vp]),
     "dlx_poly_plan_create": (_c_int, [ctypes.POINTER(PolyDesc), _c_vp, ctypes.POINTER(_c_vp)]),
+    "dlx_poly_plan_create_batched": (_c_int, [ctypes.POINTER(PolyDesc), _c_vp, _c_int,
+                                              ctypes.POINTER(_c_vp)]),
+    "dlx_poly_forward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_int, _c_vp]),
+    "dlx_poly_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
+    "dlx_poly_backward_sum": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_poly_plan_destroy": (_c_int, [_c_vp]),
     "dlx_poly_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "dlx_poly_psf": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl, _c_dbl, _c_vp,

@@ -93,6 +93,62 @@ def poly_psf(plan, amp, opd, phase, weights, normalise=False, tilt=None):
     return PolyPSF.apply(plan, bool(normalise), amp, opd, phase, weights, tilt)
 
 
+class PolySources(torch.autograd.Function):
+    """Summed PSF of many point sources sharing one pupil (sources.py:392-411).
+
+    Each source is an object of a batched plan: its own tilt (position) and
+    spectral weights (spectrum x flux); the DFT operands of every wavelength
+    are shared, so one launch covers wavelengths x sources.
+    """
+
+    @staticmethod
+    def forward(ctx, plan, normalise, base_tilt, amp, opd, phase, weights, positions):
+        amp_scale = kernels.amp_norm(amp.detach()) if (normalise and amp is not None) else None
+        w = weights.detach().contiguous()
+        pos = positions.detach().to(torch.float64).cpu()
+        tilts = [(float(pos[s, 0]) + base_tilt[0], float(pos[s, 1]) + base_tilt[1])
+                 for s in range(pos.shape[0])]
+        ctx.plan, ctx.normalise, ctx.tilts = plan, normalise, tilts
+        ctx.pos_device = positions.device
+        ctx.save_for_backward(amp, opd, phase, weights, amp_scale)
+        out = torch.empty((plan.n_out, plan.n_out), dtype=torch.float32, device=w.device)
+        objs = [dict(amp=_d(amp), amp_scale=amp_scale, opd=_d(opd), phase=_d(phase), weights=w[s],
+                     tilt=tilts[s]) for s in range(len(tilts))]
+        plan.forward_objects(objs, psf_sum=out)
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        amp, opd, phase, weights, amp_scale = ctx.saved_tensors
+        plan = ctx.plan
+        S = len(ctx.tilts)
+        n, dev = plan.n_in, g.device
+        g = g.contiguous()
+        want_amp = ctx.needs_input_grad[3] and amp is not None
+        want_opd = ctx.needs_input_grad[4] and opd is not None
+        want_ph = ctx.needs_input_grad[5] and phase is not None
+        g_amp = torch.empty((n, n), device=dev) if want_amp else None
+        g_opd = torch.empty((n, n), device=dev) if want_opd else None
+        g_ph = torch.empty((n, n), device=dev) if want_ph else None
+        g_w = torch.empty_like(weights, dtype=torch.float32) if ctx.needs_input_grad[6] else None
+        g_t = torch.empty((S, 2), device=dev) if ctx.needs_input_grad[7] else None
+        w = weights.detach().contiguous()
+        objs = [dict(amp=_d(amp), amp_scale=amp_scale, opd=_d(opd), phase=_d(phase), weights=w[s],
+                     tilt=ctx.tilts[s], g_psf=g, g_w=None if g_w is None else g_w[s],
+                     g_tilt=None if g_t is None else g_t[s]) for s in range(S)]
+        plan.backward_objects(objs, sum_grads={"amp": g_amp, "opd": g_opd, "phase": g_ph})
+        if g_amp is not None and ctx.normalise:
+            g_amp = kernels.amp_norm_backward(amp.detach(), g_amp)
+        g_pos = None if g_t is None else g_t.to(device=ctx.pos_device, dtype=torch.float64)
+        return None, None, None, g_amp, g_opd, g_ph, g_w, g_pos
+
+
+def poly_sources(plan, amp, opd, phase, weights, positions, normalise=False, base_tilt=(0.0, 0.0)):
+    """Summed PSF of sources at ``positions`` [S, 2] (radians) with weights [S, L]."""
+    return PolySources.apply(plan, bool(normalise), (float(base_tilt[0]), float(base_tilt[1])),
+                             amp, opd, phase, weights, positions)
+
+
 class LinearTransform(torch.autograd.Function):
     """A cached MFT or FFT plan applied to complex64 fields; backward is the adjoint."""
 

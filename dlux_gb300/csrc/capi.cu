@@ -10,6 +10,7 @@
 // where Ax[x][u] is dLux's transfer_matrix (utils/propagation.py:67-127) and
 // AxT its transpose. Every GEMM is "D = A * B^T" with both operands
 // K-contiguous, so all stores are row-major and coalesced.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -139,10 +140,30 @@ struct TwoStep {
   size_t elem_bytes() const { return variant == DLX_VARIANT_SPLIT_BF16 ? 8 : 8; }
   size_t mat_bytes() const { return (size_t)batch * n_in * n_out * elem_bytes(); }
 
+  // The tensor-core form streams cached split DFT matrices through TMA. With
+  // DLX_TC_GEN_A=1 in the environment at plan creation it instead builds the
+  // DFT operand inside the GEMM from `axes` (no cached matrices, half the
+  // operand bytes; measured slower at 512^3, 0.52 vs 0.36 ms per launch).
+  bool gen_a = false;
+  DevBuf axes;                 // DftAxis [2][b]: x axes then y axes (kept on the device)
+
+  struct AOp {
+    const void* mat;
+    const DftAxis* axes;
+    bool rows_out;
+  };
+  AOp opATx() const { return {atx.p, axes.as<DftAxis>(), true}; }
+  AOp opANx() const { return {anx.p, axes.as<DftAxis>(), false}; }
+  AOp opATy() const { return {ATy(), axes.as<DftAxis>() + (shared_xy ? 0 : batch), true}; }
+  AOp opANy() const { return {ANy(), axes.as<DftAxis>() + (shared_xy ? 0 : batch), false}; }
+
   int build(const std::vector<DftAxis>& ax_x, const std::vector<DftAxis>& ax_y,
             const std::vector<float>& alphas) {
     shared_xy = std::memcmp(ax_x.data(), ax_y.data(), sizeof(DftAxis) * batch) == 0;
-    DevBuf axes;
+    if (variant == DLX_VARIANT_SPLIT_BF16) {
+      const char* env = getenv("DLX_TC_GEN_A");
+      gen_a = env && env[0] == '1';
+    }
     DLX_TRY(axes.alloc(sizeof(DftAxis) * batch * 2));
     int st = DLX_OK;
     do {
@@ -152,24 +173,26 @@ struct TwoStep {
         e = cudaMemcpy(axes.as<DftAxis>() + batch, ax_y.data(), sizeof(DftAxis) * batch,
                        cudaMemcpyHostToDevice);
       if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(axes)"); break; }
-      if ((st = atx.alloc(mat_bytes())) != DLX_OK) break;
-      if ((st = anx.alloc(mat_bytes())) != DLX_OK) break;
-      if (!shared_xy) {
-        if ((st = aty.alloc(mat_bytes())) != DLX_OK) break;
-        if ((st = any.alloc(mat_bytes())) != DLX_OK) break;
-      }
-      const bool split = variant == DLX_VARIANT_SPLIT_BF16;
-      auto gen = [&](DevBuf& buf, const DftAxis* ax, bool t_layout) {
-        const int rows = t_layout ? n_out : n_in, cols = t_layout ? n_in : n_out;
-        return launch_dft_gen(ax, batch, rows, cols, t_layout, split ? nullptr : buf.as<float2>(),
-                              (long long)rows * cols, split ? buf.as<__nv_bfloat16>() : nullptr,
-                              0);
-      };
-      if ((st = gen(atx, axes.as<DftAxis>(), true)) != DLX_OK) break;
-      if ((st = gen(anx, axes.as<DftAxis>(), false)) != DLX_OK) break;
-      if (!shared_xy) {
-        if ((st = gen(aty, axes.as<DftAxis>() + batch, true)) != DLX_OK) break;
-        if ((st = gen(any, axes.as<DftAxis>() + batch, false)) != DLX_OK) break;
+      if (!gen_a) {
+        if ((st = atx.alloc(mat_bytes())) != DLX_OK) break;
+        if ((st = anx.alloc(mat_bytes())) != DLX_OK) break;
+        if (!shared_xy) {
+          if ((st = aty.alloc(mat_bytes())) != DLX_OK) break;
+          if ((st = any.alloc(mat_bytes())) != DLX_OK) break;
+        }
+        const bool split = variant == DLX_VARIANT_SPLIT_BF16;
+        auto gen = [&](DevBuf& buf, const DftAxis* ax, bool t_layout) {
+          const int rows = t_layout ? n_out : n_in, cols = t_layout ? n_in : n_out;
+          return launch_dft_gen(ax, batch, rows, cols, t_layout,
+                                split ? nullptr : buf.as<float2>(), (long long)rows * cols,
+                                split ? buf.as<__nv_bfloat16>() : nullptr, 0);
+        };
+        if ((st = gen(atx, axes.as<DftAxis>(), true)) != DLX_OK) break;
+        if ((st = gen(anx, axes.as<DftAxis>(), false)) != DLX_OK) break;
+        if (!shared_xy) {
+          if ((st = gen(aty, axes.as<DftAxis>() + batch, true)) != DLX_OK) break;
+          if ((st = gen(any, axes.as<DftAxis>() + batch, false)) != DLX_OK) break;
+        }
       }
       if ((st = alpha.alloc(sizeof(float) * batch)) != DLX_OK) break;
       e = cudaMemcpy(alpha.p, alphas.data(), sizeof(float) * batch, cudaMemcpyHostToDevice);
@@ -197,7 +220,6 @@ struct TwoStep {
       e = cudaDeviceSynchronize();
       if (e != cudaSuccess) { st = check_cuda(e, "transfer-matrix generation"); break; }
     } while (0);
-    axes.release();
     return st;
   }
   const void* ATy() const { return shared_xy ? atx.p : aty.p; }
@@ -205,11 +227,11 @@ struct TwoStep {
   void release() {
     atx.release(); aty.release(); anx.release(); any.release();
     alpha.release(); inv_lambda.release(); kvec.release(); inv_lambda_ff.release();
+    axes.release();
   }
   size_t footprint() const {
     return atx.bytes + aty.bytes + anx.bytes + any.bytes + alpha.bytes + inv_lambda.bytes +
-           inv_lambda_ff.bytes +
-           kvec.bytes;
+           inv_lambda_ff.bytes + kvec.bytes + axes.bytes;
   }
 };
 
@@ -283,10 +305,17 @@ GemmArgs gemm_split(int batch, int M, int N, int K, const void* A, bool conj_a, 
   return g;
 }
 
-GemmArgs gemm_for(int variant, int batch, int M, int N, int K, const void* A, bool conj_a,
-                  const void* B, const EpiArgs& epi) {
-  return variant == DLX_VARIANT_SPLIT_BF16 ? gemm_split(batch, M, N, K, A, conj_a, B, epi)
-                                           : gemm_c64(batch, M, N, K, A, conj_a, B, epi);
+// A is a cached DFT matrix of the plan (op.mat) or, in the tensor-core form
+// with generated operands, its axis description (op.axes).
+GemmArgs gemm_for(int variant, int batch, int M, int N, int K, const TwoStep::AOp& op,
+                  bool conj_a, const void* B, const EpiArgs& epi) {
+  if (variant != DLX_VARIANT_SPLIT_BF16) return gemm_c64(batch, M, N, K, op.mat, conj_a, B, epi);
+  GemmArgs g = gemm_split(batch, M, N, K, op.mat, conj_a, B, epi);
+  if (!op.mat) {
+    g.a_axes = op.axes;
+    g.a_rows_are_out = op.rows_out;
+  }
+  return g;
 }
 
 EpiArgs epi_store(int variant, void* out, const float* alpha) {
@@ -342,10 +371,10 @@ struct TwoStepPlan {
       field = in_split.p;
     }
     // D1[u][y] = sum_x AxT[u][x] E[y][x]
-    DLX_TRY(run_gemm(v, gemm_for(v, B, M, N, N, ts.atx.p, false, field,
+    DLX_TRY(run_gemm(v, gemm_for(v, B, M, N, N, ts.opATx(), false, field,
                                  epi_store(v, mid.p, nullptr)), s));
     // F[v][u] = alpha sum_y AyT[v][y] D1[u][y]
-    DLX_TRY(run_gemm(v, gemm_for(v, B, M, M, N, ts.ATy(), false, mid.p,
+    DLX_TRY(run_gemm(v, gemm_for(v, B, M, M, N, ts.opATy(), false, mid.p,
                                  epi_c64(out, ts.alpha.as<float>())), s));
     return DLX_OK;
   }
@@ -359,10 +388,10 @@ struct TwoStepPlan {
       g = gout_split.p;
     }
     // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
-    DLX_TRY(run_gemm(v, gemm_for(v, B, N, M, M, ts.anx.p, true, g,
+    DLX_TRY(run_gemm(v, gemm_for(v, B, N, M, M, ts.opANx(), true, g,
                                  epi_store(v, mid.p, nullptr)), s));
     // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v]
-    DLX_TRY(run_gemm(v, gemm_for(v, B, N, N, M, ts.ANy(), true, mid.p,
+    DLX_TRY(run_gemm(v, gemm_for(v, B, N, N, M, ts.opANy(), true, mid.p,
                                  epi_c64(gin, ts.alpha.as<float>())), s));
     return DLX_OK;
   }
@@ -686,17 +715,23 @@ int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
-// Fused polychromatic PSF plan.
+// Fused polychromatic PSF plan over a batch of objects.
+//
+// A plan serves up to max_objects independent objects (requests or point
+// sources) per launch. Batch element b = l * R + r holds wavelength l of
+// object r, so the per-wavelength DFT operands are shared (A index = b / R).
+// Larger object counts run in chunks of max_objects.
 // ---------------------------------------------------------------------------
 struct dlx_poly_plan_s {
   TwoStep ts;
   double pixel_scale_in = 0;
-  DevBuf field;      // E: [L][N][N] c64 or [L][4][N][N] split
-  DevBuf mid;        // D1 [L][M][N] / Xt [L][N][M]
-  DevBuf fbar;       // [L][M][M] c64 or split
-  DevBuf planes;     // intensity [L][M][M] f32, or pre/pim [2][L][N][N] f32
+  int max_obj = 1;
+  DevBuf field;      // E: [L*R][N][N] c64 or [L*R][4][N][N] split
+  DevBuf mid;        // D1 [L*R][M][N] / Xt [L*R][N][M]
+  DevBuf fbar;       // [L*R][M][M] c64 or split
+  DevBuf planes;     // intensity [L*R][M][M] f32, or pre/pim [2][L*R][N][N] f32
   DevBuf partial;    // double reduction partials
-  int nparts = 64;
+  int nparts = 1024; // pixel chunks of the reverse reductions (enough blocks to fill the GPU)
 
   size_t footprint() const {
     return ts.footprint() + field.bytes + mid.bytes + fbar.bytes + planes.bytes + partial.bytes;
@@ -705,28 +740,136 @@ struct dlx_poly_plan_s {
     ts.release(); field.release(); mid.release(); fbar.release(); planes.release();
     partial.release();
   }
-  int build_field(const float* amp, const float* amp_scale, const float* opd,
-                  const float* phase, const float* weights, double tx, double ty,
-                  cudaStream_t s) {
+
+  static void tables(const dlx_poly_object* objs, int n, ObjTable* t, OutTable* o) {
+    *t = ObjTable{};
+    *o = OutTable{};
+    t->n = n;
+    o->n = n;
+    for (int r = 0; r < n; ++r) {
+      const dlx_poly_object& q = objs[r];
+      t->o[r] = ObjDesc{q.amp, q.amp_scale, q.opd, q.phase, q.weights, q.g_psf, q.tilt_x,
+                        q.tilt_y};
+      o->o[r] = ObjOut{q.psf, q.g_amp, q.g_opd, q.g_phase, q.g_w, q.g_tilt};
+    }
+  }
+
+  int build_field(const ObjTable& t, cudaStream_t s) {
     PhasorArgs a{};
-    a.amp = amp; a.amp_scale = amp_scale; a.opd = opd; a.phase = phase; a.weights = weights;
+    a.objs = t;
     a.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
     a.const_scale = 1.0;
-    a.batch = ts.batch; a.n = ts.n_in;
-    a.pixel_scale = pixel_scale_in; a.tilt_x = tx; a.tilt_y = ty;
+    a.batch = ts.batch * t.n;
+    a.n = ts.n_in;
+    a.pixel_scale = pixel_scale_in;
     if (ts.variant == DLX_VARIANT_SPLIT_BF16) a.out_split = field.as<__nv_bfloat16>();
     else a.out_c64 = field.as<float2>();
     return launch_phasor(a, nullptr, s);
   }
+
+  GemmArgs gemm(const TwoStep::AOp& op, int R, int M, int N, int K, bool conj, const void* B,
+                const EpiArgs& e) const {
+    GemmArgs g = gemm_for(ts.variant, ts.batch * R, M, N, K, op, conj, B, e);
+    g.a_batch_div = R;
+    g.a_bs = (long long)M * K;
+    return g;
+  }
+
+  int forward_chunk(const dlx_poly_object* objs, int R, float* psf_sum, int accumulate,
+                    cudaStream_t s) {
+    const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    ObjTable t;
+    OutTable o;
+    tables(objs, R, &t, &o);
+    DLX_TRY(build_field(t, s));
+    EpiArgs e1 = epi_store(v, mid.p, nullptr);
+    e1.objs = t;
+    DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
+    EpiArgs e{};
+    e.kind = EPI_INTENSITY;
+    e.objs = t;
+    e.alpha = ts.alpha.as<float>();
+    e.out_f32 = planes.as<float>();
+    DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, e), s));
+    ObjReduceArgs ra{};
+    ra.objs = t;
+    ra.outs = o;
+    ra.L = L;
+    ra.npix = (long long)M * M;
+    ra.planes = planes.as<float>();
+    ra.psf_sum = psf_sum;
+    ra.accumulate = accumulate;
+    return launch_obj_psf_reduce(ra, s);
+  }
+
+  int backward_chunk(const dlx_poly_object* objs, int R, cudaStream_t s, float* sum_amp = nullptr,
+                     float* sum_opd = nullptr, float* sum_phase = nullptr,
+                     bool sum_pixels = false, bool accumulate_sum = false) {
+    const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    ObjTable t;
+    OutTable o;
+    tables(objs, R, &t, &o);
+    for (int r = 0; r < R; ++r)
+      if (!t.o[r].G) return fail(DLX_ERR_ARG, "poly backward: every object needs g_psf");
+    // Recompute the forward fields (nothing is stored between the passes).
+    DLX_TRY(build_field(t, s));
+    EpiArgs e1 = epi_store(v, mid.p, nullptr);
+    e1.objs = t;
+    DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
+    // Fbar[v][u] = 2 alpha G[v][u] D[v][u]
+    EpiArgs eg{};
+    eg.kind = EPI_GRADF;
+    eg.objs = t;
+    eg.alpha = ts.alpha.as<float>();
+    if (v == DLX_VARIANT_SPLIT_BF16) eg.out_split = fbar.as<__nv_bfloat16>();
+    else eg.out_c64 = fbar.as<float2>();
+    DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, eg), s));
+    // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
+    EpiArgs e3 = epi_store(v, mid.p, nullptr);
+    e3.objs = t;
+    DLX_TRY(run_gemm(v, gemm(ts.opANx(), R, N, M, M, true, fbar.p, e3), s));
+    // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v] -> pupil-gradient planes
+    float* pre = planes.as<float>();
+    float* pim = pre + (size_t)L * R * N * N;
+    EpiArgs ep{};
+    ep.kind = EPI_PUPIL;
+    ep.objs = t;
+    ep.alpha = ts.alpha.as<float>();
+    ep.out_f32 = pre;
+    ep.out_f32b = pim;
+    ep.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
+    ep.pixel_scale = pixel_scale_in;
+    DLX_TRY(run_gemm(v, gemm(ts.opANy(), R, N, N, M, true, mid.p, ep), s));
+    ObjReduceArgs ra{};
+    ra.objs = t;
+    ra.outs = o;
+    ra.L = L;
+    ra.npix = (long long)N * N;
+    ra.pre = pre;
+    ra.pim = pim;
+    ra.k_dev = ts.kvec.as<double>();
+    ra.n_side = N;
+    ra.pixel_scale = pixel_scale_in;
+    ra.partial_ws = partial.as<double>();
+    ra.nparts = nparts;
+    ra.sum_pixels = sum_pixels ? 1 : 0;
+    ra.sum_g_amp = sum_amp;
+    ra.sum_g_opd = sum_opd;
+    ra.sum_g_phase = sum_phase;
+    ra.accumulate_sum = accumulate_sum ? 1 : 0;
+    return launch_obj_pupil_reduce(ra, s);
+  }
 };
 
-extern "C" {
-
-int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan* plan) {
+static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects,
+                       dlx_poly_plan* plan) {
   if (!d || !wl || !plan) return fail(DLX_ERR_ARG, "poly_plan_create: null pointer");
   *plan = nullptr;
   if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0)
     return fail(DLX_ERR_SHAPE, "poly_plan_create: sizes must be positive");
+  if (max_objects <= 0 || max_objects > kMaxObj)
+    return fail(DLX_ERR_ARG, "poly_plan_create: max_objects must lie in [1, " +
+                                 std::to_string(kMaxObj) + "]");
   if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
     return fail(DLX_ERR_ARG, "poly_plan_create: pixel scales must be positive");
   DLX_TRY(validate_variant(d->variant));
@@ -738,6 +881,7 @@ int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan
   ts.batch = L; ts.n_in = N; ts.n_out = M; ts.variant = d->variant;
   ts.wl.assign(wl, wl + L);
   p->pixel_scale_in = d->pixel_scale_in;
+  p->max_obj = max_objects;
   std::vector<DftAxis> ax(L);
   std::vector<float> alphas(L);
   for (int b = 0; b < L; ++b) {
@@ -751,15 +895,16 @@ int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan
                                  d->focal_length);
   }
   int st = ts.build(ax, ax, alphas);
-  const size_t l = L, n = N, m = M;
-  if (st == DLX_OK) st = p->field.alloc(l * n * n * 8);
-  if (st == DLX_OK) st = p->mid.alloc(l * n * m * 8);
-  if (st == DLX_OK) st = p->fbar.alloc(l * m * m * 8);
+  const size_t lr = (size_t)L * max_objects, n = N, m = M;
+  if (st == DLX_OK) st = p->field.alloc(lr * n * n * 8);
+  if (st == DLX_OK) st = p->mid.alloc(lr * n * m * 8);
+  if (st == DLX_OK) st = p->fbar.alloc(lr * m * m * 8);
   if (st == DLX_OK) {
-    const size_t a = l * m * m * 4, b = 2 * l * n * n * 4;
+    const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
     st = p->planes.alloc(a > b ? a : b);
   }
-  if (st == DLX_OK) st = p->partial.alloc(sizeof(double) * (size_t)p->nparts * (L + 2));
+  if (st == DLX_OK)
+    st = p->partial.alloc(sizeof(double) * (size_t)p->nparts * max_objects * (L + 2));
   if (st != DLX_OK) {
     p->release();
     delete p;
@@ -767,6 +912,17 @@ int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan
   }
   *plan = p;
   return DLX_OK;
+}
+
+extern "C" {
+
+int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan* plan) {
+  return poly_create(d, wl, 1, plan);
+}
+
+int dlx_poly_plan_create_batched(const dlx_poly_desc* d, const double* wl, int max_objects,
+                                 dlx_poly_plan* plan) {
+  return poly_create(d, wl, max_objects, plan);
 }
 
 int dlx_poly_plan_destroy(dlx_poly_plan plan) {
@@ -783,22 +939,52 @@ int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes) {
   return DLX_OK;
 }
 
+int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                     float* psf_sum, int accumulate, void* stream) {
+  if (!plan || (n_objects > 0 && !objs)) return fail(DLX_ERR_ARG, "poly_forward: null pointer");
+  if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_forward: negative object count");
+  cudaStream_t s = as_stream(stream);
+  for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
+    const int R = std::min(plan->max_obj, n_objects - o0);
+    DLX_TRY(plan->forward_chunk(objs + o0, R, psf_sum, (o0 > 0) ? 1 : accumulate, s));
+  }
+  return DLX_OK;
+}
+
+int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                      void* stream) {
+  if (!plan || (n_objects > 0 && !objs)) return fail(DLX_ERR_ARG, "poly_backward: null pointer");
+  if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_backward: negative object count");
+  cudaStream_t s = as_stream(stream);
+  for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
+    const int R = std::min(plan->max_obj, n_objects - o0);
+    DLX_TRY(plan->backward_chunk(objs + o0, R, s));
+  }
+  return DLX_OK;
+}
+
+int dlx_poly_backward_sum(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                          float* g_amp, float* g_opd, float* g_phase, void* stream) {
+  if (!plan || (n_objects > 0 && !objs))
+    return fail(DLX_ERR_ARG, "poly_backward_sum: null pointer");
+  if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_backward_sum: negative object count");
+  cudaStream_t s = as_stream(stream);
+  for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
+    const int R = std::min(plan->max_obj, n_objects - o0);
+    DLX_TRY(plan->backward_chunk(objs + o0, R, s, g_amp, g_opd, g_phase, true, o0 > 0));
+  }
+  return DLX_OK;
+}
+
 int dlx_poly_psf(dlx_poly_plan plan, const float* amp, const float* amp_scale, const float* opd,
                  const float* phase, const float* weights, double tilt_x, double tilt_y,
                  float* psf_out, void* stream) {
   if (!plan || !psf_out) return fail(DLX_ERR_ARG, "poly_psf: null pointer");
-  cudaStream_t s = as_stream(stream);
-  dlx_poly_plan_s& p = *plan;
-  const int L = p.ts.batch, N = p.ts.n_in, M = p.ts.n_out, v = p.ts.variant;
-  DLX_TRY(p.build_field(amp, amp_scale, opd, phase, weights, tilt_x, tilt_y, s));
-  DLX_TRY(run_gemm(v, gemm_for(v, L, M, N, N, p.ts.atx.p, false, p.field.p,
-                               epi_store(v, p.mid.p, nullptr)), s));
-  EpiArgs e{};
-  e.kind = EPI_INTENSITY;
-  e.alpha = p.ts.alpha.as<float>();
-  e.out_f32 = p.planes.as<float>();
-  DLX_TRY(run_gemm(v, gemm_for(v, L, M, M, N, p.ts.ATy(), false, p.mid.p, e), s));
-  return launch_plane_sum(p.planes.as<float>(), L, (long long)M * M, psf_out, s);
+  dlx_poly_object o{};
+  o.amp = amp; o.amp_scale = amp_scale; o.opd = opd; o.phase = phase; o.weights = weights;
+  o.tilt_x = tilt_x; o.tilt_y = tilt_y;
+  o.psf = psf_out;
+  return dlx_poly_forward(plan, &o, 1, nullptr, 0, stream);
 }
 
 int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_scale,
@@ -806,45 +992,13 @@ int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_sca
                       double tilt_y, const float* g_psf, float* g_amp, float* g_opd,
                       float* g_phase, float* g_w, void* stream) {
   if (!plan || !g_psf) return fail(DLX_ERR_ARG, "poly_psf_grad: null pointer");
-  cudaStream_t s = as_stream(stream);
-  dlx_poly_plan_s& p = *plan;
-  const int L = p.ts.batch, N = p.ts.n_in, M = p.ts.n_out, v = p.ts.variant;
-  // Recompute the forward fields (nothing is stored between the passes).
-  DLX_TRY(p.build_field(amp, amp_scale, opd, phase, weights, tilt_x, tilt_y, s));
-  DLX_TRY(run_gemm(v, gemm_for(v, L, M, N, N, p.ts.atx.p, false, p.field.p,
-                               epi_store(v, p.mid.p, nullptr)), s));
-  // Fbar[v][u] = 2 alpha G[v][u] D[v][u]
-  EpiArgs eg{};
-  eg.kind = EPI_GRADF;
-  eg.alpha = p.ts.alpha.as<float>();
-  eg.G = g_psf;
-  if (v == DLX_VARIANT_SPLIT_BF16) eg.out_split = p.fbar.as<__nv_bfloat16>();
-  else eg.out_c64 = p.fbar.as<float2>();
-  DLX_TRY(run_gemm(v, gemm_for(v, L, M, M, N, p.ts.ATy(), false, p.mid.p, eg), s));
-  // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
-  DLX_TRY(run_gemm(v, gemm_for(v, L, N, M, M, p.ts.anx.p, true, p.fbar.p,
-                               epi_store(v, p.mid.p, nullptr)), s));
-  // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v] -> pupil-gradient planes
-  float* pre = p.planes.as<float>();
-  float* pim = pre + (size_t)L * N * N;
-  EpiArgs ep{};
-  ep.kind = EPI_PUPIL;
-  ep.alpha = p.ts.alpha.as<float>();
-  ep.out_f32 = pre;
-  ep.out_f32b = pim;
-  ep.amp = amp; ep.amp_scale = amp_scale; ep.opd = opd; ep.phase = phase; ep.weights = weights;
-  ep.inv_lambda_ff = p.ts.inv_lambda_ff.as<float2>();
-  ep.pixel_scale = p.pixel_scale_in; ep.tilt_x = tilt_x; ep.tilt_y = tilt_y;
-  DLX_TRY(run_gemm(v, gemm_for(v, L, N, N, M, p.ts.ANy(), true, p.mid.p, ep), s));
-  PupilReduceArgs r{};
-  r.pre = pre; r.pim = pim; r.amp = amp; r.amp_scale = amp_scale; r.weights = weights;
-  r.k_dev = p.ts.kvec.as<double>();
-  r.batch = L; r.npix = (long long)N * N;
-  r.g_amp = g_amp; r.g_opd = g_opd; r.g_phase = g_phase;
-  r.g_w = weights ? g_w : nullptr;
-  r.partial_ws = p.partial.as<double>();
-  r.nparts = p.nparts;
-  return launch_pupil_reduce(r, s);
+  dlx_poly_object o{};
+  o.amp = amp; o.amp_scale = amp_scale; o.opd = opd; o.phase = phase; o.weights = weights;
+  o.tilt_x = tilt_x; o.tilt_y = tilt_y;
+  o.g_psf = g_psf;
+  o.g_amp = g_amp; o.g_opd = g_opd; o.g_phase = g_phase;
+  o.g_w = weights ? g_w : nullptr;
+  return dlx_poly_backward(plan, &o, 1, stream);
 }
 
 }  // extern "C"

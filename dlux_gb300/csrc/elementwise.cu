@@ -68,33 +68,48 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
   if (p >= npix) return;
   const int y = (int)(p / a.n);
   const int x = (int)(p - (long long)y * a.n);
-  // Per pixel, once: optical path (m) and phase (cycles) in FP64, kept as float pairs.
   const double half = 0.5 * (a.n - 1);
   const double X = ((double)x - half) * a.pixel_scale;
   const double Y = ((double)y - half) * a.pixel_scale;
-  const FF path = ff_from_double((a.opd ? (double)a.opd[p] : 0.0) + a.tilt_x * X + a.tilt_y * Y);
-  const FF ph_cyc = ff_from_double(a.phase ? (double)a.phase[p] * (0.5 / CUDART_PI) : 0.0);
-  float amp = a.amp ? a.amp[p] : 1.0f;
-  if (a.amp_scale) amp *= *a.amp_scale;
-  amp *= (float)a.const_scale;
-  for (int b = 0; b < a.batch; ++b) {
-    const float2 il2 = a.inv_lambda_ff ? a.inv_lambda_ff[b] : inv_lambda_arg.v[b];
-    float2 u = cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
-    float sc = amp;
-    if (a.weights) sc *= sqrtf(a.weights[b]);
-    float2 v = make_float2(u.x * sc, u.y * sc);
-    const long long o = (long long)b * npix + p;
-    if (a.in) v = cmul(a.in[o], v);
-    if (a.out_c64) a.out_c64[o] = v;
-    if (a.out_split) {
-      __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p;
-      __nv_bfloat16 h, l;
-      split_bf16(v.x, h, l);
-      base[0] = h;
-      base[npix] = l;
-      split_bf16(v.y, h, l);
-      base[2 * npix] = h;
-      base[3 * npix] = l;
+  // Objects r of a batched plan (b = l * R + r), or one object described by
+  // the plain fields of PhasorArgs.
+  const int R = a.objs.n > 0 ? a.objs.n : 1;
+  const int L = a.batch / R;
+  for (int r = 0; r < R; ++r) {
+    const bool obj = a.objs.n > 0;
+    const float* o_amp = obj ? a.objs.o[r].amp : a.amp;
+    const float* o_scale = obj ? a.objs.o[r].amp_scale : a.amp_scale;
+    const float* o_opd = obj ? a.objs.o[r].opd : a.opd;
+    const float* o_phase = obj ? a.objs.o[r].phase : a.phase;
+    const float* o_w = obj ? a.objs.o[r].weights : a.weights;
+    const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
+    const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
+    // Per pixel and object, once: optical path (m) and phase (cycles) in FP64, as float pairs.
+    const FF path = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
+    const FF ph_cyc = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+    float amp = o_amp ? o_amp[p] : 1.0f;
+    if (o_scale) amp *= *o_scale;
+    amp *= (float)a.const_scale;
+    for (int wl = 0; wl < L; ++wl) {
+      const int b = wl * R + r;
+      const float2 il2 = a.inv_lambda_ff ? a.inv_lambda_ff[wl] : inv_lambda_arg.v[wl];
+      float2 u = cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
+      float sc = amp;
+      if (o_w) sc *= sqrtf(o_w[wl]);
+      float2 v = make_float2(u.x * sc, u.y * sc);
+      const long long o = (long long)b * npix + p;
+      if (a.in) v = cmul(a.in[o], v);
+      if (a.out_c64) a.out_c64[o] = v;
+      if (a.out_split) {
+        __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p;
+        __nv_bfloat16 h, lo;
+        split_bf16(v.x, h, lo);
+        base[0] = h;
+        base[npix] = lo;
+        split_bf16(v.y, h, lo);
+        base[2 * npix] = h;
+        base[3 * npix] = lo;
+      }
     }
   }
 }
@@ -176,22 +191,6 @@ int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cuda
   if (npix == 0) return DLX_OK;
   psf_sum_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(in, batch, npix, psf);
   DLX_LAUNCH_CHECK("psf_sum_kernel");
-  return DLX_OK;
-}
-
-__global__ void plane_sum_kernel(const float* __restrict__ planes, int batch, long long npix,
-                                 float* __restrict__ out) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npix) return;
-  float acc = 0.f;
-  for (int b = 0; b < batch; ++b) acc += planes[(long long)b * npix + p];
-  out[p] = acc;
-}
-
-int launch_plane_sum(const float* planes, int batch, long long npix, float* out, cudaStream_t s) {
-  if (npix == 0) return DLX_OK;
-  plane_sum_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(planes, batch, npix, out);
-  DLX_LAUNCH_CHECK("plane_sum_kernel");
   return DLX_OK;
 }
 
@@ -436,63 +435,172 @@ int launch_downsample_backward(const float* in, const float* g_out, int n_in, in
 }
 
 // ---------------------------------------------------------------------------
-// Reduction of per-wavelength pupil-gradient planes (reverse of the phasor).
+// Batched-object reductions (b = l * R + r): per-object wavelength sums of the
+// intensity planes and of the pupil-gradient planes, plus the per-object
+// weight and tilt gradients. Fixed summation order, so results are
+// reproducible and independent of which other objects share the batch.
 // ---------------------------------------------------------------------------
-__global__ void pupil_reduce_pix_kernel(PupilReduceArgs a) {
+__global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
-  float sre = 0.f, sim = 0.f, sk = 0.f;
-  for (int b = 0; b < a.batch; ++b) {
-    const long long o = (long long)b * a.npix + p;
-    const float re = a.pre[o], im = a.pim[o];
-    sre += re;
-    sim += im;
-    sk += (float)a.k_dev[b] * im;
+  const int R = a.objs.n;
+  float total = 0.f;
+  for (int r = 0; r < R; ++r) {
+    float s = 0.f;
+    for (int l = 0; l < a.L; ++l) s += a.planes[((long long)l * R + r) * a.npix + p];
+    if (a.outs.o[r].psf) a.outs.o[r].psf[p] = s;
+    total += s;
   }
-  if (a.g_amp) a.g_amp[p] = sre;
-  if (a.g_phase) a.g_phase[p] = sim;
-  if (a.g_opd) a.g_opd[p] = sk;
+  if (a.psf_sum) a.psf_sum[p] = a.accumulate ? a.psf_sum[p] + total : total;
 }
 
-__global__ void pupil_reduce_w_partial_kernel(PupilReduceArgs a) {
+int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s) {
+  if (a.npix == 0 || a.objs.n == 0) return DLX_OK;
+  obj_psf_reduce_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
+  DLX_LAUNCH_CHECK("obj_psf_reduce_kernel");
+  return DLX_OK;
+}
+
+// Pixel gradients summed over every object of the batch (shared pupil).
+__global__ void obj_pupil_sum_kernel(ObjReduceArgs a) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  const int R = a.objs.n;
+  float sre = 0.f, sim = 0.f, sk = 0.f;
+  for (int r = 0; r < R; ++r)
+    for (int l = 0; l < a.L; ++l) {
+      const long long o = ((long long)l * R + r) * a.npix + p;
+      const float im = a.pim[o];
+      sre += a.pre[o];
+      sim += im;
+      sk += (float)a.k_dev[l] * im;
+    }
+  if (a.sum_g_amp) a.sum_g_amp[p] = a.accumulate_sum ? a.sum_g_amp[p] + sre : sre;
+  if (a.sum_g_phase) a.sum_g_phase[p] = a.accumulate_sum ? a.sum_g_phase[p] + sim : sim;
+  if (a.sum_g_opd) a.sum_g_opd[p] = a.accumulate_sum ? a.sum_g_opd[p] + sk : sk;
+}
+
+__global__ void obj_pupil_pix_kernel(ObjReduceArgs a) {
   __shared__ double smem[32];
-  const int b = blockIdx.y;
+  const int r = blockIdx.y;
+  const int R = a.objs.n;
+  ObjOut out = a.outs.o[r];
+  if (a.sum_pixels) out.g_amp = out.g_phase = out.g_opd = nullptr;
+  if (!out.g_amp && !out.g_phase && !out.g_opd && !out.g_tilt) return;  // block-uniform
   const long long chunk = (a.npix + a.nparts - 1) / a.nparts;
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(a.npix, lo + chunk);
-  const float* pre = a.pre + (long long)b * a.npix;
+  const double half = 0.5 * (a.n_side - 1);
+  double tx = 0.0, ty = 0.0;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    float sre = 0.f, sim = 0.f, sk = 0.f;
+    for (int l = 0; l < a.L; ++l) {
+      const long long o = ((long long)l * R + r) * a.npix + p;
+      const float im = a.pim[o];
+      sre += a.pre[o];
+      sim += im;
+      sk += (float)a.k_dev[l] * im;
+    }
+    if (out.g_amp) out.g_amp[p] = sre;
+    if (out.g_phase) out.g_phase[p] = sim;
+    if (out.g_opd) out.g_opd[p] = sk;
+    const int y = (int)(p / a.n_side);
+    const int x = (int)(p - (long long)y * a.n_side);
+    tx += ((double)x - half) * a.pixel_scale * (double)sk;
+    ty += ((double)y - half) * a.pixel_scale * (double)sk;
+  }
+  if (out.g_tilt) {
+    const double sx = block_sum<256>(tx, smem);
+    const double sy = block_sum<256>(ty, smem);
+    if (threadIdx.x == 0) {
+      double* part = a.partial_ws + ((long long)r * a.nparts + blockIdx.x) * 2;
+      part[0] = sx;
+      part[1] = sy;
+    }
+  }
+}
+
+__global__ void obj_w_partial_kernel(ObjReduceArgs a) {
+  __shared__ double smem[32];
+  const int R = a.objs.n;
+  const int r = blockIdx.y % R;
+  const int l = blockIdx.y / R;
+  const ObjDesc& od = a.objs.o[r];
+  const long long chunk = (a.npix + a.nparts - 1) / a.nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(a.npix, lo + chunk);
+  const float* pre = a.pre + ((long long)l * R + r) * a.npix;
   double acc = 0.0;
   for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x)
-    acc += (double)pre[p] * (a.amp ? (double)a.amp[p] : 1.0);
-  double t = block_sum<256>(acc, smem);
-  if (a.amp_scale) t *= (double)*a.amp_scale;
-  if (threadIdx.x == 0) a.partial_ws[(long long)b * a.nparts + blockIdx.x] = t;
+    acc += (double)pre[p] * (od.amp ? (double)od.amp[p] : 1.0);
+  const double t = block_sum<256>(acc, smem);
+  if (threadIdx.x == 0) {
+    double* part = a.partial_ws + (long long)R * a.nparts * 2;
+    part[((long long)r * a.L + l) * a.nparts + blockIdx.x] = t;
+  }
 }
 
-__global__ void pupil_reduce_w_finish_kernel(PupilReduceArgs a) {
+__global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
   __shared__ double smem[32];
-  const int b = blockIdx.x;
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < a.nparts; i += blockDim.x)
-    acc += a.partial_ws[(long long)b * a.nparts + i];
-  double t = block_sum<256>(acc, smem);
-  // d/dw of sqrt(w): pre already carries sqrt(w_b); sum amp*pre = Re<E, Ebar>/1.
-  if (threadIdx.x == 0) a.g_w[b] = (float)(t / (2.0 * (double)a.weights[b]));
+  const int r = blockIdx.x;
+  const int R = a.objs.n;
+  const ObjDesc& od = a.objs.o[r];
+  const ObjOut& out = a.outs.o[r];
+  if (out.g_tilt) {
+    double sx = 0.0, sy = 0.0;
+    for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) {
+      sx += a.partial_ws[((long long)r * a.nparts + i) * 2];
+      sy += a.partial_ws[((long long)r * a.nparts + i) * 2 + 1];
+    }
+    const double tx = block_sum<256>(sx, smem);
+    const double ty = block_sum<256>(sy, smem);
+    if (threadIdx.x == 0) {
+      out.g_tilt[0] = (float)tx;
+      out.g_tilt[1] = (float)ty;
+    }
+  }
+  if (want_w && out.g_w) {
+    const double* part = a.partial_ws + (long long)R * a.nparts * 2;
+    for (int l = 0; l < a.L; ++l) {
+      double acc = 0.0;
+      for (int i = threadIdx.x; i < a.nparts; i += blockDim.x)
+        acc += part[((long long)r * a.L + l) * a.nparts + i];
+      const double t = block_sum<256>(acc, smem);
+      if (threadIdx.x == 0) {
+        double v = t;
+        if (od.amp_scale) v *= (double)*od.amp_scale;
+        const double w = od.weights ? (double)od.weights[l] : 1.0;
+        out.g_w[l] = (float)(v / (2.0 * w));
+      }
+    }
+  }
 }
 
-int launch_pupil_reduce(const PupilReduceArgs& a, cudaStream_t s) {
-  if (a.npix == 0) return DLX_OK;
-  if (a.g_amp || a.g_phase || a.g_opd) {
-    pupil_reduce_pix_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
-    DLX_LAUNCH_CHECK("pupil_reduce_pix_kernel");
+int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s) {
+  const int R = a.objs.n;
+  if (a.npix == 0 || R == 0) return DLX_OK;
+  if (a.sum_pixels) {
+    obj_pupil_sum_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("obj_pupil_sum_kernel");
   }
-  if (a.g_w) {
-    dim3 grid(a.nparts, a.batch);
-    pupil_reduce_w_partial_kernel<<<grid, 256, 0, s>>>(a);
-    DLX_LAUNCH_CHECK("pupil_reduce_w_partial_kernel");
-    pupil_reduce_w_finish_kernel<<<a.batch, 256, 0, s>>>(a);
-    DLX_LAUNCH_CHECK("pupil_reduce_w_finish_kernel");
+  bool per_obj = false;
+  for (int r = 0; r < R; ++r) {
+    const ObjOut& o = a.outs.o[r];
+    per_obj |= o.g_tilt != nullptr ||
+               (!a.sum_pixels && (o.g_amp || o.g_phase || o.g_opd));
   }
+  if (per_obj) {
+    obj_pupil_pix_kernel<<<dim3(a.nparts, R), 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("obj_pupil_pix_kernel");
+  }
+  bool want_w = false;
+  for (int r = 0; r < R; ++r) want_w |= a.outs.o[r].g_w != nullptr;
+  if (want_w) {
+    obj_w_partial_kernel<<<dim3(a.nparts, R * a.L), 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("obj_w_partial_kernel");
+  }
+  obj_finish_kernel<<<R, 256, 0, s>>>(a, want_w ? 1 : 0);
+  DLX_LAUNCH_CHECK("obj_finish_kernel");
   return DLX_OK;
 }
 

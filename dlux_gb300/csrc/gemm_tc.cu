@@ -107,6 +107,16 @@ __device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile 
   }
 }
 
+// Warp-uniform bounded wait: lane 0 polls, the verdict is broadcast, so the
+// whole warp leaves together (required before .sync.aligned tcgen05 ops).
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort_flag, int* status) {
+  int ok = 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag, status) ? 1 : 0;
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  return ok != 0;
+}
+
 __device__ __forceinline__ void fence_barrier_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
@@ -243,7 +253,10 @@ __device__ __forceinline__ void epi_chunk32(const EpiArgs& e, int b, int m, int 
       if (n0 + j < N) epi_apply(e, b, m, n0 + j, M, N, make_float2(re[j], im[j]));
     return;
   }
-  const float a = e.alpha ? e.alpha[b] : 1.0f;
+  const int R = epi_objects(e);
+  const int wl = b / R;
+  const int obj = b - wl * R;
+  const float a = e.alpha ? e.alpha[wl] : 1.0f;
   const long long plane = (long long)M * N;
   const long long row = (long long)m * N + n0;
   switch (e.kind) {
@@ -278,7 +291,8 @@ __device__ __forceinline__ void epi_chunk32(const EpiArgs& e, int b, int m, int 
       break;
     }
     case EPI_GRADF: {
-      const float4* gp = reinterpret_cast<const float4*>(e.G + row);
+      const float* G = e.objs.n > 0 ? e.objs.o[obj].G : e.G;
+      const float4* gp = reinterpret_cast<const float4*>(G + row);
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const float4 g = __ldg(gp + j);
@@ -456,7 +470,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int row = q * 32 + lane;
     uint32_t acc_ph = 0;
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
-      if (!mbar_wait(tfull, acc_ph, abort_flag, p.status)) break;
+      if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
       tc_fence_after();
       const int b = w / (p.mt * p.nt);
       const int r = w - b * p.mt * p.nt;
@@ -484,6 +498,299 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty);
       acc_ph ^= 1u;
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) {
+    __syncwarp();
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// ------------------ generated-A variant (DFT operand built in the CTA) -------
+//
+// Every A operand of the MFT/FFT GEMMs is a DFT matrix whose phase is affine
+// along K for a fixed row: phase(row, k) = theta0(row) + k * delta(row)
+// cycles (DftAxis, FP64 coefficients). Instead of streaming the split matrix
+// from memory, four generator warps build each 128 x 32 A stage in shared
+// memory: one thread per row keeps the 32 step factors cis(t * delta) in
+// registers (computed once per tile), forms cis(theta0 + 32 kb delta) once per
+// stage, and multiplies. Both phases are reduced with the error-free FP32
+// scheme of cis_ff, so every element is within a few FP32 ulps of the cached
+// matrix. Only the field operand B goes through TMA, which halves the bytes
+// per stage and leaves room for a 4-deep B pipeline.
+constexpr int GA_STAGES = 2;
+constexpr int GB_STAGES = 4;
+constexpr int G_A_BYTES = 4 * A_PLANE_BYTES;   // 32 KB
+constexpr int G_B_BYTES = 4 * B_PLANE_BYTES;   // 32 KB
+constexpr int G_SMEM_BYTES = GA_STAGES * G_A_BYTES + GB_STAGES * G_B_BYTES + 1024 + 256;
+constexpr int G_THREADS = 320;  // TMA, MMA, 4 epilogue warps, 4 generator warps
+
+struct TcGenParams {
+  int batch, M, N, K;
+  int a_batch_div;
+  int mt, nt, total;
+  int conj_a;
+  int rows_are_out;
+  const DftAxis* axes;
+  int* status;
+  EpiArgs epi;
+};
+
+// cis(2 pi (n * delta + theta)) for an integer n < 2^24 and float pairs delta,
+// theta; the reduction is exact up to FP32 rounding of the final argument.
+__device__ __forceinline__ float2 cis_affine(float n, FF delta, FF theta) {
+  const float p = n * delta.hi;
+  const float e = fmaf(n, delta.hi, -p);
+  float r = (p - rintf(p)) + theta.hi;
+  r = r + (fmaf(n, delta.lo, e) + theta.lo);
+  r = r - rintf(r);
+  float s, c;
+  sincospif(2.0f * r, &s, &c);
+  return make_float2(c, s);
+}
+
+__global__ void __launch_bounds__(G_THREADS, 1)
+    tc_cgemm_gen_kernel(const __grid_constant__ CUtensorMap tmB, const TcGenParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  uint8_t* abuf = smem;                                 // GA_STAGES x 32 KB
+  uint8_t* bbuf = smem + GA_STAGES * G_A_BYTES;         // GB_STAGES x 32 KB
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(bbuf + GB_STAGES * G_B_BYTES);
+  uint64_t* bempty = bfull + GB_STAGES;
+  uint64_t* afull = bempty + GB_STAGES;
+  uint64_t* aempty = afull + GA_STAGES;
+  uint64_t* tfull = aempty + GA_STAGES;
+  uint64_t* tempty = tfull + 1;
+  uint64_t* mdone = tempty + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nkb = (p.K + TC_BK - 1) / TC_BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < GB_STAGES; ++s) {
+      mbar_init(&bfull[s], 1);
+      mbar_init(&bempty[s], 1);
+    }
+    for (int s = 0; s < GA_STAGES; ++s) {
+      mbar_init(&afull[s], 4);
+      mbar_init(&aempty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, 4);
+    mbar_init(mdone, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+    prefetch_tmap(&tmB);
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ------------------------- TMA producer (field B) -------------------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t ph = 0, issued_mask = 0, issued_ph = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+        const int b = w / (p.mt * p.nt);
+        const int r = w - b * p.mt * p.nt;
+        const int nt = r - (r / p.nt) * p.nt;
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&bempty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+          mbar_expect_tx(&bfull[stage], G_B_BYTES);
+          uint8_t* base = bbuf + stage * G_B_BYTES;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            tma_load_3d(base + q * B_PLANE_BYTES, &tmB, &bfull[stage], kb * TC_BK, nt * TC_BN,
+                        b * 4 + q);
+          issued_mask |= 1u << stage;
+          issued_ph = (issued_ph & ~(1u << stage)) | (ph << stage);
+          if (++stage == GB_STAGES) { stage = 0; ph ^= 1u; }
+        }
+      }
+      if (!ok)
+        for (int s = 0; s < GB_STAGES; ++s)
+          if (issued_mask & (1u << s))
+            mbar_wait(&bfull[s], (issued_ph >> s) & 1u, abort_flag, p.status, false);
+    }
+  } else if (warp == 1) {
+    // ------------------------------- MMA issuer -------------------------------
+    if (lane == 0) {
+      const uint32_t id_pos = make_idesc(false);
+      const uint32_t id_neg = make_idesc(true);
+      const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
+      const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
+      const uint32_t m_re = tmem, m_im = tmem + TC_BN;
+      const uint32_t c_re = tmem + 2 * TC_BN, c_im = tmem + 3 * TC_BN;
+      int sb = 0, sa = 0;
+      uint32_t phb = 0, pha = 0, acc_ph = 0;
+      bool ok = true;
+      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        tc_fence_after();
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!mbar_wait(&bfull[sb], phb, abort_flag, p.status)) { ok = false; break; }
+          if (!mbar_wait(&afull[sa], pha, abort_flag, p.status)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t s_a = smem_u32(abuf + sa * G_A_BYTES);
+          const uint32_t s_b = smem_u32(bbuf + sb * G_B_BYTES);
+#pragma unroll
+          for (int j = 0; j < TC_BK / 16; ++j) {
+            const uint32_t ko = j * 32;
+            const uint64_t arh = make_desc(s_a + 0 * A_PLANE_BYTES + ko);
+            const uint64_t arl = make_desc(s_a + 1 * A_PLANE_BYTES + ko);
+            const uint64_t aih = make_desc(s_a + 2 * A_PLANE_BYTES + ko);
+            const uint64_t ail = make_desc(s_a + 3 * A_PLANE_BYTES + ko);
+            const uint64_t brh = make_desc(s_b + 0 * B_PLANE_BYTES + ko);
+            const uint64_t brl = make_desc(s_b + 1 * B_PLANE_BYTES + ko);
+            const uint64_t bih = make_desc(s_b + 2 * B_PLANE_BYTES + ko);
+            const uint64_t bil = make_desc(s_b + 3 * B_PLANE_BYTES + ko);
+            const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+            mma_bf16(m_re, arh, brh, id_pos, acc);
+            mma_bf16(m_re, aih, bih, id_rii, 1u);
+            mma_bf16(c_re, arh, brl, id_pos, acc);
+            mma_bf16(c_re, arl, brh, id_pos, 1u);
+            mma_bf16(c_re, aih, bil, id_rii, 1u);
+            mma_bf16(c_re, ail, bih, id_rii, 1u);
+            mma_bf16(m_im, arh, bih, id_pos, acc);
+            mma_bf16(m_im, aih, brh, id_iir, 1u);
+            mma_bf16(c_im, arh, bil, id_pos, acc);
+            mma_bf16(c_im, arl, bih, id_pos, 1u);
+            mma_bf16(c_im, aih, brl, id_iir, 1u);
+            mma_bf16(c_im, ail, brh, id_iir, 1u);
+          }
+          mma_commit(&bempty[sb]);
+          mma_commit(&aempty[sa]);
+          if (++sb == GB_STAGES) { sb = 0; phb ^= 1u; }
+          if (++sa == GA_STAGES) { sa = 0; pha ^= 1u; }
+        }
+        if (!ok) break;
+        mma_commit(tfull);
+        acc_ph ^= 1u;
+      }
+      mma_commit(mdone);
+      mbar_wait(mdone, 0, abort_flag, p.status, false);
+    }
+  } else if (warp < 6) {
+    // -------------------------------- epilogue --------------------------------
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    uint32_t acc_ph = 0;
+    for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
+      if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
+      tc_fence_after();
+      const int b = w / (p.mt * p.nt);
+      const int r = w - b * p.mt * p.nt;
+      const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
+      const int m = mt * TC_BM + row;
+      const int nbase = nt * TC_BN;
+      const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int c = 0; c < TC_BN / 32; ++c) {
+        if (nbase + c * 32 >= p.N) break;
+        float re[32], im[32], t[32];
+        tmem_ld32(lane_addr + c * 32, re);
+        tmem_ld32(lane_addr + TC_BN + c * 32, im);
+        tmem_ld32(lane_addr + 2 * TC_BN + c * 32, t);
+        tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) re[i] += t[i];
+        tmem_ld32(lane_addr + 3 * TC_BN + c * 32, t);
+        tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 32; ++i) im[i] += t[i];
+        if (m < p.M) epi_chunk32(p.epi, b, m, nbase + c * 32, p.M, p.N, re, im);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tempty);
+      acc_ph ^= 1u;
+    }
+  } else {
+    // ------------------------ A generators (one row each) ---------------------
+    const int r = threadIdx.x - 192;  // 0..127
+    const uint32_t swz = (uint32_t)((r >> 1) & 3);
+    int sa = 0;
+    uint32_t pha = 0;
+    bool ok = true;
+    for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+      const int b = w / (p.mt * p.nt);
+      const int rr = w - b * p.mt * p.nt;
+      const int mt = rr / p.nt;
+      const DftAxis ax = p.axes[b / p.a_batch_div];
+      const int R = mt * TC_BM + r;
+      const bool live = R < p.M;
+      // Row phase: theta0 + k * delta cycles (FP64 once per row and tile).
+      double coef, delta, theta;
+      if (p.rows_are_out) {
+        coef = ax.a_out * (double)R + ax.b_out;
+        delta = ax.sigma * coef * ax.a_in + ax.g_in;
+        theta = ax.sigma * coef * ax.b_in + ax.d_in + ax.g_out * (double)R + ax.d_out;
+      } else {
+        coef = ax.a_in * (double)R + ax.b_in;
+        delta = ax.sigma * coef * ax.a_out + ax.g_out;
+        theta = ax.sigma * coef * ax.b_out + ax.d_out + ax.g_in * (double)R + ax.d_in;
+      }
+      const FF dff = ff_from_double(delta);
+      const FF tff = ff_from_double(theta - rint(theta));
+      const FF zero{0.f, 0.f};
+      float2 step[32];
+#pragma unroll
+      for (int t = 0; t < 32; ++t) step[t] = cis_affine((float)t, dff, zero);
+      for (int kb = 0; kb < nkb; ++kb) {
+        if (!warp_wait(&aempty[sa], pha ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        const float2 base = cis_affine((float)(kb * TC_BK), dff, tff);
+        uint8_t* tile = abuf + sa * G_A_BYTES + r * 64;
+        const int kvalid = p.K - kb * TC_BK;  // columns beyond K must be zero
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            float2 v[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+              const int t = c * 8 + h * 2 + e;
+              v[e] = (live && t < kvalid) ? cmul(base, step[t]) : make_float2(0.f, 0.f);
+            }
+            __nv_bfloat16 h0, l0, h1, l1;
+            split_bf16(v[0].x, h0, l0);
+            split_bf16(v[1].x, h1, l1);
+            rh[h] = pack_bf16(h0, h1);
+            rl[h] = pack_bf16(l0, l1);
+            split_bf16(v[0].y, h0, l0);
+            split_bf16(v[1].y, h1, l1);
+            ih[h] = pack_bf16(h0, h1);
+            il[h] = pack_bf16(l0, l1);
+          }
+          // 64B swizzle: 16-byte chunk c of row r sits at chunk c ^ ((r >> 1) & 3).
+          const uint32_t off = ((uint32_t)c ^ swz) << 4;
+          *reinterpret_cast<uint4*>(tile + 0 * A_PLANE_BYTES + off) =
+              make_uint4(rh[0], rh[1], rh[2], rh[3]);
+          *reinterpret_cast<uint4*>(tile + 1 * A_PLANE_BYTES + off) =
+              make_uint4(rl[0], rl[1], rl[2], rl[3]);
+          *reinterpret_cast<uint4*>(tile + 2 * A_PLANE_BYTES + off) =
+              make_uint4(ih[0], ih[1], ih[2], ih[3]);
+          *reinterpret_cast<uint4*>(tile + 3 * A_PLANE_BYTES + off) =
+              make_uint4(il[0], il[1], il[2], il[3]);
+        }
+        // Make the generic-proxy stores visible to the tensor core, then signal.
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&afull[sa]);
+        if (++sa == GA_STAGES) { sa = 0; pha ^= 1u; }
+      }
     }
   }
 
@@ -532,8 +839,10 @@ void init_once() {
     return;
   }
   if (cudaFuncSetAttribute(tc_cgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           SMEM_BYTES) != cudaSuccess) {
-    g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tc_cgemm_kernel) failed");
+                           SMEM_BYTES) != cudaSuccess ||
+      cudaFuncSetAttribute(tc_cgemm_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           G_SMEM_BYTES) != cudaSuccess) {
+    g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tensor-core GEMM) failed");
     return;
   }
 }
@@ -573,8 +882,28 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if (g.batch <= 0 || g.M <= 0 || g.N <= 0) return DLX_OK;
   if (g.K % 8 != 0 || g.N % 8 != 0)
     return fail(DLX_ERR_SHAPE, "split-BF16 GEMM needs K and N to be multiples of 8");
-  if (!g.As || !g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
   const int div = g.a_batch_div > 0 ? g.a_batch_div : 1;
+  if (g.a_axes) {
+    if (!g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
+    CUtensorMap tb;
+    DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, g.batch, TC_BN));
+    TcGenParams p{};
+    p.batch = g.batch; p.M = g.M; p.N = g.N; p.K = g.K;
+    p.a_batch_div = div;
+    p.mt = (g.M + TC_BM - 1) / TC_BM;
+    p.nt = (g.N + TC_BN - 1) / TC_BN;
+    p.total = g.batch * p.mt * p.nt;
+    p.conj_a = g.conj_a ? 1 : 0;
+    p.rows_are_out = g.a_rows_are_out ? 1 : 0;
+    p.axes = g.a_axes;
+    p.status = g_status;
+    p.epi = g.epi;
+    const int grid = p.total < g_num_sms ? p.total : g_num_sms;
+    tc_cgemm_gen_kernel<<<grid, G_THREADS, G_SMEM_BYTES, s>>>(tb, p);
+    DLX_LAUNCH_CHECK("tc_cgemm_gen_kernel");
+    return DLX_OK;
+  }
+  if (!g.As || !g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
   const int nA = (g.batch + div - 1) / div;
   CUtensorMap ta, tb;
   DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, TC_BM));

@@ -20,7 +20,38 @@ int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool 
                    float2* out_c64, long long out_batch_stride, __nv_bfloat16* out_split,
                    cudaStream_t s);
 
+// Independent objects (requests, sources) evaluated in one batch: batch index
+// b = l * n + r for wavelength l and object r, so the per-wavelength DFT
+// operand is shared by all objects (A index = b / n). Passed by value.
+constexpr int kMaxObj = 32;
+struct ObjDesc {
+  const float* amp;        // nullable [N][N]
+  const float* amp_scale;  // nullable device scalar
+  const float* opd;        // nullable [N][N]
+  const float* phase;      // nullable [N][N]
+  const float* weights;    // nullable [L]
+  const float* G;          // [M][M] cotangent (reverse pass)
+  double tilt_x, tilt_y;
+};
+struct ObjTable {
+  int n;                   // 0: not used (single-object fields of the enclosing struct)
+  ObjDesc o[kMaxObj];
+};
+struct ObjOut {
+  float* psf;              // [M][M] per-object PSF, nullable
+  float* g_amp;            // [N][N], nullable
+  float* g_opd;
+  float* g_phase;
+  float* g_w;              // [L]
+  float* g_tilt;           // [2]
+};
+struct OutTable {
+  int n;
+  ObjOut o[kMaxObj];
+};
+
 struct PhasorArgs {
+  ObjTable objs;           // when objs.n > 0 the per-object fields replace the ones below
   const float2* in;        // nullable [b][n][n]
   const float* amp;        // nullable [n][n]
   const float* opd;        // nullable [n][n]
@@ -39,7 +70,6 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
 int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
                                 __nv_bfloat16* out_split, cudaStream_t s);
 int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cudaStream_t s);
-int launch_plane_sum(const float* planes, int batch, long long npix, float* out, cudaStream_t s);
 int launch_power_scale(const float2* in, int batch, long long npix, double value, float* out,
                        cudaStream_t s);
 int launch_amp_norm(const float* amp, long long npix, double value, float* out_scale,
@@ -55,26 +85,33 @@ int launch_downsample(const float* in, int n_in, int k, int mean, const float* f
 int launch_downsample_backward(const float* in, const float* g_out, int n_in, int k, int mean,
                                const float* flat, float* g_in, float* g_flat, cudaStream_t s);
 
-// Reduction of the per-wavelength pupil-gradient planes:
-// g_amp = sum_b pre[b], g_phase = sum_b pim[b], g_opd = sum_b k_b pim[b],
-// g_w[b] = sum_p amp[p] pre[b][p] / (2 w_b) (two-level, deterministic).
-struct PupilReduceArgs {
-  const float* pre;
+// Per-object reductions of a batched plan (b = l * R + r).
+struct ObjReduceArgs {
+  ObjTable objs;
+  OutTable outs;
+  int L;                     // wavelengths
+  long long npix;            // pixels per plane
+  const float* planes;       // intensity planes [L*R][npix]
+  float* psf_sum;            // nullable: sum over objects (and wavelengths)
+  int accumulate;            // add into psf_sum instead of overwriting it
+  const float* pre;          // pupil planes [L*R][npix]
   const float* pim;
-  const float* amp;       // nullable (1)
-  const float* amp_scale; // nullable device scalar multiplying amp
-  const float* weights;   // [b]
-  const double* k_dev;    // [b] 2 pi / lambda_b
-  int batch;
-  long long npix;
-  float* g_amp;
-  float* g_opd;
-  float* g_phase;
-  float* g_w;
-  double* partial_ws;     // >= batch * nparts doubles
+  const double* k_dev;       // [L] 2 pi / lambda
+  int n_side;                // pupil side (tilt gradients)
+  double pixel_scale;
+  double* partial_ws;        // >= R * nparts * (L + 2) doubles
   int nparts;
+  // Pixel gradients summed over all objects into these (objects share one
+  // pupil); when set, outs.o[r].g_amp/g_opd/g_phase are ignored.
+  float* sum_g_amp;
+  float* sum_g_opd;
+  float* sum_g_phase;
+  int sum_pixels;
+  int accumulate_sum;        // add into the sums instead of overwriting them
 };
-int launch_pupil_reduce(const PupilReduceArgs& a, cudaStream_t s);
+int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s);
+int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s);
+
 
 // --- gemm_fp32.cu / gemm_tc.cu ---------------------------------------------
 // Complex GEMM D[b][m][n] = sum_k opA(A[b][m][k]) * B[b][n][k], opA = conj if conj_a.
@@ -89,7 +126,8 @@ enum EpiKind {
 
 struct EpiArgs {
   int kind;
-  const float* alpha;        // [b] device
+  ObjTable objs;             // objects of a batched plan (objs.n == 0: single object below)
+  const float* alpha;        // [wavelength] device
   float2* out_c64;
   __nv_bfloat16* out_split;
   float* out_f32;            // intensity planes, or pre planes for EPI_PUPIL
@@ -115,6 +153,11 @@ struct GemmArgs {
   const __nv_bfloat16* Bs;  // split form [b][4][N][K]
   int a_batch_div;          // A batch index = b / a_batch_div (split form)
   bool conj_a;
+  // Tensor-core form only: when a_axes is set, A is not read from memory but
+  // generated in the CTA as the DFT matrix of a_axes[b / a_batch_div]; rows
+  // are output indices (a_rows_are_out) or input indices.
+  const DftAxis* a_axes;
+  bool a_rows_are_out;
   EpiArgs epi;
 };
 

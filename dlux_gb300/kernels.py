@@ -223,19 +223,52 @@ class PolyPlan(_Plan):
     _destroy = "dlx_poly_plan_destroy"
 
     def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
-                 focal_length=None, variant=None):
+                 focal_length=None, variant=None, max_objects=1):
         super().__init__()
         _lib.require_cuda()
         self.wavelengths = tuple(float(w) for w in wavelengths)
         self.n_in, self.n_out = int(n_in), int(n_out)
         self.pixel_scale_in = float(pixel_scale_in)
+        self.max_objects = int(max_objects)
         self.variant = resolve_variant(self.n_in, self.n_out, variant)
         d = _lib.PolyDesc(len(self.wavelengths), self.n_in, self.n_out, float(pixel_scale_in),
                           float(pixel_scale_out),
                           float(focal_length) if focal_length is not None else 0.0,
                           self.variant)
-        call("dlx_poly_plan_create", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
-             ctypes.byref(self.handle))
+        call("dlx_poly_plan_create_batched", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
+             self.max_objects, ctypes.byref(self.handle))
+
+    # ---- batched objects (requests or point sources) ----
+    _OBJ_FIELDS = ("amp", "amp_scale", "opd", "phase", "weights", "psf", "g_psf", "g_amp",
+                   "g_opd", "g_phase", "g_w", "g_tilt")
+
+    @classmethod
+    def _object_array(cls, objs):
+        arr = (_lib.PolyObject * max(1, len(objs)))()
+        for i, o in enumerate(objs):
+            for f in cls._OBJ_FIELDS:
+                t = o.get(f)
+                setattr(arr[i], f, ptr(t.contiguous() if t is not None else None))
+            tilt = o.get("tilt", (0.0, 0.0))
+            arr[i].tilt_x, arr[i].tilt_y = float(tilt[0]), float(tilt[1])
+        return arr
+
+    def forward_objects(self, objs, psf_sum=None, accumulate=False):
+        """PSFs of several objects: dicts with amp/amp_scale/opd/phase/weights/tilt/psf."""
+        arr = self._object_array(objs)
+        call("dlx_poly_forward", self.handle, ctypes.cast(arr, ctypes.c_void_p), len(objs),
+             ptr(psf_sum), int(bool(accumulate)), _stream())
+
+    def backward_objects(self, objs, sum_grads=None):
+        """Reverse pass; ``sum_grads`` ({"amp","opd","phase"} tensors) sums pixel gradients."""
+        arr = self._object_array(objs)
+        if sum_grads is None:
+            call("dlx_poly_backward", self.handle, ctypes.cast(arr, ctypes.c_void_p), len(objs),
+                 _stream())
+        else:
+            call("dlx_poly_backward_sum", self.handle, ctypes.cast(arr, ctypes.c_void_p),
+                 len(objs), ptr(sum_grads.get("amp")), ptr(sum_grads.get("opd")),
+                 ptr(sum_grads.get("phase")), _stream())
 
     @property
     def footprint(self) -> int:
@@ -309,14 +342,15 @@ def get_fft_plan(wavelengths, n_in, pixel_scale_in, pad=2, focal_length=None, in
 
 
 def get_poly_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,
-                  variant=None):
+                  variant=None, max_objects=1):
     wl = tuple(float(w) for w in wavelengths)
     v = resolve_variant(n_in, n_out, variant)
     key = (wl, int(n_in), float(pixel_scale_in), int(n_out), float(pixel_scale_out),
-           None if focal_length is None else float(focal_length), v)
+           None if focal_length is None else float(focal_length), v, int(max_objects))
     return poly_plans.get(key, lambda: PolyPlan(wl, n_in, pixel_scale_in, n_out, pixel_scale_out,
                                                 focal_length,
-                                                "fp32" if v == 0 else "split_bf16"))
+                                                "fp32" if v == 0 else "split_bf16",
+                                                max_objects))
 
 
 # ---------------------------------------------------------------------------

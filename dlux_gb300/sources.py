@@ -100,10 +100,32 @@ class PointSources(Source):
             wfs = [optics.propagate(src.spectrum.wavelengths, p, wt, return_wf=True)
                    for p, wt in zip(src.position, weights)]
             return wfs[0].set(phasor=torch.stack([wf.phasor for wf in wfs]))
-        psf = None
-        for p, wt in zip(src.position, weights):
-            one = optics.propagate(src.spectrum.wavelengths, p, wt)
-            psf = one if psf is None else psf + one
+        psf = self._fused(optics, src, weights)
+        if psf is None:
+            for p, wt in zip(src.position, weights):
+                one = optics.propagate(src.spectrum.wavelengths, p, wt)
+                psf = one if psf is None else psf + one
         if return_psf:
             return PSF(psf, optics._psf_pixel_scale())
         return psf
+
+    @staticmethod
+    def _fused(optics, src, weights):
+        """All sources in batched launches when the optics fold into one pupil."""
+        from . import autograd
+
+        if not hasattr(optics, "fused_pupil"):
+            return None
+        fused = optics.fused_pupil()
+        if fused is None:
+            return None
+        amp, flag, opd, phase, tilt = fused
+        wl = [float(v) for v in torch.as_tensor(src.spectrum.wavelengths,
+                                               dtype=torch.float64).reshape(-1)]
+        n_src = src.position.shape[0]
+        npix, ps = optics._focal_sampling()
+        from . import kernels
+        plan = kernels.get_poly_plan(wl, optics.wf_npixels, optics.diameter / optics.wf_npixels,
+                                     npix, ps, None, None, max_objects=min(n_src, 32))
+        return autograd.poly_sources(plan, amp, opd, phase, weights.to(torch.float32),
+                                     src.position, flag, tilt)

@@ -219,6 +219,48 @@ typedef struct {
 
 int dlx_poly_plan_create(const dlx_poly_desc* desc, const double* wavelengths_host,
                          dlx_poly_plan* plan);
+
+/* One independent object of a batched evaluation: a request of the serving
+ * loop, or one point source of PointSources.model (sources.py:392-411, which
+ * vmaps optics.propagate over positions). All pointers are device pointers;
+ * any may be NULL where the matching quantity is absent or not wanted.
+ * weights [L] carry the source's spectral weights times its flux. */
+typedef struct {
+  const float* amp;        /* [N][N] pupil amplitude (NULL: 1) */
+  const float* amp_scale;  /* device scalar multiplying amp (e.g. from dlx_amp_norm) */
+  const float* opd;        /* [N][N] OPD in metres */
+  const float* phase;      /* [N][N] phase in radians */
+  const float* weights;    /* [L] */
+  double tilt_x, tilt_y;   /* source offset in radians (the initial wavefront tilt) */
+  float* psf;              /* [M][M] output of dlx_poly_forward (NULL: only summed) */
+  const float* g_psf;      /* [M][M] cotangent for dlx_poly_backward */
+  float* g_amp;            /* [N][N] d/d effective amplitude */
+  float* g_opd;            /* [N][N] */
+  float* g_phase;          /* [N][N] */
+  float* g_w;              /* [L] */
+  float* g_tilt;           /* [2] d/d (tilt_x, tilt_y) */
+} dlx_poly_object;
+
+/* Plan for up to max_objects (<= 32) objects per launch; the per-wavelength
+ * DFT operands are shared by all objects of a batch, so the GEMMs run over
+ * L x objects fields in one launch. */
+int dlx_poly_plan_create_batched(const dlx_poly_desc* desc, const double* wavelengths_host,
+                                 int max_objects, dlx_poly_plan* plan);
+/* PSFs of n_objects objects (any count; runs in chunks of the plan's capacity):
+ * per-object PSFs into objs[r].psf and/or their sum into psf_sum (added to its
+ * contents when accumulate != 0). The sum over objects is the PointSources
+ * image (sources.py:409-411). */
+int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                     float* psf_sum, int accumulate, void* stream);
+/* Reverse pass for every object with its own cotangent objs[r].g_psf. */
+int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                      void* stream);
+/* Same, for objects that share one pupil (the sources of one scene): the
+ * pupil-pixel gradients are summed over all objects into g_amp / g_opd /
+ * g_phase ([N][N], any may be NULL; overwritten), while g_w and g_tilt stay
+ * per object (source fluxes and positions). */
+int dlx_poly_backward_sum(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                          float* g_amp, float* g_opd, float* g_phase, void* stream);
 int dlx_poly_plan_destroy(dlx_poly_plan plan);
 /* Device bytes the plan holds (cached DFT matrices plus intermediates). */
 int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
