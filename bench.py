@@ -16,6 +16,7 @@ is made between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--variant split_bf16|fp32]
   python bench.py --impl reference   # the CPU restatement of the same step
+  python bench.py --workload serving # mixed-shape request stream through the server
 """
 
 from __future__ import annotations
@@ -305,6 +306,69 @@ def time_e2e(args, objs, world):
     return dt, h2d, d2h
 
 
+def run_serving(args):
+    """Seeded Poisson stream of mixed-shape requests through dlux_gb300.serving.
+
+    N in {128, 256, 512, 1024}, M in {64, 128, 256, 512}, L uniform on 1..64 over
+    0.8-1.2 um, 4..36 Zernike coefficients from N(0, 50 nm), 30 % of requests ask for
+    the coefficient gradient of <G, PSF> with G ~ N(0, 1). Arrivals are Poisson at
+    --rate requests/s. Plans of every bucket in the stream are made resident first
+    (within the 150 GB budget); a warm-up stream of a different seed runs before the
+    timed one. Latency is submit -> result on the host (pinned copies included).
+    """
+    import torch
+    from dlux_gb300 import serving
+
+    out = {}
+    variants = [args.variant] + (["fp32"] if args.variant == "split_bf16" and
+                                 not args.no_fp32_compare else [])
+    for variant in variants:
+        srv = serving.PSFServer(max_batch=8, n_slots=4, hbm_budget=150e9, k_max=36,
+                                limits=(1024, 512, 64), variant=variant, timeout_s=120.0)
+        times, reqs = serving.poisson_stream(args.requests, args.rate, seed=SEED)
+        _, warm = serving.poisson_stream(max(args.requests // 4, 50), args.rate, seed=SEED + 1)
+        keys = sorted({r.key for r in reqs} | {r.key for r in warm})
+        t0 = time.perf_counter()
+        resident = srv.prewarm(keys)
+        t_prewarm = time.perf_counter() - t0
+        srv.start()
+        serving.replay(srv, np.zeros(len(warm)), warm)      # warm-up: back to back
+        for r in warm:
+            r.result(120.0)
+        srv.completed.clear()
+        clocks = ClockSampler(torch.cuda.current_device())
+        clocks.start()
+        serving.replay(srv, times, reqs)
+        clk = clocks.stop()
+        srv.stop()
+        rep = srv.report(reqs)
+        srv.close()
+        rep.update(variant=variant, buckets=len(keys), resident_buckets=resident,
+                   prewarm_s=t_prewarm, clocks=clk)
+        out[variant] = rep
+    main_rep = out[args.variant]
+    line = {
+        "metric": "served requests/sec (mixed PSF and PSF+grad stream)",
+        "value": main_rep.get("throughput_rps"), "unit": "req/s", "n_gpus": 1,
+        "steps": args.requests, "warmup": max(args.requests // 4, 50),
+        "ms_per_step": 1e3 / main_rep["throughput_rps"] if main_rep.get("throughput_rps")
+        else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
+        "data": "synthetic (seeded Poisson stream)",
+        "config": {"workload": f"serving: Poisson {args.rate:g} req/s, N in 128-1024, M in "
+                               "64-512, L in 1..64, K in 4..36, 30% gradients",
+                   "requests": args.requests, "rate_hz": args.rate, "max_batch": 8,
+                   "slots": 4, "hbm_budget_gb": 150},
+        "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
+        "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
+        "clocks": main_rep["clocks"],
+        "serving": out,
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def load_peaks():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -323,6 +387,9 @@ def main():
     ap.add_argument("--variant", default="split_bf16", choices=["split_bf16", "fp32"])
     ap.add_argument("--no-fp32-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="psf_grad", choices=["psf_grad", "serving"])
+    ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
                     help="wavelength count (64 is the benchmark workload; smaller values "
                          "make the bounded cases used for profiling captures)")
@@ -338,6 +405,8 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if args.workload == "serving":
+        return run_serving(args) if rank == 0 else 0
     if world > 1:
         torch.distributed.init_process_group("nccl")
 

@@ -56,7 +56,7 @@ class PolyDesc(ctypes.Structure):
     _fields_ = [
         ("n_wavelengths", _c_int), ("n_in", _c_int), ("n_out", _c_int),
         ("pixel_scale_in", _c_dbl), ("pixel_scale_out", _c_dbl), ("focal_length", _c_dbl),
-        ("variant", _c_int),
+        ("variant", _c_int), ("operand_mode", _c_int),
     ]
 
 
@@ -67,6 +67,16 @@ class PolyObject(ctypes.Structure):
         ("weights", _c_vp), ("tilt_x", _c_dbl), ("tilt_y", _c_dbl), ("psf", _c_vp),
         ("g_psf", _c_vp), ("g_amp", _c_vp), ("g_opd", _c_vp), ("g_phase", _c_vp),
         ("g_w", _c_vp), ("g_tilt", _c_vp),
+    ]
+
+
+class ServeBatch(ctypes.Structure):
+    """dlx_serve_batch: one batch of serving requests that share a plan."""
+    _fields_ = [
+        ("n_objects", _c_int), ("n_grad", _c_int), ("n_coeffs", _c_int),
+        ("basis", _c_vp), ("amp", _c_vp), ("amp_scale", _c_vp),
+        ("h_coeffs", _c_vp), ("h_weights", _c_vp), ("h_g_psf", _c_vp), ("h_psf", _c_vp),
+        ("h_grad", _c_vp), ("d_work", _c_vp), ("d_work_bytes", ctypes.c_size_t),
     ]
 
 
@@ -104,11 +114,21 @@ _SIGNATURES = {
     "dlx_poly_plan_create": (_c_int, [ctypes.POINTER(PolyDesc), _c_vp, ctypes.POINTER(_c_vp)]),
     "dlx_poly_plan_create_batched": (_c_int, [ctypes.POINTER(PolyDesc), _c_vp, _c_int,
                                               ctypes.POINTER(_c_vp)]),
+    "dlx_poly_plan_create_shared": (_c_int, [ctypes.POINTER(PolyDesc), _c_vp, _c_int,
+                                             ctypes.POINTER(_c_vp)]),
+    "dlx_poly_workspace_bytes": (_c_int, [ctypes.POINTER(PolyDesc), _c_int,
+                                          ctypes.POINTER(ctypes.c_size_t)]),
+    "dlx_poly_attach_workspace": (_c_int, [_c_vp, _c_vp, ctypes.c_size_t]),
     "dlx_poly_forward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_int, _c_vp]),
     "dlx_poly_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "dlx_poly_backward_sum": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_poly_plan_destroy": (_c_int, [_c_vp]),
     "dlx_poly_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "dlx_poly_plan_info": (_c_int, [_c_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
+                                    ctypes.POINTER(_c_int), ctypes.POINTER(_c_int)]),
+    "dlx_serve_workspace_bytes": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int,
+                                           ctypes.POINTER(ctypes.c_size_t)]),
+    "dlx_serve_run": (_c_int, [_c_vp, ctypes.POINTER(ServeBatch), _c_vp]),
     "dlx_poly_psf": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl, _c_dbl, _c_vp,
                               _c_vp]),
     "dlx_poly_psf_grad": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_dbl, _c_dbl,

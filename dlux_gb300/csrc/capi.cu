@@ -105,7 +105,15 @@ DftAxis fft_axis(const dlx_fft_desc& d, double wl) {
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool owned = true;  // false: a view into caller-provided workspace
+  void view(void* ptr, size_t n) {
+    release();
+    p = ptr;
+    bytes = n;
+    owned = false;
+  }
   int alloc(size_t n) {
+    owned = true;
     if (n == 0) return DLX_OK;
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) {
@@ -118,10 +126,12 @@ struct DevBuf {
     return DLX_OK;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
     p = nullptr;
     bytes = 0;
+    owned = true;
   }
+  size_t owned_bytes() const { return owned ? bytes : 0; }
   template <class T>
   T* as() const { return reinterpret_cast<T*>(p); }
 };
@@ -140,10 +150,10 @@ struct TwoStep {
   size_t elem_bytes() const { return variant == DLX_VARIANT_SPLIT_BF16 ? 8 : 8; }
   size_t mat_bytes() const { return (size_t)batch * n_in * n_out * elem_bytes(); }
 
-  // The tensor-core form streams cached split DFT matrices through TMA. With
-  // DLX_TC_GEN_A=1 in the environment at plan creation it instead builds the
-  // DFT operand inside the GEMM from `axes` (no cached matrices, half the
-  // operand bytes; measured slower at 512^3, 0.52 vs 0.36 ms per launch).
+  // The tensor-core form streams cached split DFT matrices through TMA, or
+  // (operand_mode 1) builds the DFT operand inside the GEMM from `axes`: no
+  // cached matrices and half the operand bytes, but measured slower at 512^3
+  // (0.52 vs 0.36 ms per launch); it suits plans that must stay small.
   bool gen_a = false;
   DevBuf axes;                 // DftAxis [2][b]: x axes then y axes (kept on the device)
 
@@ -158,12 +168,9 @@ struct TwoStep {
   AOp opANy() const { return {ANy(), axes.as<DftAxis>() + (shared_xy ? 0 : batch), false}; }
 
   int build(const std::vector<DftAxis>& ax_x, const std::vector<DftAxis>& ax_y,
-            const std::vector<float>& alphas) {
+            const std::vector<float>& alphas, bool generate_operand = false) {
     shared_xy = std::memcmp(ax_x.data(), ax_y.data(), sizeof(DftAxis) * batch) == 0;
-    if (variant == DLX_VARIANT_SPLIT_BF16) {
-      const char* env = getenv("DLX_TC_GEN_A");
-      gen_a = env && env[0] == '1';
-    }
+    gen_a = variant == DLX_VARIANT_SPLIT_BF16 && generate_operand;
     DLX_TRY(axes.alloc(sizeof(DftAxis) * batch * 2));
     int st = DLX_OK;
     do {
@@ -733,8 +740,10 @@ struct dlx_poly_plan_s {
   DevBuf partial;    // double reduction partials
   int nparts = 1024; // pixel chunks of the reverse reductions (enough blocks to fill the GPU)
 
+  // Device bytes this plan owns: an attached workspace belongs to the caller.
   size_t footprint() const {
-    return ts.footprint() + field.bytes + mid.bytes + fbar.bytes + planes.bytes + partial.bytes;
+    return ts.footprint() + field.owned_bytes() + mid.owned_bytes() + fbar.owned_bytes() +
+           planes.owned_bytes() + partial.owned_bytes();
   }
   void release() {
     ts.release(); field.release(); mid.release(); fbar.release(); planes.release();
@@ -778,6 +787,8 @@ struct dlx_poly_plan_s {
   int forward_chunk(const dlx_poly_object* objs, int R, float* psf_sum, int accumulate,
                     cudaStream_t s) {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    if (!field.p)
+      return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
     ObjTable t;
     OutTable o;
     tables(objs, R, &t, &o);
@@ -806,6 +817,8 @@ struct dlx_poly_plan_s {
                      float* sum_opd = nullptr, float* sum_phase = nullptr,
                      bool sum_pixels = false, bool accumulate_sum = false) {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    if (!field.p)
+      return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
     ObjTable t;
     OutTable o;
     tables(objs, R, &t, &o);
@@ -861,8 +874,20 @@ struct dlx_poly_plan_s {
   }
 };
 
+// Byte sizes of the per-call buffers of a plan: field, mid, fbar, planes, partial.
+static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[5]) {
+  const size_t lr = (size_t)L * R, n = N, m = M;
+  sz[0] = lr * n * n * 8;
+  sz[1] = lr * n * m * 8;
+  sz[2] = lr * m * m * 8;
+  const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
+  sz[3] = a > b ? a : b;
+  sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
+  for (int i = 0; i < 5; ++i) sz[i] = (sz[i] + 255) / 256 * 256;
+}
+
 static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects,
-                       dlx_poly_plan* plan) {
+                       dlx_poly_plan* plan, bool own_workspace = true) {
   if (!d || !wl || !plan) return fail(DLX_ERR_ARG, "poly_plan_create: null pointer");
   *plan = nullptr;
   if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0)
@@ -894,17 +919,20 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
     alphas[b] = (float)mft_alpha(wl[b], N, d->pixel_scale_in, M, d->pixel_scale_out,
                                  d->focal_length);
   }
-  int st = ts.build(ax, ax, alphas);
-  const size_t lr = (size_t)L * max_objects, n = N, m = M;
-  if (st == DLX_OK) st = p->field.alloc(lr * n * n * 8);
-  if (st == DLX_OK) st = p->mid.alloc(lr * n * m * 8);
-  if (st == DLX_OK) st = p->fbar.alloc(lr * m * m * 8);
-  if (st == DLX_OK) {
-    const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
-    st = p->planes.alloc(a > b ? a : b);
+  if (d->operand_mode != 0 && d->operand_mode != 1) {
+    delete p;
+    return fail(DLX_ERR_ARG, "poly_plan_create: operand_mode must be 0 or 1");
   }
-  if (st == DLX_OK)
-    st = p->partial.alloc(sizeof(double) * (size_t)p->nparts * max_objects * (L + 2));
+  int st = ts.build(ax, ax, alphas, d->operand_mode == 1);
+  if (st == DLX_OK && own_workspace) {
+    size_t sz[5];
+    poly_ws_sizes(L, N, M, max_objects, p->nparts, sz);
+    if (st == DLX_OK) st = p->field.alloc(sz[0]);
+    if (st == DLX_OK) st = p->mid.alloc(sz[1]);
+    if (st == DLX_OK) st = p->fbar.alloc(sz[2]);
+    if (st == DLX_OK) st = p->planes.alloc(sz[3]);
+    if (st == DLX_OK) st = p->partial.alloc(sz[4]);
+  }
   if (st != DLX_OK) {
     p->release();
     delete p;
@@ -925,6 +953,44 @@ int dlx_poly_plan_create_batched(const dlx_poly_desc* d, const double* wl, int m
   return poly_create(d, wl, max_objects, plan);
 }
 
+int dlx_poly_plan_create_shared(const dlx_poly_desc* d, const double* wl, int max_objects,
+                                dlx_poly_plan* plan) {
+  return poly_create(d, wl, max_objects, plan, false);
+}
+
+int dlx_poly_workspace_bytes(const dlx_poly_desc* d, int max_objects, size_t* bytes) {
+  if (!d || !bytes) return fail(DLX_ERR_ARG, "poly_workspace_bytes: null pointer");
+  if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0 || max_objects <= 0)
+    return fail(DLX_ERR_SHAPE, "poly_workspace_bytes: sizes must be positive");
+  size_t sz[5];
+  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, 1024, sz);
+  *bytes = sz[0] + sz[1] + sz[2] + sz[3] + sz[4];
+  return DLX_OK;
+}
+
+int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes) {
+  if (!plan || !workspace) return fail(DLX_ERR_ARG, "poly_attach_workspace: null pointer");
+  if ((uintptr_t)workspace % 256 != 0)
+    return fail(DLX_ERR_ARG, "poly_attach_workspace: workspace must be 256-byte aligned");
+  size_t sz[5];
+  poly_ws_sizes(plan->ts.batch, plan->ts.n_in, plan->ts.n_out, plan->max_obj, plan->nparts, sz);
+  const size_t need = sz[0] + sz[1] + sz[2] + sz[3] + sz[4];
+  if (bytes < need)
+    return fail(DLX_ERR_SHAPE, "poly_attach_workspace: " + std::to_string(bytes) +
+                                   " bytes given, " + std::to_string(need) + " needed");
+  char* w = static_cast<char*>(workspace);
+  plan->field.view(w, sz[0]);
+  w += sz[0];
+  plan->mid.view(w, sz[1]);
+  w += sz[1];
+  plan->fbar.view(w, sz[2]);
+  w += sz[2];
+  plan->planes.view(w, sz[3]);
+  w += sz[3];
+  plan->partial.view(w, sz[4]);
+  return DLX_OK;
+}
+
 int dlx_poly_plan_destroy(dlx_poly_plan plan) {
   if (!plan) return DLX_OK;
   cudaDeviceSynchronize();
@@ -936,6 +1002,16 @@ int dlx_poly_plan_destroy(dlx_poly_plan plan) {
 int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes) {
   if (!plan || !bytes) return fail(DLX_ERR_ARG, "poly_plan_footprint: null pointer");
   *bytes = plan->footprint();
+  return DLX_OK;
+}
+
+int dlx_poly_plan_info(dlx_poly_plan plan, int* n_wavelengths, int* n_in, int* n_out,
+                       int* max_objects) {
+  if (!plan) return fail(DLX_ERR_ARG, "poly_plan_info: null plan");
+  if (n_wavelengths) *n_wavelengths = plan->ts.batch;
+  if (n_in) *n_in = plan->ts.n_in;
+  if (n_out) *n_out = plan->ts.n_out;
+  if (max_objects) *max_objects = plan->max_obj;
   return DLX_OK;
 }
 

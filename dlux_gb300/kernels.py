@@ -223,7 +223,8 @@ class PolyPlan(_Plan):
     _destroy = "dlx_poly_plan_destroy"
 
     def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
-                 focal_length=None, variant=None, max_objects=1):
+                 focal_length=None, variant=None, max_objects=1, operand_mode=0,
+                 own_workspace=True):
         super().__init__()
         _lib.require_cuda()
         self.wavelengths = tuple(float(w) for w in wavelengths)
@@ -231,12 +232,24 @@ class PolyPlan(_Plan):
         self.pixel_scale_in = float(pixel_scale_in)
         self.max_objects = int(max_objects)
         self.variant = resolve_variant(self.n_in, self.n_out, variant)
-        d = _lib.PolyDesc(len(self.wavelengths), self.n_in, self.n_out, float(pixel_scale_in),
-                          float(pixel_scale_out),
-                          float(focal_length) if focal_length is not None else 0.0,
-                          self.variant)
-        call("dlx_poly_plan_create_batched", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
-             self.max_objects, ctypes.byref(self.handle))
+        self.operand_mode = int(operand_mode) if self.variant == _lib.VARIANT_SPLIT_BF16 else 0
+        self.desc = _lib.PolyDesc(len(self.wavelengths), self.n_in, self.n_out,
+                                  float(pixel_scale_in), float(pixel_scale_out),
+                                  float(focal_length) if focal_length is not None else 0.0,
+                                  self.variant, self.operand_mode)
+        fn = "dlx_poly_plan_create_batched" if own_workspace else "dlx_poly_plan_create_shared"
+        call(fn, ctypes.byref(self.desc), _lib.dbl_array(self.wavelengths), self.max_objects,
+             ctypes.byref(self.handle))
+
+    def workspace_bytes(self) -> int:
+        n = ctypes.c_size_t(0)
+        call("dlx_poly_workspace_bytes", ctypes.byref(self.desc), self.max_objects,
+             ctypes.byref(n))
+        return int(n.value)
+
+    def attach_workspace(self, ws: torch.Tensor) -> None:
+        """Use ``ws`` (a 256-byte aligned uint8 CUDA tensor) for the per-call buffers."""
+        call("dlx_poly_attach_workspace", self.handle, ptr(ws), ws.numel() * ws.element_size())
 
     # ---- batched objects (requests or point sources) ----
     _OBJ_FIELDS = ("amp", "amp_scale", "opd", "phase", "weights", "psf", "g_psf", "g_amp",

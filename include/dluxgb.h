@@ -215,6 +215,8 @@ typedef struct {
   double pixel_scale_out; /* rad/pixel (angular) or m/pixel */
   double focal_length;    /* <= 0: angular */
   int variant;            /* DLX_VARIANT_* */
+  int operand_mode;       /* split form only: 0 = cached DFT matrices streamed by TMA,
+                             1 = DFT operand generated inside the GEMM (no cached matrices) */
 } dlx_poly_desc;
 
 int dlx_poly_plan_create(const dlx_poly_desc* desc, const double* wavelengths_host,
@@ -246,6 +248,18 @@ typedef struct {
  * L x objects fields in one launch. */
 int dlx_poly_plan_create_batched(const dlx_poly_desc* desc, const double* wavelengths_host,
                                  int max_objects, dlx_poly_plan* plan);
+/* A plan that owns only its cached per-wavelength state (DFT operands,
+ * scales); the per-call buffers come from caller workspace attached with
+ * dlx_poly_attach_workspace before each use. Lets many resident plans (e.g.
+ * one per serving bucket) share a few workspaces, one per stream in use.
+ * dlx_poly_workspace_bytes gives the size a plan of this description needs. */
+int dlx_poly_plan_create_shared(const dlx_poly_desc* desc, const double* wavelengths_host,
+                                int max_objects, dlx_poly_plan* plan);
+int dlx_poly_workspace_bytes(const dlx_poly_desc* desc, int max_objects, size_t* bytes);
+/* workspace: 256-byte aligned device memory of at least the size above. The
+ * plan uses it until another workspace is attached; the caller keeps it alive
+ * and must not use it for anything else while the plan's work is in flight. */
+int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes);
 /* PSFs of n_objects objects (any count; runs in chunks of the plan's capacity):
  * per-object PSFs into objs[r].psf and/or their sum into psf_sum (added to its
  * contents when accumulate != 0). The sum over objects is the PointSources
@@ -262,8 +276,42 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
 int dlx_poly_backward_sum(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
                           float* g_amp, float* g_opd, float* g_phase, void* stream);
 int dlx_poly_plan_destroy(dlx_poly_plan plan);
-/* Device bytes the plan holds (cached DFT matrices plus intermediates). */
+/* Device bytes the plan owns: cached DFT matrices, plus its intermediates
+ * unless it was made with dlx_poly_plan_create_shared. */
 int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
+/* Shape of a plan; any output pointer may be NULL. */
+int dlx_poly_plan_info(dlx_poly_plan plan, int* n_wavelengths, int* n_in, int* n_out,
+                       int* max_objects);
+
+/* ---- Serving batch ----
+ * No counterpart in dLux, which has no serving loop. One batch of requests
+ * that share a plan (same N, M and wavelengths), each with its own Zernike
+ * coefficients and spectral weights; the first n_grad requests also want
+ * d<g_psf, PSF>/d coefficients. Everything is stream-ordered on `stream`:
+ * host->device copies of the inputs, OPD = basis . coefficients per request,
+ * the fused forward (and reverse) pass, the coefficient gradient and the
+ * device->host copies of PSFs and gradients. The call allocates nothing and
+ * synchronises nothing, so a batch can be captured in a CUDA graph once
+ * the plan's workspace is attached and replayed while the buffers stay put.
+ * Host buffers must be pinned for the copies to be asynchronous. */
+typedef struct dlx_serve_batch {
+  int n_objects;           /* R, 1..max_objects of the plan */
+  int n_grad;              /* 0..R: requests 0..n_grad-1 want gradients */
+  int n_coeffs;            /* K: basis terms (coefficients zero-padded to K) */
+  const float* basis;      /* device [K][N][N] */
+  const float* amp;        /* device [N][N] aperture transmission */
+  const float* amp_scale;  /* device scalar multiplying amp, or NULL for 1 */
+  const float* h_coeffs;   /* host [R][K] */
+  const float* h_weights;  /* host [R][L] */
+  const float* h_g_psf;    /* host [n_grad][M][M] cotangents (NULL if n_grad == 0) */
+  float* h_psf;            /* host [R][M][M] result */
+  float* h_grad;           /* host [n_grad][K] result (NULL if n_grad == 0) */
+  void* d_work;            /* device scratch of dlx_serve_workspace_bytes, 256-B aligned */
+  size_t d_work_bytes;
+} dlx_serve_batch;
+int dlx_serve_workspace_bytes(int max_objects, int n_coeffs, int n_in, int n_out,
+                              int n_wavelengths, size_t* bytes);
+int dlx_serve_run(dlx_poly_plan plan, const dlx_serve_batch* batch, void* stream);
 /* psf_out [M][M] = polychromatic PSF. amp, amp_scale (device scalar that
  * multiplies amp, e.g. from dlx_amp_norm), opd, phase and weights ([L]) are
  * device pointers and may be NULL (1, 1, 0, 0, 1). tilt is the source offset

@@ -142,3 +142,38 @@ def test_point_sources_flux_and_position_gradients(cuda):
             d[s, k] = h
             gp[s, k] = (loss(p0 + d, f0) - loss(p0 - d, f0)) / (2 * h)
     assert rel(pos.grad.numpy(), gp) < 1e-3
+
+
+def test_shared_plan_workspace_and_generated_operand(cuda):
+    """A plan without its own buffers, run on an attached workspace, gives the same bits
+    as a plan that owns them; the generated-operand form matches the oracle."""
+    from dlux_gb300 import kernels
+    n, m, L = 128, 64, 3
+    o = objects(n, L, 1, 21)[0]
+    wls = np.linspace(0.8e-6, 1.2e-6, L)
+    ps = float(O.arcsec2rad(0.01))
+    amp = dev(o["T"])
+    scale = kernels.amp_norm(amp)
+    args = (amp, scale, dev(o["opd"]), None, dev(o["w"]))
+    own = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", max_objects=2)
+    shared = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", max_objects=2,
+                              own_workspace=False)
+    assert shared.footprint < own.footprint
+    with pytest.raises(Exception):
+        shared.psf(*args)                      # no workspace attached yet
+    nbytes = shared.workspace_bytes()
+    buf = torch.empty(nbytes + 256, dtype=torch.uint8, device="cuda")
+    off = (-buf.data_ptr()) % 256
+    with pytest.raises(ValueError):
+        shared.attach_workspace(buf[off:off + nbytes - 256])    # too small
+    shared.attach_workspace(buf[off:off + nbytes])
+    a = own.psf(*args).cpu().numpy()
+    b = shared.psf(*args).cpu().numpy()
+    assert np.array_equal(a, b)
+    gen = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", operand_mode=1)
+    c = gen.psf(*args).cpu().numpy()
+    ref = O.poly_psf(o["T"], o["opd"], wls, o["w"], 1.0, m, ps)
+    print(f"generated-operand psf: rel L2 {rel(c, ref):.2e}; loaded {rel(a, ref):.2e}")
+    assert rel(c, ref) < 1e-5
+    with pytest.raises(ValueError):
+        kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", operand_mode=7)
