@@ -729,6 +729,9 @@ int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k
 // object r, so the per-wavelength DFT operands are shared (A index = b / R).
 // Larger object counts run in chunks of max_objects.
 // ---------------------------------------------------------------------------
+// Pixel chunks of the reverse-pass reductions (enough blocks to fill the GPU).
+constexpr int kPolyParts = 1024;
+
 struct dlx_poly_plan_s {
   TwoStep ts;
   double pixel_scale_in = 0;
@@ -738,16 +741,17 @@ struct dlx_poly_plan_s {
   DevBuf fbar;       // [L*R][M][M] c64 or split
   DevBuf planes;     // intensity [L*R][M][M] f32, or pre/pim [2][L*R][N][N] f32
   DevBuf partial;    // double reduction partials
-  int nparts = 1024; // pixel chunks of the reverse reductions (enough blocks to fill the GPU)
+  DevBuf pathff;     // [R][N][N] float4 (path, phase) pairs of the reverse pass
+  int nparts = kPolyParts;
 
   // Device bytes this plan owns: an attached workspace belongs to the caller.
   size_t footprint() const {
     return ts.footprint() + field.owned_bytes() + mid.owned_bytes() + fbar.owned_bytes() +
-           planes.owned_bytes() + partial.owned_bytes();
+           planes.owned_bytes() + partial.owned_bytes() + pathff.owned_bytes();
   }
   void release() {
     ts.release(); field.release(); mid.release(); fbar.release(); planes.release();
-    partial.release();
+    partial.release(); pathff.release();
   }
 
   static void tables(const dlx_poly_object* objs, int n, ObjTable* t, OutTable* o) {
@@ -763,8 +767,9 @@ struct dlx_poly_plan_s {
     }
   }
 
-  int build_field(const ObjTable& t, cudaStream_t s) {
+  int build_field(const ObjTable& t, cudaStream_t s, float4* out_path = nullptr) {
     PhasorArgs a{};
+    a.out_path = out_path;
     a.objs = t;
     a.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
     a.const_scale = 1.0;
@@ -825,7 +830,7 @@ struct dlx_poly_plan_s {
     for (int r = 0; r < R; ++r)
       if (!t.o[r].G) return fail(DLX_ERR_ARG, "poly backward: every object needs g_psf");
     // Recompute the forward fields (nothing is stored between the passes).
-    DLX_TRY(build_field(t, s));
+    DLX_TRY(build_field(t, s, pathff.as<float4>()));
     EpiArgs e1 = epi_store(v, mid.p, nullptr);
     e1.objs = t;
     DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
@@ -852,6 +857,7 @@ struct dlx_poly_plan_s {
     ep.out_f32b = pim;
     ep.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
     ep.pixel_scale = pixel_scale_in;
+    ep.path = pathff.as<float4>();
     DLX_TRY(run_gemm(v, gemm(ts.opANy(), R, N, N, M, true, mid.p, ep), s));
     ObjReduceArgs ra{};
     ra.objs = t;
@@ -874,8 +880,9 @@ struct dlx_poly_plan_s {
   }
 };
 
-// Byte sizes of the per-call buffers of a plan: field, mid, fbar, planes, partial.
-static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[5]) {
+// Byte sizes of the per-call buffers of a plan: field, mid, fbar, planes, partial, pathff.
+constexpr int kPolyBuffers = 6;
+static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[kPolyBuffers]) {
   const size_t lr = (size_t)L * R, n = N, m = M;
   sz[0] = lr * n * n * 8;
   sz[1] = lr * n * m * 8;
@@ -883,7 +890,8 @@ static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[5]) 
   const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
   sz[3] = a > b ? a : b;
   sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
-  for (int i = 0; i < 5; ++i) sz[i] = (sz[i] + 255) / 256 * 256;
+  sz[5] = sizeof(float4) * (size_t)R * n * n;
+  for (int i = 0; i < kPolyBuffers; ++i) sz[i] = (sz[i] + 255) / 256 * 256;
 }
 
 static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects,
@@ -925,13 +933,14 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
   }
   int st = ts.build(ax, ax, alphas, d->operand_mode == 1);
   if (st == DLX_OK && own_workspace) {
-    size_t sz[5];
+    size_t sz[kPolyBuffers];
     poly_ws_sizes(L, N, M, max_objects, p->nparts, sz);
     if (st == DLX_OK) st = p->field.alloc(sz[0]);
     if (st == DLX_OK) st = p->mid.alloc(sz[1]);
     if (st == DLX_OK) st = p->fbar.alloc(sz[2]);
     if (st == DLX_OK) st = p->planes.alloc(sz[3]);
     if (st == DLX_OK) st = p->partial.alloc(sz[4]);
+    if (st == DLX_OK) st = p->pathff.alloc(sz[5]);
   }
   if (st != DLX_OK) {
     p->release();
@@ -962,9 +971,10 @@ int dlx_poly_workspace_bytes(const dlx_poly_desc* d, int max_objects, size_t* by
   if (!d || !bytes) return fail(DLX_ERR_ARG, "poly_workspace_bytes: null pointer");
   if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0 || max_objects <= 0)
     return fail(DLX_ERR_SHAPE, "poly_workspace_bytes: sizes must be positive");
-  size_t sz[5];
-  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, 1024, sz);
-  *bytes = sz[0] + sz[1] + sz[2] + sz[3] + sz[4];
+  size_t sz[kPolyBuffers];
+  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, kPolyParts, sz);
+  *bytes = 0;
+  for (int i = 0; i < kPolyBuffers; ++i) *bytes += sz[i];
   return DLX_OK;
 }
 
@@ -972,9 +982,10 @@ int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes)
   if (!plan || !workspace) return fail(DLX_ERR_ARG, "poly_attach_workspace: null pointer");
   if ((uintptr_t)workspace % 256 != 0)
     return fail(DLX_ERR_ARG, "poly_attach_workspace: workspace must be 256-byte aligned");
-  size_t sz[5];
+  size_t sz[kPolyBuffers];
   poly_ws_sizes(plan->ts.batch, plan->ts.n_in, plan->ts.n_out, plan->max_obj, plan->nparts, sz);
-  const size_t need = sz[0] + sz[1] + sz[2] + sz[3] + sz[4];
+  size_t need = 0;
+  for (int i = 0; i < kPolyBuffers; ++i) need += sz[i];
   if (bytes < need)
     return fail(DLX_ERR_SHAPE, "poly_attach_workspace: " + std::to_string(bytes) +
                                    " bytes given, " + std::to_string(need) + " needed");
@@ -988,6 +999,8 @@ int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes)
   plan->planes.view(w, sz[3]);
   w += sz[3];
   plan->partial.view(w, sz[4]);
+  w += sz[4];
+  plan->pathff.view(w, sz[5]);
   return DLX_OK;
 }
 

@@ -87,6 +87,7 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
     // Per pixel and object, once: optical path (m) and phase (cycles) in FP64, as float pairs.
     const FF path = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
     const FF ph_cyc = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+    if (a.out_path) a.out_path[(long long)r * npix + p] = make_float4(path.hi, path.lo, ph_cyc.hi, ph_cyc.lo);
     float amp = o_amp ? o_amp[p] : 1.0f;
     if (o_scale) amp *= *o_scale;
     amp *= (float)a.const_scale;

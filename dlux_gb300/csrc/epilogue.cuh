@@ -29,6 +29,12 @@ __device__ __forceinline__ int epi_objects(const EpiArgs& e) { return e.objs.n >
 __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int l, int r, int y, int x,
                                                     int n, long long p) {
   // Same arithmetic as the phasor kernel so that forward and reverse agree.
+  const float2 il = e.inv_lambda_ff[l];
+  if (e.path) {
+    // the phasor kernel's own (path, phase) pairs: no FP64 work per wavelength
+    const float4 q = e.path[(long long)r * n * n + p];
+    return cis_ff(FF{q.x, q.y}, FF{il.x, il.y}, FF{q.z, q.w});
+  }
   const bool obj = e.objs.n > 0;
   const float* opd = obj ? e.objs.o[r].opd : e.opd;
   const float* phase = obj ? e.objs.o[r].phase : e.phase;
@@ -39,8 +45,36 @@ __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int l, int
   const double Y = ((double)y - half) * e.pixel_scale;
   const FF path = ff_from_double((opd ? (double)opd[p] : 0.0) + tx * X + ty * Y);
   const FF ph = ff_from_double(phase ? (double)phase[p] * (0.5 / CUDART_PI) : 0.0);
-  const float2 il = e.inv_lambda_ff[l];
   return cis_ff(path, FF{il.x, il.y}, ph);
+}
+
+// ---- per-element epilogues; l = wavelength, r = object, a = alpha_l ----
+__device__ __forceinline__ void epi_gradf_value(const EpiArgs& e, int r, float a, long long idx,
+                                                float2& v) {
+  // cotangent of F = alpha * D for <G, |F|^2>: 2 G F = 2 alpha G D
+  const float* G = e.objs.n > 0 ? e.objs.o[r].G : e.G;
+  const float g = 2.0f * a * G[idx];
+  v = make_float2(g * v.x, g * v.y);
+}
+
+__device__ __forceinline__ void epi_pupil_store(const EpiArgs& e, int b, int l, int r, float a,
+                                                int m, int n, int N, long long plane,
+                                                long long idx, float2 v) {
+  // D = Ebar / alpha at pupil pixel (y = m, x = n), square pupil M == N.
+  const bool obj = e.objs.n > 0;
+  const float* amp_p = obj ? e.objs.o[r].amp : e.amp;
+  const float* amp_s = obj ? e.objs.o[r].amp_scale : e.amp_scale;
+  const float* w_p = obj ? e.objs.o[r].weights : e.weights;
+  const float2 eb = make_float2(a * v.x, a * v.y);
+  const float2 u = pupil_unit_phasor(e, l, r, m, n, N, idx);
+  const float sw = w_p ? sqrtf(w_p[l]) : 1.0f;
+  float amp = amp_p ? amp_p[idx] : 1.0f;
+  if (amp_s) amp *= *amp_s;
+  // conj(u) * eb
+  const float re = u.x * eb.x + u.y * eb.y;
+  const float im = u.x * eb.y - u.y * eb.x;
+  e.out_f32[(long long)b * plane + idx] = sw * re;
+  e.out_f32b[(long long)b * plane + idx] = amp * sw * im;
 }
 
 __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n, int M, int N,
@@ -65,32 +99,125 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       break;
     }
     case EPI_GRADF: {
-      // cotangent of F = alpha * D for <G, |F|^2>: 2 G F = 2 alpha G D
-      const float* G = e.objs.n > 0 ? e.objs.o[r].G : e.G;
-      const float g = 2.0f * a * G[idx];
-      float2 w = make_float2(g * v.x, g * v.y);
+      epi_gradf_value(e, r, a, idx, v);
       if (e.out_split)
-        store_split(e.out_split + (long long)b * 4 * plane, plane, idx, w);
+        store_split(e.out_split + (long long)b * 4 * plane, plane, idx, v);
       else
-        e.out_c64[(long long)b * plane + idx] = w;
+        e.out_c64[(long long)b * plane + idx] = v;
       break;
     }
     case EPI_PUPIL: {
-      // D = Ebar / alpha at pupil pixel (y = m, x = n), square pupil M == N.
+      epi_pupil_store(e, b, l, r, a, m, n, N, plane, idx, v);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Column form used by the tensor-core kernels: one thread holds 32 values
+// D[b][m0 + j][n], j = 0..31, of one output column n, and the 32 lanes of a
+// warp hold consecutive n. Every load and store below is therefore one
+// contiguous segment per warp. Rows m >= M are skipped; n < N is the
+// caller's check.
+__device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0, int M, int N,
+                                          const float* re, const float* im) {
+  const int R = epi_objects(e);
+  const int l = b / R;
+  const int r = b - l * R;
+  const float a = e.alpha ? e.alpha[l] : 1.0f;
+  const long long plane = (long long)M * N;
+  const int mc = M - m0 < 32 ? M - m0 : 32;
+  const long long idx0 = (long long)m0 * N + n;
+  switch (e.kind) {
+    case EPI_C64: {
+      float2* o = e.out_c64 + (long long)b * plane + idx0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < mc) o[(long long)j * N] = make_float2(a * re[j], a * im[j]);
+      break;
+    }
+    case EPI_SPLIT: {
+      __nv_bfloat16* o = e.out_split + (long long)b * 4 * plane + idx0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < mc) store_split(o, plane, (long long)j * N, make_float2(a * re[j], a * im[j]));
+      break;
+    }
+    case EPI_INTENSITY: {
+      float* o = e.out_f32 + (long long)b * plane + idx0;
+      const float a2 = a * a;
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
+      break;
+    }
+    case EPI_GRADF: {
+      // all 32 loads first, so their latencies overlap
+      const float* G = (e.objs.n > 0 ? e.objs.o[r].G : e.G) + idx0;
+      float g[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) g[j] = j < mc ? __ldg(G + (long long)j * N) : 0.0f;
+      const float s = 2.0f * a;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < mc) {
+          const float gj = s * g[j];
+          const float2 v = make_float2(gj * re[j], gj * im[j]);
+          if (e.out_split)
+            store_split(e.out_split + (long long)b * 4 * plane + idx0, plane, (long long)j * N,
+                        v);
+          else
+            e.out_c64[(long long)b * plane + idx0 + (long long)j * N] = v;
+        }
+      }
+      break;
+    }
+    case EPI_PUPIL: {
+      if (!e.path) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (j < mc)
+            epi_pupil_store(e, b, l, r, a, m0 + j, n, N, plane, idx0 + (long long)j * N,
+                            make_float2(re[j], im[j]));
+        break;
+      }
+      // Same arithmetic as epi_pupil_store with the (path, phase) pairs of the
+      // phasor kernel; loads are issued eight rows at a time ahead of the math.
       const bool obj = e.objs.n > 0;
       const float* amp_p = obj ? e.objs.o[r].amp : e.amp;
       const float* amp_s = obj ? e.objs.o[r].amp_scale : e.amp_scale;
       const float* w_p = obj ? e.objs.o[r].weights : e.weights;
-      const float2 eb = make_float2(a * v.x, a * v.y);
-      const float2 u = pupil_unit_phasor(e, l, r, m, n, N, idx);
       const float sw = w_p ? sqrtf(w_p[l]) : 1.0f;
-      float amp = amp_p ? amp_p[idx] : 1.0f;
-      if (amp_s) amp *= *amp_s;
-      // conj(u) * eb
-      const float re = u.x * eb.x + u.y * eb.y;
-      const float im = u.x * eb.y - u.y * eb.x;
-      e.out_f32[(long long)b * plane + idx] = sw * re;
-      e.out_f32b[(long long)b * plane + idx] = amp * sw * im;
+      const float2 il = e.inv_lambda_ff[l];
+      const float4* path = e.path + (long long)r * N * N + idx0;
+      float* o_re = e.out_f32 + (long long)b * plane + idx0;
+      float* o_im = e.out_f32b + (long long)b * plane + idx0;
+#pragma unroll
+      for (int j0 = 0; j0 < 32; j0 += 8) {
+        float4 q[8];
+        float am[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int j = j0 + t;
+          q[t] = j < mc ? __ldg(path + (long long)j * N) : make_float4(0.f, 0.f, 0.f, 0.f);
+          am[t] = (amp_p && j < mc) ? __ldg(amp_p + idx0 + (long long)j * N) : 1.0f;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int j = j0 + t;
+          if (j < mc) {
+            const float2 eb = make_float2(a * re[j], a * im[j]);
+            const float2 u = cis_ff(FF{q[t].x, q[t].y}, FF{il.x, il.y}, FF{q[t].z, q[t].w});
+            float amp = am[t];
+            if (amp_s) amp *= *amp_s;
+            const float pr = u.x * eb.x + u.y * eb.y;
+            const float pi = u.x * eb.y - u.y * eb.x;
+            o_re[(long long)j * N] = sw * pr;
+            o_im[(long long)j * N] = amp * sw * pi;
+          }
+        }
+      }
       break;
     }
     default:

@@ -19,13 +19,21 @@
 // FP32. This keeps the polychromatic PSF within 1e-5 (relative L2) of the FP64
 // oracle at 512 x 512 x 512.
 //
-// CTA tile: 128 complex rows of A x 128 complex rows of B. TMEM holds main and
-// cross accumulators for the real and imaginary parts (4 x 128 fp32 columns =
-// all 512 columns). K is staged 32 elements at a time (64-byte rows, 64B
-// swizzle) by TMA in a 3-stage mbarrier pipeline (64 KB per stage). Warp
-// roles: warp 0 issues TMA,
-// warp 1 issues MMA (one thread each), warps 2-5 drain TMEM through the
-// shared epilogues. The kernel is persistent over (batch, m-tile, n-tile)
+// CTA tile: 128 complex rows of A x 128 complex rows of B. The tensor core
+// accumulates the transposed tile, so TMEM lane i holds output column n0 + i
+// and TMEM column j output row m0 + j. The epilogue threads then each drain
+// one output column, and the 32 lanes of a warp write 32 consecutive
+// elements of a row: every epilogue store and side-input load is one
+// contiguous segment. TMEM holds main and cross accumulators for the real and
+// imaginary parts (4 x 128 fp32 columns = all 512 columns). K is staged 32
+// elements at a time (64-byte rows, 64B swizzle) by TMA in a 3-stage mbarrier
+// pipeline (64 KB per stage). Warp roles: warp 0 issues TMA, warp 1 issues
+// MMA (one thread each), warps 2-9 drain TMEM through the shared epilogues,
+// two warps per TMEM lane quarter taking alternate 32-row chunks, so that the
+// epilogue's memory traffic has enough loads in flight. The MMAs of the next
+// tile wait for the drain (no TMEM is left for a second accumulator set), so
+// the epilogue's speed adds directly to the tile time.
+// The kernel is persistent over (batch, m-tile, n-tile)
 // work items. Every mbarrier wait is bounded by a wall-clock limit; on
 // expiry the CTA records DLX_ERR_TIMEOUT in a device status word, drains its
 // own in-flight copies and MMAs, frees TMEM and exits.
@@ -47,7 +55,8 @@ constexpr int A_PLANE_BYTES = TC_BM * TC_BK * 2;                         // 8 KB
 constexpr int B_PLANE_BYTES = TC_BN * TC_BK * 2;                         // 8 KB
 constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;       // 64 KB
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 320;  // TMA, MMA, 8 epilogue warps (two per TMEM lane quarter)
+constexpr int TC_EPI_WARPS = 8;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
 
@@ -206,119 +215,19 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 }
 
 // Instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major,
-// M = 128, N = 256, optional negation of A.
+// optional negation of the first operand. The MMA computes the transposed
+// tile D^T[n][m] = sum_k B[n][k] A[m][k]: its first operand is the B tile
+// (MMA M = TC_BN rows -> TMEM lanes) and its second the A tile (MMA N = TC_BM
+// -> TMEM columns). Negating either factor negates the product, so the sign
+// bit serves the -Ai*Bi and conj(A) terms unchanged.
 __host__ __device__ constexpr uint32_t make_idesc(bool neg_a) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((neg_a ? 1u : 0u) << 13) |
-         ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+         ((uint32_t)(TC_BM >> 3) << 17) | ((uint32_t)(TC_BN >> 4) << 24);
 }
 
 // --------------------------- vectorised epilogue ----------------------------
 __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
-}
-
-// Writes 32 consecutive complex values of one row as four split planes.
-__device__ __forceinline__ void store_split32(__nv_bfloat16* base_b, long long plane,
-                                              long long row, const float* re, const float* im) {
-  uint32_t rh[16], rl[16], ih[16], il[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    __nv_bfloat16 h0, l0, h1, l1;
-    split_bf16(re[2 * j], h0, l0);
-    split_bf16(re[2 * j + 1], h1, l1);
-    rh[j] = pack_bf16(h0, h1);
-    rl[j] = pack_bf16(l0, l1);
-    split_bf16(im[2 * j], h0, l0);
-    split_bf16(im[2 * j + 1], h1, l1);
-    ih[j] = pack_bf16(h0, h1);
-    il[j] = pack_bf16(l0, l1);
-  }
-  uint4* p0 = reinterpret_cast<uint4*>(base_b + row);
-  uint4* p1 = reinterpret_cast<uint4*>(base_b + plane + row);
-  uint4* p2 = reinterpret_cast<uint4*>(base_b + 2 * plane + row);
-  uint4* p3 = reinterpret_cast<uint4*>(base_b + 3 * plane + row);
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    p0[q] = make_uint4(rh[4 * q], rh[4 * q + 1], rh[4 * q + 2], rh[4 * q + 3]);
-    p1[q] = make_uint4(rl[4 * q], rl[4 * q + 1], rl[4 * q + 2], rl[4 * q + 3]);
-    p2[q] = make_uint4(ih[4 * q], ih[4 * q + 1], ih[4 * q + 2], ih[4 * q + 3]);
-    p3[q] = make_uint4(il[4 * q], il[4 * q + 1], il[4 * q + 2], il[4 * q + 3]);
-  }
-}
-
-__device__ __forceinline__ void epi_chunk32(const EpiArgs& e, int b, int m, int n0, int M, int N,
-                                            float* re, float* im) {
-  if (n0 + 32 > N) {
-    for (int j = 0; j < 32; ++j)
-      if (n0 + j < N) epi_apply(e, b, m, n0 + j, M, N, make_float2(re[j], im[j]));
-    return;
-  }
-  const int R = epi_objects(e);
-  const int wl = b / R;
-  const int obj = b - wl * R;
-  const float a = e.alpha ? e.alpha[wl] : 1.0f;
-  const long long plane = (long long)M * N;
-  const long long row = (long long)m * N + n0;
-  switch (e.kind) {
-    case EPI_C64: {
-      float4* o = reinterpret_cast<float4*>(e.out_c64 + (long long)b * plane + row);
-#pragma unroll
-      for (int j = 0; j < 16; ++j)
-        o[j] = make_float4(a * re[2 * j], a * im[2 * j], a * re[2 * j + 1], a * im[2 * j + 1]);
-      break;
-    }
-    case EPI_SPLIT: {
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        re[j] *= a;
-        im[j] *= a;
-      }
-      store_split32(e.out_split + (long long)b * 4 * plane, plane, row, re, im);
-      break;
-    }
-    case EPI_INTENSITY: {
-      const float a2 = a * a;
-      float4* o = reinterpret_cast<float4*>(e.out_f32 + (long long)b * plane + row);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        float4 v;
-        v.x = a2 * (re[4 * j] * re[4 * j] + im[4 * j] * im[4 * j]);
-        v.y = a2 * (re[4 * j + 1] * re[4 * j + 1] + im[4 * j + 1] * im[4 * j + 1]);
-        v.z = a2 * (re[4 * j + 2] * re[4 * j + 2] + im[4 * j + 2] * im[4 * j + 2]);
-        v.w = a2 * (re[4 * j + 3] * re[4 * j + 3] + im[4 * j + 3] * im[4 * j + 3]);
-        o[j] = v;
-      }
-      break;
-    }
-    case EPI_GRADF: {
-      const float* G = e.objs.n > 0 ? e.objs.o[obj].G : e.G;
-      const float4* gp = reinterpret_cast<const float4*>(G + row);
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const float4 g = __ldg(gp + j);
-        const float gg[4] = {g.x, g.y, g.z, g.w};
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const float s = 2.0f * a * gg[t];
-          re[4 * j + t] *= s;
-          im[4 * j + t] *= s;
-        }
-      }
-      if (e.out_split) {
-        store_split32(e.out_split + (long long)b * 4 * plane, plane, row, re, im);
-      } else {
-        float4* o = reinterpret_cast<float4*>(e.out_c64 + (long long)b * plane + row);
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          o[j] = make_float4(re[2 * j], im[2 * j], re[2 * j + 1], im[2 * j + 1]);
-      }
-      break;
-    }
-    default: {
-      for (int j = 0; j < 32; ++j) epi_apply(e, b, m, n0 + j, M, N, make_float2(re[j], im[j]));
-      break;
-    }
-  }
 }
 
 // --------------------------------- kernel -----------------------------------
@@ -355,7 +264,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, 4);
+    mbar_init(tempty, TC_EPI_WARPS);
     mbar_init(mdone, 1);
     *abort_flag = 0;
     fence_barrier_init();
@@ -413,8 +322,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
       const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
       // main (hi*hi) and cross (hi*lo + lo*hi) accumulators, real and imaginary
-      const uint32_t m_re = tmem, m_im = tmem + TC_BN;
-      const uint32_t c_re = tmem + 2 * TC_BN, c_im = tmem + 3 * TC_BN;
+      const uint32_t m_re = tmem, m_im = tmem + TC_BM;
+      const uint32_t c_re = tmem + 2 * TC_BM, c_im = tmem + 3 * TC_BM;
       int stage = 0;
       uint32_t ph = 0, acc_ph = 0;
       bool ok = true;
@@ -439,19 +348,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint64_t bil = make_desc(sb + 3 * B_PLANE_BYTES + ko);
             const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
             // Re += Ar Br -/+ Ai Bi
-            mma_bf16(m_re, arh, brh, id_pos, acc);
-            mma_bf16(m_re, aih, bih, id_rii, 1u);
-            mma_bf16(c_re, arh, brl, id_pos, acc);
-            mma_bf16(c_re, arl, brh, id_pos, 1u);
-            mma_bf16(c_re, aih, bil, id_rii, 1u);
-            mma_bf16(c_re, ail, bih, id_rii, 1u);
+            mma_bf16(m_re, brh, arh, id_pos, acc);
+            mma_bf16(m_re, bih, aih, id_rii, 1u);
+            mma_bf16(c_re, brl, arh, id_pos, acc);
+            mma_bf16(c_re, brh, arl, id_pos, 1u);
+            mma_bf16(c_re, bil, aih, id_rii, 1u);
+            mma_bf16(c_re, bih, ail, id_rii, 1u);
             // Im += Ar Bi +/- Ai Br
-            mma_bf16(m_im, arh, bih, id_pos, acc);
-            mma_bf16(m_im, aih, brh, id_iir, 1u);
-            mma_bf16(c_im, arh, bil, id_pos, acc);
-            mma_bf16(c_im, arl, bih, id_pos, 1u);
-            mma_bf16(c_im, aih, brl, id_iir, 1u);
-            mma_bf16(c_im, ail, brh, id_iir, 1u);
+            mma_bf16(m_im, bih, arh, id_pos, acc);
+            mma_bf16(m_im, brh, aih, id_iir, 1u);
+            mma_bf16(c_im, bil, arh, id_pos, acc);
+            mma_bf16(c_im, bih, arl, id_pos, 1u);
+            mma_bf16(c_im, brl, aih, id_iir, 1u);
+            mma_bf16(c_im, brh, ail, id_iir, 1u);
           }
           mma_commit(&empty[stage]);
           if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
@@ -466,8 +375,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {
     // -------------------------------- epilogue --------------------------------
+    // TMEM lane = output column n, TMEM column = output row m (see the MMA
+    // issue): each thread drains one column of the tile, 32 rows at a time.
     const int q = warp & 3;  // TMEM lane quarter this warp may access
-    const int row = q * 32 + lane;
+    const int half = (warp - 2) >> 2;  // the two warps of a quarter take alternate chunks
     uint32_t acc_ph = 0;
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
       if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
@@ -475,24 +386,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int b = w / (p.mt * p.nt);
       const int r = w - b * p.mt * p.nt;
       const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
-      const int m = mt * TC_BM + row;
-      const int nbase = nt * TC_BN;
+      const int n = nt * TC_BN + q * 32 + lane;
+      const int mbase = mt * TC_BM;
       const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int c = 0; c < TC_BN / 32; ++c) {
-        if (nbase + c * 32 >= p.N) break;  // warp-uniform
+      for (int c = half; c < TC_BM / 32; c += 2) {
+        if (mbase + c * 32 >= p.M) break;  // warp-uniform
         float re[32], im[32], cre[32], cim[32];
         tmem_ld32(lane_addr + c * 32, re);
-        tmem_ld32(lane_addr + TC_BN + c * 32, im);
-        tmem_ld32(lane_addr + 2 * TC_BN + c * 32, cre);
-        tmem_ld32(lane_addr + 3 * TC_BN + c * 32, cim);
+        tmem_ld32(lane_addr + TC_BM + c * 32, im);
+        tmem_ld32(lane_addr + 2 * TC_BM + c * 32, cre);
+        tmem_ld32(lane_addr + 3 * TC_BM + c * 32, cim);
         tmem_ld_wait();
 #pragma unroll
         for (int t = 0; t < 32; ++t) {
           re[t] += cre[t];
           im[t] += cim[t];
         }
-        if (m < p.M) epi_chunk32(p.epi, b, m, nbase + c * 32, p.M, p.N, re, im);
+        if (n < p.N) epi_col32(p.epi, b, n, mbase + c * 32, p.M, p.N, re, im);
       }
       tc_fence_before();
       __syncwarp();
@@ -631,8 +542,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       const uint32_t id_neg = make_idesc(true);
       const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
       const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
-      const uint32_t m_re = tmem, m_im = tmem + TC_BN;
-      const uint32_t c_re = tmem + 2 * TC_BN, c_im = tmem + 3 * TC_BN;
+      const uint32_t m_re = tmem, m_im = tmem + TC_BM;
+      const uint32_t c_re = tmem + 2 * TC_BM, c_im = tmem + 3 * TC_BM;
       int sb = 0, sa = 0;
       uint32_t phb = 0, pha = 0, acc_ph = 0;
       bool ok = true;
@@ -657,18 +568,18 @@ __global__ void __launch_bounds__(G_THREADS, 1)
             const uint64_t bih = make_desc(s_b + 2 * B_PLANE_BYTES + ko);
             const uint64_t bil = make_desc(s_b + 3 * B_PLANE_BYTES + ko);
             const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
-            mma_bf16(m_re, arh, brh, id_pos, acc);
-            mma_bf16(m_re, aih, bih, id_rii, 1u);
-            mma_bf16(c_re, arh, brl, id_pos, acc);
-            mma_bf16(c_re, arl, brh, id_pos, 1u);
-            mma_bf16(c_re, aih, bil, id_rii, 1u);
-            mma_bf16(c_re, ail, bih, id_rii, 1u);
-            mma_bf16(m_im, arh, bih, id_pos, acc);
-            mma_bf16(m_im, aih, brh, id_iir, 1u);
-            mma_bf16(c_im, arh, bil, id_pos, acc);
-            mma_bf16(c_im, arl, bih, id_pos, 1u);
-            mma_bf16(c_im, aih, brl, id_iir, 1u);
-            mma_bf16(c_im, ail, brh, id_iir, 1u);
+            mma_bf16(m_re, brh, arh, id_pos, acc);
+            mma_bf16(m_re, bih, aih, id_rii, 1u);
+            mma_bf16(c_re, brl, arh, id_pos, acc);
+            mma_bf16(c_re, brh, arl, id_pos, 1u);
+            mma_bf16(c_re, bil, aih, id_rii, 1u);
+            mma_bf16(c_re, bih, ail, id_rii, 1u);
+            mma_bf16(m_im, bih, arh, id_pos, acc);
+            mma_bf16(m_im, brh, aih, id_iir, 1u);
+            mma_bf16(c_im, bil, arh, id_pos, acc);
+            mma_bf16(c_im, bih, arl, id_pos, 1u);
+            mma_bf16(c_im, brl, aih, id_iir, 1u);
+            mma_bf16(c_im, brh, ail, id_iir, 1u);
           }
           mma_commit(&bempty[sb]);
           mma_commit(&aempty[sa]);
@@ -684,8 +595,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     }
   } else if (warp < 6) {
     // -------------------------------- epilogue --------------------------------
-    const int q = warp & 3;
-    const int row = q * 32 + lane;
+    const int q = warp & 3;  // column-per-thread drain, as in tc_cgemm_kernel
     uint32_t acc_ph = 0;
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
       if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
@@ -693,24 +603,24 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       const int b = w / (p.mt * p.nt);
       const int r = w - b * p.mt * p.nt;
       const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
-      const int m = mt * TC_BM + row;
-      const int nbase = nt * TC_BN;
+      const int n = nt * TC_BN + q * 32 + lane;
+      const int mbase = mt * TC_BM;
       const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int c = 0; c < TC_BN / 32; ++c) {
-        if (nbase + c * 32 >= p.N) break;
+      for (int c = 0; c < TC_BM / 32; ++c) {
+        if (mbase + c * 32 >= p.M) break;
         float re[32], im[32], t[32];
         tmem_ld32(lane_addr + c * 32, re);
-        tmem_ld32(lane_addr + TC_BN + c * 32, im);
-        tmem_ld32(lane_addr + 2 * TC_BN + c * 32, t);
+        tmem_ld32(lane_addr + TC_BM + c * 32, im);
+        tmem_ld32(lane_addr + 2 * TC_BM + c * 32, t);
         tmem_ld_wait();
 #pragma unroll
         for (int i = 0; i < 32; ++i) re[i] += t[i];
-        tmem_ld32(lane_addr + 3 * TC_BN + c * 32, t);
+        tmem_ld32(lane_addr + 3 * TC_BM + c * 32, t);
         tmem_ld_wait();
 #pragma unroll
         for (int i = 0; i < 32; ++i) im[i] += t[i];
-        if (m < p.M) epi_chunk32(p.epi, b, m, nbase + c * 32, p.M, p.N, re, im);
+        if (n < p.N) epi_col32(p.epi, b, n, mbase + c * 32, p.M, p.N, re, im);
       }
       tc_fence_before();
       __syncwarp();

@@ -64,6 +64,9 @@ struct PhasorArgs {
   double pixel_scale, tilt_x, tilt_y;
   float2* out_c64;             // one of the two outputs
   __nv_bfloat16* out_split;    // [b][4][n][n]
+  // nullable [object][n][n]: (path hi, path lo, phase hi, phase lo) per pixel, the
+  // wavelength-independent inputs of cis_ff, for the reverse pass's epilogue
+  float4* out_path;
 };
 int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream_t s);
 
@@ -141,6 +144,7 @@ struct EpiArgs {
   const float* weights;      // [b] nullable (1)
   const float2* inv_lambda_ff;  // [b] (hi, lo) of 1/lambda
   double pixel_scale, tilt_x, tilt_y;
+  const float4* path;        // nullable [object][n][n] from PhasorArgs::out_path
 };
 
 struct GemmArgs {
