@@ -741,7 +741,7 @@ struct dlx_poly_plan_s {
   DevBuf fbar;       // [L*R][M][M] c64 or split
   DevBuf planes;     // intensity [L*R][M][M] f32, or pre/pim [2][L*R][N][N] f32
   DevBuf partial;    // double reduction partials
-  DevBuf pathff;     // [R][N][N] float4 (path, phase) pairs of the reverse pass
+  DevBuf pathff;     // [R][N][N] float4 (path, phase) pairs, then [R][3][N][N] pixel sums
   int nparts = kPolyParts;
 
   // Device bytes this plan owns: an attached workspace belongs to the caller.
@@ -846,6 +846,36 @@ struct dlx_poly_plan_s {
     EpiArgs e3 = epi_store(v, mid.p, nullptr);
     e3.objs = t;
     DLX_TRY(run_gemm(v, gemm(ts.opANx(), R, N, M, M, true, fbar.p, e3), s));
+    ObjReduceArgs ra{};
+    ra.objs = t;
+    ra.outs = o;
+    ra.L = L;
+    ra.npix = (long long)N * N;
+    ra.k_dev = ts.kvec.as<double>();
+    ra.n_side = N;
+    ra.pixel_scale = pixel_scale_in;
+    ra.partial_ws = partial.as<double>();
+    ra.nparts = nparts;
+    ra.sum_pixels = sum_pixels ? 1 : 0;
+    ra.sum_g_amp = sum_amp;
+    ra.sum_g_opd = sum_opd;
+    ra.sum_g_phase = sum_phase;
+    ra.accumulate_sum = accumulate_sum ? 1 : 0;
+    if (L <= kFusedPupilMaxL) {
+      // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v] as complex planes; the
+      // fused reduction forms the per-wavelength pupil terms and sums them.
+      EpiArgs ec{};
+      ec.kind = EPI_C64;
+      ec.objs = t;
+      ec.alpha = ts.alpha.as<float>();
+      ec.out_c64 = planes.as<float2>();
+      DLX_TRY(run_gemm(v, gemm(ts.opANy(), R, N, N, M, true, mid.p, ec), s));
+      ra.ebar = planes.as<float2>();
+      ra.path = pathff.as<float4>();
+      ra.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
+      ra.pix_scratch = reinterpret_cast<float*>(pathff.as<float4>() + (size_t)R * N * N);
+      return launch_obj_pupil_fused(ra, s);
+    }
     // Ebar[y][x] = alpha sum_v conj(Ay[y][v]) Xt[x][v] -> pupil-gradient planes
     float* pre = planes.as<float>();
     float* pim = pre + (size_t)L * R * N * N;
@@ -859,23 +889,8 @@ struct dlx_poly_plan_s {
     ep.pixel_scale = pixel_scale_in;
     ep.path = pathff.as<float4>();
     DLX_TRY(run_gemm(v, gemm(ts.opANy(), R, N, N, M, true, mid.p, ep), s));
-    ObjReduceArgs ra{};
-    ra.objs = t;
-    ra.outs = o;
-    ra.L = L;
-    ra.npix = (long long)N * N;
     ra.pre = pre;
     ra.pim = pim;
-    ra.k_dev = ts.kvec.as<double>();
-    ra.n_side = N;
-    ra.pixel_scale = pixel_scale_in;
-    ra.partial_ws = partial.as<double>();
-    ra.nparts = nparts;
-    ra.sum_pixels = sum_pixels ? 1 : 0;
-    ra.sum_g_amp = sum_amp;
-    ra.sum_g_opd = sum_opd;
-    ra.sum_g_phase = sum_phase;
-    ra.accumulate_sum = accumulate_sum ? 1 : 0;
     return launch_obj_pupil_reduce(ra, s);
   }
 };
@@ -890,7 +905,7 @@ static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[kPol
   const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
   sz[3] = a > b ? a : b;
   sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
-  sz[5] = sizeof(float4) * (size_t)R * n * n;
+  sz[5] = (sizeof(float4) + 3 * sizeof(float)) * (size_t)R * n * n;  // (path, phase) + pixel sums
   for (int i = 0; i < kPolyBuffers; ++i) sz[i] = (sz[i] + 255) / 256 * 256;
 }
 

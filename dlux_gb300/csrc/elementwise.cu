@@ -3,6 +3,8 @@
 // each is written for coalesced access with one pixel per thread and a
 // wavelength loop inside the thread where the inputs are shared across the
 // batch.
+#include <atomic>
+
 #include "kernels.h"
 
 #include <math_constants.h>
@@ -575,6 +577,147 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
       }
     }
   }
+}
+
+// Fused reverse-pass pupil reduction. One block covers a chunk of pixels of
+// one object; every thread owns a pixel and walks the wavelengths, forming
+// the same per-wavelength planes as the pre/pim path from the pupil field
+// Ebar and the unit phasor (recomputed from the phasor kernel's pairs):
+//   pre_l = sqrt(w_l) Re(conj(u_l) Ebar_l),  pim_l = amp sqrt(w_l) Im(conj(u_l) Ebar_l)
+// and summing them at once: pixel gradients (g_amp = sum pre, g_phase = sum
+// pim, g_opd = sum k_l pim), tilt partials, and weight partials
+// sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
+__global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
+  extern __shared__ double wpart[];  // [8 warps][L] weight partials
+  __shared__ double tsm[32];
+  const int r = blockIdx.y;
+  const int R = a.objs.n;
+  const ObjDesc od = a.objs.o[r];
+  const ObjOut out = a.outs.o[r];
+  const bool pix_out = !a.sum_pixels && (out.g_amp || out.g_phase || out.g_opd);
+  const bool w_out = want_w && out.g_w;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (w_out)
+    for (int i = threadIdx.x; i < 8 * a.L; i += blockDim.x) wpart[i] = 0.0;
+  __syncthreads();
+  const long long chunk = (a.npix + a.nparts - 1) / a.nparts;
+  const long long lo = (long long)blockIdx.x * chunk;
+  const long long hi = min(a.npix, lo + chunk);
+  const double half = 0.5 * (a.n_side - 1);
+  const float4* path = a.path + (long long)r * a.npix;
+  double tx = 0.0, ty = 0.0;
+  for (long long p0 = lo; p0 < hi; p0 += blockDim.x) {  // block-uniform trip count
+    const long long p = p0 + threadIdx.x;
+    const bool live = p < hi;
+    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+    float amp_raw = 1.0f, amp = 1.0f;
+    if (live) {
+      q = path[p];
+      amp_raw = od.amp ? od.amp[p] : 1.0f;
+      amp = amp_raw;
+      if (od.amp_scale) amp *= *od.amp_scale;
+    }
+    float sre = 0.f, sim = 0.f, sk = 0.f;
+    for (int l = 0; l < a.L; ++l) {
+      float pre = 0.f;
+      if (live) {
+        const float2 eb = a.ebar[((long long)l * R + r) * a.npix + p];
+        const float2 il = a.inv_lambda_ff[l];
+        const float2 u = cis_ff(FF{q.x, q.y}, FF{il.x, il.y}, FF{q.z, q.w});
+        const float sw = od.weights ? sqrtf(od.weights[l]) : 1.0f;
+        const float pr = u.x * eb.x + u.y * eb.y;
+        const float pi = u.x * eb.y - u.y * eb.x;
+        pre = sw * pr;
+        const float pim = amp * sw * pi;
+        sre += pre;
+        sim += pim;
+        sk += (float)a.k_dev[l] * pim;
+      }
+      if (w_out) {  // warp-uniform
+        float v = pre * amp_raw;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) wpart[warp * a.L + l] += (double)v;
+      }
+    }
+    if (live) {
+      if (pix_out) {
+        if (out.g_amp) out.g_amp[p] = sre;
+        if (out.g_phase) out.g_phase[p] = sim;
+        if (out.g_opd) out.g_opd[p] = sk;
+      }
+      if (a.sum_pixels) {
+        float* sc = a.pix_scratch + (long long)r * 3 * a.npix;
+        sc[p] = sre;
+        sc[a.npix + p] = sim;
+        sc[2 * a.npix + p] = sk;
+      }
+      const int y = (int)(p / a.n_side);
+      const int x = (int)(p - (long long)y * a.n_side);
+      tx += ((double)x - half) * a.pixel_scale * (double)sk;
+      ty += ((double)y - half) * a.pixel_scale * (double)sk;
+    }
+  }
+  if (out.g_tilt) {
+    const double sx = block_sum<256>(tx, tsm);
+    const double sy = block_sum<256>(ty, tsm);
+    if (threadIdx.x == 0) {
+      double* part = a.partial_ws + ((long long)r * a.nparts + blockIdx.x) * 2;
+      part[0] = sx;
+      part[1] = sy;
+    }
+  }
+  if (w_out) {
+    __syncthreads();
+    double* part = a.partial_ws + (long long)R * a.nparts * 2;
+    for (int l = threadIdx.x; l < a.L; l += blockDim.x) {
+      double t = 0.0;
+      for (int w = 0; w < 8; ++w) t += wpart[w * a.L + l];
+      part[((long long)r * a.L + l) * a.nparts + blockIdx.x] = t;
+    }
+  }
+}
+
+// Sum of the per-object pixel gradients over the objects, in object order.
+__global__ void obj_pupil_sumr_kernel(ObjReduceArgs a) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.npix) return;
+  float sre = 0.f, sim = 0.f, sk = 0.f;
+  for (int r = 0; r < a.objs.n; ++r) {
+    const float* sc = a.pix_scratch + (long long)r * 3 * a.npix;
+    sre += sc[p];
+    sim += sc[a.npix + p];
+    sk += sc[2 * a.npix + p];
+  }
+  if (a.sum_g_amp) a.sum_g_amp[p] = a.accumulate_sum ? a.sum_g_amp[p] + sre : sre;
+  if (a.sum_g_phase) a.sum_g_phase[p] = a.accumulate_sum ? a.sum_g_phase[p] + sim : sim;
+  if (a.sum_g_opd) a.sum_g_opd[p] = a.accumulate_sum ? a.sum_g_opd[p] + sk : sk;
+}
+
+int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s) {
+  const int R = a.objs.n;
+  if (a.npix == 0 || R == 0) return DLX_OK;
+  if (a.L > kFusedPupilMaxL)
+    return fail(DLX_ERR_SHAPE, "fused pupil reduction: too many wavelengths");
+  bool want_w = false;
+  for (int r = 0; r < R; ++r) want_w |= a.outs.o[r].g_w != nullptr;
+  const size_t smem = want_w ? sizeof(double) * 8 * (size_t)a.L : 0;
+  static std::atomic<bool> attr_done{false};  // host side, once per process
+  if (smem > 48 * 1024 && !attr_done.load()) {
+    DLX_TRY_CUDA(cudaFuncSetAttribute(obj_pupil_fused_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(sizeof(double) * 8 * kFusedPupilMaxL)));
+    attr_done.store(true);
+  }
+  obj_pupil_fused_kernel<<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
+  DLX_LAUNCH_CHECK("obj_pupil_fused_kernel");
+  if (a.sum_pixels) {
+    obj_pupil_sumr_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
+    DLX_LAUNCH_CHECK("obj_pupil_sumr_kernel");
+  }
+  obj_finish_kernel<<<R, 256, 0, s>>>(a, want_w ? 1 : 0);
+  DLX_LAUNCH_CHECK("obj_finish_kernel");
+  return DLX_OK;
 }
 
 int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s) {

@@ -389,25 +389,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int n = nt * TC_BN + q * 32 + lane;
       const int mbase = mt * TC_BM;
       const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
-#pragma unroll 1
-      for (int c = half; c < TC_BM / 32; c += 2) {
-        if (mbase + c * 32 >= p.M) break;  // warp-uniform
-        float re[32], im[32], cre[32], cim[32];
-        tmem_ld32(lane_addr + c * 32, re);
-        tmem_ld32(lane_addr + TC_BM + c * 32, im);
-        tmem_ld32(lane_addr + 2 * TC_BM + c * 32, cre);
-        tmem_ld32(lane_addr + 3 * TC_BM + c * 32, cim);
-        tmem_ld_wait();
+      // Drain both chunks of this warp (rows c0 and c0 + 64) into registers,
+      // hand TMEM back to the MMA warp, then run the epilogue from registers
+      // while the next tile's MMAs proceed.
+      const int c0 = half, c1 = half + 2;
+      const bool has0 = mbase + c0 * 32 < p.M, has1 = mbase + c1 * 32 < p.M;  // warp-uniform
+      float re0[32], im0[32], re1[32], im1[32];
+      {
+        float t[32];
+        if (has0) {
+          tmem_ld32(lane_addr + c0 * 32, re0);
+          tmem_ld32(lane_addr + 2 * TC_BM + c0 * 32, t);
+          tmem_ld_wait();
 #pragma unroll
-        for (int t = 0; t < 32; ++t) {
-          re[t] += cre[t];
-          im[t] += cim[t];
+          for (int i = 0; i < 32; ++i) re0[i] += t[i];
+          tmem_ld32(lane_addr + TC_BM + c0 * 32, im0);
+          tmem_ld32(lane_addr + 3 * TC_BM + c0 * 32, t);
+          tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 32; ++i) im0[i] += t[i];
         }
-        if (n < p.N) epi_col32(p.epi, b, n, mbase + c * 32, p.M, p.N, re, im);
+        if (has1) {
+          tmem_ld32(lane_addr + c1 * 32, re1);
+          tmem_ld32(lane_addr + 2 * TC_BM + c1 * 32, t);
+          tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 32; ++i) re1[i] += t[i];
+          tmem_ld32(lane_addr + TC_BM + c1 * 32, im1);
+          tmem_ld32(lane_addr + 3 * TC_BM + c1 * 32, t);
+          tmem_ld_wait();
+#pragma unroll
+          for (int i = 0; i < 32; ++i) im1[i] += t[i];
+        }
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty);
+      if (n < p.N) {
+        if (has0) epi_col32(p.epi, b, n, mbase + c0 * 32, p.M, p.N, re0, im0);
+        if (has1) epi_col32(p.epi, b, n, mbase + c1 * 32, p.M, p.N, re1, im1);
+      }
       acc_ph ^= 1u;
     }
   }

@@ -111,9 +111,19 @@ struct ObjReduceArgs {
   float* sum_g_phase;
   int sum_pixels;
   int accumulate_sum;        // add into the sums instead of overwriting them
+  // Fused form (launch_obj_pupil_fused): the reverse pass's pupil field
+  // Ebar [L*R][npix] (alpha applied) and the phasor kernel's (path, phase)
+  // pairs [R][npix] replace the pre/pim planes.
+  const float2* ebar;
+  const float4* path;
+  const float2* inv_lambda_ff;  // [L]
+  float* pix_scratch;        // [R][3][npix] per-object pixel sums (sum_pixels only)
 };
 int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s);
 int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s);
+// Largest wavelength count the fused pupil reduction accepts.
+constexpr int kFusedPupilMaxL = 3072;
+int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s);
 
 
 // --- gemm_fp32.cu / gemm_tc.cu ---------------------------------------------
