@@ -17,6 +17,7 @@ is made between steps.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--variant split_bf16|fp32]
   python bench.py --impl reference   # the CPU restatement of the same step
   python bench.py --workload serving # mixed-shape request stream through the server
+  python bench.py --workload cfg1|cfg3|cfg4   # the other measured configurations
 """
 
 from __future__ import annotations
@@ -43,6 +44,11 @@ N_WAVELENGTHS = 64
 NOLLS = list(range(4, 25))
 SEED = 2
 METRIC = "PSF+grad evals/sec"
+# DRAM bytes (read + write) of one tensor-core GEMM launch per wavelength, from an ncu
+# capture of a 16-wavelength launch of this workload (71.0 MB / 16). Traffic grows in
+# proportion to the wavelength count (each wavelength is an independent GEMM on its own
+# operands).
+GEMM_DRAM_BYTES_PER_WAVELENGTH = (67.35e6 + 3.57e6) / 16
 
 
 def config_dict(extra=None):
@@ -369,6 +375,157 @@ def run_serving(args):
     return 0
 
 
+# ----------------------------------------------------------------------------
+# The other measured configurations (not the default line)
+# ----------------------------------------------------------------------------
+def cfg_workload(name, variant):
+    """(step function, metric, unit, flops per step, description) of one configuration.
+
+    cfg1: latency of one PSF + coefficient gradient, 256^2 pupil (10% obscuration),
+          Noll 4-13 ~ N(0, 50 nm), one wavelength 1 um, 128^2 PSF at 0.02", loss sum(R*PSF).
+    cfg3: phase retrieval, 512^2 pupil, amplitude T(1 + N(0, 0.01)), Noll 4-39 ~ N(0, 40 nm),
+          32 wavelengths 0.9-1.1 um equal weights, 256^2 detector at 0.02" with flat field
+          1 + N(0, 0.02), Poisson NLL of Poisson(1e6-photon) data; gradients w.r.t.
+          coefficients, amplitude and flat.
+    cfg4: 1024 point sources, 1024^2 pupil (10% obscuration), Noll 4-24 ~ N(0, 30 nm),
+          positions U(-2, 2)", fluxes 10^U(2, 6), 16 wavelengths 0.8-1.2 um, one 128^2 image
+          at 0.02"; gradients of sum(R*image) w.r.t. positions and fluxes.
+    """
+    import torch
+    import dlux_gb300 as dl
+    import dlux_gb300.utils as dlu
+
+    dl.set_variant(variant)
+    dev = "cuda"
+    f32 = dict(dtype=torch.float32, device=dev)
+    if name == "cfg1":
+        rng = np.random.default_rng(1)
+        T, B = dlu.circular_aperture(256, 1.0, oversample=1, secondary_diameter=0.1,
+                                     zernike_nolls=list(range(4, 14)))
+        c0 = torch.as_tensor(rng.normal(0, 50e-9, 10), **f32)
+        R = torch.as_tensor(rng.normal(size=(128, 128)), **f32)
+        optics = dl.AngularOpticalSystem(256, 1.0, [dl.TransmissiveLayer(T, normalise=True),
+                                                    dl.BasisLayer(B, c0)], 128, 0.02, 1)
+        wls = [1e-6]
+
+        def run():
+            c = c0.detach().requires_grad_(True)
+            psf = optics.set("layers.BasisLayer.coefficients", c).propagate(wls)
+            loss = (psf * R).sum()
+            loss.backward()
+            return loss
+        flops = 3 * 8 * (128 * 256 ** 2 + 128 ** 2 * 256)
+        return run, "PSF+grad latency", "ms", flops, "256^2 pupil, 1 lambda, 128^2 PSF"
+    if name == "cfg3":
+        rng = np.random.default_rng(3)
+        T, B = dlu.circular_aperture(512, 1.0, oversample=1, secondary_diameter=0.1,
+                                     zernike_nolls=list(range(4, 40)))
+        Tn = T.cpu().numpy() if hasattr(T, "cpu") else np.asarray(T)
+        A0 = torch.as_tensor(Tn * (1 + rng.normal(0, 0.01, Tn.shape)), **f32)
+        c0 = torch.as_tensor(rng.normal(0, 40e-9, 36), **f32)
+        flat0 = torch.as_tensor(1 + rng.normal(0, 0.02, (256, 256)), **f32)
+        wls = np.linspace(0.9e-6, 1.1e-6, 32)
+        optics = dl.AngularOpticalSystem(512, 1.0, [dl.TransmissiveLayer(A0, normalise=True),
+                                                    dl.BasisLayer(B, c0)], 256, 0.02, 1)
+        with torch.no_grad():
+            psf = optics.propagate(wls) * flat0
+            lam = psf * (1e6 / psf.sum())
+        data = torch.poisson(lam.double(), generator=torch.Generator(device=dev).manual_seed(3)).float()
+        scale = float(1e6 / psf.sum())
+
+        def run():
+            A = A0.detach().requires_grad_(True)
+            c = c0.detach().requires_grad_(True)
+            flat = flat0.detach().requires_grad_(True)
+            sys_ = optics.set(["layers.TransmissiveLayer.transmission",
+                               "layers.BasisLayer.coefficients"], [A, c])
+            det = dl.LayeredDetector([dl.ApplyPixelResponse(flat)])
+            img = det.model(sys_.propagate(wls, return_psf=True)) * scale
+            loss = (img - data * torch.log(img)).sum()
+            loss.backward()
+            return loss
+        flops = 3 * 32 * 8 * (256 * 512 ** 2 + 256 ** 2 * 512)
+        return run, "phase-retrieval loss+grad evals/sec", "evals/s", flops, \
+            "512^2 pupil, 36 Zernikes, 32 lambda, 256^2 detector, Poisson NLL"
+    if name == "cfg4":
+        rng = np.random.default_rng(4)
+        T, B = dlu.circular_aperture(1024, 1.0, oversample=1, secondary_diameter=0.1,
+                                     zernike_nolls=list(range(4, 25)))
+        c0 = torch.as_tensor(rng.normal(0, 30e-9, 21), **f32)
+        S = 1024
+        pos0 = torch.as_tensor(rng.uniform(-2, 2, (S, 2)) * np.pi / 180 / 3600,
+                               dtype=torch.float64)
+        flux0 = torch.as_tensor(10 ** rng.uniform(2, 6, S), **f32)
+        R = torch.as_tensor(rng.normal(size=(128, 128)), **f32)
+        wls = np.linspace(0.8e-6, 1.2e-6, 16)
+        optics = dl.AngularOpticalSystem(1024, 1.0, [dl.TransmissiveLayer(T, normalise=True),
+                                                     dl.BasisLayer(B, c0)], 128, 0.02, 1)
+
+        def run():
+            pos = pos0.detach().requires_grad_(True)
+            flux = flux0.detach().requires_grad_(True)
+            img = dl.PointSources(wls, position=pos, flux=flux).model(optics)
+            loss = (img * R).sum()
+            loss.backward()
+            return loss
+        flops = 3 * S * 16 * 8 * (128 * 1024 ** 2 + 128 ** 2 * 1024)
+        return run, "scene (1024 sources) loss+grad evals/sec", "evals/s", flops, \
+            "1024 point sources, 1024^2 pupil, 16 lambda, 128^2 image"
+    raise ValueError(name)
+
+
+def run_config(args):
+    import torch
+    import dlux_gb300._lib as L
+    import ctypes
+
+    out = {}
+    variants = [args.variant] + (["fp32"] if args.variant == "split_bf16" and
+                                 not args.no_fp32_compare else [])
+    for variant in variants:
+        run, metric, unit, flops, desc = cfg_workload(args.workload, variant)
+        for _ in range(max(3, args.warmup)):
+            run()
+        torch.cuda.synchronize()
+        lib = L.load()
+        clocks = ClockSampler(torch.cuda.current_device())
+        clocks.start()
+        time.sleep(0.3)
+        L.check(lib.dlx_gemm_timing_begin())
+        times = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            run()
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        tot, cnt, fl = ctypes.c_double(0), ctypes.c_int(0), ctypes.c_double(0)
+        L.check(lib.dlx_gemm_timing_end(ctypes.byref(tot), ctypes.byref(cnt), ctypes.byref(fl)))
+        clk = clocks.stop()
+        t = np.array(times)
+        gemm_tf = fl.value / (tot.value * 1e-3) / 1e12 if tot.value > 0 else None
+        out[variant] = {"ms_mean": float(t.mean()), "ms_p50": float(np.percentile(t, 50)),
+                        "ms_p99": float(np.percentile(t, 99)),
+                        "evals_per_s": 1e3 / float(t.mean()),
+                        "algorithmic_tflops": flops / (t.mean() * 1e-3) / 1e12,
+                        "gemm_tflops": gemm_tf,
+                        "gemm_share": tot.value / t.sum() if t.sum() > 0 else None,
+                        "clocks": clk}
+    main = out[args.variant]
+    value = main["ms_p50"] if args.workload == "cfg1" else main["evals_per_s"]
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": main["ms_mean"],
+            "higher_is_better": args.workload != "cfg1", "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": f"{args.workload}: {desc}"}, "p50_ms": main["ms_p50"],
+            "p99_ms": main["ms_p99"], "clocks": main["clocks"], "variants": out}
+    print(json.dumps(line))
+    return 0
+
+
 def load_peaks():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -387,7 +544,8 @@ def main():
     ap.add_argument("--variant", default="split_bf16", choices=["split_bf16", "fp32"])
     ap.add_argument("--no-fp32-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="psf_grad", choices=["psf_grad", "serving"])
+    ap.add_argument("--workload", default="psf_grad",
+                    choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
@@ -407,6 +565,8 @@ def main():
     torch.cuda.set_device(local)
     if args.workload == "serving":
         return run_serving(args) if rank == 0 else 0
+    if args.workload in ("cfg1", "cfg3", "cfg4"):
+        return run_config(args) if rank == 0 else 0
     if world > 1:
         torch.distributed.init_process_group("nccl")
 
@@ -430,7 +590,10 @@ def main():
         flops_launch = g["flops"] / g["launches"]
         achieved = flops_launch / (avg_ms * 1e-3) / 1e12
         roofline = {"bound": "tensor", "achieved": achieved, "peak": tflops, "unit": "TFLOP/s",
-                    "frac": achieved / tflops, "traffic": None,
+                    "frac": achieved / tflops,
+                    "traffic": GEMM_DRAM_BYTES_PER_WAVELENGTH * N_WAVELENGTHS,
+                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                      "16-wavelength launch, scaled to the launch's wavelengths",
                     "peak_source": f"{src} bf16 dense (burst)",
                     "kernel": "tc_cgemm_kernel" if args.variant == "split_bf16" else
                               "cgemm_fp32_kernel",
