@@ -23,6 +23,7 @@ is made between steps.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -329,8 +330,9 @@ def run_serving(args):
     variants = [args.variant] + (["fp32"] if args.variant == "split_bf16" and
                                  not args.no_fp32_compare else [])
     for variant in variants:
-        srv = serving.PSFServer(max_batch=8, n_slots=4, hbm_budget=150e9, k_max=36,
-                                limits=(1024, 512, 64), variant=variant, timeout_s=120.0)
+        srv = serving.PSFServer(max_batch=8, n_slots=args.slots, hbm_budget=150e9, k_max=36,
+                                limits=(1024, 512, 64), variant=variant, timeout_s=120.0,
+                                graph_after=args.graph_after)
         times, reqs = serving.poisson_stream(args.requests, args.rate, seed=SEED)
         _, warm = serving.poisson_stream(max(args.requests // 4, 50), args.rate, seed=SEED + 1)
         keys = sorted({r.key for r in reqs} | {r.key for r in warm})
@@ -344,7 +346,12 @@ def run_serving(args):
         srv.completed.clear()
         clocks = ClockSampler(torch.cuda.current_device())
         clocks.start()
-        serving.replay(srv, times, reqs)
+        gc.collect()
+        gc.disable()        # no collector pauses inside the timed stream
+        try:
+            serving.replay(srv, times, reqs)
+        finally:
+            gc.enable()
         clk = clocks.stop()
         srv.stop()
         rep = srv.report(reqs)
@@ -365,7 +372,7 @@ def run_serving(args):
         "config": {"workload": f"serving: Poisson {args.rate:g} req/s, N in 128-1024, M in "
                                "64-512, L in 1..64, K in 4..36, 30% gradients",
                    "requests": args.requests, "rate_hz": args.rate, "max_batch": 8,
-                   "slots": 4, "hbm_budget_gb": 150},
+                   "slots": args.slots, "graph_after": args.graph_after, "hbm_budget_gb": 150},
         "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
         "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
         "clocks": main_rep["clocks"],
@@ -548,6 +555,9 @@ def main():
                     choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
+    ap.add_argument("--slots", type=int, default=4, help="serving: concurrent stream slots")
+    ap.add_argument("--graph-after", type=int, default=8,
+                    help="serving: capture a batch shape as a CUDA graph after this many uses")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
                     help="wavelength count (64 is the benchmark workload; smaller values "
                          "make the bounded cases used for profiling captures)")

@@ -842,6 +842,50 @@ struct dlx_poly_plan_s {
     if (v == DLX_VARIANT_SPLIT_BF16) eg.out_split = fbar.as<__nv_bfloat16>();
     else eg.out_c64 = fbar.as<float2>();
     DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, eg), s));
+    return reverse_from_fbar(t, o, R, s, sum_amp, sum_opd, sum_phase, sum_pixels,
+                             accumulate_sum);
+  }
+
+  // PSF and reverse pass in one sweep, for objects whose cotangent g_psf is
+  // known before the forward pass (serving requests, linear functionals): the
+  // forward's y-contraction writes the intensity planes and F̄ = 2αG⊙D at
+  // once, so the reverse pass starts at the adjoint GEMMs with no recompute.
+  int forward_backward_chunk(const dlx_poly_object* objs, int R, cudaStream_t s) {
+    const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    if (!field.p)
+      return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
+    ObjTable t;
+    OutTable o;
+    tables(objs, R, &t, &o);
+    for (int r = 0; r < R; ++r)
+      if (!t.o[r].G) return fail(DLX_ERR_ARG, "poly forward_backward: every object needs g_psf");
+    DLX_TRY(build_field(t, s, pathff.as<float4>()));
+    EpiArgs e1 = epi_store(v, mid.p, nullptr);
+    e1.objs = t;
+    DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
+    EpiArgs e{};
+    e.kind = EPI_PSF_GRADF;
+    e.objs = t;
+    e.alpha = ts.alpha.as<float>();
+    e.out_f32 = planes.as<float>();
+    if (v == DLX_VARIANT_SPLIT_BF16) e.out_split = fbar.as<__nv_bfloat16>();
+    else e.out_c64 = fbar.as<float2>();
+    DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, e), s));
+    ObjReduceArgs rp{};
+    rp.objs = t;
+    rp.outs = o;
+    rp.L = L;
+    rp.npix = (long long)M * M;
+    rp.planes = planes.as<float>();
+    DLX_TRY(launch_obj_psf_reduce(rp, s));
+    return reverse_from_fbar(t, o, R, s, nullptr, nullptr, nullptr, false, false);
+  }
+
+  // Adjoint GEMMs from F̄ (in `fbar`) and the pupil reductions.
+  int reverse_from_fbar(const ObjTable& t, const OutTable& o, int R, cudaStream_t s,
+                        float* sum_amp, float* sum_opd, float* sum_phase, bool sum_pixels,
+                        bool accumulate_sum) {
+    const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
     EpiArgs e3 = epi_store(v, mid.p, nullptr);
     e3.objs = t;
@@ -1063,6 +1107,19 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
   for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
     const int R = std::min(plan->max_obj, n_objects - o0);
     DLX_TRY(plan->backward_chunk(objs + o0, R, s));
+  }
+  return DLX_OK;
+}
+
+int dlx_poly_forward_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                              void* stream) {
+  if (!plan || (n_objects > 0 && !objs))
+    return fail(DLX_ERR_ARG, "poly_forward_backward: null pointer");
+  if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_forward_backward: negative object count");
+  cudaStream_t s = as_stream(stream);
+  for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
+    const int R = std::min(plan->max_obj, n_objects - o0);
+    DLX_TRY(plan->forward_backward_chunk(objs + o0, R, s));
   }
   return DLX_OK;
 }

@@ -64,8 +64,25 @@ int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool 
 // 319-327; optics.py:77-96; optical_systems.py:213-215).
 // One thread per pixel; the wavelength loop reuses amp/opd/phase.
 // ---------------------------------------------------------------------------
-__global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
+__global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) {
+  // cached: per-wavelength 1/lambda pairs and per-(object, wavelength)
+  // sqrt(weight) staged once per block in shared memory
+  extern __shared__ float psm[];
   const long long npix = (long long)a.n * a.n;
+  const int R = a.objs.n > 0 ? a.objs.n : 1;
+  const int L = a.batch / R;
+  float2* c_il = reinterpret_cast<float2*>(psm);
+  float* c_sw = psm + 2 * L;
+  if (cached) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+      c_il[i] = a.inv_lambda_ff ? a.inv_lambda_ff[i] : inv_lambda_arg.v[i];
+    for (int i = threadIdx.x; i < R * L; i += blockDim.x) {
+      const int r = i / L, wl = i - (i / L) * L;
+      const float* o_w = a.objs.n > 0 ? a.objs.o[r].weights : a.weights;
+      c_sw[i] = o_w ? sqrtf(o_w[wl]) : 1.0f;
+    }
+    __syncthreads();
+  }
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
   const int y = (int)(p / a.n);
@@ -75,8 +92,6 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
   const double Y = ((double)y - half) * a.pixel_scale;
   // Objects r of a batched plan (b = l * R + r), or one object described by
   // the plain fields of PhasorArgs.
-  const int R = a.objs.n > 0 ? a.objs.n : 1;
-  const int L = a.batch / R;
   for (int r = 0; r < R; ++r) {
     const bool obj = a.objs.n > 0;
     const float* o_amp = obj ? a.objs.o[r].amp : a.amp;
@@ -95,10 +110,12 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg) {
     amp *= (float)a.const_scale;
     for (int wl = 0; wl < L; ++wl) {
       const int b = wl * R + r;
-      const float2 il2 = a.inv_lambda_ff ? a.inv_lambda_ff[wl] : inv_lambda_arg.v[wl];
+      const float2 il2 = cached ? c_il[wl]
+                                : (a.inv_lambda_ff ? a.inv_lambda_ff[wl] : inv_lambda_arg.v[wl]);
       float2 u = cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
       float sc = amp;
-      if (o_w) sc *= sqrtf(o_w[wl]);
+      if (cached) sc *= c_sw[r * L + wl];
+      else if (o_w) sc *= sqrtf(o_w[wl]);
       float2 v = make_float2(u.x * sc, u.y * sc);
       const long long o = (long long)b * npix + p;
       if (a.in) v = cmul(a.in[o], v);
@@ -125,7 +142,12 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     for (int i = 0; i < kMaxBatchArg; ++i) dummy.v[i] = make_float2(0.f, 0.f);
     inv_lambda_arg = &dummy;
   }
-  phasor_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(a, *inv_lambda_arg);
+  const int R = a.objs.n > 0 ? a.objs.n : 1;
+  const int L = a.batch / R;
+  // stage the per-wavelength factors in shared memory when they fit in 32 KB
+  const size_t smem = sizeof(float) * (size_t)(2 * L + R * L);
+  const int cached = smem <= 32 * 1024 ? 1 : 0;
+  phasor_kernel<<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg, cached);
   DLX_LAUNCH_CHECK("phasor_kernel");
   return DLX_OK;
 }
@@ -346,10 +368,21 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(npix, lo + chunk);
   const float* row = basis + (long long)k * npix;
-  double acc = 0.0;
-  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x)
-    acc += (double)__ldg(row + p) * (double)__ldg(g + p);
-  double t = block_sum<256>(acc, smem);
+  // Error-free FP32 accumulation (FP64 arithmetic is slow on this GPU): each
+  // product is split exactly into p + e (fmaf), the running sum is kept as a
+  // float pair with Knuth's TwoSum, and only the per-thread pair is widened.
+  float hi_s = 0.f, lo_s = 0.f;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    const float x = __ldg(row + p), y = __ldg(g + p);
+    const float pr = x * y;
+    const float pe = fmaf(x, y, -pr);
+    const float t = hi_s + pr;
+    const float bv = t - hi_s;
+    const float err = (hi_s - (t - bv)) + (pr - bv);
+    hi_s = t;
+    lo_s += err + pe;
+  }
+  double t = block_sum<256>((double)hi_s + (double)lo_s, smem);
   if (threadIdx.x == 0) partial[(long long)k * nparts + blockIdx.x] = t;
 }
 
@@ -588,7 +621,11 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
 // pim, g_opd = sum k_l pim), tilt partials, and weight partials
 // sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
 __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
-  extern __shared__ double wpart[];  // [8 warps][L] weight partials
+  // dynamic shared memory: [L] float4 (1/lambda hi, lo, sqrt(w), k) then, when
+  // weight gradients are wanted, [8 warps][L] double partials
+  extern __shared__ double dyn[];
+  float4* lam = reinterpret_cast<float4*>(dyn);
+  double* wpart = dyn + 2 * a.L;
   __shared__ double tsm[32];
   const int r = blockIdx.y;
   const int R = a.objs.n;
@@ -597,6 +634,11 @@ __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, i
   const bool pix_out = !a.sum_pixels && (out.g_amp || out.g_phase || out.g_opd);
   const bool w_out = want_w && out.g_w;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int l = threadIdx.x; l < a.L; l += blockDim.x) {
+    const float2 il = a.inv_lambda_ff[l];
+    lam[l] = make_float4(il.x, il.y, od.weights ? sqrtf(od.weights[l]) : 1.0f,
+                         (float)a.k_dev[l]);
+  }
   if (w_out)
     for (int i = threadIdx.x; i < 8 * a.L; i += blockDim.x) wpart[i] = 0.0;
   __syncthreads();
@@ -622,16 +664,16 @@ __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, i
       float pre = 0.f;
       if (live) {
         const float2 eb = a.ebar[((long long)l * R + r) * a.npix + p];
-        const float2 il = a.inv_lambda_ff[l];
-        const float2 u = cis_ff(FF{q.x, q.y}, FF{il.x, il.y}, FF{q.z, q.w});
-        const float sw = od.weights ? sqrtf(od.weights[l]) : 1.0f;
+        const float4 c = lam[l];
+        const float2 u = cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
+        const float sw = c.z;
         const float pr = u.x * eb.x + u.y * eb.y;
         const float pi = u.x * eb.y - u.y * eb.x;
         pre = sw * pr;
         const float pim = amp * sw * pi;
         sre += pre;
         sim += pim;
-        sk += (float)a.k_dev[l] * pim;
+        sk += c.w * pim;
       }
       if (w_out) {  // warp-uniform
         float v = pre * amp_raw;
@@ -701,12 +743,12 @@ int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s) {
     return fail(DLX_ERR_SHAPE, "fused pupil reduction: too many wavelengths");
   bool want_w = false;
   for (int r = 0; r < R; ++r) want_w |= a.outs.o[r].g_w != nullptr;
-  const size_t smem = want_w ? sizeof(double) * 8 * (size_t)a.L : 0;
+  const size_t smem = sizeof(float4) * (size_t)a.L + (want_w ? sizeof(double) * 8 * (size_t)a.L : 0);
   static std::atomic<bool> attr_done{false};  // host side, once per process
   if (smem > 48 * 1024 && !attr_done.load()) {
     DLX_TRY_CUDA(cudaFuncSetAttribute(obj_pupil_fused_kernel,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(double) * 8 * kFusedPupilMaxL)));
+                                      (int)(sizeof(double) * 10 * kFusedPupilMaxL)));
     attr_done.store(true);
   }
   obj_pupil_fused_kernel<<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);

@@ -98,7 +98,10 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
       break;
     }
-    case EPI_GRADF: {
+    case EPI_GRADF:
+    case EPI_PSF_GRADF: {
+      if (e.kind == EPI_PSF_GRADF)
+        e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
       epi_gradf_value(e, r, a, idx, v);
       if (e.out_split)
         store_split(e.out_split + (long long)b * 4 * plane, plane, idx, v);
@@ -152,7 +155,15 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
         if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
       break;
     }
-    case EPI_GRADF: {
+    case EPI_GRADF:
+    case EPI_PSF_GRADF: {
+      if (e.kind == EPI_PSF_GRADF) {
+        float* o = e.out_f32 + (long long)b * plane + idx0;
+        const float a2 = a * a;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
+      }
       // all 32 loads first, so their latencies overlap
       const float* G = (e.objs.n > 0 ? e.objs.o[r].G : e.G) + idx0;
       float g[32];

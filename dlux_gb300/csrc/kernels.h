@@ -122,7 +122,7 @@ struct ObjReduceArgs {
 int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s);
 int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s);
 // Largest wavelength count the fused pupil reduction accepts.
-constexpr int kFusedPupilMaxL = 3072;
+constexpr int kFusedPupilMaxL = 2048;
 int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s);
 
 
@@ -135,6 +135,7 @@ enum EpiKind {
   EPI_INTENSITY = 2, // out_f32[b][m][n] = alpha_b^2 |D|^2
   EPI_GRADF = 3,     // out[b][m][n] = 2 alpha_b G[m][n] D    (c64 or split)
   EPI_PUPIL = 4,     // pupil-gradient planes from D = Ebar_unscaled[b][y=m][x=n]
+  EPI_PSF_GRADF = 5, // both EPI_INTENSITY (out_f32) and EPI_GRADF (out_split / out_c64)
 };
 
 struct EpiArgs {

@@ -114,15 +114,16 @@ int dlx_serve_run(dlx_poly_plan plan, const dlx_serve_batch* b, void* stream) {
     objs[r].opd = opd + r * n2;
     objs[r].weights = weights + (size_t)r * L;
     objs[r].psf = psf + r * m2;
-  }
-  DLX_TRY(dlx_poly_forward(plan, objs, R, nullptr, 0, s));
-  if (G > 0) {
-    for (int r = 0; r < G; ++r) {
-      objs[r].psf = nullptr;
+    if (r < G) {
       objs[r].g_psf = g_psf + r * m2;
       objs[r].g_opd = g_opd + r * n2;
     }
-    DLX_TRY(dlx_poly_backward(plan, objs, G, s));
+  }
+  // Gradient requests (the first G) know their cotangent up front: PSF and
+  // reverse pass in one sweep. The others take the forward pass only.
+  if (G > 0) DLX_TRY(dlx_poly_forward_backward(plan, objs, G, s));
+  if (R > G) DLX_TRY(dlx_poly_forward(plan, objs + G, R - G, nullptr, 0, s));
+  if (G > 0) {
     for (int r = 0; r < G; ++r)
       DLX_TRY(launch_basis_grad(b->basis, g_opd + r * n2, K, (long long)n2, grad + (size_t)r * K,
                                 partial + (size_t)r * K * kServeParts, kServeParts, s));

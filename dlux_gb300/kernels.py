@@ -272,6 +272,12 @@ class PolyPlan(_Plan):
         call("dlx_poly_forward", self.handle, ctypes.cast(arr, ctypes.c_void_p), len(objs),
              ptr(psf_sum), int(bool(accumulate)), _stream())
 
+    def forward_backward_objects(self, objs):
+        """PSF and reverse pass in one sweep; every object needs its cotangent g_psf."""
+        arr = self._object_array(objs)
+        call("dlx_poly_forward_backward", self.handle, ctypes.cast(arr, ctypes.c_void_p),
+             len(objs), _stream())
+
     def backward_objects(self, objs, sum_grads=None):
         """Reverse pass; ``sum_grads`` ({"amp","opd","phase"} tensors) sums pixel gradients."""
         arr = self._object_array(objs)

@@ -304,15 +304,22 @@ class PSFServer:
                 return out
 
     def _oldest_bucket(self, skip):
-        best, t_best = None, None
+        # `pending` holds only buckets with queued requests, so this scan is
+        # over the buckets in the queue, not over every bucket ever seen.
+        best, t_best, empty = None, None, []
         for key, dq in self.pending.items():
             while dq and dq[0].cancelled:
                 self.stats["cancelled"] += 1
                 _finish(dq.popleft(), RequestCancelled("request cancelled"))
-            if not dq or key in skip:
+            if not dq:
+                empty.append(key)
+                continue
+            if key in skip:
                 continue
             if best is None or dq[0].t_submit < t_best:
                 best, t_best = key, dq[0].t_submit
+        for key in empty:
+            del self.pending[key]
         return best
 
     def _dispatch(self):
@@ -337,6 +344,8 @@ class PSFServer:
                     _finish(r, RequestCancelled("request cancelled"))
                     continue
                 reqs.append(r)
+            if not dq:
+                del self.pending[key]
             if not reqs:
                 continue
             reqs.sort(key=lambda r: not r.want_grad)   # gradient requests first (stable)
@@ -413,8 +422,12 @@ class PSFServer:
         lat = np.array([r.latency for r in done]) * 1e3
         t0 = min(r.t_submit for r in done)
         t1 = max(r.t_done for r in done)
+        wait = np.array([r.t_launch - r.t_submit for r in done]) * 1e3
+        service = np.array([r.t_done - r.t_launch for r in done]) * 1e3
         out.update(throughput_rps=len(done) / max(t1 - t0, 1e-9),
                    p50_ms=float(np.percentile(lat, 50)), p99_ms=float(np.percentile(lat, 99)),
+                   p99_queue_ms=float(np.percentile(wait, 99)),
+                   p99_service_ms=float(np.percentile(service, 99)),
                    mean_batch=self.stats["launched"] / max(self.stats["batches"], 1))
         by_n = collections.defaultdict(list)
         for r, l in zip(done, lat):

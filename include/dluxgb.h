@@ -269,6 +269,14 @@ int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obje
 /* Reverse pass for every object with its own cotangent objs[r].g_psf. */
 int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
                       void* stream);
+/* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
+ * is known before the forward pass (a serving request, a linear functional):
+ * writes objs[r].psf (optional) and the gradient outputs like
+ * dlx_poly_backward, without recomputing the forward fields (4 instead of 6
+ * GEMMs). No dLux counterpart: JAX's reverse mode always runs after its
+ * forward pass. */
+int dlx_poly_forward_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
+                              void* stream);
 /* Same, for objects that share one pupil (the sources of one scene): the
  * pupil-pixel gradients are summed over all objects into g_amp / g_opd /
  * g_phase ([N][N], any may be NULL; overwritten), while g_w and g_tilt stay
