@@ -415,12 +415,16 @@ def cfg_workload(name, variant):
                                                     dl.BasisLayer(B, c0)], 128, 0.02, 1)
         wls = [1e-6]
 
-        def run():
-            c = c0.detach().requires_grad_(True)
+        def step(c_in):
+            c = c_in.detach().requires_grad_(True)
             psf = optics.set("layers.BasisLayer.coefficients", c).propagate(wls)
             loss = (psf * R).sum()
             loss.backward()
-            return loss
+            return loss.detach(), c.grad
+
+        def run():
+            return step(c0)
+        run.step, run.c0 = step, c0
         flops = 3 * 8 * (128 * 256 ** 2 + 128 ** 2 * 256)
         return run, "PSF+grad latency", "ms", flops, "256^2 pupil, 1 lambda, 128^2 PSF"
     if name == "cfg3":
@@ -513,13 +517,44 @@ def run_config(args):
         clk = clocks.stop()
         t = np.array(times)
         gemm_tf = fl.value / (tot.value * 1e-3) / 1e12 if tot.value > 0 else None
+        graphed = None
+        if hasattr(run, "step"):
+            # the same step replayed as one CUDA graph, device time and end to end
+            from dlux_gb300.graphs import GraphedStep
+            gstep = GraphedStep(run.step, run.c0)
+            host_c = run.c0.detach().cpu().pin_memory()
+            out_l = torch.empty((), dtype=torch.float32).pin_memory()
+            out_g = torch.empty(run.c0.shape, dtype=torch.float32).pin_memory()
+            dev_c = torch.empty_like(run.c0)
+            gt, et = [], []
+            for i in range(args.steps + 3):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                h0 = time.perf_counter()
+                dev_c.copy_(host_c, non_blocking=True)
+                e0.record()
+                loss, g = gstep(dev_c)
+                e1.record()
+                out_l.copy_(loss, non_blocking=True)
+                out_g.copy_(g, non_blocking=True)
+                torch.cuda.synchronize()
+                if i >= 3:
+                    et.append((time.perf_counter() - h0) * 1e3)
+                    gt.append(e0.elapsed_time(e1))
+            gt, et = np.array(gt), np.array(et)
+            graphed = {"device_ms_p50": float(np.percentile(gt, 50)),
+                       "device_ms_p99": float(np.percentile(gt, 99)),
+                       "e2e_ms_p50": float(np.percentile(et, 50)),
+                       "e2e_ms_p99": float(np.percentile(et, 99)),
+                       "h2d_bytes": host_c.numel() * 4, "d2h_bytes": 4 + out_g.numel() * 4}
         out[variant] = {"ms_mean": float(t.mean()), "ms_p50": float(np.percentile(t, 50)),
                         "ms_p99": float(np.percentile(t, 99)),
                         "evals_per_s": 1e3 / float(t.mean()),
                         "algorithmic_tflops": flops / (t.mean() * 1e-3) / 1e12,
                         "gemm_tflops": gemm_tf,
                         "gemm_share": tot.value / t.sum() if t.sum() > 0 else None,
-                        "clocks": clk}
+                        "graphed": graphed, "clocks": clk}
     main = out[args.variant]
     value = main["ms_p50"] if args.workload == "cfg1" else main["evals_per_s"]
     line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,

@@ -1,0 +1,40 @@
+"""A whole PSF + gradient step replayed as one CUDA graph gives the eager step's bits."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_graphed_step_matches_eager(cuda):
+    import dlux_gb300 as dl
+    import dlux_gb300.utils as dlu
+    from dlux_gb300.graphs import GraphedStep
+
+    rng = np.random.default_rng(7)
+    T, B = dlu.circular_aperture(128, 1.0, oversample=1, secondary_diameter=0.1,
+                                 zernike_nolls=list(range(4, 14)))
+    c0 = torch.as_tensor(rng.normal(0, 50e-9, 10), dtype=torch.float32, device="cuda")
+    R = torch.as_tensor(rng.normal(size=(64, 64)), dtype=torch.float32, device="cuda")
+    optics = dl.AngularOpticalSystem(128, 1.0, [dl.TransmissiveLayer(T, normalise=True),
+                                                dl.BasisLayer(B, c0)], 64, 0.04, 1)
+
+    def step(c_in):
+        c = c_in.detach().requires_grad_(True)
+        psf = optics.set("layers.BasisLayer.coefficients", c).propagate([1e-6, 1.2e-6])
+        loss = (psf * R).sum()
+        loss.backward()
+        return loss.detach(), c.grad
+
+    g = GraphedStep(step, c0)
+    for seed in (1, 2):
+        c = torch.as_tensor(np.random.default_rng(seed).normal(0, 50e-9, 10),
+                            dtype=torch.float32, device="cuda")
+        loss_g, grad_g = (t.clone() for t in g(c))
+        loss_e, grad_e = step(c)
+        torch.cuda.synchronize()
+        assert torch.equal(loss_g, loss_e)
+        assert torch.equal(grad_g, grad_e)
+    with pytest.raises(ValueError):
+        g(torch.zeros(3, device="cuda"))
