@@ -48,12 +48,24 @@ __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int l, int
   return cis_ff(path, FF{il.x, il.y}, ph);
 }
 
+// F-bar input of EPI_DOT: split planes (hi + lo) or complex64.
+__device__ __forceinline__ float2 epi_read_in(const EpiArgs& e, int b, long long plane,
+                                              long long idx) {
+  if (e.in_split) {
+    const __nv_bfloat16* p = e.in_split + (long long)b * 4 * plane + idx;
+    return make_float2(__bfloat162float(p[0]) + __bfloat162float(p[plane]),
+                       __bfloat162float(p[2 * plane]) + __bfloat162float(p[3 * plane]));
+  }
+  return e.in_c64[(long long)b * plane + idx];
+}
+
 // ---- per-element epilogues; l = wavelength, r = object, a = alpha_l ----
-__device__ __forceinline__ void epi_gradf_value(const EpiArgs& e, int r, float a, long long idx,
-                                                float2& v) {
+__device__ __forceinline__ void epi_gradf_value(const EpiArgs& e, int b, int r, float a,
+                                                long long idx, float2& v) {
   // cotangent of F = alpha * D for <G, |F|^2>: 2 G F = 2 alpha G D
   const float* G = e.objs.n > 0 ? e.objs.o[r].G : e.G;
-  const float g = 2.0f * a * G[idx];
+  float g = 2.0f * a * G[idx];
+  if (e.bweight) g *= e.bweight[b];
   v = make_float2(g * v.x, g * v.y);
 }
 
@@ -102,7 +114,7 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
     case EPI_PSF_GRADF: {
       if (e.kind == EPI_PSF_GRADF)
         e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
-      epi_gradf_value(e, r, a, idx, v);
+      epi_gradf_value(e, b, r, a, idx, v);
       if (e.out_split)
         store_split(e.out_split + (long long)b * 4 * plane, plane, idx, v);
       else
@@ -111,6 +123,24 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
     }
     case EPI_PUPIL: {
       epi_pupil_store(e, b, l, r, a, m, n, N, plane, idx, v);
+      break;
+    }
+    case EPI_SPLIT2: {
+      const float2 av = make_float2(a * v.x, a * v.y);
+      const float w = e.colw[n];
+      if (e.out_split) {
+        store_split(e.out_split + (long long)b * 4 * plane, plane, idx, av);
+        store_split(e.out_split2 + (long long)b * 4 * plane, plane, idx,
+                    make_float2(w * av.x, w * av.y));
+      } else {
+        e.out_c64[(long long)b * plane + idx] = av;
+        e.out_c642[(long long)b * plane + idx] = make_float2(w * av.x, w * av.y);
+      }
+      break;
+    }
+    case EPI_DOT: {
+      const float2 fb = epi_read_in(e, b, plane, idx);
+      e.out_f32[(long long)b * plane + idx] = e.kf[l] * a * (fb.y * v.x - fb.x * v.y);
       break;
     }
     default:
@@ -123,6 +153,10 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
 // warp hold consecutive n. Every load and store below is therefore one
 // contiguous segment per warp. Rows m >= M are skipped; n < N is the
 // caller's check.
+// KIND >= 0 fixes the epilogue at compile time (one kernel instantiation per
+// kind keeps each instantiation's registers to its own epilogue); -1 reads
+// e.kind at run time.
+template <int KIND = -1>
 __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0, int M, int N,
                                           const float* re, const float* im) {
   const int R = epi_objects(e);
@@ -132,7 +166,7 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
   const long long plane = (long long)M * N;
   const int mc = M - m0 < 32 ? M - m0 : 32;
   const long long idx0 = (long long)m0 * N + n;
-  switch (e.kind) {
+  switch (KIND >= 0 ? KIND : e.kind) {
     case EPI_C64: {
       float2* o = e.out_c64 + (long long)b * plane + idx0;
 #pragma unroll
@@ -157,7 +191,7 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
     }
     case EPI_GRADF:
     case EPI_PSF_GRADF: {
-      if (e.kind == EPI_PSF_GRADF) {
+      if ((KIND >= 0 ? KIND : e.kind) == EPI_PSF_GRADF) {
         float* o = e.out_f32 + (long long)b * plane + idx0;
         const float a2 = a * a;
 #pragma unroll
@@ -169,7 +203,7 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
       float g[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) g[j] = j < mc ? __ldg(G + (long long)j * N) : 0.0f;
-      const float s = 2.0f * a;
+      const float s = 2.0f * a * (e.bweight ? e.bweight[b] : 1.0f);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         if (j < mc) {
@@ -181,6 +215,42 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
           else
             e.out_c64[(long long)b * plane + idx0 + (long long)j * N] = v;
         }
+      }
+      break;
+    }
+    case EPI_SPLIT2: {
+      const float w = e.colw[n];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        if (j < mc) {
+          const float2 av = make_float2(a * re[j], a * im[j]);
+          const long long o = idx0 + (long long)j * N;
+          if (e.out_split) {
+            store_split(e.out_split + (long long)b * 4 * plane, plane, o, av);
+            store_split(e.out_split2 + (long long)b * 4 * plane, plane, o,
+                        make_float2(w * av.x, w * av.y));
+          } else {
+            e.out_c64[(long long)b * plane + o] = av;
+            e.out_c642[(long long)b * plane + o] = make_float2(w * av.x, w * av.y);
+          }
+        }
+      }
+      break;
+    }
+    case EPI_DOT: {
+      const float ka = e.kf[l] * a;
+      float* o = e.out_f32 + (long long)b * plane + idx0;
+#pragma unroll
+      for (int j0 = 0; j0 < 32; j0 += 8) {
+        float2 fb[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          fb[t] = j0 + t < mc ? epi_read_in(e, b, plane, idx0 + (long long)(j0 + t) * N)
+                              : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+          if (j0 + t < mc)
+            o[(long long)(j0 + t) * N] = ka * (fb[t].y * re[j0 + t] - fb[t].x * im[j0 + t]);
       }
       break;
     }

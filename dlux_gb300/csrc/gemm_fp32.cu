@@ -32,7 +32,7 @@ __global__ __launch_bounds__(THREADS) void cgemm_fp32_kernel(GemmArgs g) {
   const int M = g.M, N = g.N, K = g.K;
 
   const float2* Ab = g.A + (long long)(b / (g.a_batch_div > 0 ? g.a_batch_div : 1)) * g.a_bs;
-  const float2* Bb = g.B + (long long)b * g.b_bs;
+  const float2* Bb = g.B + (long long)(b / (g.b_batch_div > 0 ? g.b_batch_div : 1)) * g.b_bs;
 
   // Global load mapping: A: row = tid/2, k = (tid&1)*4 .. +3 ; B: row = tid/4, k = (tid&3)*2 .. +1
   const int a_row = tid >> 1, a_k = (tid & 1) * 4;

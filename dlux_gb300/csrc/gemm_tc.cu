@@ -198,6 +198,38 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* out) {
   for (int i = 0; i < 32; ++i) out[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld_wait();
+
+// 32 lanes x 16 consecutive 32-bit TMEM columns -> 16 registers per thread.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) out[i] = __uint_as_float(r[i]);
+}
+
+// main + cross accumulators of 32 output rows starting at TMEM column `col`,
+// loaded 16 columns at a time so that only 16 temporaries are live.
+__device__ __forceinline__ void tmem_sum32(uint32_t lane_addr, uint32_t col, uint32_t cross_off,
+                                           float* out) {
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float t[16];
+    tmem_ld16(lane_addr + col + 16 * h, out + 16 * h);
+    tmem_ld16(lane_addr + cross_off + col + 16 * h, t);
+    tmem_ld_wait();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) out[16 * h + i] += t[i];
+  }
+}
+
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
@@ -233,13 +265,14 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) 
 // --------------------------------- kernel -----------------------------------
 struct TcParams {
   int batch, M, N, K;
-  int a_batch_div;
+  int a_batch_div, b_batch_div;
   int mt, nt, total;
   int conj_a;
   int* status;
   EpiArgs epi;
 };
 
+template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_cgemm_kernel(const __grid_constant__ CUtensorMap tmA,
                     const __grid_constant__ CUtensorMap tmB, const TcParams p) {
@@ -300,7 +333,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 #pragma unroll
           for (int q = 0; q < 4; ++q)
             tma_load_3d(base + 4 * A_PLANE_BYTES + q * B_PLANE_BYTES, &tmB, &full[stage],
-                        kb * TC_BK, nt * TC_BN, b * 4 + q);
+                        kb * TC_BK, nt * TC_BN, (b / p.b_batch_div) * 4 + q);
           issued_mask |= 1u << stage;
           issued_ph = (issued_ph & ~(1u << stage)) | (ph << stage);
           if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
@@ -395,39 +428,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int c0 = half, c1 = half + 2;
       const bool has0 = mbase + c0 * 32 < p.M, has1 = mbase + c1 * 32 < p.M;  // warp-uniform
       float re0[32], im0[32], re1[32], im1[32];
-      {
-        float t[32];
-        if (has0) {
-          tmem_ld32(lane_addr + c0 * 32, re0);
-          tmem_ld32(lane_addr + 2 * TC_BM + c0 * 32, t);
-          tmem_ld_wait();
-#pragma unroll
-          for (int i = 0; i < 32; ++i) re0[i] += t[i];
-          tmem_ld32(lane_addr + TC_BM + c0 * 32, im0);
-          tmem_ld32(lane_addr + 3 * TC_BM + c0 * 32, t);
-          tmem_ld_wait();
-#pragma unroll
-          for (int i = 0; i < 32; ++i) im0[i] += t[i];
-        }
-        if (has1) {
-          tmem_ld32(lane_addr + c1 * 32, re1);
-          tmem_ld32(lane_addr + 2 * TC_BM + c1 * 32, t);
-          tmem_ld_wait();
-#pragma unroll
-          for (int i = 0; i < 32; ++i) re1[i] += t[i];
-          tmem_ld32(lane_addr + TC_BM + c1 * 32, im1);
-          tmem_ld32(lane_addr + 3 * TC_BM + c1 * 32, t);
-          tmem_ld_wait();
-#pragma unroll
-          for (int i = 0; i < 32; ++i) im1[i] += t[i];
-        }
+      if (has0) {
+        tmem_sum32(lane_addr, c0 * 32, 2 * TC_BM, re0);
+        tmem_sum32(lane_addr, TC_BM + c0 * 32, 2 * TC_BM, im0);
+      }
+      if (has1) {
+        tmem_sum32(lane_addr, c1 * 32, 2 * TC_BM, re1);
+        tmem_sum32(lane_addr, TC_BM + c1 * 32, 2 * TC_BM, im1);
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty);
       if (n < p.N) {
-        if (has0) epi_col32(p.epi, b, n, mbase + c0 * 32, p.M, p.N, re0, im0);
-        if (has1) epi_col32(p.epi, b, n, mbase + c1 * 32, p.M, p.N, re1, im1);
+        if (has0) epi_col32<KIND>(p.epi, b, n, mbase + c0 * 32, p.M, p.N, re0, im0);
+        if (has1) epi_col32<KIND>(p.epi, b, n, mbase + c1 * 32, p.M, p.N, re1, im1);
       }
       acc_ph ^= 1u;
     }
@@ -463,7 +477,7 @@ constexpr int G_THREADS = 320;  // TMA, MMA, 4 epilogue warps, 4 generator warps
 
 struct TcGenParams {
   int batch, M, N, K;
-  int a_batch_div;
+  int a_batch_div, b_batch_div;
   int mt, nt, total;
   int conj_a;
   int rows_are_out;
@@ -545,7 +559,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
           for (int q = 0; q < 4; ++q)
             tma_load_3d(base + q * B_PLANE_BYTES, &tmB, &bfull[stage], kb * TC_BK, nt * TC_BN,
-                        b * 4 + q);
+                        (b / p.b_batch_div) * 4 + q);
           issued_mask |= 1u << stage;
           issued_ph = (issued_ph & ~(1u << stage)) | (ph << stage);
           if (++stage == GB_STAGES) { stage = 0; ph ^= 1u; }
@@ -735,6 +749,32 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 }
 
 // ------------------------------- host side ----------------------------------
+using LoadedKernel = void (*)(CUtensorMap, CUtensorMap, TcParams);
+
+// One instantiation of the loaded-operand kernel per epilogue kind.
+LoadedKernel loaded_kernel(int kind) {
+  switch (kind) {
+    case EPI_C64: return tc_cgemm_kernel<EPI_C64>;
+    case EPI_SPLIT: return tc_cgemm_kernel<EPI_SPLIT>;
+    case EPI_INTENSITY: return tc_cgemm_kernel<EPI_INTENSITY>;
+    case EPI_GRADF: return tc_cgemm_kernel<EPI_GRADF>;
+    case EPI_PUPIL: return tc_cgemm_kernel<EPI_PUPIL>;
+    case EPI_PSF_GRADF: return tc_cgemm_kernel<EPI_PSF_GRADF>;
+    case EPI_SPLIT2: return tc_cgemm_kernel<EPI_SPLIT2>;
+    case EPI_DOT: return tc_cgemm_kernel<EPI_DOT>;
+    default: return nullptr;
+  }
+}
+
+const void* const* loaded_kernels() {
+  static const void* all[] = {
+      (const void*)tc_cgemm_kernel<EPI_C64>,       (const void*)tc_cgemm_kernel<EPI_SPLIT>,
+      (const void*)tc_cgemm_kernel<EPI_INTENSITY>, (const void*)tc_cgemm_kernel<EPI_GRADF>,
+      (const void*)tc_cgemm_kernel<EPI_PUPIL>,     (const void*)tc_cgemm_kernel<EPI_PSF_GRADF>,
+      (const void*)tc_cgemm_kernel<EPI_SPLIT2>,    (const void*)tc_cgemm_kernel<EPI_DOT>,
+      nullptr};
+  return all;
+}
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
 int g_cc = 0;
@@ -769,8 +809,11 @@ void init_once() {
     g_init_status = fail(DLX_ERR_NOMEM, "status word allocation failed");
     return;
   }
-  if (cudaFuncSetAttribute(tc_cgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           SMEM_BYTES) != cudaSuccess ||
+  bool attr_ok = true;
+  for (const void* const* k = loaded_kernels(); *k; ++k)
+    attr_ok = attr_ok && cudaFuncSetAttribute(*k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              SMEM_BYTES) == cudaSuccess;
+  if (!attr_ok ||
       cudaFuncSetAttribute(tc_cgemm_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            G_SMEM_BYTES) != cudaSuccess) {
     g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tensor-core GEMM) failed");
@@ -814,13 +857,16 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if (g.K % 8 != 0 || g.N % 8 != 0)
     return fail(DLX_ERR_SHAPE, "split-BF16 GEMM needs K and N to be multiples of 8");
   const int div = g.a_batch_div > 0 ? g.a_batch_div : 1;
+  const int bdiv = g.b_batch_div > 0 ? g.b_batch_div : 1;
+  const int nB = (g.batch + bdiv - 1) / bdiv;
   if (g.a_axes) {
     if (!g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
     CUtensorMap tb;
-    DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, g.batch, TC_BN));
+    DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, nB, TC_BN));
     TcGenParams p{};
     p.batch = g.batch; p.M = g.M; p.N = g.N; p.K = g.K;
     p.a_batch_div = div;
+    p.b_batch_div = bdiv;
     p.mt = (g.M + TC_BM - 1) / TC_BM;
     p.nt = (g.N + TC_BN - 1) / TC_BN;
     p.total = g.batch * p.mt * p.nt;
@@ -838,10 +884,11 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const int nA = (g.batch + div - 1) / div;
   CUtensorMap ta, tb;
   DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, TC_BM));
-  DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, g.batch, TC_BN));
+  DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, nB, TC_BN));
   TcParams p{};
   p.batch = g.batch; p.M = g.M; p.N = g.N; p.K = g.K;
   p.a_batch_div = div;
+  p.b_batch_div = bdiv;
   p.mt = (g.M + TC_BM - 1) / TC_BM;
   p.nt = (g.N + TC_BN - 1) / TC_BN;
   p.total = g.batch * p.mt * p.nt;
@@ -849,7 +896,9 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   p.status = g_status;
   p.epi = g.epi;
   const int grid = p.total < g_num_sms ? p.total : g_num_sms;
-  tc_cgemm_kernel<<<grid, TC_THREADS, SMEM_BYTES, s>>>(ta, tb, p);
+  LoadedKernel kern = loaded_kernel(g.epi.kind);
+  if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
+  kern<<<grid, TC_THREADS, SMEM_BYTES, s>>>(ta, tb, p);
   DLX_LAUNCH_CHECK("tc_cgemm_kernel");
   return DLX_OK;
 }

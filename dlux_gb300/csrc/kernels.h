@@ -136,6 +136,8 @@ enum EpiKind {
   EPI_GRADF = 3,     // out[b][m][n] = 2 alpha_b G[m][n] D    (c64 or split)
   EPI_PUPIL = 4,     // pupil-gradient planes from D = Ebar_unscaled[b][y=m][x=n]
   EPI_PSF_GRADF = 5, // both EPI_INTENSITY (out_f32) and EPI_GRADF (out_split / out_c64)
+  EPI_SPLIT2 = 6,    // EPI_SPLIT / EPI_C64, plus the same values times colw[n] into out_*2
+  EPI_DOT = 7,       // out_f32 = k_l alpha_l (Fb.im D.re - Fb.re D.im), Fb read from in_*
 };
 
 struct EpiArgs {
@@ -156,6 +158,14 @@ struct EpiArgs {
   const float2* inv_lambda_ff;  // [b] (hi, lo) of 1/lambda
   double pixel_scale, tilt_x, tilt_y;
   const float4* path;        // nullable [object][n][n] from PhasorArgs::out_path
+  // many-source scenes
+  const float* bweight;      // nullable [b]: extra factor of the EPI_GRADF cotangent
+  const float* colw;         // [n] weights of EPI_SPLIT2's second output
+  __nv_bfloat16* out_split2; // EPI_SPLIT2 second output (tensor-core form)
+  float2* out_c642;          // EPI_SPLIT2 second output (FP32 form)
+  const __nv_bfloat16* in_split;  // EPI_DOT: F-bar [b][4][m][n] (tensor-core form)
+  const float2* in_c64;      // EPI_DOT: F-bar [b][m][n] (FP32 form)
+  const float* kf;           // EPI_DOT: [wavelength] 2 pi / lambda
 };
 
 struct GemmArgs {
@@ -167,6 +177,7 @@ struct GemmArgs {
   const __nv_bfloat16* As;  // split form [b][4][M][K]
   const __nv_bfloat16* Bs;  // split form [b][4][N][K]
   int a_batch_div;          // A batch index = b / a_batch_div (split form)
+  int b_batch_div;          // B batch index = b / b_batch_div (0 or 1: B per batch element)
   bool conj_a;
   // Tensor-core form only: when a_axes is set, A is not read from memory but
   // generated in the CTA as the DFT matrix of a_axes[b / a_batch_div]; rows
