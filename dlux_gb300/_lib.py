@@ -70,6 +70,14 @@ class PolyObject(ctypes.Structure):
     ]
 
 
+class SceneDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_wavelengths", _c_int), ("n_in", _c_int), ("n_out", _c_int),
+        ("pixel_scale_in", _c_dbl), ("pixel_scale_out", _c_dbl), ("focal_length", _c_dbl),
+        ("variant", _c_int), ("max_sources", _c_int),
+    ]
+
+
 class ServeBatch(ctypes.Structure):
     """dlx_serve_batch: one batch of serving requests that share a plan."""
     _fields_ = [
@@ -127,6 +135,13 @@ _SIGNATURES = {
     "dlx_poly_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "dlx_poly_plan_info": (_c_int, [_c_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                     ctypes.POINTER(_c_int), ctypes.POINTER(_c_int)]),
+    "dlx_scene_plan_create": (_c_int, [ctypes.POINTER(SceneDesc), _c_vp, ctypes.POINTER(_c_vp)]),
+    "dlx_scene_plan_destroy": (_c_int, [_c_vp]),
+    "dlx_scene_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "dlx_scene_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_int, _c_vp,
+                                   _c_int, _c_vp]),
+    "dlx_scene_backward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_int,
+                                    _c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_serve_workspace_bytes": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int,
                                            ctypes.POINTER(ctypes.c_size_t)]),
     "dlx_serve_run": (_c_int, [_c_vp, ctypes.POINTER(ServeBatch), _c_vp]),

@@ -149,6 +149,44 @@ def poly_sources(plan, amp, opd, phase, weights, positions, normalise=False, bas
                              amp, opd, phase, weights, positions)
 
 
+class ScenePSF(torch.autograd.Function):
+    """Summed image of many point sources through one pupil (sources.py:392-411),
+    differentiable w.r.t. the source positions and the per-(source, wavelength)
+    weights. The pupil (amplitude, OPD, phase) is a constant here; the tilt of
+    each source is an output-coordinate shift of its DFT matrices."""
+
+    @staticmethod
+    def forward(ctx, plan, amp, amp_scale, opd, phase, weights, positions, base_tilt):
+        pos = positions.detach().to(device="cuda", dtype=torch.float64)
+        if base_tilt[0] != 0.0 or base_tilt[1] != 0.0:
+            pos = pos + torch.tensor(base_tilt, dtype=torch.float64, device=pos.device)
+        w = weights.detach().to(torch.float32).contiguous()
+        ctx.plan, ctx.pos_device = plan, positions.device
+        ctx.save_for_backward(amp, amp_scale, opd, phase, w, pos)
+        return plan.forward(_d(amp), amp_scale, _d(opd), _d(phase), pos, w)
+
+    @staticmethod
+    def backward(ctx, g):
+        amp, amp_scale, opd, phase, w, pos = ctx.saved_tensors
+        want_w = ctx.needs_input_grad[5]
+        want_pos = ctx.needs_input_grad[6]
+        if not (want_w or want_pos):
+            return None, None, None, None, None, None, None, None
+        g_pos, g_w = ctx.plan.backward(_d(amp), amp_scale, _d(opd), _d(phase), pos, w,
+                                       g.contiguous(), want_pos, want_w)
+        if g_pos is not None:
+            g_pos = g_pos.to(device=ctx.pos_device, dtype=torch.float64)
+        return None, None, None, None, None, g_w, g_pos, None
+
+
+def scene_psf(plan, amp, opd, phase, weights, positions, normalise=False,
+              base_tilt=(0.0, 0.0)):
+    """Summed image of sources at ``positions`` [S, 2] (rad) with weights [S, L]."""
+    amp_scale = kernels.amp_norm(amp.detach()) if (normalise and amp is not None) else None
+    return ScenePSF.apply(plan, amp, amp_scale, opd, phase, weights, positions,
+                          (float(base_tilt[0]), float(base_tilt[1])))
+
+
 class LinearTransform(torch.autograd.Function):
     """A cached MFT or FFT plan applied to complex64 fields; backward is the adjoint."""
 

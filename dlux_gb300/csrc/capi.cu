@@ -347,6 +347,10 @@ EpiArgs epi_c64(void* out, const float* alpha) {
 }
 
 }  // namespace
+
+// The GEMM launcher of every plan type, with the optional per-launch timing.
+int run_gemm_timed(int variant, const GemmArgs& g, cudaStream_t s) { return run_gemm(variant, g, s); }
+
 }  // namespace dlx
 
 using namespace dlx;
@@ -821,7 +825,7 @@ struct dlx_poly_plan_s {
   int backward_chunk(const dlx_poly_object* objs, int R, cudaStream_t s, float* sum_amp = nullptr,
                      float* sum_opd = nullptr, float* sum_phase = nullptr,
                      bool sum_pixels = false, bool accumulate_sum = false) {
-    const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
+    const int N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
     ObjTable t;

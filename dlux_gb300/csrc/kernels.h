@@ -188,6 +188,8 @@ struct GemmArgs {
 };
 
 int launch_gemm_fp32(const GemmArgs& g, cudaStream_t s);
+// Either form by variant, bracketed by CUDA events while dlx_gemm_timing is on.
+int run_gemm_timed(int variant, const GemmArgs& g, cudaStream_t s);
 int launch_gemm_tc(const GemmArgs& g, cudaStream_t s);
 bool tc_supported();
 

@@ -48,6 +48,8 @@ def resolve_variant(n_in: int, n_out: int, variant: str | None = None) -> int:
     are multiples of 8 (the TMA row-pitch rule), the FP32 form otherwise.
     """
     v = variant if variant is not None else _default_variant
+    if isinstance(v, int) and v in (_lib.VARIANT_FP32, _lib.VARIANT_SPLIT_BF16):
+        return v
     if v == "fp32":
         return _lib.VARIANT_FP32
     if v == "split_bf16":
@@ -331,9 +333,60 @@ class PolyPlan(_Plan):
         return {"amp": g_amp, "opd": g_opd, "phase": g_ph, "w": g_w}
 
 
+class ScenePlan(_Plan):
+    """Many point sources through one pupil: per-source tilt as a DFT output shift."""
+
+    _destroy = "dlx_scene_plan_destroy"
+
+    def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                 focal_length=None, variant=None, max_sources=32):
+        super().__init__()
+        _lib.require_cuda()
+        self.wavelengths = tuple(float(w) for w in wavelengths)
+        self.n_in, self.n_out = int(n_in), int(n_out)
+        self.variant = resolve_variant(self.n_in, self.n_out, variant)
+        self.desc = _lib.SceneDesc(len(self.wavelengths), self.n_in, self.n_out,
+                                   float(pixel_scale_in), float(pixel_scale_out),
+                                   float(focal_length) if focal_length is not None else 0.0,
+                                   self.variant, int(max_sources))
+        call("dlx_scene_plan_create", ctypes.byref(self.desc), _lib.dbl_array(self.wavelengths),
+             ctypes.byref(self.handle))
+
+    @property
+    def footprint(self) -> int:
+        n = ctypes.c_size_t(0)
+        call("dlx_scene_plan_footprint", self.handle, ctypes.byref(n))
+        return int(n.value)
+
+    def forward(self, amp, amp_scale, opd, phase, positions, weights, out=None):
+        """Summed image of sources at positions [S, 2] (rad, float64) with weights [S, L]."""
+        positions = positions.to(device="cuda", dtype=torch.float64).contiguous()
+        weights = weights.to(device="cuda", dtype=torch.float32).contiguous()
+        S = positions.shape[0]
+        if out is None:
+            out = torch.empty((self.n_out, self.n_out), dtype=torch.float32, device="cuda")
+        call("dlx_scene_forward", self.handle, ptr(_contig(amp)), ptr(amp_scale),
+             ptr(_contig(opd)), ptr(_contig(phase)), ptr(positions), ptr(weights), S, ptr(out), 0,
+             _stream())
+        return out
+
+    def backward(self, amp, amp_scale, opd, phase, positions, weights, g_image, want_pos=True,
+                 want_w=True):
+        positions = positions.to(device="cuda", dtype=torch.float64).contiguous()
+        weights = weights.to(device="cuda", dtype=torch.float32).contiguous()
+        S = positions.shape[0]
+        g_pos = torch.empty((S, 2), dtype=torch.float32, device="cuda") if want_pos else None
+        g_w = torch.empty(weights.shape, dtype=torch.float32, device="cuda") if want_w else None
+        call("dlx_scene_backward", self.handle, ptr(_contig(amp)), ptr(amp_scale),
+             ptr(_contig(opd)), ptr(_contig(phase)), ptr(positions), ptr(weights), S,
+             ptr(g_image.contiguous()), ptr(g_pos), ptr(g_w), _stream())
+        return g_pos, g_w
+
+
 mft_plans = _PlanCache(16)
 fft_plans = _PlanCache(8)
 poly_plans = _PlanCache(8)
+scene_plans = _PlanCache(4)
 
 
 def get_mft_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,
@@ -358,6 +411,17 @@ def get_fft_plan(wavelengths, n_in, pixel_scale_in, pad=2, focal_length=None, in
     return fft_plans.get(key, lambda: FFTPlan(wl, n_in, pixel_scale_in, pad, focal_length,
                                               inverse, ramps,
                                               "fp32" if v == 0 else "split_bf16"))
+
+
+def get_scene_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                   focal_length=None, variant=None, max_sources=32):
+    wl = tuple(float(w) for w in wavelengths)
+    v = resolve_variant(n_in, n_out, variant)
+    key = (wl, int(n_in), float(pixel_scale_in), int(n_out), float(pixel_scale_out),
+           None if focal_length is None else float(focal_length), v, int(max_sources),
+           torch.cuda.current_device())
+    return scene_plans.get(key, lambda: ScenePlan(wl, n_in, pixel_scale_in, n_out, pixel_scale_out,
+                                                  focal_length, v, max_sources))
 
 
 def get_poly_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,

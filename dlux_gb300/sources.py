@@ -125,7 +125,16 @@ class PointSources(Source):
         n_src = src.position.shape[0]
         npix, ps = optics._focal_sampling()
         from . import kernels
-        plan = kernels.get_poly_plan(wl, optics.wf_npixels, optics.diameter / optics.wf_npixels,
+        n_in = optics.wf_npixels
+        pupil_grad = any(t is not None and t.requires_grad for t in (amp, opd, phase))
+        if not pupil_grad and npix <= n_in:
+            # The pupil is fixed: tilt each source through its DFT matrices and
+            # share one pupil field per wavelength.
+            plan = kernels.get_scene_plan(wl, n_in, optics.diameter / n_in, npix, ps, None, None,
+                                          max_sources=min(n_src, 32))
+            return autograd.scene_psf(plan, amp, opd, phase, weights.to(torch.float32),
+                                      src.position, flag, tilt)
+        plan = kernels.get_poly_plan(wl, n_in, optics.diameter / n_in,
                                      npix, ps, None, None, max_objects=min(n_src, 32))
         return autograd.poly_sources(plan, amp, opd, phase, weights.to(torch.float32),
                                      src.position, flag, tilt)

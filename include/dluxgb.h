@@ -291,6 +291,41 @@ int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
 int dlx_poly_plan_info(dlx_poly_plan plan, int* n_wavelengths, int* n_in, int* n_out,
                        int* max_objects);
 
+/* ---- a20/a21: many point sources through one pupil ---------------------
+ * Replaces PointSources.model (sources.py:392-411) for a pupil that does not
+ * need gradients: image [M][M] = sum_s sum_l weights[s][l] PSF_l(position_s),
+ * with the source tilt (wavefronts.py:370-395) folded into per-source DFT
+ * matrices (an output-coordinate shift) instead of a tilted pupil field per
+ * source. positions: device double [S][2] (rad, x then y); weights: device
+ * float [S][L] (spectrum x flux). amp/amp_scale/opd/phase as dlx_poly_psf.
+ * The reverse pass gives d/d(position) (float [S][2]) and d/d(weights)
+ * (float [S][L]); either output may be NULL. Sources are processed
+ * max_sources (<= 32) at a time.
+ */
+typedef struct dlx_scene_plan_s* dlx_scene_plan;
+typedef struct {
+  int n_wavelengths;
+  int n_in;                /* pupil side N */
+  int n_out;               /* PSF side M */
+  double pixel_scale_in;   /* pupil pixel (m) */
+  double pixel_scale_out;  /* PSF pixel (rad, or m with focal_length) */
+  double focal_length;     /* <= 0: angular */
+  int variant;             /* DLX_VARIANT_* */
+  int max_sources;         /* sources per launch, 1..32 */
+} dlx_scene_desc;
+int dlx_scene_plan_create(const dlx_scene_desc* desc, const double* wavelengths_host,
+                          dlx_scene_plan* plan);
+int dlx_scene_plan_destroy(dlx_scene_plan plan);
+int dlx_scene_plan_footprint(dlx_scene_plan plan, size_t* bytes);
+int dlx_scene_forward(dlx_scene_plan plan, const float* amp, const float* amp_scale,
+                      const float* opd, const float* phase, const double* positions,
+                      const float* weights, int n_sources, float* image, int accumulate,
+                      void* stream);
+int dlx_scene_backward(dlx_scene_plan plan, const float* amp, const float* amp_scale,
+                       const float* opd, const float* phase, const double* positions,
+                       const float* weights, int n_sources, const float* g_image, float* g_pos,
+                       float* g_weights, void* stream);
+
 /* ---- Serving batch ----
  * No counterpart in dLux, which has no serving loop. One batch of requests
  * that share a plan (same N, M and wavelengths), each with its own Zernike
