@@ -12,6 +12,7 @@ from .base import Base  # noqa: F401
 from .coordinates import CoordSpec  # noqa: F401
 from .wavefronts import Wavefront  # noqa: F401
 from .psfs import PSF  # noqa: F401
+from .layers import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401
 from .layers import (OpticalLayer, TransmissiveLayer, AberratedLayer, BasisLayer,  # noqa: F401
                      Tilt, Normalise, Optic, BasisOptic, MFT, FFT, DetectorLayer,
                      ApplyPixelResponse, Downsample, AddConstant, ApplySaturation)

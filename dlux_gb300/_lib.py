@@ -70,6 +70,15 @@ class PolyObject(ctypes.Structure):
     ]
 
 
+class ApertureDesc(ctypes.Structure):
+    """dlx_aperture_desc: a dynamic circular aperture and its coordinate transformation."""
+    _fields_ = [
+        ("npixels", _c_int), ("pixel_scale", _c_dbl), ("translation", _c_dbl * 2),
+        ("rotation", _c_dbl), ("compression", _c_dbl * 2), ("shear", _c_dbl * 2),
+        ("radius", _c_dbl), ("softening", _c_dbl), ("occulting", _c_int),
+    ]
+
+
 class SceneDesc(ctypes.Structure):
     _fields_ = [
         ("n_wavelengths", _c_int), ("n_in", _c_int), ("n_out", _c_int),
@@ -135,6 +144,11 @@ _SIGNATURES = {
     "dlx_poly_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "dlx_poly_plan_info": (_c_int, [_c_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                     ctypes.POINTER(_c_int), ctypes.POINTER(_c_int)]),
+    "dlx_zernike_table": (_c_int, [_c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
+    "dlx_aberrated_aperture": (_c_int, [ctypes.POINTER(ApertureDesc), _c_vp, _c_int, _c_vp,
+                                        _c_vp, _c_vp, _c_vp]),
+    "dlx_aberrated_aperture_grad": (_c_int, [ctypes.POINTER(ApertureDesc), _c_vp, _c_int,
+                                             _c_vp, _c_vp, _c_vp]),
     "dlx_scene_plan_create": (_c_int, [ctypes.POINTER(SceneDesc), _c_vp, ctypes.POINTER(_c_vp)]),
     "dlx_scene_plan_destroy": (_c_int, [_c_vp]),
     "dlx_scene_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),

@@ -187,6 +187,27 @@ def scene_psf(plan, amp, opd, phase, weights, positions, normalise=False,
                           (float(base_tilt[0]), float(base_tilt[1])))
 
 
+class DynamicZernike(torch.autograd.Function):
+    """OPD = sum_j c_j Z_j of a dynamic aperture, evaluated per pixel on the device
+    (polynomials.py:20-51); the reverse pass recomputes the Zernikes per pixel."""
+
+    @staticmethod
+    def forward(ctx, desc, noll, coeffs):
+        ctx.desc, ctx.noll = desc, list(noll)
+        _, opd = kernels.aberrated_aperture(desc, noll, coeffs.detach(), want_trans=False)
+        return opd
+
+    @staticmethod
+    def backward(ctx, g):
+        if not ctx.needs_input_grad[2]:
+            return None, None, None
+        return None, None, kernels.aberrated_aperture_grad(ctx.desc, ctx.noll, g.contiguous())
+
+
+def dynamic_zernike(desc, noll, coeffs):
+    return DynamicZernike.apply(desc, list(noll), coeffs)
+
+
 class LinearTransform(torch.autograd.Function):
     """A cached MFT or FFT plan applied to complex64 fields; backward is the adjoint."""
 

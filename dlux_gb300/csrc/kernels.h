@@ -126,6 +126,29 @@ constexpr int kFusedPupilMaxL = 2048;
 int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s);
 
 
+// --- zernike.cu: dynamic aperture + Zernike aberrations ----------------------
+constexpr int kMaxZern = 64;       // terms per call
+constexpr int kMaxZernCoeff = 9;   // radial coefficients per term ((n - |m|)/2 + 1)
+struct ZernTable {                 // passed by value
+  int K;
+  int n[kMaxZern], m[kMaxZern], nc[kMaxZern];
+  float norm[kMaxZern];
+  float c[kMaxZern][kMaxZernCoeff];  // highest power of rho^2 first
+};
+struct ZernAperture {
+  int n;                  // pixels per side
+  float pixel_scale;      // m
+  float translation[2], shear[2], compression[2];
+  float rot_c, rot_s;     // cos(-rotation), sin(-rotation)
+  float radius;           // m (also the Zernike normalisation extent)
+  float clip;             // soft-edge half width, m
+  int occulting;
+};
+int launch_aperture_eval(const ZernAperture& a, const ZernTable& z, const float* coeffs,
+                         unsigned* minmax_ws, float* trans, float* opd, cudaStream_t s);
+int launch_zernike_grad(const ZernAperture& a, const ZernTable& z, const float* g, double* partial,
+                        int nparts, float* g_coeffs, cudaStream_t s);
+
 // --- gemm_fp32.cu / gemm_tc.cu ---------------------------------------------
 // Complex GEMM D[b][m][n] = sum_k opA(A[b][m][k]) * B[b][n][k], opA = conj if conj_a.
 // Epilogue kinds shared by both arithmetic forms.

@@ -383,6 +383,51 @@ class ScenePlan(_Plan):
         return g_pos, g_w
 
 
+def aperture_desc(npixels, pixel_scale, radius, softening=1.0, occulting=False,
+                  translation=None, rotation=None, compression=None, shear=None):
+    """dlx_aperture_desc of a dynamic circular aperture under a CoordTransform."""
+    d = _lib.ApertureDesc()
+    d.npixels = int(npixels)
+    d.pixel_scale = float(pixel_scale)
+    t = (0.0, 0.0) if translation is None else tuple(float(v) for v in translation)
+    c = (1.0, 1.0) if compression is None else tuple(float(v) for v in compression)
+    sh = (0.0, 0.0) if shear is None else tuple(float(v) for v in shear)
+    d.translation[0], d.translation[1] = t
+    d.compression[0], d.compression[1] = c
+    d.shear[0], d.shear[1] = sh
+    d.rotation = 0.0 if rotation is None else float(rotation)
+    d.radius = float(radius)
+    d.softening = float(softening)
+    d.occulting = int(bool(occulting))
+    return d
+
+
+def _noll_array(noll):
+    arr = (ctypes.c_int * max(1, len(noll)))(*[int(j) for j in noll])
+    return arr
+
+
+def aberrated_aperture(desc, noll, coeffs, want_trans=True, want_opd=True):
+    """(transmission, opd) [N, N] of a dynamic aperture; either may be skipped (None)."""
+    dev = _lib.require_cuda()
+    n = desc.npixels
+    trans = torch.empty((n, n), dtype=torch.float32, device=dev) if want_trans else None
+    opd = torch.empty((n, n), dtype=torch.float32, device=dev) if want_opd else None
+    c = None if coeffs is None else _f32(coeffs, dev)
+    call("dlx_aberrated_aperture", ctypes.byref(desc), _noll_array(noll), len(noll), ptr(c),
+         ptr(trans), ptr(opd), _stream())
+    return trans, opd
+
+
+def aberrated_aperture_grad(desc, noll, g_opd):
+    """d<g_opd, opd>/d coefficients [K]."""
+    dev = g_opd.device
+    g = torch.empty((len(noll),), dtype=torch.float32, device=dev)
+    call("dlx_aberrated_aperture_grad", ctypes.byref(desc), _noll_array(noll), len(noll),
+         ptr(g_opd.contiguous()), ptr(g), _stream())
+    return g
+
+
 mft_plans = _PlanCache(16)
 fft_plans = _PlanCache(8)
 poly_plans = _PlanCache(8)

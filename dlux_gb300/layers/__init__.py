@@ -6,3 +6,4 @@ from .optics import Optic, BasisOptic  # noqa: F401
 from .propagators import MFT, FFT  # noqa: F401
 from .detector_layers import (DetectorLayer, ApplyPixelResponse, Downsample,  # noqa: F401
                               AddConstant, ApplySaturation)
+from .apertures import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401

@@ -42,9 +42,11 @@ class PupilAccumulator:
     A = prod(pre) / N^2 without one (the 1/N^2 initial field, wavefronts.py:111).
     """
 
-    def __init__(self, npixels, wavefront=None):
+    def __init__(self, npixels, wavefront=None, pixel_scale=None):
         self.n = npixels
         self.wavefront = wavefront
+        self.pixel_scale = (pixel_scale if pixel_scale is not None else
+                            (wavefront.pixel_scale if wavefront is not None else None))
         self.pre, self.post = [], []
         self.normalised = False
         self.opd = None

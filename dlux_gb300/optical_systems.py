@@ -202,7 +202,7 @@ class ParametricLayeredOpticalSystem(ParametricOpticalSystem, LayeredOpticalSyst
 
     def fused_pupil(self):
         """(amp, normalise, opd, phase, tilt) if every layer folds into one pupil, else None."""
-        acc = PupilAccumulator(self.wf_npixels)
+        acc = PupilAccumulator(self.wf_npixels, pixel_scale=self.diameter / self.wf_npixels)
         try:
             for layer in self.layers.values():
                 layer.fuse(acc)

@@ -291,6 +291,35 @@ int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
 int dlx_poly_plan_info(dlx_poly_plan plan, int* n_wavelengths, int* n_in, int* n_out,
                        int* max_objects);
 
+/* ---- a12: dynamic aberrated circular aperture ----------------------------
+ * Replaces AberratedAperture over a CircularAperture (layers/apertures.py:
+ * 240-312, 643-800): the soft-edged transmission (utils/geometry.py:49-91,
+ * 229-255) and OPD = sum_j coeffs[j] Z_noll[j] (polynomials.py:20-51,
+ * utils/zernikes.py:122-294) evaluated per pixel on the device after dLux's
+ * CoordTransform (coordinates.py:240-320: translate, shear, compress,
+ * rotate). No basis array is read or stored. Up to 64 terms, radial order
+ * <= 16 (both outputs may be NULL). dlx_aberrated_aperture_grad returns
+ * d<g_opd, opd>/d coeffs. dlx_zernike_table is host-only: the (n, m) of each
+ * Noll index and its radial coefficients (9 per term, highest power of
+ * rho^2 first).
+ */
+typedef struct {
+  int npixels;             /* wavefront side N */
+  double pixel_scale;      /* m per pixel */
+  double translation[2];   /* m */
+  double rotation;         /* rad, clockwise */
+  double compression[2];
+  double shear[2];
+  double radius;           /* m; also the extent the Zernikes are normalised to */
+  double softening;        /* soft edge width in pixels (> 0) */
+  int occulting;
+} dlx_aperture_desc;
+int dlx_zernike_table(const int* noll, int n_terms, int* n_out, int* m_out, float* coeffs_out);
+int dlx_aberrated_aperture(const dlx_aperture_desc* desc, const int* noll_host, int n_terms,
+                           const float* coeffs, float* transmission, float* opd, void* stream);
+int dlx_aberrated_aperture_grad(const dlx_aperture_desc* desc, const int* noll_host, int n_terms,
+                                const float* g_opd, float* g_coeffs, void* stream);
+
 /* ---- a20/a21: many point sources through one pupil ---------------------
  * Replaces PointSources.model (sources.py:392-411) for a pupil that does not
  * need gradients: image [M][M] = sum_s sum_l weights[s][l] PSF_l(position_s),

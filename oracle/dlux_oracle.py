@@ -429,6 +429,61 @@ def combine(arrays, oversample=1, use_sum=False):
     return downsample(arr, oversample)
 
 
+def coord_transform(coords, translation=None, rotation=None, compression=None, shear=None):
+    """CoordTransform.__call__ (coordinates.py:305-314): translate, shear, compress, rotate.
+
+    translate: coords - t (utils/coordinates.py:23-39); shear: coords + coords^T * s,
+    the transposed planes of a square xy grid (utils/coordinates.py:61-78); compress:
+    coords * c (:42-58); rotate clockwise (:81-101).
+    """
+    coords = np.asarray(coords, np.float64)
+    if translation is not None:
+        coords = coords - np.asarray(translation, np.float64)[:, None, None]
+    if shear is not None:
+        coords = coords + np.transpose(coords, (0, 2, 1)) * np.asarray(shear, np.float64)[:, None, None]
+    if compression is not None:
+        coords = coords * np.asarray(compression, np.float64)[:, None, None]
+    if rotation is not None:
+        coords = _rotate_coords(coords, float(rotation))
+    return coords
+
+
+def soften(distances, clip_dist, invert=False):
+    """Clip to +-clip_dist, then rescale by the array's min/max (utils/geometry.py:49-91)."""
+    d = np.asarray(distances, np.float64)
+    if invert:
+        d = -d
+    d = np.clip(d, -clip_dist, clip_dist)
+    if d.max() == d.min():
+        return (d > 0).astype(np.float64)
+    return (d - d.min()) / (d.max() - d.min())
+
+
+def soft_circle(coords, radius, clip_dist=0.1, invert=False):
+    """utils/geometry.py:229-255 with circ_distance :405-418."""
+    return soften(-(np.hypot(coords[0], coords[1]) - radius), clip_dist, invert)
+
+
+def aberrated_circular_aperture(npixels, diameter, radius, noll, coefficients,
+                                transformation=None, softening=1.0, occulting=False):
+    """AberratedAperture(CircularAperture(radius, ...), noll, coefficients) on a
+    wavefront of ``npixels`` over ``diameter``: (transmission, opd).
+
+    Transmission: CircularAperture.transmission (layers/apertures.py:302-306) with
+    clip = pixel_scale * softening / 2. OPD: eval_basis of the dynamic Zernikes at the
+    transformed coordinates divided by the extent (= radius)
+    (layers/apertures.py:754-771; polynomials.py:20-51, nsides = 0).
+    """
+    coords = pixel_coords(npixels, diameter)
+    pixel_scale = diameter / npixels
+    t = transformation or {}
+    c = coord_transform(coords, **t)
+    trans = soft_circle(c, radius, pixel_scale * softening / 2, occulting)
+    basis = np.array([zernike(j, c / radius, 2.0) for j in noll])
+    opd = np.tensordot(basis, np.asarray(coefficients, np.float64), axes=(0, 0))
+    return trans, opd, basis
+
+
 def circular_aperture(npixels, diameter, oversample=5, secondary_diameter=None,
                       spider_width=None, spider_angles=None, zernike_nolls=None,
                       zernike_oversize=0.01):
