@@ -8,7 +8,11 @@ spider vanes, 21 Noll Zernikes (j = 4..24) with N(0, 30 nm) coefficients,
 downsample to 128 x 128. One step = one PSF evaluation plus the gradient of
 sum(R * image) (R a seeded N(0, 1) 128 x 128 array) with respect to the 21
 coefficients, through the public API (AngularOpticalSystem.propagate,
-LayeredDetector, torch autograd -> the hand-written reverse kernels).
+LayeredDetector, torch autograd -> the hand-written reverse kernels). The step
+is captured once as a CUDA graph (dlux_gb300.graphs.GraphedStep, the counterpart
+of jax.jit of the step) and replayed: `value` times the replays with the inputs
+resident, `e2e` adds the pinned host copies every step. The eager step is also
+timed (`eager_value`); it gives the per-launch GEMM times of the roofline.
 
 Every step touches ~1 GB of device memory (cached DFT matrices plus the
 per-wavelength fields), far more than the 129 MB L2, so no explicit L2 flush
@@ -222,15 +226,24 @@ def build_workload(variant):
 
 def step(optics, detector, wls, w, R, c):
     """One PSF + gradient evaluation through the public API."""
-    import dlux_gb300 as dl
-
     c = c.detach().requires_grad_(True)
     sys_ = optics.set("layers.BasisLayer.coefficients", c)
     psf = sys_.propagate(wls, weights=w, return_psf=True)
     img = detector.model(psf)
     loss = (img * R).sum()
     loss.backward()
-    return loss, c.grad, img
+    return loss.detach(), c.grad, img.detach()
+
+
+def graphed_step(objs):
+    """The same step captured once as a CUDA graph (dlux_gb300.graphs.GraphedStep): the
+    GB300 counterpart of jax.jit of the step. Coefficients in, (loss, grad, image) out."""
+    from dlux_gb300.graphs import GraphedStep
+    import torch
+
+    optics, detector, wls, w, R, coeffs = objs
+    c0 = torch.as_tensor(coeffs, dtype=torch.float32, device="cuda")
+    return GraphedStep(lambda c: step(optics, detector, wls, w, R, c), c0), c0
 
 
 def time_gpu(args, variant, rank, world, measure_roofline=True):
@@ -278,30 +291,55 @@ def time_gpu(args, variant, rank, world, measure_roofline=True):
             "objects": (optics, detector, wls, w, R, coeffs)}
 
 
-def time_e2e(args, objs, world):
-    """Same step with the coefficients copied from pinned host memory and the
+def time_graphed(args, gstep, c0, world):
+    """Device throughput of the graphed step with the inputs resident (CUDA events)."""
+    import torch
+
+    for _ in range(max(3, args.warmup)):
+        gstep(c0)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        gstep(c0)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def time_e2e(args, gstep, world):
+    """The graphed step with the coefficients copied from pinned host memory and the
     loss, gradient and image read back every step."""
     import torch
 
-    optics, detector, wls, w, R, coeffs = objs
-    host_c = torch.as_tensor(coeffs, dtype=torch.float32).pin_memory()
+    optics_coeffs = gstep.static_in[0]
+    host_c = optics_coeffs.detach().cpu().pin_memory()
     out_img = torch.empty((128, 128), dtype=torch.float32).pin_memory()
     out_g = torch.empty((len(NOLLS),), dtype=torch.float32).pin_memory()
     out_l = torch.empty((), dtype=torch.float32).pin_memory()
     c = torch.empty((len(NOLLS),), dtype=torch.float32, device="cuda")
     for _ in range(2):
         c.copy_(host_c, non_blocking=True)
-        step(optics, detector, wls, w, R, c)
+        gstep(c)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         c.copy_(host_c, non_blocking=True)
-        loss, g, img = step(optics, detector, wls, w, R, c)
-        out_l.copy_(loss.detach(), non_blocking=True)
+        loss, g, img = gstep(c)
+        out_l.copy_(loss, non_blocking=True)
         out_g.copy_(g, non_blocking=True)
-        out_img.copy_(img.detach(), non_blocking=True)
+        out_img.copy_(img, non_blocking=True)
         torch.cuda.current_stream().synchronize()
     dt = time.perf_counter() - t0
     if world > 1:
@@ -615,17 +653,26 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl")
 
-    res = time_gpu(args, args.variant, rank, world)
-    ms_step = res["ms_total"] / args.steps
-    value = world * args.steps / (res["ms_total"] / 1e3)
-    e2e_dt, h2d, d2h = time_e2e(args, res["objects"], world)
+    res = time_gpu(args, args.variant, rank, world)      # eager: roofline and launch count
+    eager_value = world * args.steps / (res["ms_total"] / 1e3)
+    gstep, c0 = graphed_step(res["objects"])
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    ms_total = time_graphed(args, gstep, c0, world)
+    clk = clocks.stop()
+    ms_step = ms_total / args.steps
+    value = world * args.steps / (ms_total / 1e3)
+    e2e_dt, h2d, d2h = time_e2e(args, gstep, world)
     e2e_value = world * args.steps / e2e_dt
 
     fp32 = None
     if not args.no_fp32_compare and args.variant == "split_bf16":
         r2 = time_gpu(args, "fp32", rank, world, measure_roofline=False)
-        fp32 = {"value": world * args.steps / (r2["ms_total"] / 1e3),
-                "ms_per_step": r2["ms_total"] / args.steps}
+        g2, c2 = graphed_step(r2["objects"])
+        ms2 = time_graphed(args, g2, c2, world)
+        fp32 = {"value": world * args.steps / (ms2 / 1e3), "ms_per_step": ms2 / args.steps,
+                "eager_value": world * args.steps / (r2["ms_total"] / 1e3)}
 
     hbm, tflops, src = load_peaks()
     g = res["gemm"]
@@ -667,9 +714,12 @@ def main():
             "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": res["launches"],
+            "execution": "one CUDA graph per step (dlux_gb300.graphs.GraphedStep over the "
+                         "public API; the same kernels as the eager step)",
+            "eager_value": eager_value,
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "clocks": res["clocks"],
+            "clocks": clk,
             "fp32_form": fp32,
             "speedup_vs_fp32": (value / fp32["value"]) if fp32 else None,
         }
