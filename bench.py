@@ -22,6 +22,7 @@ is made between steps.
   python bench.py --impl reference   # the CPU restatement of the same step
   python bench.py --workload serving # mixed-shape request stream through the server
   python bench.py --workload cfg1|cfg3|cfg4   # the other measured configurations
+  python bench.py --workload fft     # FFT propagation: radix line FFTs vs DFT-GEMM forms
 """
 
 from __future__ import annotations
@@ -523,6 +524,58 @@ def cfg_workload(name, variant):
     raise ValueError(name)
 
 
+def run_fft(args):
+    """Padded centred FFT propagation (layers/propagators.py FFT, utils/propagation.py:8-64):
+    forward + adjoint of a batch of 16 wavelengths at N = --fft-n (1024), pad = 2, for the
+    radix-2 line-FFT form and the two DFT-GEMM forms. Unit: plane transforms (forward +
+    adjoint of one wavelength) per second. Roofline of the radix form: algorithmic bytes =
+    input + output of every pass, (N^2 + N P) 8 + (N P + P^2) 8 per direction."""
+    import torch
+    from dlux_gb300 import kernels
+
+    n, pad, L = args.fft_n, 2, 16
+    P = n * pad
+    rng = np.random.default_rng(5)
+    x = torch.as_tensor((rng.normal(size=(L, n, n)) + 1j * rng.normal(size=(L, n, n))) / n,
+                        dtype=torch.complex64, device="cuda")
+    y = torch.as_tensor((rng.normal(size=(L, P, P)) + 1j * rng.normal(size=(L, P, P))) / P,
+                        dtype=torch.complex64, device="cuda")
+    wls = np.linspace(0.8e-6, 1.2e-6, L)
+    out = {}
+    for form in ("radix", "split_bf16", "fp32"):
+        plan = kernels.FFTPlan(wls, n, 1.0 / n, pad, None, False, variant=form)
+        for _ in range(max(3, args.warmup)):
+            plan.forward(x)
+            plan.adjoint(y)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            plan.forward(x)
+            plan.adjoint(y)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        out[form] = {"ms_per_step": ms, "planes_per_s": L / (ms * 1e-3)}
+        plan.close()
+    hbm, _, src = load_peaks()
+    bytes_step = L * 2 * ((n * n + n * P) * 8 + (n * P + P * P) * 8)
+    achieved = bytes_step / (out["radix"]["ms_per_step"] * 1e-3) / 1e9
+    line = {"metric": "FFT propagation forward+adjoint planes/sec", "value":
+            out["radix"]["planes_per_s"], "unit": "planes/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["radix"]["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": f"padded centred FFT, N={n}, pad={pad}, {L} wavelengths, "
+                                   "forward + adjoint"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "peak_source": f"{src} copy bandwidth"},
+            "forms": out}
+    print(json.dumps(line))
+    return 0
+
+
 def run_config(args):
     import torch
     import dlux_gb300._lib as L
@@ -625,10 +678,11 @@ def main():
     ap.add_argument("--no-fp32-compare", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="psf_grad",
-                    choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4"])
+                    choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent stream slots")
+    ap.add_argument("--fft-n", type=int, default=1024, help="fft: pupil side (pad 2)")
     ap.add_argument("--graph-after", type=int, default=8,
                     help="serving: capture a batch shape as a CUDA graph after this many uses")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
@@ -650,6 +704,8 @@ def main():
         return run_serving(args) if rank == 0 else 0
     if args.workload in ("cfg1", "cfg3", "cfg4"):
         return run_config(args) if rank == 0 else 0
+    if args.workload == "fft":
+        return run_fft(args) if rank == 0 else 0
     if world > 1:
         torch.distributed.init_process_group("nccl")
 

@@ -28,6 +28,7 @@ DLX_ERR_UNSUPPORTED = 6
 
 VARIANT_FP32 = 0
 VARIANT_SPLIT_BF16 = 1
+VARIANT_RADIX = 2          # FFT plans only: radix-2 line FFTs
 
 _c_int = ctypes.c_int
 _c_dbl = ctypes.c_double

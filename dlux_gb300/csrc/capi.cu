@@ -419,6 +419,8 @@ struct dlx_mft_plan_s {
 };
 struct dlx_fft_plan_s {
   TwoStepPlan p;
+  bool radix = false;  // DLX_VARIANT_RADIX: line FFTs instead of the DFT-GEMM pair
+  RadixFft rf;
 };
 
 extern "C" {
@@ -557,6 +559,29 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
   if (d->batch <= 0 || d->n_in <= 0 || d->pad <= 0)
     return fail(DLX_ERR_SHAPE, "fft_plan_create: batch, n_in and pad must be positive");
   if (!(d->pixel_scale_in > 0)) return fail(DLX_ERR_ARG, "fft_plan_create: pixel scale <= 0");
+  if (d->variant == DLX_VARIANT_RADIX) {
+    auto* p = new (std::nothrow) dlx_fft_plan_s();
+    if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+    p->radix = true;
+    std::vector<DftAxis> ax(d->batch);
+    std::vector<float> alphas(d->batch, 1.0f / (float)(d->n_in * d->pad));
+    for (int b = 0; b < d->batch; ++b) {
+      if (!(wl[b] > 0)) {
+        delete p;
+        return fail(DLX_ERR_ARG, "fft_plan_create: wavelengths must be positive");
+      }
+      ax[b] = fft_axis(*d, wl[b]);
+    }
+    const int st = radix_fft_create(&p->rf, d->batch, d->n_in, d->pad, d->inverse != 0,
+                                    ax.data(), alphas.data());
+    if (st != DLX_OK) {
+      radix_fft_release(&p->rf);
+      delete p;
+      return st;
+    }
+    *plan = p;
+    return DLX_OK;
+  }
   DLX_TRY(validate_variant(d->variant));
   DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_in * d->pad));
   auto* p = new (std::nothrow) dlx_fft_plan_s();
@@ -587,6 +612,7 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
 int dlx_fft_plan_destroy(dlx_fft_plan plan) {
   if (!plan) return DLX_OK;
   cudaDeviceSynchronize();
+  radix_fft_release(&plan->rf);
   plan->p.release();
   delete plan;
   return DLX_OK;
@@ -594,11 +620,17 @@ int dlx_fft_plan_destroy(dlx_fft_plan plan) {
 
 int dlx_fft_forward(dlx_fft_plan plan, const void* in, void* out, void* stream) {
   if (!plan || !in || !out) return fail(DLX_ERR_ARG, "fft_forward: null pointer");
+  if (plan->radix)
+    return radix_fft_forward(plan->rf, static_cast<const float2*>(in), static_cast<float2*>(out),
+                             as_stream(stream));
   return plan->p.forward(in, out, as_stream(stream));
 }
 
 int dlx_fft_adjoint(dlx_fft_plan plan, const void* gout, void* gin, void* stream) {
   if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "fft_adjoint: null pointer");
+  if (plan->radix)
+    return radix_fft_adjoint(plan->rf, static_cast<const float2*>(gout), static_cast<float2*>(gin),
+                             as_stream(stream));
   return plan->p.adjoint(gout, gin, as_stream(stream));
 }
 

@@ -1,0 +1,251 @@
+// fft.cu -- the padded, centred 2-D FFT of dLux (utils/propagation.py:8-64,
+// utils/fourier.py:14-78, wavefronts.py:654-727) as radix-2 FFTs of lines in
+// shared memory, for large pad * N where the exact DFT-GEMM pair costs
+// O(P^2 N).
+//
+// The DFT-GEMM form uses A[k][j] = exp(2 pi i s (j + npad - c)(k - c) / P)
+// times the input and output phase ramps. Since exp(2 pi i s j' k' / P) is
+// P-periodic in j' and k', that is a plain length-P FFT whose input element j
+// sits at slot (j + npad - c) mod P and whose output element k is read at slot
+// (k - c) mod P. One kernel covers every pass. It loads n_in elements of each
+// line through an input ramp, scatters them into bit-reversed slots, runs
+// log2(P) in-place butterfly stages and gathers n_out elements through an
+// output ramp and a scale:
+//   forward   rows:    N lines of N -> P   (x), into tmp [N][P]
+//             columns: P lines of N -> P   (y), from tmp into out [P][P]
+//   adjoint   rows:    P lines of P -> N   (x, conjugate), into tmp [P][N]
+//             columns: N lines of P -> N   (y, conjugate), into gin [N][N]
+// Ramps exp(2 pi i (g j + d)) are reduced exactly in FP32 pairs (cis_ff), and
+// the twiddles exp(2 pi i s k / P) come from sincospif of an exact argument.
+#include <atomic>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+
+namespace dlx {
+
+struct LineRamp {  // per batch element
+  float2 g_in, d_in, g_out, d_out;  // float pairs (hi, lo), cycles per index / cycles
+  float scale;
+  int ramp_in, ramp_out;            // 0: the ramp is identically 1 (skipped)
+};
+
+namespace {
+
+// Lines of one launch: line l of batch b starts at base + b * bs + l * ls and
+// its elements are es apart.
+struct LineIO {
+  long long bs, ls, es;
+};
+
+template <int LPB>
+__global__ void __launch_bounds__(256) fft_lines_kernel(
+    const float2* __restrict__ in, LineIO io_in, int n_in, int off_in,
+    float2* __restrict__ out, LineIO io_out, int n_out, int off_out, int lines, int log2p,
+    float sign, const LineRamp* __restrict__ ramps) {
+  extern __shared__ float2 sm[];
+  const int P = 1 << log2p;
+  float2* tw = sm;             // [P/2] twiddles
+  float2* x = sm + P / 2;      // [LPB][P]
+  const int b = blockIdx.y;
+  const int l0 = blockIdx.x * LPB;
+  const LineRamp rp = ramps[b];
+  for (int k = threadIdx.x; k < P / 2; k += blockDim.x) {
+    float s, c;
+    sincospif(2.0f * (float)k / (float)P, &s, &c);
+    tw[k] = make_float2(c, sign * s);
+  }
+  for (int i = threadIdx.x; i < LPB * P; i += blockDim.x) x[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  // load: consecutive threads take consecutive addresses (line-major when the
+  // lines are adjacent in memory, element-major otherwise)
+  const bool line_fast = io_in.ls == 1;
+  for (int t = threadIdx.x; t < LPB * n_in; t += blockDim.x) {
+    const int li = line_fast ? t % LPB : t / n_in;
+    const int e = line_fast ? t / LPB : t % n_in;
+    const int l = l0 + li;
+    if (l >= lines) continue;
+    float2 v = in[(long long)b * io_in.bs + (long long)l * io_in.ls + (long long)e * io_in.es];
+    if (rp.ramp_in)
+      v = cmul(v, cis_ff(FF{(float)e, 0.f}, FF{rp.g_in.x, rp.g_in.y}, FF{rp.d_in.x, rp.d_in.y}));
+    int slot = (e + off_in) % P;
+    if (slot < 0) slot += P;
+    x[li * P + (int)(__brev((unsigned)slot) >> (32 - log2p))] = v;
+  }
+  __syncthreads();
+  for (int s = 1; s <= log2p; ++s) {
+    const int half = 1 << (s - 1);
+    const int tstep = P >> s;
+    for (int t = threadIdx.x; t < LPB * (P / 2); t += blockDim.x) {
+      const int li = t / (P / 2);
+      const int i = t - li * (P / 2);
+      const int grp = i >> (s - 1);
+      const int pos = i & (half - 1);
+      const int k0 = li * P + (grp << s) + pos;
+      const int k1 = k0 + half;
+      const float2 w = tw[pos * tstep];
+      const float2 u = x[k0];
+      const float2 v = cmul(x[k1], w);
+      x[k0] = make_float2(u.x + v.x, u.y + v.y);
+      x[k1] = make_float2(u.x - v.x, u.y - v.y);
+    }
+    __syncthreads();
+  }
+  const bool oline_fast = io_out.ls == 1;
+  for (int t = threadIdx.x; t < LPB * n_out; t += blockDim.x) {
+    const int li = oline_fast ? t % LPB : t / n_out;
+    const int o = oline_fast ? t / LPB : t % n_out;
+    const int l = l0 + li;
+    if (l >= lines) continue;
+    int slot = (o + off_out) % P;
+    if (slot < 0) slot += P;
+    float2 v = x[li * P + slot];
+    if (rp.ramp_out)
+      v = cmul(v, cis_ff(FF{(float)o, 0.f}, FF{rp.g_out.x, rp.g_out.y},
+                         FF{rp.d_out.x, rp.d_out.y}));
+    v.x *= rp.scale;
+    v.y *= rp.scale;
+    out[(long long)b * io_out.bs + (long long)l * io_out.ls + (long long)o * io_out.es] = v;
+  }
+}
+
+// Few lines per block keeps several blocks resident per SM (the butterfly
+// stages are latency-bound); two lines keep column loads at 16-byte segments.
+int lines_per_block(int P) { return P <= 1024 ? 4 : 2; }
+
+int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* out, LineIO io_out,
+                 int n_out, int off_out, int lines, int batch, int log2p, float sign,
+                 const LineRamp* ramps, cudaStream_t s) {
+  const int P = 1 << log2p;
+  const int lpb = lines_per_block(P);
+  const size_t smem = sizeof(float2) * ((size_t)P / 2 + (size_t)lpb * P);
+  static std::atomic<bool> attr_done{false};  // host side, once per process
+  if (!attr_done.load()) {
+    const int lim = 160 * 1024;  // covers P <= 8192 at every lines-per-block choice
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<8>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    attr_done.store(true);
+  }
+  dim3 grid((lines + lpb - 1) / lpb, batch);
+  switch (lpb) {
+    case 8:
+      fft_lines_kernel<8><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
+                                                  off_out, lines, log2p, sign, ramps);
+      break;
+    case 4:
+      fft_lines_kernel<4><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
+                                                  off_out, lines, log2p, sign, ramps);
+      break;
+    default:
+      fft_lines_kernel<2><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
+                                                  off_out, lines, log2p, sign, ramps);
+      break;
+  }
+  DLX_LAUNCH_CHECK("fft_lines_kernel");
+  return DLX_OK;
+}
+
+}  // namespace
+
+int radix_fft_create(RadixFft* f, int batch, int N, int pad, bool inverse, const DftAxis* axes,
+                     const float* alphas) {
+  f->batch = batch;
+  f->N = N;
+  f->P = N * pad;
+  int lg = 0;
+  while ((1 << lg) < f->P) ++lg;
+  if ((1 << lg) != f->P || f->P > 8192)
+    return fail(DLX_ERR_SHAPE, "radix FFT: pad * n_in must be a power of two <= 8192");
+  f->log2p = lg;
+  f->npad = (N * (pad - 1)) / 2;
+  f->c = f->P / 2;
+  f->sign = inverse ? 1.0f : -1.0f;
+  std::vector<LineRamp> rx(batch), ry(batch), rax(batch), ray(batch);
+  auto ff2 = [](double v) {
+    const FF f = ff_from_double(v);
+    return make_float2(f.hi, f.lo);
+  };
+  for (int b = 0; b < batch; ++b) {
+    const DftAxis& ax = axes[b];
+    LineRamp r{};
+    r.g_in = ff2(ax.g_in);
+    r.d_in = ff2(ax.d_in);
+    r.g_out = ff2(ax.g_out);
+    r.d_out = ff2(ax.d_out);
+    r.scale = (float)ax.scale;
+    r.ramp_in = (ax.g_in != 0.0 || ax.d_in != 0.0) ? 1 : 0;
+    r.ramp_out = (ax.g_out != 0.0 || ax.d_out != 0.0) ? 1 : 0;
+    rx[b] = r;
+    r.scale = (float)ax.scale * alphas[b];  // the normalisation goes on the last pass
+    ry[b] = r;
+    // adjoint: the conjugate output ramp on the input side and vice versa
+    LineRamp q{};
+    q.g_in = ff2(-ax.g_out);
+    q.d_in = ff2(-ax.d_out);
+    q.g_out = ff2(-ax.g_in);
+    q.d_out = ff2(-ax.d_in);
+    q.scale = (float)ax.scale;
+    q.ramp_in = r.ramp_out;
+    q.ramp_out = r.ramp_in;
+    rax[b] = q;
+    q.scale = (float)ax.scale * alphas[b];
+    ray[b] = q;
+  }
+  for (auto* pr : {&f->ramps_x, &f->ramps_y, &f->ramps_ax, &f->ramps_ay})
+    DLX_TRY_CUDA(cudaMalloc(pr, sizeof(LineRamp) * batch));
+  DLX_TRY_CUDA(cudaMemcpy(f->ramps_x, rx.data(), sizeof(LineRamp) * batch, cudaMemcpyHostToDevice));
+  DLX_TRY_CUDA(cudaMemcpy(f->ramps_y, ry.data(), sizeof(LineRamp) * batch, cudaMemcpyHostToDevice));
+  DLX_TRY_CUDA(cudaMemcpy(f->ramps_ax, rax.data(), sizeof(LineRamp) * batch, cudaMemcpyHostToDevice));
+  DLX_TRY_CUDA(cudaMemcpy(f->ramps_ay, ray.data(), sizeof(LineRamp) * batch, cudaMemcpyHostToDevice));
+  const cudaError_t e = cudaMalloc(&f->tmp, sizeof(float2) * (size_t)batch * N * f->P);
+  if (e != cudaSuccess) {
+    f->tmp = nullptr;
+    cudaGetLastError();
+    return fail(DLX_ERR_NOMEM, "radix FFT: workspace allocation failed");
+  }
+  return DLX_OK;
+}
+
+void radix_fft_release(RadixFft* f) {
+  for (LineRamp* r : {f->ramps_x, f->ramps_y, f->ramps_ax, f->ramps_ay})
+    if (r) cudaFree(r);
+  if (f->tmp) cudaFree(f->tmp);
+  f->ramps_x = f->ramps_y = f->ramps_ax = f->ramps_ay = nullptr;
+  f->tmp = nullptr;
+}
+
+// out [b][P][P] = FFT of in [b][N][N] (the forward of the DFT-GEMM FFT plan).
+int radix_fft_forward(const RadixFft& f, const float2* in, float2* out, cudaStream_t s) {
+  const int N = f.N, P = f.P, off_in = f.npad - f.c, off_out = -f.c;
+  // rows: line y of N elements (x), output row of P into tmp[b][y][:]
+  DLX_TRY(launch_lines(in, LineIO{(long long)N * N, N, 1}, N, off_in, f.tmp,
+                       LineIO{(long long)N * P, P, 1}, P, off_out, N, f.batch, f.log2p, f.sign,
+                       f.ramps_x, s));
+  // columns: line kx of N elements (y, stride P), output column of P into out
+  return launch_lines(f.tmp, LineIO{(long long)N * P, 1, P}, N, off_in, out,
+                      LineIO{(long long)P * P, 1, P}, P, off_out, P, f.batch, f.log2p, f.sign,
+                      f.ramps_y, s);
+}
+
+// gin [b][N][N] = adjoint applied to gout [b][P][P].
+int radix_fft_adjoint(const RadixFft& f, const float2* gout, float2* gin, cudaStream_t s) {
+  const int N = f.N, P = f.P;
+  // The adjoint reads slot (k - c) and writes slot (j + npad - c), with the
+  // opposite sign and the conjugate ramps swapped between input and output.
+  // rows: line ky of P elements (kx), output N elements (x) into tmp[b][ky][:]
+  DLX_TRY(launch_lines(gout, LineIO{(long long)P * P, P, 1}, P, -f.c, f.tmp,
+                       LineIO{(long long)P * N, N, 1}, N, f.npad - f.c, P, f.batch, f.log2p,
+                       -f.sign, f.ramps_ax, s));
+  // columns: line x of P elements (ky, stride N), output N elements (y) into gin
+  return launch_lines(f.tmp, LineIO{(long long)P * N, 1, N}, P, -f.c, gin,
+                      LineIO{(long long)N * N, 1, N}, N, f.npad - f.c, N, f.batch, f.log2p,
+                      -f.sign, f.ramps_ay, s);
+}
+
+}  // namespace dlx

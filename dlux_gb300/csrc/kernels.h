@@ -149,6 +149,23 @@ int launch_aperture_eval(const ZernAperture& a, const ZernTable& z, const float*
 int launch_zernike_grad(const ZernAperture& a, const ZernTable& z, const float* g, double* partial,
                         int nparts, float* g_coeffs, cudaStream_t s);
 
+// --- fft.cu: radix-2 form of the padded centred FFT --------------------------
+struct LineRamp;
+struct RadixFft {
+  int batch = 0, N = 0, P = 0, log2p = 0, npad = 0, c = 0;
+  float sign = -1.0f;           // forward transform direction
+  LineRamp* ramps_x = nullptr;  // device [batch]: forward x, forward y (with the
+  LineRamp* ramps_y = nullptr;  // normalisation), adjoint x, adjoint y
+  LineRamp* ramps_ax = nullptr;
+  LineRamp* ramps_ay = nullptr;
+  float2* tmp = nullptr;        // device [batch][N][P]
+};
+int radix_fft_create(RadixFft* f, int batch, int N, int pad, bool inverse, const DftAxis* axes,
+                     const float* alphas);
+void radix_fft_release(RadixFft* f);
+int radix_fft_forward(const RadixFft& f, const float2* in, float2* out, cudaStream_t s);
+int radix_fft_adjoint(const RadixFft& f, const float2* gout, float2* gin, cudaStream_t s);
+
 // --- gemm_fp32.cu / gemm_tc.cu ---------------------------------------------
 // Complex GEMM D[b][m][n] = sum_k opA(A[b][m][k]) * B[b][n][k], opA = conj if conj_a.
 // Epilogue kinds shared by both arithmetic forms.

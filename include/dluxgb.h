@@ -35,6 +35,7 @@ extern "C" {
 /* ---- MFT arithmetic forms ---------------------------------------------- */
 #define DLX_VARIANT_FP32 0       /* FP32 complex GEMM on the CUDA cores */
 #define DLX_VARIANT_SPLIT_BF16 1 /* BF16 hi/lo three-product tcgen05 GEMM, FP32 accumulation */
+#define DLX_VARIANT_RADIX 2      /* FFT plans only: radix-2 line FFTs in FP32 (pad * N a power of 2) */
 
 /* Thread-local message of the last failing call ("" if none). */
 const char* dlx_last_error(void);
