@@ -15,12 +15,13 @@ from .psfs import PSF  # noqa: F401
 from .layers import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401
 from .layers import (OpticalLayer, TransmissiveLayer, AberratedLayer, BasisLayer,  # noqa: F401
                      Tilt, Normalise, Optic, BasisOptic, MFT, FFT, DetectorLayer,
-                     ApplyPixelResponse, Downsample, AddConstant, ApplySaturation)
+                     ApplyPixelResponse, Downsample, AddConstant, ApplySaturation,
+                     ApplyJitter)
 from .optical_systems import (OpticalSystem, LayeredOpticalSystem,  # noqa: F401
                               ParametricLayeredOpticalSystem, AngularOpticalSystem,
                               CartesianOpticalSystem)
 from .spectra import Spectrum  # noqa: F401
-from .sources import PointSource, PointSources  # noqa: F401
+from .sources import PointSource, PointSources, ResolvedSource, PointResolvedSource  # noqa: F401
 from .detectors import LayeredDetector  # noqa: F401
 from .instruments import Telescope  # noqa: F401
 from .kernels import set_variant, get_variant, tensor_core_available  # noqa: F401

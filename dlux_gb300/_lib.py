@@ -145,6 +145,10 @@ _SIGNATURES = {
     "dlx_poly_plan_footprint": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_size_t)]),
     "dlx_poly_plan_info": (_c_int, [_c_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                     ctypes.POINTER(_c_int), ctypes.POINTER(_c_int)]),
+    "dlx_conv2d_same": (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_vp, _c_int, _c_int, _c_vp,
+                                 _c_vp]),
+    "dlx_conv2d_same_backward": (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_vp, _c_int, _c_int,
+                                          _c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_zernike_table": (_c_int, [_c_vp, _c_int, _c_vp, _c_vp, _c_vp]),
     "dlx_aberrated_aperture": (_c_int, [ctypes.POINTER(ApertureDesc), _c_vp, _c_int, _c_vp,
                                         _c_vp, _c_vp, _c_vp]),

@@ -208,6 +208,31 @@ def dynamic_zernike(desc, noll, coeffs):
     return DynamicZernike.apply(desc, list(noll), coeffs)
 
 
+class Conv2dSame(torch.autograd.Function):
+    """jax.scipy.signal.convolve(x, kernel, mode="same") with both gradients."""
+
+    @staticmethod
+    def forward(ctx, x, kernel):
+        ctx.save_for_backward(x, kernel)
+        return kernels.conv2d_same(x.detach().to(torch.float32), kernel.detach())
+
+    @staticmethod
+    def backward(ctx, g):
+        x, kernel = ctx.saved_tensors
+        gx, gk = kernels.conv2d_same_backward(x.detach().to(torch.float32), kernel.detach(),
+                                              g.contiguous(), ctx.needs_input_grad[0],
+                                              ctx.needs_input_grad[1])
+        if gk is not None:
+            gk = gk.to(kernel.dtype)
+        return gx, gk
+
+
+def conv2d_same(x, kernel):
+    if not isinstance(kernel, torch.Tensor):
+        kernel = torch.as_tensor(kernel, dtype=torch.float32, device=x.device)
+    return Conv2dSame.apply(x, kernel.to(device=x.device))
+
+
 class LinearTransform(torch.autograd.Function):
     """A cached MFT or FFT plan applied to complex64 fields; backward is the adjoint."""
 

@@ -1,0 +1,155 @@
+// conv.cu -- 2-D convolution of a PSF with a small kernel, mode "same"
+// (jax.scipy.signal.convolve as used by PSF.convolve, psfs.py:93-110;
+// ResolvedSource / PointResolvedSource, sources.py:490-521 and :711-748;
+// ApplyJitter, layers/detector_layers.py:134-199).
+//
+// out[i][j] = sum_{a,b} in[i + s0 - a][j + s1 - b] k[a][b], s = (K - 1) / 2 (the
+// centre crop of the full convolution), zero outside `in`. The reverse pass
+// needs:
+//   g_in[m][n] = sum_{a,b} g_out[m - s0 + a][n - s1 + b] k[a][b]  (a correlation:
+//                the same kernel flipped, with the mirrored offset)
+//   g_k[a][b]  = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - b]
+// A 32 x 32 output tile and its halo are staged in shared memory, and so is the
+// kernel. The kernel gradient gives each kernel element one block with a
+// fixed summation order.
+#include <string>
+
+#include "kernels.h"
+
+namespace dlx {
+namespace {
+
+constexpr int CT = 32;  // output tile side
+
+// flip = 0: convolution (out = in * k); flip = 1: correlation (out[m] = sum g[m - s + a] k[a]).
+__global__ void conv2d_same_kernel(const float* __restrict__ in, int H, int W,
+                                   const float* __restrict__ k, int K0, int K1, int flip,
+                                   float* __restrict__ out) {
+  extern __shared__ float sm[];
+  const int s0 = (K0 - 1) / 2, s1 = (K1 - 1) / 2;
+  const int TH = CT + K0 - 1, TW = CT + K1 - 1;
+  float* tile = sm;               // [TH][TW]
+  float* ks = sm + TH * TW;       // [K0][K1]
+  const int b = blockIdx.z;
+  const float* inb = in + (long long)b * H * W;
+  const int i0 = blockIdx.y * CT, j0 = blockIdx.x * CT;
+  // input rows needed: convolution i + s0 - a for a in [0, K0) -> [i0 + s0 - K0 + 1, i0 + CT - 1 + s0];
+  // correlation m - s0 + a -> [i0 - s0, i0 + CT - 1 - s0 + K0 - 1]
+  const int r_lo = flip ? i0 - s0 : i0 + s0 - K0 + 1;
+  const int c_lo = flip ? j0 - s1 : j0 + s1 - K1 + 1;
+  for (int t = threadIdx.x; t < TH * TW; t += blockDim.x) {
+    const int r = r_lo + t / TW, c = c_lo + t % TW;
+    tile[t] = (r >= 0 && r < H && c >= 0 && c < W) ? inb[(long long)r * W + c] : 0.0f;
+  }
+  for (int t = threadIdx.x; t < K0 * K1; t += blockDim.x) ks[t] = k[t];
+  __syncthreads();
+  for (int t = threadIdx.x; t < CT * CT; t += blockDim.x) {
+    const int ti = t / CT, tj = t % CT;
+    const int i = i0 + ti, j = j0 + tj;
+    if (i >= H || j >= W) continue;
+    float acc = 0.0f;
+    for (int a = 0; a < K0; ++a) {
+      // tile row of input index (convolution) i + s0 - a, (correlation) i - s0 + a
+      const int tr = flip ? ti + a : ti + K0 - 1 - a;
+      const float* row = tile + tr * TW;
+      const float* krow = ks + a * K1;
+      for (int bb = 0; bb < K1; ++bb) {
+        const int tc = flip ? tj + bb : tj + K1 - 1 - bb;
+        acc = fmaf(row[tc], krow[bb], acc);
+      }
+    }
+    out[(long long)b * H * W + (long long)i * W + j] = acc;
+  }
+}
+
+// g_k[a][b] = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - b] over every batch
+// element; one block per kernel element, float-pair accumulation per thread.
+__global__ void conv2d_kgrad_kernel(const float* __restrict__ in, const float* __restrict__ g,
+                                    int H, int W, int batch, int K0, int K1,
+                                    float* __restrict__ g_k) {
+  __shared__ double smem[32];
+  const int a = blockIdx.x / K1, bb = blockIdx.x % K1;
+  const int s0 = (K0 - 1) / 2, s1 = (K1 - 1) / 2;
+  float hi = 0.f, lo = 0.f;
+  const long long npix = (long long)H * W;
+  for (int b = 0; b < batch; ++b) {
+    const float* inb = in + b * npix;
+    const float* gb = g + b * npix;
+    for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
+      const int i = (int)(p / W), j = (int)(p % W);
+      const int r = i + s0 - a, c = j + s1 - bb;
+      if (r < 0 || r >= H || c < 0 || c >= W) continue;
+      const float x = gb[p], y = inb[(long long)r * W + c];
+      const float pr = x * y;
+      const float pe = fmaf(x, y, -pr);
+      const float t = hi + pr;
+      const float bv = t - hi;
+      lo += ((hi - (t - bv)) + (pr - bv)) + pe;
+      hi = t;
+    }
+  }
+  double v = (double)hi + (double)lo;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += smem[w];
+    g_k[blockIdx.x] = (float)t;
+  }
+}
+
+int check_conv(int batch, int H, int W, int K0, int K1) {
+  if (batch <= 0 || H <= 0 || W <= 0 || K0 <= 0 || K1 <= 0)
+    return fail(DLX_ERR_SHAPE, "conv2d: sizes must be positive");
+  if (K0 > 128 || K1 > 128)
+    return fail(DLX_ERR_SHAPE, "conv2d: kernels up to 128 x 128 are supported");
+  return DLX_OK;
+}
+
+int launch_conv(const float* in, int batch, int H, int W, const float* k, int K0, int K1, int flip,
+                float* out, cudaStream_t s) {
+  const size_t smem = sizeof(float) * ((size_t)(CT + K0 - 1) * (CT + K1 - 1) + (size_t)K0 * K1);
+  if (smem > 48 * 1024)
+    DLX_TRY_CUDA(cudaFuncSetAttribute(conv2d_same_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((W + CT - 1) / CT, (H + CT - 1) / CT, batch);
+  conv2d_same_kernel<<<grid, 256, smem, s>>>(in, H, W, k, K0, K1, flip, out);
+  DLX_LAUNCH_CHECK("conv2d_same_kernel");
+  return DLX_OK;
+}
+
+}  // namespace
+}  // namespace dlx
+
+using namespace dlx;
+
+extern "C" {
+
+int dlx_conv2d_same(const float* in, int batch, int height, int width, const float* kernel,
+                    int k0, int k1, float* out, void* stream) {
+  DLX_TRY(check_conv(batch, height, width, k0, k1));
+  if (!in || !kernel || !out) return fail(DLX_ERR_ARG, "conv2d: null pointer");
+  return launch_conv(in, batch, height, width, kernel, k0, k1, 0, out,
+                     static_cast<cudaStream_t>(stream));
+}
+
+int dlx_conv2d_same_backward(const float* in, int batch, int height, int width,
+                             const float* kernel, int k0, int k1, const float* g_out,
+                             float* g_in, float* g_kernel, void* stream) {
+  DLX_TRY(check_conv(batch, height, width, k0, k1));
+  if (!g_out || (g_in && !kernel) || (g_kernel && !in))
+    return fail(DLX_ERR_ARG, "conv2d_backward: null pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (g_in) DLX_TRY(launch_conv(g_out, batch, height, width, kernel, k0, k1, 1, g_in, s));
+  if (g_kernel) {
+    conv2d_kgrad_kernel<<<k0 * k1, 256, 0, s>>>(in, g_out, height, width, batch, k0, k1,
+                                                g_kernel);
+    DLX_LAUNCH_CHECK("conv2d_kgrad_kernel");
+  }
+  return DLX_OK;
+}
+
+}  // extern "C"

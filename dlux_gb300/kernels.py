@@ -452,6 +452,30 @@ def aberrated_aperture_grad(desc, noll, g_opd):
     return g
 
 
+def conv2d_same(x, kernel):
+    """[..., H, W] images convolved with a [K0, K1] kernel, mode "same"."""
+    x = _contig(x)
+    k = _contig(kernel.to(device=x.device, dtype=torch.float32))
+    H, W = x.shape[-2:]
+    B = x.numel() // (H * W)
+    out = torch.empty_like(x)
+    call("dlx_conv2d_same", ptr(x), B, H, W, ptr(k), k.shape[0], k.shape[1], ptr(out), _stream())
+    return out
+
+
+def conv2d_same_backward(x, kernel, g, want_x=True, want_k=True):
+    x = _contig(x)
+    k = _contig(kernel.to(device=x.device, dtype=torch.float32))
+    g = _contig(g)
+    H, W = x.shape[-2:]
+    B = x.numel() // (H * W)
+    gx = torch.empty_like(x) if want_x else None
+    gk = torch.empty_like(k) if want_k else None
+    call("dlx_conv2d_same_backward", ptr(x), B, H, W, ptr(k), k.shape[0], k.shape[1], ptr(g),
+         ptr(gx), ptr(gk), _stream())
+    return gx, gk
+
+
 mft_plans = _PlanCache(16)
 fft_plans = _PlanCache(8)
 poly_plans = _PlanCache(8)

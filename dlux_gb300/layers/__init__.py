@@ -5,5 +5,5 @@ from .optical_layers import (BaseLayer, OpticalLayer, TransmissiveLayer,  # noqa
 from .optics import Optic, BasisOptic  # noqa: F401
 from .propagators import MFT, FFT  # noqa: F401
 from .detector_layers import (DetectorLayer, ApplyPixelResponse, Downsample,  # noqa: F401
-                              AddConstant, ApplySaturation)
+                              AddConstant, ApplySaturation, ApplyJitter)
 from .apertures import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401

@@ -7,7 +7,7 @@ import torch
 from .optical_layers import BaseLayer, as_array
 
 __all__ = ["DetectorLayer", "ApplyPixelResponse", "Downsample", "AddConstant",
-           "ApplySaturation"]
+           "ApplySaturation", "ApplyJitter"]
 
 
 class DetectorLayer(BaseLayer):
@@ -46,6 +46,40 @@ class AddConstant(DetectorLayer):
 
     def __call__(self, psf):
         return psf + self.value
+
+
+def gaussian_kernel(std, npixels, extent=5.0):
+    """Normalised separable Gaussian on linspace(-extent, extent, npixels) per axis
+    (utils/math.py:20-69), as a differentiable torch tensor."""
+    std = std if isinstance(std, torch.Tensor) else torch.as_tensor(float(std),
+                                                                   dtype=torch.float64)
+    x = torch.linspace(-extent, extent, int(npixels), dtype=torch.float64, device=std.device)
+    g = torch.exp(-0.5 * (x / std) ** 2) / (std * (2 * torch.pi) ** 0.5)
+    k = g[None, :] * g[:, None]
+    return k / k.sum()
+
+
+class ApplyJitter(DetectorLayer):
+    """Convolution with a Gaussian of standard deviation ``sigma`` (layers/detector_layers.py:
+    134-199): the kernel is built on kernel_size * oversample points and summed down by
+    ``oversample``; the convolution runs on the device."""
+
+    def __init__(self, sigma, kernel_size=9, oversample=3):
+        self.kernel_size = int(kernel_size)
+        if self.kernel_size <= 0:
+            raise ValueError("kernel_size must be greater than 0.")
+        self.sigma = sigma if isinstance(sigma, torch.Tensor) else torch.as_tensor(
+            float(sigma), dtype=torch.float64)
+        self.oversample = int(oversample)
+
+    @property
+    def kernel(self):
+        k = gaussian_kernel(self.sigma, self.kernel_size * self.oversample)
+        n, o = self.kernel_size, self.oversample
+        return k.reshape(n, o, n, o).sum(dim=(1, 3)).to(torch.float32)
+
+    def __call__(self, psf):
+        return psf.convolve(self.kernel)
 
 
 class ApplySaturation(DetectorLayer):

@@ -33,6 +33,12 @@ class PSF(Base):
         return self.set(data=autograd.downsample(self.data, n, mean=False),
                         pixel_scale=self.pixel_scale * n)
 
+    def convolve(self, other, method="auto"):
+        """Convolution with ``other``, mode "same" (psfs.py:93-110), on the device."""
+        if method not in ("auto", "direct", "fft"):
+            raise ValueError("method must be 'auto', 'direct' or 'fft'.")
+        return self.set(data=autograd.conv2d_same(self.data, other))
+
     def resize(self, npixels):
         return self.set(data=array_ops.resize(self.data, npixels))
 

@@ -8,7 +8,8 @@ from . import spectra
 from .base import Base
 from .psfs import PSF
 
-__all__ = ["BaseSource", "Source", "PointSource", "PointSources"]
+__all__ = ["BaseSource", "Source", "PointSource", "PointSources", "ResolvedSource",
+           "PointResolvedSource"]
 
 
 def _validate_return_mode(return_wf, return_psf):
@@ -138,3 +139,69 @@ class PointSources(Source):
                                      npix, ps, None, None, max_objects=min(n_src, 32))
         return autograd.poly_sources(plan, amp, opd, phase, weights.to(torch.float32),
                                      src.position, flag, tilt)
+
+
+_CONV_ERR = ("Wavefront information cannot be preserved through convolution. Convolution can "
+             "only operate on PSFs (incoherent light). Please use return_wf=False to get the "
+             "PSF array or return_psf=True to get a PSF object.")
+
+
+class ResolvedSource(PointSource):
+    """A point-source PSF convolved with a normalised 2-d ``distribution``
+    (sources.py:414-521); the convolution runs on the device."""
+
+    def __init__(self, wavelengths=None, position=(0.0, 0.0), flux=1.0, distribution=None,
+                 weights=None, spectrum=None):
+        super().__init__(wavelengths, position, flux, weights, spectrum)
+        if distribution is None:
+            distribution = torch.ones((3, 3), dtype=torch.float32)
+        d = distribution if isinstance(distribution, torch.Tensor) else torch.as_tensor(
+            distribution, dtype=torch.float32)
+        if d.dim() != 2:
+            raise ValueError("distribution must be a 2d array.")
+        self.distribution = (d / d.sum()).to(_dev())
+
+    def normalise(self):
+        floor = torch.clamp(self.distribution, min=0.0)
+        return self.set(["spectrum", "distribution"],
+                        [self.spectrum.normalise(), floor / floor.sum()])
+
+    def model(self, optics, return_wf=False, return_psf=False):
+        from . import autograd
+        _validate_return_mode(return_wf, return_psf)
+        if return_wf:
+            raise NotImplementedError(_CONV_ERR)
+        src = self.normalise()
+        weights = src.spectrum.weights * src.flux.to(src.spectrum.weights.device)
+        psf = optics.propagate(src.spectrum.wavelengths, src.position, weights, return_psf=True)
+        conv = autograd.conv2d_same(psf.data, src.distribution)
+        return PSF(conv, psf.pixel_scale) if return_psf else conv
+
+
+class PointResolvedSource(ResolvedSource):
+    """A point source plus a resolved distribution sharing one position, with the flux
+    split by ``contrast`` (sources.py:638-748, utils/source.py:8-26)."""
+
+    def __init__(self, wavelengths=None, position=(0.0, 0.0), flux=1.0, distribution=None,
+                 contrast=1.0, spectrum=None, weights=None):
+        super().__init__(wavelengths, position, flux, distribution, weights, spectrum)
+        self.contrast = contrast if isinstance(contrast, torch.Tensor) else torch.as_tensor(
+            float(contrast), dtype=torch.float32, device=_dev())
+
+    def model(self, optics, return_wf=False, return_psf=False):
+        from . import autograd
+        _validate_return_mode(return_wf, return_psf)
+        if return_wf:
+            raise NotImplementedError(_CONV_ERR)
+        src = self.normalise()
+        w = src.spectrum.weights
+        c = src.contrast.to(w.device)
+        flux = src.flux.to(w.device)
+        # fluxes_from_contrast: 2 (contrast * mean, mean) / (1 + contrast)
+        f_point = 2 * c * flux / (1 + c)
+        f_resolved = 2 * flux / (1 + c)
+        point = optics.propagate(src.spectrum.wavelengths, src.position, w * f_point,
+                                 return_psf=True)
+        resolved = optics.propagate(src.spectrum.wavelengths, src.position, w * f_resolved)
+        out = point.data + autograd.conv2d_same(resolved, src.distribution)
+        return PSF(out, point.pixel_scale) if return_psf else out

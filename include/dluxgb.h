@@ -321,6 +321,21 @@ int dlx_aberrated_aperture(const dlx_aperture_desc* desc, const int* noll_host, 
 int dlx_aberrated_aperture_grad(const dlx_aperture_desc* desc, const int* noll_host, int n_terms,
                                 const float* g_opd, float* g_coeffs, void* stream);
 
+/* ---- PSF convolution, mode "same" ---------------------------------------
+ * Replaces jax.scipy.signal.convolve(psf, kernel, mode="same") of
+ * PSF.convolve (psfs.py:93-110), ResolvedSource / PointResolvedSource
+ * (sources.py:490-521, 711-748) and ApplyJitter
+ * (layers/detector_layers.py:134-199): out[i][j] = sum_{a,b}
+ * in[i + (K0-1)/2 - a][j + (K1-1)/2 - b] kernel[a][b], zero outside `in`, for a
+ * batch of [H][W] images and one [K0][K1] kernel (sides <= 128). The backward
+ * gives d/d in and d/d kernel (summed over the batch); either may be NULL.
+ */
+int dlx_conv2d_same(const float* in, int batch, int height, int width, const float* kernel,
+                    int k0, int k1, float* out, void* stream);
+int dlx_conv2d_same_backward(const float* in, int batch, int height, int width,
+                             const float* kernel, int k0, int k1, const float* g_out,
+                             float* g_in, float* g_kernel, void* stream);
+
 /* ---- a20/a21: many point sources through one pupil ---------------------
  * Replaces PointSources.model (sources.py:392-411) for a pupil that does not
  * need gradients: image [M][M] = sum_s sum_l weights[s][l] PSF_l(position_s),

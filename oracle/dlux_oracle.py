@@ -484,6 +484,34 @@ def aberrated_circular_aperture(npixels, diameter, radius, noll, coefficients,
     return trans, opd, basis
 
 
+def convolve_same(array, kernel):
+    """jax.scipy.signal.convolve(array, kernel, mode="same") (psfs.py:93-110; sources.py:516,
+    :745): the full 2-d convolution, cropped at offset (K - 1) // 2 per axis."""
+    a = np.asarray(array, np.float64)
+    k = np.asarray(kernel, np.float64)
+    H, W = a.shape
+    K0, K1 = k.shape
+    full = np.zeros((H + K0 - 1, W + K1 - 1))
+    for i in range(K0):
+        for j in range(K1):
+            full[i:i + H, j:j + W] += k[i, j] * a
+    s0, s1 = (K0 - 1) // 2, (K1 - 1) // 2
+    return full[s0:s0 + H, s1:s1 + W]
+
+
+def gaussian_kernel(std, npixels, extent=5.0):
+    """Normalised separable normal pdf on linspace(-extent, extent, n) (utils/math.py:20-69)."""
+    x = np.linspace(-extent, extent, npixels)
+    g = np.exp(-0.5 * (x / std) ** 2) / (std * math.sqrt(2 * math.pi))
+    k = g[None, :] * g[:, None]
+    return k / k.sum()
+
+
+def jitter_kernel(sigma, kernel_size=9, oversample=3):
+    """ApplyJitter.kernel (layers/detector_layers.py:181-196): summed down by oversample."""
+    return downsample(gaussian_kernel(sigma, kernel_size * oversample), oversample, mean=False)
+
+
 def circular_aperture(npixels, diameter, oversample=5, secondary_diameter=None,
                       spider_width=None, spider_angles=None, zernike_nolls=None,
                       zernike_oversize=0.01):
