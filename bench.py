@@ -502,7 +502,7 @@ def cfg_workload(name, variant):
         T, B = dlu.circular_aperture(1024, 1.0, oversample=1, secondary_diameter=0.1,
                                      zernike_nolls=list(range(4, 25)))
         c0 = torch.as_tensor(rng.normal(0, 30e-9, 21), **f32)
-        S = 1024
+        S = int(getattr(cfg_workload, "sources", 1024))
         pos0 = torch.as_tensor(rng.uniform(-2, 2, (S, 2)) * np.pi / 180 / 3600,
                                dtype=torch.float64)
         flux0 = torch.as_tensor(10 ** rng.uniform(2, 6, S), **f32)
@@ -519,8 +519,8 @@ def cfg_workload(name, variant):
             loss.backward()
             return loss
         flops = 3 * S * 16 * 8 * (128 * 1024 ** 2 + 128 ** 2 * 1024)
-        return run, "scene (1024 sources) loss+grad evals/sec", "evals/s", flops, \
-            "1024 point sources, 1024^2 pupil, 16 lambda, 128^2 image"
+        return run, f"scene ({S} sources) loss+grad evals/sec", "evals/s", flops, \
+            f"{S} point sources, 1024^2 pupil, 16 lambda, 128^2 image"
     raise ValueError(name)
 
 
@@ -683,6 +683,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
     ap.add_argument("--slots", type=int, default=4, help="serving: concurrent stream slots")
     ap.add_argument("--fft-n", type=int, default=1024, help="fft: pupil side (pad 2)")
+    ap.add_argument("--scene-sources", type=int, default=1024,
+                    help="cfg4: point sources (1024 is the measured configuration)")
     ap.add_argument("--graph-after", type=int, default=8,
                     help="serving: capture a batch shape as a CUDA graph after this many uses")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
@@ -703,6 +705,7 @@ def main():
     if args.workload == "serving":
         return run_serving(args) if rank == 0 else 0
     if args.workload in ("cfg1", "cfg3", "cfg4"):
+        cfg_workload.sources = args.scene_sources
         return run_config(args) if rank == 0 else 0
     if args.workload == "fft":
         return run_fft(args) if rank == 0 else 0
