@@ -20,6 +20,11 @@ __device__ __forceinline__ void store_split(__nv_bfloat16* base_b, long long pla
   base_b[3 * plane + idx] = l;
 }
 
+// (t.x + i t.y)(x + i y): the per-column phasor of EpiArgs::coltilt.
+__device__ __forceinline__ float2 ctilt(float2 t, float x, float y) {
+  return make_float2(t.x * x - t.y * y, t.x * y + t.y * x);
+}
+
 // Wavelength and object of batch element b (b = l * R + r for a batched plan
 // of R objects; R = 1 otherwise).
 __device__ __forceinline__ int epi_objects(const EpiArgs& e) { return e.objs.n > 0 ? e.objs.n : 1; }
@@ -97,6 +102,9 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
   const float a = e.alpha ? e.alpha[l] : 1.0f;
   const long long plane = (long long)M * N;
   const long long idx = (long long)m * N + n;
+  if (e.coltilt && (e.kind == EPI_C64 || e.kind == EPI_SPLIT || e.kind == EPI_SPLIT2)) {
+    v = ctilt(e.coltilt[(long long)b * N + n], v.x, v.y);
+  }
   switch (e.kind) {
     case EPI_C64: {
       e.out_c64[(long long)b * plane + idx] = make_float2(a * v.x, a * v.y);
@@ -167,18 +175,25 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
   const int mc = M - m0 < 32 ? M - m0 : 32;
   const long long idx0 = (long long)m0 * N + n;
   switch (KIND >= 0 ? KIND : e.kind) {
-    case EPI_C64: {
-      float2* o = e.out_c64 + (long long)b * plane + idx0;
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < mc) o[(long long)j * N] = make_float2(a * re[j], a * im[j]);
-      break;
-    }
+    case EPI_C64:
     case EPI_SPLIT: {
-      __nv_bfloat16* o = e.out_split + (long long)b * 4 * plane + idx0;
+      // (a, 0) without a tilt: a re - 0 im and a im + 0 re are exactly a re, a im
+      float2 t = make_float2(a, 0.f);
+      if (e.coltilt) {
+        const float2 c = e.coltilt[(long long)b * N + n];
+        t = make_float2(a * c.x, a * c.y);
+      }
+      if ((KIND >= 0 ? KIND : e.kind) == EPI_C64) {
+        float2* o = e.out_c64 + (long long)b * plane + idx0;
 #pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < mc) store_split(o, plane, (long long)j * N, make_float2(a * re[j], a * im[j]));
+        for (int j = 0; j < 32; ++j)
+          if (j < mc) o[(long long)j * N] = ctilt(t, re[j], im[j]);
+      } else {
+        __nv_bfloat16* o = e.out_split + (long long)b * 4 * plane + idx0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (j < mc) store_split(o, plane, (long long)j * N, ctilt(t, re[j], im[j]));
+      }
       break;
     }
     case EPI_INTENSITY: {
@@ -220,10 +235,11 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
     }
     case EPI_SPLIT2: {
       const float w = e.colw[n];
+      const float2 t = e.coltilt ? e.coltilt[(long long)b * N + n] : make_float2(1.f, 0.f);
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         if (j < mc) {
-          const float2 av = make_float2(a * re[j], a * im[j]);
+          const float2 av = ctilt(t, a * re[j], a * im[j]);
           const long long o = idx0 + (long long)j * N;
           if (e.out_split) {
             store_split(e.out_split + (long long)b * 4 * plane, plane, o, av);

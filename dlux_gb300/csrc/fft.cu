@@ -16,7 +16,8 @@
 //   adjoint   rows:    P lines of P -> N   (x, conjugate), into tmp [P][N]
 //             columns: N lines of P -> N   (y, conjugate), into gin [N][N]
 // Ramps exp(2 pi i (g j + d)) are reduced exactly in FP32 pairs (cis_ff), and
-// the twiddles exp(2 pi i s k / P) come from sincospif of an exact argument.
+// the twiddles exp(2 pi i s k / P) come from sincospif of an exact argument,
+// one table per plan with every stage's twiddles contiguous.
 #include <atomic>
 #include <cmath>
 #include <string>
@@ -40,22 +41,38 @@ struct LineIO {
   long long bs, ls, es;
 };
 
+// Shared-memory slot of element k of line li (P elements per line). The low
+// four index bits are XORed with four high bits and with a per-line pattern,
+// so that one wavefront of 16 threads (8-byte words) lands in 16 distinct bank
+// pairs for the bit-reversed scatter (consecutive slots -> k differing in the
+// high bits), for the butterflies (consecutive k) and for the gathers, also
+// when a wavefront spans several lines (the column passes):
+//   2 lines x 8 elements:  pattern 9 flips bits 0 and 3 of the second line;
+//   4 lines x 4 elements:  pattern 5 li gives distinct low and high bit pairs.
+// Every map is a bijection on [0, P) (only the low nibble changes, by a value
+// that depends on the other bits); for P < 16 it is the identity.
+template <int LPB>
+__device__ __forceinline__ int smem_slot(int li, int k, int sh, int P) {
+  const int g = P < 16 ? 0 : (LPB == 2 ? 9 * li : (LPB == 4 ? 5 * li : li)) & 15;
+  return li * P + (k ^ (((k >> sh) & 15) ^ g));
+}
+
 template <int LPB>
 __global__ void __launch_bounds__(256) fft_lines_kernel(
     const float2* __restrict__ in, LineIO io_in, int n_in, int off_in,
     float2* __restrict__ out, LineIO io_out, int n_out, int off_out, int lines, int log2p,
-    float sign, const LineRamp* __restrict__ ramps) {
+    float sign, const LineRamp* __restrict__ ramps, const float2* __restrict__ twg) {
   extern __shared__ float2 sm[];
   const int P = 1 << log2p;
-  float2* tw = sm;             // [P/2] twiddles
-  float2* x = sm + P / 2;      // [LPB][P]
+  const int sh = log2p - 4 > 4 ? log2p - 4 : 4;  // >= 4: the XOR never reads the low nibble
+  float2* tw = sm;             // [P - 1]: stage of half-length h at [h - 1, 2h - 1)
+  float2* x = sm + (P - 1);    // [LPB][P], slots by smem_slot
   const int b = blockIdx.y;
   const int l0 = blockIdx.x * LPB;
   const LineRamp rp = ramps[b];
-  for (int k = threadIdx.x; k < P / 2; k += blockDim.x) {
-    float s, c;
-    sincospif(2.0f * (float)k / (float)P, &s, &c);
-    tw[k] = make_float2(c, sign * s);
+  for (int k = threadIdx.x; k < P - 1; k += blockDim.x) {
+    const float2 w = twg[k];
+    tw[k] = make_float2(w.x, sign * w.y);
   }
   for (int i = threadIdx.x; i < LPB * P; i += blockDim.x) x[i] = make_float2(0.f, 0.f);
   __syncthreads();
@@ -70,26 +87,27 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
     float2 v = in[(long long)b * io_in.bs + (long long)l * io_in.ls + (long long)e * io_in.es];
     if (rp.ramp_in)
       v = cmul(v, cis_ff(FF{(float)e, 0.f}, FF{rp.g_in.x, rp.g_in.y}, FF{rp.d_in.x, rp.d_in.y}));
-    int slot = (e + off_in) % P;
-    if (slot < 0) slot += P;
-    x[li * P + (int)(__brev((unsigned)slot) >> (32 - log2p))] = v;
+    const int slot = (e + off_in) & (P - 1);  // P is a power of two: also for e + off_in < 0
+    const int k = log2p > 0 ? (int)(__brev((unsigned)slot) >> (32 - log2p)) : 0;
+    x[smem_slot<LPB>(li, k, sh, P)] = v;
   }
   __syncthreads();
+  const int hp = log2p - 1;  // P / 2 = 1 << hp butterflies per line
   for (int s = 1; s <= log2p; ++s) {
     const int half = 1 << (s - 1);
-    const int tstep = P >> s;
     for (int t = threadIdx.x; t < LPB * (P / 2); t += blockDim.x) {
-      const int li = t / (P / 2);
-      const int i = t - li * (P / 2);
+      const int li = t >> hp;
+      const int i = t & ((P / 2) - 1);
       const int grp = i >> (s - 1);
       const int pos = i & (half - 1);
-      const int k0 = li * P + (grp << s) + pos;
-      const int k1 = k0 + half;
-      const float2 w = tw[pos * tstep];
-      const float2 u = x[k0];
-      const float2 v = cmul(x[k1], w);
-      x[k0] = make_float2(u.x + v.x, u.y + v.y);
-      x[k1] = make_float2(u.x - v.x, u.y - v.y);
+      const int k0 = (grp << s) + pos;
+      const int i0 = smem_slot<LPB>(li, k0, sh, P);
+      const int i1 = smem_slot<LPB>(li, k0 + half, sh, P);
+      const float2 w = tw[half - 1 + pos];
+      const float2 u = x[i0];
+      const float2 v = cmul(x[i1], w);
+      x[i0] = make_float2(u.x + v.x, u.y + v.y);
+      x[i1] = make_float2(u.x - v.x, u.y - v.y);
     }
     __syncthreads();
   }
@@ -99,9 +117,8 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
     const int o = oline_fast ? t / LPB : t % n_out;
     const int l = l0 + li;
     if (l >= lines) continue;
-    int slot = (o + off_out) % P;
-    if (slot < 0) slot += P;
-    float2 v = x[li * P + slot];
+    const int slot = (o + off_out) & (P - 1);
+    float2 v = x[smem_slot<LPB>(li, slot, sh, P)];
     if (rp.ramp_out)
       v = cmul(v, cis_ff(FF{(float)o, 0.f}, FF{rp.g_out.x, rp.g_out.y},
                          FF{rp.d_out.x, rp.d_out.y}));
@@ -111,19 +128,32 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
   }
 }
 
+// Twiddles of every butterfly stage, stage by stage: entry h - 1 + pos of the
+// stage with half-length h is exp(i pi pos / h) (the direction's sign is
+// applied when a block copies the table). pos / h is exact in FP32.
+__global__ void fft_twiddle_kernel(int P, float2* __restrict__ tw) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P - 1) return;
+  const int h = 1 << (31 - __clz(k + 1));  // largest power of two <= k + 1
+  const int pos = k + 1 - h;
+  float sn, cs;
+  sincospif((float)pos / (float)h, &sn, &cs);
+  tw[k] = make_float2(cs, sn);
+}
+
 // Few lines per block keeps several blocks resident per SM (the butterfly
 // stages are latency-bound); two lines keep column loads at 16-byte segments.
 int lines_per_block(int P) { return P <= 1024 ? 4 : 2; }
 
 int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* out, LineIO io_out,
                  int n_out, int off_out, int lines, int batch, int log2p, float sign,
-                 const LineRamp* ramps, cudaStream_t s) {
+                 const LineRamp* ramps, const float2* tw, cudaStream_t s) {
   const int P = 1 << log2p;
   const int lpb = lines_per_block(P);
-  const size_t smem = sizeof(float2) * ((size_t)P / 2 + (size_t)lpb * P);
+  const size_t smem = sizeof(float2) * ((size_t)P - 1 + (size_t)lpb * P);
   static std::atomic<bool> attr_done{false};  // host side, once per process
   if (!attr_done.load()) {
-    const int lim = 160 * 1024;  // covers P <= 8192 at every lines-per-block choice
+    const int lim = 200 * 1024;  // covers P <= 8192 at the lines-per-block choice above
     DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<8>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4>,
@@ -136,15 +166,15 @@ int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* o
   switch (lpb) {
     case 8:
       fft_lines_kernel<8><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps);
+                                                  off_out, lines, log2p, sign, ramps, tw);
       break;
     case 4:
       fft_lines_kernel<4><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps);
+                                                  off_out, lines, log2p, sign, ramps, tw);
       break;
     default:
       fft_lines_kernel<2><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps);
+                                                  off_out, lines, log2p, sign, ramps, tw);
       break;
   }
   DLX_LAUNCH_CHECK("fft_lines_kernel");
@@ -209,6 +239,13 @@ int radix_fft_create(RadixFft* f, int batch, int N, int pad, bool inverse, const
     cudaGetLastError();
     return fail(DLX_ERR_NOMEM, "radix FFT: workspace allocation failed");
   }
+  if (f->P > 1) {
+    DLX_TRY_CUDA(cudaMalloc(&f->tw, sizeof(float2) * (size_t)(f->P - 1)));
+    fft_twiddle_kernel<<<(f->P - 1 + 255) / 256, 256>>>(f->P, f->tw);
+    DLX_LAUNCH_CHECK("fft_twiddle_kernel");
+    // the table is read from the caller's streams, which need not wait for this one
+    DLX_TRY_CUDA(cudaDeviceSynchronize());
+  }
   return DLX_OK;
 }
 
@@ -216,8 +253,10 @@ void radix_fft_release(RadixFft* f) {
   for (LineRamp* r : {f->ramps_x, f->ramps_y, f->ramps_ax, f->ramps_ay})
     if (r) cudaFree(r);
   if (f->tmp) cudaFree(f->tmp);
+  if (f->tw) cudaFree(f->tw);
   f->ramps_x = f->ramps_y = f->ramps_ax = f->ramps_ay = nullptr;
   f->tmp = nullptr;
+  f->tw = nullptr;
 }
 
 // out [b][P][P] = FFT of in [b][N][N] (the forward of the DFT-GEMM FFT plan).
@@ -226,11 +265,11 @@ int radix_fft_forward(const RadixFft& f, const float2* in, float2* out, cudaStre
   // rows: line y of N elements (x), output row of P into tmp[b][y][:]
   DLX_TRY(launch_lines(in, LineIO{(long long)N * N, N, 1}, N, off_in, f.tmp,
                        LineIO{(long long)N * P, P, 1}, P, off_out, N, f.batch, f.log2p, f.sign,
-                       f.ramps_x, s));
+                       f.ramps_x, f.tw, s));
   // columns: line kx of N elements (y, stride P), output column of P into out
   return launch_lines(f.tmp, LineIO{(long long)N * P, 1, P}, N, off_in, out,
                       LineIO{(long long)P * P, 1, P}, P, off_out, P, f.batch, f.log2p, f.sign,
-                      f.ramps_y, s);
+                      f.ramps_y, f.tw, s);
 }
 
 // gin [b][N][N] = adjoint applied to gout [b][P][P].
@@ -241,11 +280,11 @@ int radix_fft_adjoint(const RadixFft& f, const float2* gout, float2* gin, cudaSt
   // rows: line ky of P elements (kx), output N elements (x) into tmp[b][ky][:]
   DLX_TRY(launch_lines(gout, LineIO{(long long)P * P, P, 1}, P, -f.c, f.tmp,
                        LineIO{(long long)P * N, N, 1}, N, f.npad - f.c, P, f.batch, f.log2p,
-                       -f.sign, f.ramps_ax, s));
+                       -f.sign, f.ramps_ax, f.tw, s));
   // columns: line x of P elements (ky, stride N), output N elements (y) into gin
   return launch_lines(f.tmp, LineIO{(long long)P * N, 1, N}, P, -f.c, gin,
                       LineIO{(long long)N * N, 1, N}, N, f.npad - f.c, N, f.batch, f.log2p,
-                      -f.sign, f.ramps_ay, s);
+                      -f.sign, f.ramps_ay, f.tw, s);
 }
 
 }  // namespace dlx

@@ -159,6 +159,7 @@ struct RadixFft {
   LineRamp* ramps_ax = nullptr;
   LineRamp* ramps_ay = nullptr;
   float2* tmp = nullptr;        // device [batch][N][P]
+  float2* tw = nullptr;         // device [P - 1]: butterfly twiddles, stage by stage
 };
 int radix_fft_create(RadixFft* f, int batch, int N, int pad, bool inverse, const DftAxis* axes,
                      const float* alphas);
@@ -206,6 +207,8 @@ struct EpiArgs {
   const __nv_bfloat16* in_split;  // EPI_DOT: F-bar [b][4][m][n] (tensor-core form)
   const float2* in_c64;      // EPI_DOT: F-bar [b][m][n] (FP32 form)
   const float* kf;           // EPI_DOT: [wavelength] 2 pi / lambda
+  const float2* coltilt;     // nullable [b][n]: phasor multiplying column n of the
+                             // EPI_C64 / EPI_SPLIT / EPI_SPLIT2 outputs of batch element b
 };
 
 struct GemmArgs {

@@ -9,12 +9,18 @@
 // i.e. the untilted matrix with its output coordinates shifted. So
 //   * the pupil field E_l is built once per wavelength and shared by every
 //     source (B operand with batch divisor R);
-//   * each (source, wavelength) gets its own M x N matrices A'x, A'y, made
-//     by an error-free FP32 kernel (M x N elements instead of an N x N
-//     field per source: 8x less at N = 1024, M = 128);
+//   * the shift factors: A'[b][u][x] = A0[l][u][x] t_b[x] with the untilted
+//     matrix A0 (made once per plan by an error-free FP32 kernel) and the
+//     tilt phasor t_b[x] = exp(2 pi i x theta N dx / lambda);
+//   * each (source, wavelength) gets its own M x N matrix A'x (M x N elements
+//     instead of an N x N field per source: 8x less at N = 1024, M = 128),
+//     written by a store-bound pass A0 * tx;
+//   * the y tilt multiplies column y of the first GEMM's output D1 in its
+//     epilogue, so the second GEMM reads the shared A0 of the wavelength
+//     (F = alpha A0 (ty.D1)^T), which stays in L2;
 //   * position gradients come from dF/dtx = i k alpha A'y (A'x (X.E))^T and
-//     dF/dty = i k alpha A'y (Y.D1)^T dotted with F-bar, with no per-source
-//     pupil-plane reverse pass.
+//     dF/dty = i k alpha A'y (Y.D1)^T dotted with F-bar (again with A'y D =
+//     A0 (ty.D)), with no per-source pupil-plane reverse pass.
 // image = sum_{s,l} w[s][l] |F_{s,l}|^2 for per-(source, wavelength) weights
 // w (spectrum x flux). The reverse pass returns d/dw and d/d(position).
 #include <algorithm>
@@ -35,52 +41,105 @@ __global__ void scene_xtable_kernel(int n, double a, double b, float2* out) {
   out[i] = make_float2(f.hi, f.lo);
 }
 
-// Output coordinates of every (wavelength l, source r) batch element b = l R + r:
-// u[b][j] = a_out[l] j + b_out[l] - theta_r * inv_fringe[l] for each axis, as float pairs.
-__global__ void scene_utable_kernel(int M, int R, int L, const double* __restrict__ a_out,
-                                    const double* __restrict__ b_out,
-                                    const double* __restrict__ inv_fringe,
-                                    const double* __restrict__ pos, float2* __restrict__ ux,
-                                    float2* __restrict__ uy) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int b = blockIdx.y;
-  if (j >= M || b >= R * L) return;
-  const int l = b / R, r = b - (b / R) * R;
-  const double base = a_out[l] * (double)j + b_out[l];
-  const FF fx = ff_from_double(base - pos[2 * r] * inv_fringe[l]);
-  const FF fy = ff_from_double(base - pos[2 * r + 1] * inv_fringe[l]);
-  ux[(long long)b * M + j] = make_float2(fx.hi, fx.lo);
-  uy[(long long)b * M + j] = make_float2(fy.hi, fy.lo);
-}
-
-// A'[b][j][i] = exp(-2 pi i x_i u_bj) for both axes (blockIdx.z = 2 b + axis),
-// reduced exactly in FP32 pairs (cis_ff). Written as split planes or complex64.
-__global__ void scene_dft_kernel(int M, int N, int B, const float2* __restrict__ xin,
-                                 const float2* __restrict__ ux, const float2* __restrict__ uy,
-                                 __nv_bfloat16* __restrict__ ax_s, __nv_bfloat16* __restrict__ ay_s,
-                                 float2* __restrict__ ax_c, float2* __restrict__ ay_c) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int b = blockIdx.z >> 1, axis = blockIdx.z & 1;
-  if (i >= N || j >= M || b >= B) return;
+// A0[l][j][i] = exp(-2 pi i x_i u_lj), u_lj = a_out[l] j + b_out[l]: the untilted
+// DFT matrix of every wavelength (the same for both axes), reduced exactly in
+// FP32 pairs (cis_ff). Written as c64 and, for the tensor-core form, as split
+// planes [l][4][j][i].
+__global__ void scene_a0_kernel(int M, int N, const float2* __restrict__ xin,
+                                const double* __restrict__ a_out,
+                                const double* __restrict__ b_out, float2* __restrict__ a0,
+                                __nv_bfloat16* __restrict__ a0s) {
+  const long long mn = (long long)M * N;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int l = blockIdx.y;
+  if (p >= mn) return;
+  const int j = (int)(p / N);
+  const int i = (int)(p - (long long)j * N);
   const float2 x = xin[i];
-  const float2 u = (axis ? uy : ux)[(long long)b * M + j];
-  const float2 c = cis_ff(FF{x.x, x.y}, FF{u.x, u.y}, FF{0.f, 0.f});
+  const FF u = ff_from_double(a_out[l] * (double)j + b_out[l]);
+  const float2 c = cis_ff(FF{x.x, x.y}, u, FF{0.f, 0.f});
   const float2 v = make_float2(c.x, -c.y);  // forward transform: exp(-2 pi i t)
-  const long long plane = (long long)M * N;
-  const long long idx = (long long)j * N + i;
-  __nv_bfloat16* s = axis ? ay_s : ax_s;
-  if (s) {
-    __nv_bfloat16* base = s + (long long)b * 4 * plane + idx;
+  a0[(long long)l * mn + p] = v;
+  if (a0s) {
+    __nv_bfloat16* base = a0s + (long long)l * 4 * mn + p;
     __nv_bfloat16 h, lo;
     split_bf16(v.x, h, lo);
     base[0] = h;
-    base[plane] = lo;
+    base[mn] = lo;
     split_bf16(v.y, h, lo);
-    base[2 * plane] = h;
-    base[3 * plane] = lo;
-  } else {
-    (axis ? ay_c : ax_c)[(long long)b * plane + idx] = v;
+    base[2 * mn] = h;
+    base[3 * mn] = lo;
+  }
+}
+
+// Source tilt as a phasor per pupil column (x) and row (y): for batch element
+// b = l Rc + r,
+//   tx[b][i] = exp(+2 pi i x_i theta_{r,x} / fringe_l), ty likewise with theta_{r,y},
+// so that the tilted matrices are A'[b][j][i] = A0[l][j][i] t[b][i]
+// (exp(-2 pi i x (u - theta / fringe)) = exp(-2 pi i x u) exp(2 pi i x theta / fringe)).
+__global__ void scene_tilt_kernel(int N, int Rc, const float2* __restrict__ xin,
+                                  const double* __restrict__ inv_fringe,
+                                  const double* __restrict__ pos, float2* __restrict__ tx,
+                                  float2* __restrict__ ty) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (i >= N) return;
+  const int l = b / Rc, r = b - (b / Rc) * Rc;
+  const float2 x = xin[i];
+  const FF sx = ff_from_double(pos[2 * r] * inv_fringe[l]);
+  const FF sy = ff_from_double(pos[2 * r + 1] * inv_fringe[l]);
+  tx[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, sx, FF{0.f, 0.f});
+  ty[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, sy, FF{0.f, 0.f});
+}
+
+struct alignas(8) Bf16x4 {
+  __nv_bfloat16 v[4];
+};
+
+// A'x[b][j][i] = A0[l][j][i] tx[b][i] for the sources r0 .. r0 + rg - 1 of
+// wavelength l = blockIdx.y (r0 = blockIdx.z rg): a store-bound pass, each
+// thread holding V consecutive elements of one matrix row (V = 4 needs N % 4 == 0)
+// and reusing its A0 values for every source of the group.
+template <int V>
+__global__ void scene_ax_kernel(int M, int N, int Rc, int rg, const float2* __restrict__ a0,
+                                const float2* __restrict__ tx, __nv_bfloat16* __restrict__ ax_s,
+                                float2* __restrict__ ax_c) {
+  const long long mn = (long long)M * N;
+  const long long p0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * V;
+  const int l = blockIdx.y;
+  const int r0 = blockIdx.z * rg;
+  if (p0 >= mn) return;
+  const int i0 = (int)(p0 % N);
+  float2 a[V];
+#pragma unroll
+  for (int k = 0; k < V; ++k) a[k] = a0[(long long)l * mn + p0 + k];
+  const int r1 = r0 + rg < Rc ? r0 + rg : Rc;
+  for (int r = r0; r < r1; ++r) {
+    const long long b = (long long)l * Rc + r;
+    float2 v[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) v[k] = ctilt(tx[b * N + i0 + k], a[k].x, a[k].y);
+    if (ax_s) {
+      Bf16x4 q[4];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        split_bf16(v[k].x, q[0].v[k], q[1].v[k]);
+        split_bf16(v[k].y, q[2].v[k], q[3].v[k]);
+      }
+      __nv_bfloat16* base = ax_s + b * 4 * mn + p0;
+      if (V == 4) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16x4*>(base + c * mn) = q[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+          for (int k = 0; k < V; ++k) base[c * mn + k] = q[c].v[k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < V; ++k) ax_c[b * mn + p0 + k] = v[k];
+    }
   }
 }
 
@@ -222,32 +281,33 @@ struct dlx_scene_plan_s {
   double ps_in = 0, ps_out = 0, focal = 0;
   std::vector<double> wl;
   // constants
-  Buf alpha, kf, a_out, b_out, inv_fringe, inv_lambda_ff, xin, yw;
+  Buf alpha, kf, a_out, b_out, inv_fringe, inv_lambda_ff, xin, yw, a0, a0s;
   // workspace
-  Buf e, ex, ax, ay, d1, d1y, fbar, planes, ux, uy, bsum, bw;
+  Buf e, ex, ax, d1, d1y, fbar, planes, tx, ty, bsum, bw;
   const double* pos = nullptr;  // device [S][2] positions of the current call
 
   bool split() const { return variant == DLX_VARIANT_SPLIT_BF16; }
   size_t elem() const { return 8; }  // bytes per complex element (split planes or c64)
 
   void release() {
-    for (Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw, &e, &ex,
-                   &ax, &ay, &d1, &d1y, &fbar, &planes, &ux, &uy, &bsum, &bw})
+    for (Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw, &a0,
+                   &a0s, &e, &ex, &ax, &d1, &d1y, &fbar, &planes, &tx, &ty, &bsum, &bw})
       b->release();
   }
   size_t footprint() const {
     size_t t = 0;
-    for (const Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw, &e,
-                         &ex, &ax, &ay, &d1, &d1y, &fbar, &planes, &ux, &uy, &bsum, &bw})
+    for (const Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw,
+                         &a0, &a0s, &e, &ex, &ax, &d1, &d1y, &fbar, &planes, &tx, &ty, &bsum,
+                         &bw})
       t += b->bytes;
     return t;
   }
 
-  GemmArgs gemm(int batch, int Mg, int Ng, int K, const void* A, const void* B, int b_div,
-                const EpiArgs& e) const {
+  GemmArgs gemm(int batch, int Mg, int Ng, int K, const void* A, int a_div, const void* B,
+                int b_div, const EpiArgs& e) const {
     GemmArgs g{};
     g.batch = batch; g.M = Mg; g.N = Ng; g.K = K;
-    g.a_batch_div = 1;
+    g.a_batch_div = a_div;
     g.b_batch_div = b_div;
     if (split()) {
       g.As = static_cast<const __nv_bfloat16*>(A);
@@ -287,25 +347,32 @@ struct dlx_scene_plan_s {
     return DLX_OK;
   }
 
-  // Tilted DFT matrices of sources s0 .. s0 + Rc - 1 (positions already in `pos`).
+  // Tilt phasors of sources s0 .. s0 + Rc - 1 (positions already in `pos`) and
+  // their x-axis matrices A'x. The y-axis tilt is applied by the first GEMM's
+  // epilogue (EpiArgs::coltilt), so every second GEMM reads the shared A0.
   int build_matrices(int s0, int Rc, cudaStream_t s) {
     const int B = Rc * L;
-    dim3 gu(ceil_div(M, 128), B);
-    scene_utable_kernel<<<gu, 128, 0, s>>>(M, Rc, L, a_out.as<double>(), b_out.as<double>(),
-                                           inv_fringe.as<double>(), pos + 2 * s0,
-                                           ux.as<float2>(), uy.as<float2>());
-    DLX_LAUNCH_CHECK("scene_utable_kernel");
-    dim3 blk(32, 8);
-    dim3 grd(ceil_div(N, 32), ceil_div(M, 8), 2 * B);
-    scene_dft_kernel<<<grd, blk, 0, s>>>(M, N, B, xin.as<float2>(), ux.as<float2>(),
-                                         uy.as<float2>(),
-                                         split() ? ax.as<__nv_bfloat16>() : nullptr,
-                                         split() ? ay.as<__nv_bfloat16>() : nullptr,
-                                         split() ? nullptr : ax.as<float2>(),
-                                         split() ? nullptr : ay.as<float2>());
-    DLX_LAUNCH_CHECK("scene_dft_kernel");
+    dim3 gt(ceil_div(N, 256), B);
+    scene_tilt_kernel<<<gt, 256, 0, s>>>(N, Rc, xin.as<float2>(), inv_fringe.as<double>(),
+                                         pos + 2 * s0, tx.as<float2>(), ty.as<float2>());
+    DLX_LAUNCH_CHECK("scene_tilt_kernel");
+    const long long mn = (long long)M * N;
+    const int rg = 8;
+    if (split() && N % 4 == 0) {
+      dim3 grd(ceil_div(mn / 4, 256), L, ceil_div(Rc, rg));
+      scene_ax_kernel<4><<<grd, 256, 0, s>>>(M, N, Rc, rg, a0.as<float2>(), tx.as<float2>(),
+                                             ax.as<__nv_bfloat16>(), nullptr);
+    } else {
+      dim3 grd(ceil_div(mn, 256), L, ceil_div(Rc, rg));
+      scene_ax_kernel<1><<<grd, 256, 0, s>>>(M, N, Rc, rg, a0.as<float2>(), tx.as<float2>(),
+                                             split() ? ax.as<__nv_bfloat16>() : nullptr,
+                                             split() ? nullptr : ax.as<float2>());
+    }
+    DLX_LAUNCH_CHECK("scene_ax_kernel");
     return DLX_OK;
   }
+  // The shared y-axis matrix of every wavelength (A operand, batch divisor Rc).
+  const void* ay0() const { return split() ? a0s.p : a0.p; }
 
   int forward(const float* amp, const float* amp_scale, const float* opd, const float* phase,
               const double* positions, const float* weights, int S, float* image, int accumulate,
@@ -316,14 +383,16 @@ struct dlx_scene_plan_s {
       const int Rc = std::min(R, S - s0), B = Rc * L;
       DLX_TRY(build_matrices(s0, Rc, s));
       // D1[b][u][y] = sum_x A'x[b][u][x] E_l[y][x]
+      // times the y tilt ty[b][y] (so D1 holds the y-tilted field)
       EpiArgs e1 = epi(split() ? EPI_SPLIT : EPI_C64, Rc);
       e1.alpha = nullptr;
+      e1.coltilt = ty.as<float2>();
       set_out(e1, d1.p);
-      DLX_TRY(run(gemm(B, M, N, N, ax.p, e.p, Rc, e1), s));
-      // |F[b][v][u]|^2, F = alpha_l sum_y A'y[b][v][y] D1[b][u][y]
+      DLX_TRY(run(gemm(B, M, N, N, ax.p, 1, e.p, Rc, e1), s));
+      // |F[b][v][u]|^2, F = alpha_l sum_y A0[l][v][y] D1[b][u][y]
       EpiArgs e2 = epi(EPI_INTENSITY, Rc);
       e2.out_f32 = planes.as<float>();
-      DLX_TRY(run(gemm(B, M, M, N, ay.p, d1.p, 1, e2), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1.p, 1, e2), s));
       const long long npix = (long long)M * M;
       scene_image_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(planes.as<float>(), Rc, L, npix,
                                                              weights, s0,
@@ -342,10 +411,11 @@ struct dlx_scene_plan_s {
     for (int s0 = 0; s0 < S; s0 += R) {
       const int Rc = std::min(R, S - s0), B = Rc * L;
       DLX_TRY(build_matrices(s0, Rc, s));
-      // D1 and D1Y = Y.D1 (Y along the y index = GEMM column n)
+      // D1 and D1Y = Y.D1 (Y along the y index = GEMM column n), both y-tilted
       EpiArgs e1 = epi(EPI_SPLIT2, Rc);
       e1.alpha = nullptr;
       e1.colw = yw.as<float>();
+      e1.coltilt = ty.as<float2>();
       if (split()) {
         e1.out_split = d1.as<__nv_bfloat16>();
         e1.out_split2 = d1y.as<__nv_bfloat16>();
@@ -353,7 +423,7 @@ struct dlx_scene_plan_s {
         e1.out_c64 = d1.as<float2>();
         e1.out_c642 = d1y.as<float2>();
       }
-      DLX_TRY(run(gemm(B, M, N, N, ax.p, e.p, Rc, e1), s));
+      DLX_TRY(run(gemm(B, M, N, N, ax.p, 1, e.p, Rc, e1), s));
       // intensity planes and F-bar = 2 w alpha G D
       EpiArgs e2 = epi(EPI_PSF_GRADF, Rc, g_image);
       e2.out_f32 = planes.as<float>();
@@ -363,7 +433,7 @@ struct dlx_scene_plan_s {
                                                                     bw.as<float>());
       DLX_LAUNCH_CHECK("scene_gather_weights_kernel");
       e2.bweight = bw.as<float>();
-      DLX_TRY(run(gemm(B, M, M, N, ay.p, d1.p, 1, e2), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1.p, 1, e2), s));
       if (g_w) {
         scene_bsum_kernel<<<B, 256, 0, s>>>(planes.as<float>(), npix, g_image,
                                             bsum.as<double>());
@@ -378,14 +448,15 @@ struct dlx_scene_plan_s {
       ed.out_f32 = planes.as<float>();
       if (split()) ed.in_split = fbar.as<__nv_bfloat16>();
       else ed.in_c64 = fbar.as<float2>();
-      DLX_TRY(run(gemm(B, M, M, N, ay.p, d1y.p, 1, ed), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1y.p, 1, ed), s));
       DLX_TRY(pos_reduce(Rc, s0, g_pos, 1, s));
       // d/dtx: D1X = A'x (X.E)^T (into d1), then the same dot
       EpiArgs ex1 = epi(split() ? EPI_SPLIT : EPI_C64, Rc);
       ex1.alpha = nullptr;
+      ex1.coltilt = ty.as<float2>();
       set_out(ex1, d1.p);
-      DLX_TRY(run(gemm(B, M, N, N, ax.p, ex.p, Rc, ex1), s));
-      DLX_TRY(run(gemm(B, M, M, N, ay.p, d1.p, 1, ed), s));
+      DLX_TRY(run(gemm(B, M, N, N, ax.p, 1, ex.p, Rc, ex1), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1.p, 1, ed), s));
       DLX_TRY(pos_reduce(Rc, s0, g_pos, 0, s));
     }
     return DLX_OK;
@@ -448,16 +519,21 @@ int scene_create(const dlx_scene_desc* d, const double* wl, dlx_scene_plan_s* p)
                                                  p->xin.as<float2>());
   DLX_LAUNCH_CHECK("scene_xtable_kernel");
   const size_t B = (size_t)R * L, nn = (size_t)N * N, mn = (size_t)M * N, mm = (size_t)M * M;
+  DLX_TRY(p->a0.alloc(L * mn * sizeof(float2)));
+  if (p->split()) DLX_TRY(p->a0s.alloc(L * mn * 4 * sizeof(__nv_bfloat16)));
+  scene_a0_kernel<<<dim3(ceil_div((long long)mn, 256), L), 256>>>(
+      M, N, p->xin.as<float2>(), p->a_out.as<double>(), p->b_out.as<double>(),
+      p->a0.as<float2>(), p->split() ? p->a0s.as<__nv_bfloat16>() : nullptr);
+  DLX_LAUNCH_CHECK("scene_a0_kernel");
   DLX_TRY(p->e.alloc(L * nn * p->elem()));
   DLX_TRY(p->ex.alloc(L * nn * p->elem()));
   DLX_TRY(p->ax.alloc(B * mn * p->elem()));
-  DLX_TRY(p->ay.alloc(B * mn * p->elem()));
   DLX_TRY(p->d1.alloc(B * mn * p->elem()));
   DLX_TRY(p->d1y.alloc(B * mn * p->elem()));
   DLX_TRY(p->fbar.alloc(B * mm * p->elem()));
   DLX_TRY(p->planes.alloc(B * mm * sizeof(float)));
-  DLX_TRY(p->ux.alloc(B * M * sizeof(float2)));
-  DLX_TRY(p->uy.alloc(B * M * sizeof(float2)));
+  DLX_TRY(p->tx.alloc(B * N * sizeof(float2)));
+  DLX_TRY(p->ty.alloc(B * N * sizeof(float2)));
   DLX_TRY(p->bsum.alloc(B * sizeof(double)));
   DLX_TRY(p->bw.alloc(B * sizeof(float)));
   DLX_TRY_CUDA(cudaDeviceSynchronize());

@@ -185,10 +185,10 @@ class MFTPlan(_Plan):
 
 # pad * N from which the padded FFT runs as radix-2 line FFTs instead of the
 # DFT-GEMM pair, whose cost grows as P^2 N. Measured forward + adjoint of 16
-# wavelengths: P = 1024 0.54 ms (split-BF16 GEMM) vs 0.85 ms (radix); P = 2048
-# 3.10 vs 3.75 ms; P = 4096 25.5 vs 20.2 ms. Without tensor cores (FP32 GEMM
+# wavelengths: P = 1024 0.54 ms (split-BF16 GEMM) vs 0.70 ms (radix); P = 2048
+# 3.08 vs 2.89 ms; P = 4096 24.3 vs 15.3 ms. Without tensor cores (FP32 GEMM
 # form) the radix form is faster at every measured size.
-RADIX_FFT_MIN = 4096
+RADIX_FFT_MIN = 2048
 
 
 def resolve_fft_variant(n_in, pad, variant=None):
