@@ -660,26 +660,39 @@ __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, i
       if (od.amp_scale) amp *= *od.amp_scale;
     }
     float sre = 0.f, sim = 0.f, sk = 0.f;
-    for (int l = 0; l < a.L; ++l) {
-      float pre = 0.f;
-      if (live) {
-        const float2 eb = a.ebar[((long long)l * R + r) * a.npix + p];
-        const float4 c = lam[l];
-        const float2 u = cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
-        const float sw = c.z;
-        const float pr = u.x * eb.x + u.y * eb.y;
-        const float pi = u.x * eb.y - u.y * eb.x;
-        pre = sw * pr;
-        const float pim = amp * sw * pi;
-        sre += pre;
-        sim += pim;
-        sk += c.w * pim;
-      }
-      if (w_out) {  // warp-uniform
-        float v = pre * amp_raw;
+    // The Ebar loads of four wavelengths are issued before their arithmetic,
+    // so that their latencies overlap.
+    constexpr int kPre = 4;
+    for (int l0 = 0; l0 < a.L; l0 += kPre) {
+      float2 ebq[kPre];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) wpart[warp * a.L + l] += (double)v;
+      for (int j = 0; j < kPre; ++j)
+        ebq[j] = (live && l0 + j < a.L) ? a.ebar[((long long)(l0 + j) * R + r) * a.npix + p]
+                                        : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < kPre; ++j) {
+        const int l = l0 + j;
+        if (l >= a.L) break;  // block-uniform
+        float pre = 0.f;
+        if (live) {
+          const float2 eb = ebq[j];
+          const float4 c = lam[l];
+          const float2 u = cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
+          const float sw = c.z;
+          const float pr = u.x * eb.x + u.y * eb.y;
+          const float pi = u.x * eb.y - u.y * eb.x;
+          pre = sw * pr;
+          const float pim = amp * sw * pi;
+          sre += pre;
+          sim += pim;
+          sk += c.w * pim;
+        }
+        if (w_out) {  // warp-uniform
+          float v = pre * amp_raw;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+          if (lane == 0) wpart[warp * a.L + l] += (double)v;
+        }
       }
     }
     if (live) {

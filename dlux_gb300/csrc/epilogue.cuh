@@ -213,22 +213,26 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
         for (int j = 0; j < 32; ++j)
           if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
       }
-      // all 32 loads first, so their latencies overlap
+      // 16 loads at a time, so that their latencies overlap
       const float* G = (e.objs.n > 0 ? e.objs.o[r].G : e.G) + idx0;
-      float g[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) g[j] = j < mc ? __ldg(G + (long long)j * N) : 0.0f;
       const float s = 2.0f * a * (e.bweight ? e.bweight[b] : 1.0f);
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        if (j < mc) {
-          const float gj = s * g[j];
-          const float2 v = make_float2(gj * re[j], gj * im[j]);
-          if (e.out_split)
-            store_split(e.out_split + (long long)b * 4 * plane + idx0, plane, (long long)j * N,
-                        v);
-          else
-            e.out_c64[(long long)b * plane + idx0 + (long long)j * N] = v;
+      for (int h = 0; h < 32; h += 16) {
+        float g[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          g[j] = h + j < mc ? __ldg(G + (long long)(h + j) * N) : 0.0f;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (h + j < mc) {
+            const float gj = s * g[j];
+            const float2 v = make_float2(gj * re[h + j], gj * im[h + j]);
+            if (e.out_split)
+              store_split(e.out_split + (long long)b * 4 * plane + idx0, plane,
+                          (long long)(h + j) * N, v);
+            else
+              e.out_c64[(long long)b * plane + idx0 + (long long)(h + j) * N] = v;
+          }
         }
       }
       break;

@@ -28,11 +28,14 @@
 // imaginary parts (4 x 128 fp32 columns = all 512 columns). K is staged 32
 // elements at a time (64-byte rows, 64B swizzle) by TMA in a 3-stage mbarrier
 // pipeline (64 KB per stage). Warp roles: warp 0 issues TMA, warp 1 issues
-// MMA (one thread each), warps 2-9 drain TMEM through the shared epilogues,
+// MMA (one thread each), warps 4-11 drain TMEM through the shared epilogues,
 // two warps per TMEM lane quarter taking alternate 32-row chunks, so that the
 // epilogue's memory traffic has enough loads in flight. The MMAs of the next
 // tile wait for the drain (no TMEM is left for a second accumulator set), so
-// the epilogue's speed adds directly to the tile time.
+// the drain must be short: each epilogue warp loads both of its chunks into
+// registers and releases TMEM before its stores. The warpgroups split the
+// register file unevenly (setmaxnreg): 88 per thread for TMA/MMA, 208 for the
+// epilogue, which then holds its 128 drained values without spilling.
 // The kernel is persistent over (batch, m-tile, n-tile)
 // work items. Every mbarrier wait is bounded by a wall-clock limit; on
 // expiry the CTA records DLX_ERR_TIMEOUT in a device status word, drains its
@@ -55,8 +58,19 @@ constexpr int A_PLANE_BYTES = TC_BM * TC_BK * 2;                         // 8 KB
 constexpr int B_PLANE_BYTES = TC_BN * TC_BK * 2;                         // 8 KB
 constexpr int STAGE_BYTES = 4 * A_PLANE_BYTES + 4 * B_PLANE_BYTES;       // 64 KB
 constexpr int SMEM_BYTES = TC_STAGES * STAGE_BYTES + 1024 + 256;
-constexpr int TC_THREADS = 320;  // TMA, MMA, 8 epilogue warps (two per TMEM lane quarter)
+// 384 threads in three warpgroups. Warpgroup 0: warp 0 issues TMA, warp 1
+// MMA, warps 2-3 idle; it gives registers back (setmaxnreg.dec to
+// REG_CTRL). Warpgroups 1-2 (warps 4-11) are the 8 epilogue warps, two per
+// TMEM lane quarter, raised to REG_EPI registers so that a warp holds both of
+// its drained 32-row chunks without spilling.
+constexpr int TC_THREADS = 384;
 constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_EPI_W0 = 4;  // first epilogue warp
+constexpr int REG_LAUNCH = 168, REG_CTRL = 88, REG_EPI = 208;
+// setmaxnreg.inc waits until the block's launch registers cover the split.
+static_assert(128 * REG_CTRL + 256 * REG_EPI <= TC_THREADS * REG_LAUNCH,
+              "register split exceeds the launch registers");
+static_assert(REG_LAUNCH * TC_THREADS <= 65536, "launch registers exceed the SM");
 constexpr uint32_t TMEM_COLS = 512;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
 
@@ -99,8 +113,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait. Returns false if another role aborted or the limit expired
-// (then the abort flag and the device status word are set).
-__device__ __noinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+// (then the abort flag and the device status word are set). Inlined: a call
+// inside a setmaxnreg region makes ptxas run out of memory.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
                                        int* status, bool honour_abort = true) {
   const unsigned long long t0 = globaltimer();
   for (uint32_t it = 0;; ++it) {
@@ -310,6 +325,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
+  if (warp < TC_EPI_W0) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(REG_CTRL));
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
     if (lane == 0) {
@@ -406,12 +423,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mma_commit(mdone);
       mbar_wait(mdone, 0, abort_flag, p.status, false);
     }
+  }
   } else {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(REG_EPI));
     // -------------------------------- epilogue --------------------------------
     // TMEM lane = output column n, TMEM column = output row m (see the MMA
     // issue): each thread drains one column of the tile, 32 rows at a time.
     const int q = warp & 3;  // TMEM lane quarter this warp may access
-    const int half = (warp - 2) >> 2;  // the two warps of a quarter take alternate chunks
+    const int half = (warp - TC_EPI_W0) >> 2;  // the two warps of a quarter take alternate chunks
     uint32_t acc_ph = 0;
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
       if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
@@ -810,6 +829,17 @@ void init_once() {
     return;
   }
   bool attr_ok = true;
+  // The register split of the loaded kernels needs REG_LAUNCH registers per
+  // thread at launch; refuse a build that came out with fewer.
+  for (const void* const* k = loaded_kernels(); *k; ++k) {
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, *k) != cudaSuccess || fa.numRegs < REG_LAUNCH) {
+      g_init_status = fail(DLX_ERR_UNSUPPORTED,
+                           "tensor-core GEMM: the build's register count does not cover its "
+                           "warpgroup register split");
+      return;
+    }
+  }
   for (const void* const* k = loaded_kernels(); *k; ++k)
     attr_ok = attr_ok && cudaFuncSetAttribute(*k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               SMEM_BYTES) == cudaSuccess;
