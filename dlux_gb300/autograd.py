@@ -50,7 +50,10 @@ class PolyPSF(torch.autograd.Function):
         ctx.plan, ctx.normalise, ctx.tilt = plan, normalise, t
         ctx.tilt_device = tilt.device
         ctx.save_for_backward(amp, opd, phase, weights, amp_scale)
-        return plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t)
+        psf = plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t)
+        # the backward may start from this forward's workspace if nothing used the plan since
+        ctx.token = plan.forward_token()
+        return psf
 
     @staticmethod
     def backward(ctx, g_psf):
@@ -68,7 +71,7 @@ class PolyPSF(torch.autograd.Function):
         if not want:
             return (None,) * 7
         gr = plan.grad(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(),
-                       g_psf.contiguous(), ctx.tilt, tuple(want))
+                       g_psf.contiguous(), ctx.tilt, tuple(want), reuse_token=ctx.token)
         g_amp = gr["amp"]
         if g_amp is not None and ctx.normalise:
             g_amp = kernels.amp_norm_backward(amp.detach(), g_amp)

@@ -170,7 +170,12 @@ struct TwoStep {
   int build(const std::vector<DftAxis>& ax_x, const std::vector<DftAxis>& ax_y,
             const std::vector<float>& alphas, bool generate_operand = false) {
     shared_xy = std::memcmp(ax_x.data(), ax_y.data(), sizeof(DftAxis) * batch) == 0;
-    gen_a = variant == DLX_VARIANT_SPLIT_BF16 && generate_operand;
+    // The in-CTA generator assumes a phase affine along K: no quadratic terms.
+    bool affine = true;
+    for (int b = 0; b < batch; ++b)
+      affine = affine && ax_x[b].q_in == 0.0 && ax_x[b].q_out == 0.0 &&
+               ax_y[b].q_in == 0.0 && ax_y[b].q_out == 0.0;
+    gen_a = variant == DLX_VARIANT_SPLIT_BF16 && generate_operand && affine;
     DLX_TRY(axes.alloc(sizeof(DftAxis) * batch * 2));
     int st = DLX_OK;
     do {
@@ -779,6 +784,25 @@ struct dlx_poly_plan_s {
   DevBuf partial;    // double reduction partials
   DevBuf pathff;     // [R][N][N] float4 (path, phase) pairs, then [R][3][N][N] pixel sums
   int nparts = kPolyParts;
+  // Forward-to-backward reuse (dlx_poly_forward_token / dlx_poly_reuse_forward):
+  // after a single-chunk forward, `field`, `mid` (the first-stage product D1)
+  // and `pathff` hold that forward's state until the next call on the plan.
+  unsigned long long epoch = 0;      // counts single-chunk forwards
+  unsigned long long fwd_token = 0;  // token of the intact forward state, 0 if none
+  unsigned long long reuse_req = 0;  // token the next backward may start from
+  std::vector<dlx_poly_object> fwd_objs;
+
+  static bool same_inputs(const dlx_poly_object& a, const dlx_poly_object& b) {
+    return a.amp == b.amp && a.amp_scale == b.amp_scale && a.opd == b.opd &&
+           a.phase == b.phase && a.weights == b.weights && a.tilt_x == b.tilt_x &&
+           a.tilt_y == b.tilt_y;
+  }
+  bool can_reuse(unsigned long long token, const dlx_poly_object* objs, int n) const {
+    if (token == 0 || token != fwd_token || n != (int)fwd_objs.size()) return false;
+    for (int r = 0; r < n; ++r)
+      if (!same_inputs(objs[r], fwd_objs[r])) return false;
+    return true;
+  }
 
   // Device bytes this plan owns: an attached workspace belongs to the caller.
   size_t footprint() const {
@@ -830,10 +854,12 @@ struct dlx_poly_plan_s {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
+    fwd_token = 0;
     ObjTable t;
     OutTable o;
     tables(objs, R, &t, &o);
-    DLX_TRY(build_field(t, s));
+    // the (path, phase) pairs too, so that a backward can start from this state
+    DLX_TRY(build_field(t, s, pathff.as<float4>()));
     EpiArgs e1 = epi_store(v, mid.p, nullptr);
     e1.objs = t;
     DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
@@ -854,22 +880,28 @@ struct dlx_poly_plan_s {
     return launch_obj_psf_reduce(ra, s);
   }
 
+  // reuse: `mid` and `pathff` still hold the forward state of these objects
+  // (checked by the caller), so the pupil field and D1 are not rebuilt.
   int backward_chunk(const dlx_poly_object* objs, int R, cudaStream_t s, float* sum_amp = nullptr,
                      float* sum_opd = nullptr, float* sum_phase = nullptr,
-                     bool sum_pixels = false, bool accumulate_sum = false) {
+                     bool sum_pixels = false, bool accumulate_sum = false, bool reuse = false) {
     const int N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
+    fwd_token = 0;  // the reverse pass overwrites mid
     ObjTable t;
     OutTable o;
     tables(objs, R, &t, &o);
     for (int r = 0; r < R; ++r)
       if (!t.o[r].G) return fail(DLX_ERR_ARG, "poly backward: every object needs g_psf");
-    // Recompute the forward fields (nothing is stored between the passes).
-    DLX_TRY(build_field(t, s, pathff.as<float4>()));
-    EpiArgs e1 = epi_store(v, mid.p, nullptr);
-    e1.objs = t;
-    DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
+    if (!reuse) {
+      // Recompute the forward fields.
+      DLX_TRY(build_field(t, s, pathff.as<float4>()));
+      EpiArgs e1 = epi_store(v, mid.p, nullptr);
+      e1.objs = t;
+      DLX_TRY(run_gemm(v, gemm(ts.opATx(), R, M, N, N, false, field.p, e1), s));
+    }
+    // The per-wavelength focal field is recomputed here from D1 in every case.
     // Fbar[v][u] = 2 alpha G[v][u] D[v][u]
     EpiArgs eg{};
     eg.kind = EPI_GRADF;
@@ -890,6 +922,7 @@ struct dlx_poly_plan_s {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
+    fwd_token = 0;
     ObjTable t;
     OutTable o;
     tables(objs, R, &t, &o);
@@ -1075,6 +1108,7 @@ int dlx_poly_workspace_bytes(const dlx_poly_desc* d, int max_objects, size_t* by
 
 int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes) {
   if (!plan || !workspace) return fail(DLX_ERR_ARG, "poly_attach_workspace: null pointer");
+  plan->fwd_token = 0;
   if ((uintptr_t)workspace % 256 != 0)
     return fail(DLX_ERR_ARG, "poly_attach_workspace: workspace must be 256-byte aligned");
   size_t sz[kPolyBuffers];
@@ -1132,6 +1166,10 @@ int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obje
     const int R = std::min(plan->max_obj, n_objects - o0);
     DLX_TRY(plan->forward_chunk(objs + o0, R, psf_sum, (o0 > 0) ? 1 : accumulate, s));
   }
+  if (n_objects >= 1 && n_objects <= plan->max_obj) {
+    plan->fwd_token = ++plan->epoch;
+    plan->fwd_objs.assign(objs, objs + n_objects);
+  }
   return DLX_OK;
 }
 
@@ -1140,10 +1178,26 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
   if (!plan || (n_objects > 0 && !objs)) return fail(DLX_ERR_ARG, "poly_backward: null pointer");
   if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_backward: negative object count");
   cudaStream_t s = as_stream(stream);
+  const unsigned long long req = plan->reuse_req;
+  plan->reuse_req = 0;  // a request applies to one backward call
+  const bool reuse = plan->can_reuse(req, objs, n_objects);
   for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
     const int R = std::min(plan->max_obj, n_objects - o0);
-    DLX_TRY(plan->backward_chunk(objs + o0, R, s));
+    DLX_TRY(plan->backward_chunk(objs + o0, R, s, nullptr, nullptr, nullptr, false, false,
+                                 reuse));
   }
+  return DLX_OK;
+}
+
+int dlx_poly_forward_token(dlx_poly_plan plan, unsigned long long* token) {
+  if (!plan || !token) return fail(DLX_ERR_ARG, "poly_forward_token: null pointer");
+  *token = plan->fwd_token;
+  return DLX_OK;
+}
+
+int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token) {
+  if (!plan) return fail(DLX_ERR_ARG, "poly_reuse_forward: null plan");
+  plan->reuse_req = token;
   return DLX_OK;
 }
 
@@ -1166,6 +1220,7 @@ int dlx_poly_backward_sum(dlx_poly_plan plan, const dlx_poly_object* objs, int n
     return fail(DLX_ERR_ARG, "poly_backward_sum: null pointer");
   if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_backward_sum: negative object count");
   cudaStream_t s = as_stream(stream);
+  plan->reuse_req = 0;
   for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
     const int R = std::min(plan->max_obj, n_objects - o0);
     DLX_TRY(plan->backward_chunk(objs + o0, R, s, g_amp, g_opd, g_phase, true, o0 > 0));

@@ -40,17 +40,21 @@ void note_launch();
   } while (0)
 
 // ---------------------------------------------------------------------------
-// Affine-phase DFT description. Element (i_in, j_out) of a generated matrix is
-//   exp(2 pi i * [ sigma * x_i * u_j + g_in * i + d_in + g_out * j + d_out ])
+// DFT-type axis description. Element (i_in, j_out) of a generated matrix is
+//   exp(2 pi i * [ sigma * x_i * u_j + g_in * i + d_in + g_out * j + d_out
+//                  + q_in * x_i^2 + q_out * u_j^2 ])
 // with x_i = a_in * i + b_in and u_j = a_out * j + b_out, all in FP64 cycles.
-// This covers the MFT transfer matrices (no ramps) and the padded centred FFT
-// with its separable input/output phase ramps. `scale` multiplies the result.
+// This covers the MFT transfer matrices (no ramps), the padded centred FFT
+// with its separable input/output phase ramps, and the linear canonical
+// transform kernel of an ABCD system (the quadratic chirps q_in, q_out).
+// `scale` multiplies the result.
 // ---------------------------------------------------------------------------
 struct DftAxis {
   double a_in, b_in, a_out, b_out;
   double g_in, d_in, g_out, d_out;
   double sigma;
   double scale;
+  double q_in, q_out;
 };
 
 // Round-to-nearest FP64 cycle reduction followed by the FP32 sincospi of the

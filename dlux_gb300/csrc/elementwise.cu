@@ -28,7 +28,7 @@ __global__ void dft_gen_kernel(const DftAxis* __restrict__ axes, int rows, int c
   const double x = ax.a_in * (double)i_in + ax.b_in;
   const double u = ax.a_out * (double)j_out + ax.b_out;
   const double t = ax.sigma * x * u + (ax.g_in * (double)i_in + ax.d_in) +
-                   (ax.g_out * (double)j_out + ax.d_out);
+                   (ax.g_out * (double)j_out + ax.d_out) + ax.q_in * x * x + ax.q_out * u * u;
   float2 v = cis_cycles(t);
   v.x *= (float)ax.scale;
   v.y *= (float)ax.scale;

@@ -341,8 +341,17 @@ class PolyPlan(_Plan):
              ptr(weights), float(tilt[0]), float(tilt[1]), ptr(out), _stream())
         return out
 
+    def forward_token(self) -> int:
+        """Token of the forward state the workspace still holds (0 if none)."""
+        t = ctypes.c_ulonglong(0)
+        call("dlx_poly_forward_token", self.handle, ctypes.byref(t))
+        return int(t.value)
+
     def grad(self, amp, amp_scale, opd, phase, weights, g_psf, tilt=(0.0, 0.0),
-             want=("amp", "opd", "phase", "w")):
+             want=("amp", "opd", "phase", "w"), reuse_token=0):
+        """Reverse pass. ``reuse_token`` (from forward_token() after the matching
+        psf call) lets it start from that forward's workspace when the plan has
+        not been used since; otherwise everything is recomputed."""
         amp, amp_scale, opd, phase, weights = map(_contig, (amp, amp_scale, opd, phase, weights))
         dev = g_psf.device
         n = self.n_in
@@ -351,6 +360,8 @@ class PolyPlan(_Plan):
         g_ph = torch.empty((n, n), dtype=torch.float32, device=dev) if "phase" in want else None
         g_w = (torch.empty((len(self.wavelengths),), dtype=torch.float32, device=dev)
                if "w" in want else None)
+        if reuse_token:
+            call("dlx_poly_reuse_forward", self.handle, ctypes.c_ulonglong(reuse_token))
         call("dlx_poly_psf_grad", self.handle, ptr(amp), ptr(amp_scale), ptr(opd), ptr(phase),
              ptr(weights), float(tilt[0]), float(tilt[1]), ptr(g_psf.contiguous()), ptr(g_amp),
              ptr(g_opd), ptr(g_ph), ptr(g_w), _stream())

@@ -270,6 +270,22 @@ int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obje
 /* Reverse pass for every object with its own cotangent objs[r].g_psf. */
 int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_objects,
                       void* stream);
+/* Forward-to-backward reuse, the counterpart of the residuals a jax.custom_vjp
+ * forward hands to its backward (here they stay in the plan's fixed
+ * workspace, so no memory is added). After a dlx_poly_forward of at most
+ * max_objects objects, the workspace holds that forward's pupil field, its
+ * first-stage product D1 and the path pairs until the next call on the plan.
+ * dlx_poly_forward_token returns a token for that state (0 if none is intact).
+ * dlx_poly_reuse_forward(token) lets the next dlx_poly_backward /
+ * dlx_poly_psf_grad start from it: it skips the phasor rebuild and the first
+ * MFT stage, and still recomputes the per-wavelength focal field from D1.
+ * The request covers one backward call. It is ignored, and the backward
+ * recomputes everything, if another call used the plan in between or the
+ * objects' inputs (amp, amp_scale, opd, phase, weights, tilt pointers and
+ * values) differ. The caller orders the backward after the forward on the
+ * device, as for any two calls on one plan. */
+int dlx_poly_forward_token(dlx_poly_plan plan, unsigned long long* token);
+int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token);
 /* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
  * is known before the forward pass (a serving request, a linear functional):
  * writes objs[r].psf (optional) and the gradient outputs like
