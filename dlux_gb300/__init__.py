@@ -9,7 +9,7 @@ host fallback.
 from . import utils  # noqa: F401
 from . import layers  # noqa: F401
 from .base import Base  # noqa: F401
-from .coordinates import CoordSpec  # noqa: F401
+from .coordinates import CoordSpec, PadSpec  # noqa: F401
 from .wavefronts import Wavefront  # noqa: F401
 from .psfs import PSF  # noqa: F401
 from .layers import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401

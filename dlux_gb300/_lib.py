@@ -44,6 +44,25 @@ class MftDesc(ctypes.Structure):
     ]
 
 
+class XformAxis(ctypes.Structure):
+    _fields_ = [
+        ("a_in", _c_dbl), ("b_in", _c_dbl), ("a_out", _c_dbl), ("b_out", _c_dbl),
+        ("sigma", _c_dbl), ("q_in", _c_dbl), ("q_out", _c_dbl), ("phase", _c_dbl),
+        ("scale", _c_dbl),
+    ]
+
+
+class XformDesc(ctypes.Structure):
+    _fields_ = [("batch", _c_int), ("n_in", _c_int), ("n_out", _c_int), ("variant", _c_int)]
+
+
+class AsmDesc(ctypes.Structure):
+    _fields_ = [
+        ("batch", _c_int), ("n_in", _c_int), ("n_pad", _c_int),
+        ("pixel_scale", _c_dbl), ("distance", _c_dbl), ("variant", _c_int),
+    ]
+
+
 class FftDesc(ctypes.Structure):
     _fields_ = [
         ("batch", _c_int), ("n_in", _c_int), ("pad", _c_int),
@@ -109,6 +128,15 @@ _SIGNATURES = {
     "dlx_transfer_matrix": (_c_int, [_c_vp, _c_int, _c_int, _c_dbl, _c_int, _c_dbl, _c_dbl,
                                      _c_dbl, _c_int, _c_int, _c_vp, _c_vp]),
     "dlx_mft_plan_create": (_c_int, [ctypes.POINTER(MftDesc), _c_vp, ctypes.POINTER(_c_vp)]),
+    "dlx_xform_plan_create": (_c_int, [ctypes.POINTER(XformDesc), _c_vp, _c_vp,
+                                       ctypes.POINTER(_c_vp)]),
+    "dlx_xform_plan_destroy": (_c_int, [_c_vp]),
+    "dlx_xform_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "dlx_xform_adjoint": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "dlx_asm_plan_create": (_c_int, [ctypes.POINTER(AsmDesc), _c_vp, ctypes.POINTER(_c_vp)]),
+    "dlx_asm_plan_destroy": (_c_int, [_c_vp]),
+    "dlx_asm_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
+    "dlx_asm_adjoint": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_mft_plan_destroy": (_c_int, [_c_vp]),
     "dlx_mft_forward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_mft_adjoint": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp]),

@@ -6,7 +6,7 @@ import torch
 
 from .base import Base
 
-__all__ = ["CoordSpec"]
+__all__ = ["CoordSpec", "PadSpec"]
 
 
 class CoordSpec(Base):
@@ -34,3 +34,14 @@ class CoordSpec(Base):
         if self.d is None:
             raise ValueError("d must be specified to calculate extent.")
         return self.c - (self.n / 2) * self.d, self.c + (self.n / 2) * self.d
+
+
+class PadSpec(Base):
+    """Sampling given as integer padding and cropping factors relative to an
+    input grid (dLux coordinates.py:34-72): the padded grid has n * pad pixels,
+    the cropped one (n * pad) // crop, centred on c."""
+
+    def __init__(self, pad=1, crop=1, c=0.0):
+        self.pad = int(pad)
+        self.crop = int(crop)
+        self.c = float(c)

@@ -1254,3 +1254,176 @@ int dlx_poly_psf_grad(dlx_poly_plan plan, const float* amp, const float* amp_sca
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Separable transforms with caller-described axes, and the angular-spectrum
+// propagator: the device side of dLux's ABCD propagators
+// (layers/abcd_propagators.py:245-459), whose arithmetic the reference takes
+// from the abcdLux package (lct.lct_prop, lct.lct_prop_fft, asm.asm_prop).
+// ---------------------------------------------------------------------------
+struct dlx_xform_plan_s {
+  TwoStepPlan p;
+};
+
+struct dlx_asm_plan_s {
+  TwoStepPlan fwd;   // centred DFT of the zero-padded field: N -> P
+  TwoStepPlan inv;   // centred inverse DFT: P -> P
+  DevBuf spec;       // [b][P][P] c64 spectrum
+  DevBuf zl, lam2;   // double [b]: distance / lambda, lambda^2
+  double df = 0;     // frequency step 1 / (P dx)
+  int P = 0;
+};
+
+namespace {
+
+DftAxis to_axis(const dlx_xform_axis& a) {
+  DftAxis d{};
+  d.a_in = a.a_in; d.b_in = a.b_in; d.a_out = a.a_out; d.b_out = a.b_out;
+  d.sigma = a.sigma; d.q_in = a.q_in; d.q_out = a.q_out;
+  d.d_out = a.phase;
+  d.scale = a.scale;
+  return d;
+}
+
+int make_two_step(TwoStepPlan* t, int batch, int n_in, int n_out, int variant,
+                  const std::vector<DftAxis>& ax, const std::vector<DftAxis>& ay) {
+  TwoStep& ts = t->ts;
+  ts.batch = batch; ts.n_in = n_in; ts.n_out = n_out; ts.variant = variant;
+  ts.wl.assign(batch, 1.0);  // no wavelength enters the matrices: they are given
+  std::vector<float> ones(batch, 1.0f);
+  DLX_TRY(ts.build(ax, ay, ones));
+  return t->alloc_buffers();
+}
+
+}  // namespace
+
+extern "C" {
+
+int dlx_xform_plan_create(const dlx_xform_desc* d, const dlx_xform_axis* ax_x,
+                          const dlx_xform_axis* ax_y, dlx_xform_plan* plan) {
+  if (!d || !ax_x || !ax_y || !plan) return fail(DLX_ERR_ARG, "xform_plan_create: null pointer");
+  *plan = nullptr;
+  if (d->batch <= 0 || d->n_in <= 0 || d->n_out <= 0)
+    return fail(DLX_ERR_SHAPE, "xform_plan_create: batch, n_in and n_out must be positive");
+  DLX_TRY(validate_variant(d->variant));
+  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
+  auto* p = new (std::nothrow) dlx_xform_plan_s();
+  if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+  std::vector<DftAxis> ax(d->batch), ay(d->batch);
+  for (int b = 0; b < d->batch; ++b) {
+    ax[b] = to_axis(ax_x[b]);
+    ay[b] = to_axis(ax_y[b]);
+  }
+  const int st = make_two_step(&p->p, d->batch, d->n_in, d->n_out, d->variant, ax, ay);
+  if (st != DLX_OK) {
+    p->p.release();
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return DLX_OK;
+}
+
+int dlx_xform_plan_destroy(dlx_xform_plan plan) {
+  if (!plan) return DLX_OK;
+  cudaDeviceSynchronize();
+  plan->p.release();
+  delete plan;
+  return DLX_OK;
+}
+
+int dlx_xform_forward(dlx_xform_plan plan, const void* in, void* out, void* stream) {
+  if (!plan || !in || !out) return fail(DLX_ERR_ARG, "xform_forward: null pointer");
+  return plan->p.forward(in, out, as_stream(stream));
+}
+
+int dlx_xform_adjoint(dlx_xform_plan plan, const void* gout, void* gin, void* stream) {
+  if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "xform_adjoint: null pointer");
+  return plan->p.adjoint(gout, gin, as_stream(stream));
+}
+
+int dlx_asm_plan_create(const dlx_asm_desc* d, const double* wavelengths_host,
+                        dlx_asm_plan* plan) {
+  if (!d || !wavelengths_host || !plan) return fail(DLX_ERR_ARG, "asm_plan_create: null pointer");
+  *plan = nullptr;
+  const int B = d->batch, N = d->n_in, P = d->n_pad;
+  if (B <= 0 || N <= 0 || P < N)
+    return fail(DLX_ERR_SHAPE, "asm_plan_create: need batch, n_in > 0 and n_pad >= n_in");
+  if (!(d->pixel_scale > 0)) return fail(DLX_ERR_ARG, "asm_plan_create: pixel_scale must be > 0");
+  for (int b = 0; b < B; ++b)
+    if (!(wavelengths_host[b] > 0))
+      return fail(DLX_ERR_ARG, "asm_plan_create: wavelengths must be positive");
+  DLX_TRY(validate_variant(d->variant));
+  DLX_TRY(check_split_shape(d->variant, N, P));
+  auto* p = new (std::nothrow) dlx_asm_plan_s();
+  if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
+  p->P = P;
+  p->df = 1.0 / (P * d->pixel_scale);
+  // Centred transforms (fftshift o fft o ifftshift): index j sits at j - c with
+  // c = floor(P / 2); the input lands at slot i + (P - N) / 2 of the padded grid.
+  const int c = P / 2, npad = (P - N) / 2;
+  DftAxis f{};
+  f.a_in = 1.0; f.b_in = (double)(npad - c);
+  f.a_out = 1.0; f.b_out = -(double)c;
+  f.sigma = -1.0 / P;
+  f.scale = 1.0;
+  DftAxis g{};
+  g.a_in = 1.0; g.b_in = -(double)c;
+  g.a_out = 1.0; g.b_out = -(double)c;
+  g.sigma = 1.0 / P;
+  g.scale = 1.0 / P;
+  std::vector<DftAxis> fa(B, f), ga(B, g);
+  std::vector<double> zl(B), l2(B);
+  for (int b = 0; b < B; ++b) {
+    zl[b] = d->distance / wavelengths_host[b];
+    l2[b] = wavelengths_host[b] * wavelengths_host[b];
+  }
+  int st = make_two_step(&p->fwd, B, N, P, d->variant, fa, fa);
+  if (st == DLX_OK) st = make_two_step(&p->inv, B, P, P, d->variant, ga, ga);
+  if (st == DLX_OK) st = p->spec.alloc(sizeof(float2) * (size_t)B * P * P);
+  if (st == DLX_OK) st = p->zl.alloc(sizeof(double) * B);
+  if (st == DLX_OK) st = p->lam2.alloc(sizeof(double) * B);
+  auto upload = [&](DevBuf& dst, const std::vector<double>& src) {
+    const cudaError_t e =
+        cudaMemcpy(dst.p, src.data(), sizeof(double) * src.size(), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? DLX_OK : check_cuda(e, "cudaMemcpy(asm constants)");
+  };
+  if (st == DLX_OK) st = upload(p->zl, zl);
+  if (st == DLX_OK) st = upload(p->lam2, l2);
+  if (st != DLX_OK) {
+    p->fwd.release(); p->inv.release(); p->spec.release(); p->zl.release(); p->lam2.release();
+    delete p;
+    return st;
+  }
+  *plan = p;
+  return DLX_OK;
+}
+
+int dlx_asm_plan_destroy(dlx_asm_plan plan) {
+  if (!plan) return DLX_OK;
+  cudaDeviceSynchronize();
+  plan->fwd.release(); plan->inv.release(); plan->spec.release(); plan->zl.release();
+  plan->lam2.release();
+  delete plan;
+  return DLX_OK;
+}
+
+int dlx_asm_forward(dlx_asm_plan plan, const void* in, void* out, void* stream) {
+  if (!plan || !in || !out) return fail(DLX_ERR_ARG, "asm_forward: null pointer");
+  cudaStream_t s = as_stream(stream);
+  DLX_TRY(plan->fwd.forward(in, plan->spec.p, s));
+  DLX_TRY(launch_asm_transfer(plan->spec.as<float2>(), plan->fwd.ts.batch, plan->P, plan->df,
+                              plan->zl.as<double>(), plan->lam2.as<double>(), 0, s));
+  return plan->inv.forward(plan->spec.p, out, s);
+}
+
+int dlx_asm_adjoint(dlx_asm_plan plan, const void* gout, void* gin, void* stream) {
+  if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "asm_adjoint: null pointer");
+  cudaStream_t s = as_stream(stream);
+  DLX_TRY(plan->inv.adjoint(gout, plan->spec.p, s));
+  DLX_TRY(launch_asm_transfer(plan->spec.as<float2>(), plan->fwd.ts.batch, plan->P, plan->df,
+                              plan->zl.as<double>(), plan->lam2.as<double>(), 1, s));
+  return plan->fwd.adjoint(plan->spec.p, gin, s);
+}
+
+}  // extern "C"

@@ -804,3 +804,49 @@ int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s) {
 }
 
 }  // namespace dlx
+
+namespace dlx {
+
+// ---------------------------------------------------------------------------
+// Angular-spectrum transfer function (the ASM propagator of dLux's
+// layers/abcd_propagators.py:380-459): the centred spectrum F[b][ky][kx] of a
+// field sampled at dx is multiplied by
+//   H = exp(2 pi i z sqrt(1/lambda^2 - fx^2 - fy^2))      (propagating waves)
+//   H = exp(-2 pi z sqrt(fx^2 + fy^2 - 1/lambda^2))        (evanescent waves)
+// with f = (k - floor(P/2)) / (P dx). The phase z/lambda sqrt(1 - lambda^2 f^2)
+// is formed and reduced in FP64 (it reaches ~1e6 cycles at z = 1 m); conj = 1
+// applies conj(H), the adjoint.
+// ---------------------------------------------------------------------------
+__global__ void asm_transfer_kernel(float2* __restrict__ f, int P, double df,
+                                    const double* __restrict__ zl,
+                                    const double* __restrict__ lam2, int conj) {
+  const long long npix = (long long)P * P;
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (p >= npix) return;
+  const int ky = (int)(p / P);
+  const int kx = (int)(p - (long long)ky * P);
+  const int c = P / 2;
+  const double fx = (kx - c) * df, fy = (ky - c) * df;
+  const double s = lam2[b] * (fx * fx + fy * fy);
+  float2 h;
+  if (s <= 1.0) {
+    h = cis_cycles(zl[b] * sqrt(1.0 - s));
+    if (conj) h.y = -h.y;
+  } else {
+    h = make_float2((float)exp(-2.0 * CUDART_PI * zl[b] * sqrt(s - 1.0)), 0.0f);
+  }
+  float2* q = f + (long long)b * npix + p;
+  *q = cmul(*q, h);
+}
+
+int launch_asm_transfer(float2* spec, int batch, int P, double df, const double* zl,
+                        const double* lam2, int conj, cudaStream_t s) {
+  if (batch <= 0 || P <= 0) return DLX_OK;
+  dim3 grid(ceil_div((long long)P * P, 256), batch);
+  asm_transfer_kernel<<<grid, 256, 0, s>>>(spec, P, df, zl, lam2, conj);
+  DLX_LAUNCH_CHECK("asm_transfer_kernel");
+  return DLX_OK;
+}
+
+}  // namespace dlx

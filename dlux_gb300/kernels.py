@@ -183,6 +183,93 @@ class MFTPlan(_Plan):
         return out
 
 
+class XformPlan(_Plan):
+    """Separable transform out = A_y in A_x^T with generated matrices whose axes
+    carry affine and quadratic phase terms (the linear canonical transform of
+    an ABCD system): the device side of dLux's MFTPropagator/FFTPropagator
+    (layers/abcd_propagators.py:245-370).
+
+    ``axes_x`` / ``axes_y``: one dict per batch element with keys a_in, b_in,
+    a_out, b_out, sigma, q_in, q_out, phase, scale (see dlx_xform_axis)."""
+
+    _destroy = "dlx_xform_plan_destroy"
+
+    def __init__(self, axes_x, axes_y, n_in, n_out, variant=None):
+        super().__init__()
+        _lib.require_cuda()
+        self.batch = len(axes_x)
+        if len(axes_y) != self.batch or self.batch == 0:
+            raise ValueError("axes_x and axes_y need the same, non-zero length")
+        self.n_in, self.n_out = int(n_in), int(n_out)
+        self.variant = resolve_variant(self.n_in, self.n_out, variant)
+        arr = _lib.XformAxis * self.batch
+        ax = arr(*[_lib.XformAxis(**{k: float(v) for k, v in a.items()}) for a in axes_x])
+        ay = arr(*[_lib.XformAxis(**{k: float(v) for k, v in a.items()}) for a in axes_y])
+        d = _lib.XformDesc(self.batch, self.n_in, self.n_out, self.variant)
+        call("dlx_xform_plan_create", ctypes.byref(d), ctypes.cast(ax, ctypes.c_void_p),
+             ctypes.cast(ay, ctypes.c_void_p), ctypes.byref(self.handle))
+
+    def forward(self, phasor):
+        x = phasor.reshape(self.batch, self.n_in, self.n_in).contiguous()
+        out = torch.empty((self.batch, self.n_out, self.n_out), dtype=torch.complex64,
+                          device=x.device)
+        call("dlx_xform_forward", self.handle, ptr(x), ptr(out), _stream())
+        return out
+
+    def adjoint(self, gout):
+        g = gout.reshape(self.batch, self.n_out, self.n_out).contiguous()
+        out = torch.empty((self.batch, self.n_in, self.n_in), dtype=torch.complex64,
+                          device=g.device)
+        call("dlx_xform_adjoint", self.handle, ptr(g), ptr(out), _stream())
+        return out
+
+
+class ASMPlan(_Plan):
+    """Angular-spectrum propagation over ``distance`` of fields padded from n_in
+    to n_pad pixels (the ASMPropagator of layers/abcd_propagators.py:380-459)."""
+
+    _destroy = "dlx_asm_plan_destroy"
+
+    def __init__(self, wavelengths, n_in, n_pad, pixel_scale, distance, variant=None):
+        super().__init__()
+        _lib.require_cuda()
+        self.wavelengths = tuple(float(w) for w in wavelengths)
+        self.n_in, self.n_pad = int(n_in), int(n_pad)
+        self.variant = resolve_variant(self.n_in, self.n_pad, variant)
+        d = _lib.AsmDesc(len(self.wavelengths), self.n_in, self.n_pad, float(pixel_scale),
+                         float(distance), self.variant)
+        call("dlx_asm_plan_create", ctypes.byref(d), _lib.dbl_array(self.wavelengths),
+             ctypes.byref(self.handle))
+
+    def forward(self, phasor):
+        b = len(self.wavelengths)
+        x = phasor.reshape(b, self.n_in, self.n_in).contiguous()
+        out = torch.empty((b, self.n_pad, self.n_pad), dtype=torch.complex64, device=x.device)
+        call("dlx_asm_forward", self.handle, ptr(x), ptr(out), _stream())
+        return out
+
+    def adjoint(self, gout):
+        b = len(self.wavelengths)
+        g = gout.reshape(b, self.n_pad, self.n_pad).contiguous()
+        out = torch.empty((b, self.n_in, self.n_in), dtype=torch.complex64, device=g.device)
+        call("dlx_asm_adjoint", self.handle, ptr(g), ptr(out), _stream())
+        return out
+
+
+def get_xform_plan(axes_x, axes_y, n_in, n_out, variant=None):
+    key = ("xform", tuple(tuple(sorted(a.items())) for a in axes_x),
+           tuple(tuple(sorted(a.items())) for a in axes_y), int(n_in), int(n_out),
+           resolve_variant(int(n_in), int(n_out), variant))
+    return xform_plans.get(key, lambda: XformPlan(axes_x, axes_y, n_in, n_out, variant))
+
+
+def get_asm_plan(wavelengths, n_in, n_pad, pixel_scale, distance, variant=None):
+    key = ("asm", tuple(float(w) for w in wavelengths), int(n_in), int(n_pad),
+           float(pixel_scale), float(distance), resolve_variant(int(n_in), int(n_pad), variant))
+    return xform_plans.get(key, lambda: ASMPlan(wavelengths, n_in, n_pad, pixel_scale,
+                                                distance, variant))
+
+
 # pad * N from which the padded FFT runs as radix-2 line FFTs instead of the
 # DFT-GEMM pair, whose cost grows as P^2 N. Measured forward + adjoint of 16
 # wavelengths: P = 1024 0.54 ms (split-BF16 GEMM) vs 0.70 ms (radix); P = 2048
@@ -491,6 +578,7 @@ mft_plans = _PlanCache(16)
 fft_plans = _PlanCache(8)
 poly_plans = _PlanCache(8)
 scene_plans = _PlanCache(4)
+xform_plans = _PlanCache(8)  # ABCD propagators: LCT transforms and ASM plans
 
 
 def get_mft_plan(wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out, focal_length=None,

@@ -308,6 +308,62 @@ int dlx_poly_plan_footprint(dlx_poly_plan plan, size_t* bytes);
 int dlx_poly_plan_info(dlx_poly_plan plan, int* n_wavelengths, int* n_in, int* n_out,
                        int* max_objects);
 
+/* ---- f4: ABCD propagators -------------------------------------------------
+ * Device side of dLux's MFTPropagator, FFTPropagator and ASMPropagator
+ * (layers/abcd_propagators.py:245-459). The reference takes their arithmetic
+ * from the abcdLux package (lct.lct_prop, lct.lct_prop_fft, asm.asm_prop;
+ * pyproject.toml:21 "abcdLux>=0.0.2", not vendored), restated here from the
+ * published linear canonical transform and angular-spectrum method.
+ *
+ * Separable transform: out[b] = A_y[b] in[b] A_x[b]^T with generated
+ * matrices, element (j, i) of an axis being
+ *   scale * exp(2 pi i [sigma x_i u_j + q_in x_i^2 + q_out u_j^2 + phase]),
+ *   x_i = a_in i + b_in,  u_j = a_out j + b_out      (all FP64 at creation).
+ * The LCT of an ABCD system (Collins integral) per axis is sigma = -1/(lambda B),
+ * q_in = A/(2 lambda B), q_out = D/(2 lambda B), phase = -sign(B)/8 and
+ * scale = dx/sqrt(lambda |B|). Same forms and split-BF16 tensor-core GEMMs as
+ * the MFT plan. */
+typedef struct {
+  double a_in, b_in;    /* input coordinate x_i = a_in * i + b_in */
+  double a_out, b_out;  /* output coordinate u_j = a_out * j + b_out */
+  double sigma;         /* cycles per x * u */
+  double q_in, q_out;   /* cycles per x^2 and per u^2 */
+  double phase;         /* constant phase, cycles */
+  double scale;         /* real factor */
+} dlx_xform_axis;
+typedef struct {
+  int batch, n_in, n_out;
+  int variant;          /* DLX_VARIANT_FP32 or DLX_VARIANT_SPLIT_BF16 */
+} dlx_xform_desc;
+typedef struct dlx_xform_plan_s* dlx_xform_plan;
+/* ax_x, ax_y: host arrays of batch axes each. */
+int dlx_xform_plan_create(const dlx_xform_desc* desc, const dlx_xform_axis* ax_x,
+                          const dlx_xform_axis* ax_y, dlx_xform_plan* plan);
+int dlx_xform_plan_destroy(dlx_xform_plan plan);
+/* in [batch][n_in][n_in] c64 -> out [batch][n_out][n_out] c64, and its adjoint. */
+int dlx_xform_forward(dlx_xform_plan plan, const void* in_c64, void* out_c64, void* stream);
+int dlx_xform_adjoint(dlx_xform_plan plan, const void* gout_c64, void* gin_c64, void* stream);
+
+/* Angular-spectrum propagation over `distance` (asm.asm_prop, called at
+ * layers/abcd_propagators.py:442-449): the field is zero-padded (centred) from
+ * n_in to n_pad pixels, transformed by a centred DFT, multiplied by
+ * exp(2 pi i z sqrt(1/lambda^2 - fx^2 - fy^2)) (evanescent components decay
+ * as exp(-2 pi z sqrt(f^2 - 1/lambda^2))) and transformed back; the output
+ * keeps the pixel scale. The phase is formed in FP64 on the device. */
+typedef struct {
+  int batch, n_in, n_pad;
+  double pixel_scale;   /* m */
+  double distance;      /* m */
+  int variant;
+} dlx_asm_desc;
+typedef struct dlx_asm_plan_s* dlx_asm_plan;
+int dlx_asm_plan_create(const dlx_asm_desc* desc, const double* wavelengths_host,
+                        dlx_asm_plan* plan);
+int dlx_asm_plan_destroy(dlx_asm_plan plan);
+/* in [batch][n_in][n_in] c64 -> out [batch][n_pad][n_pad] c64, and its adjoint. */
+int dlx_asm_forward(dlx_asm_plan plan, const void* in_c64, void* out_c64, void* stream);
+int dlx_asm_adjoint(dlx_asm_plan plan, const void* gout_c64, void* gin_c64, void* stream);
+
 /* ---- a12: dynamic aberrated circular aperture ----------------------------
  * Replaces AberratedAperture over a CircularAperture (layers/apertures.py:
  * 240-312, 643-800): the soft-edged transmission (utils/geometry.py:49-91,

@@ -42,6 +42,13 @@ __all__ = [
     "poly_psf",
     "poly_psf_fields",
     "poly_psf_grad",
+    "abcd_free_space",
+    "abcd_lens",
+    "abcd_mirror",
+    "abcd_fraunhofer",
+    "compose_abcd",
+    "lct_direct",
+    "asm_prop",
 ]
 
 
@@ -637,3 +644,81 @@ def poly_psf_grad(amplitude, opd, wavelengths, weights, diameter, psf_npixels_os
         g_amp += (rt(np.sqrt(w)) * np.conj(u) * Ebar).real
         g_w.append(inner.real.sum() / (2.0 * w))
     return {"g_opd": g_opd, "g_phase": g_phase, "g_amp": g_amp, "g_w": np.array(g_w)}
+
+
+# --------------------------------------------------------------------------
+# ABCD propagators: layers/abcd_propagators.py:1-491. Their arithmetic is in
+# the abcdLux package (pyproject.toml:21, "abcdLux>=0.0.2"; abcd.*, lct.lct_prop,
+# lct.lct_prop_fft, asm.asm_prop), which is not vendored with the reference
+# and has no pinned version, so these restate the published methods: ray-
+# transfer matrices, Collins' diffraction integral (the linear canonical
+# transform) and the angular-spectrum method. The reference's own tests
+# (tests/layers/test_abcd_propagators.py) pin shapes and errors only: parity
+# of values is unpinned.
+# --------------------------------------------------------------------------
+def abcd_free_space(distance):
+    """Free space over `distance` (abcd_propagators.py:36-66 -> abcd.abcd_free_space)."""
+    return np.array([[1.0, float(distance)], [0.0, 1.0]])
+
+
+def abcd_lens(focal_length):
+    """Thin lens (abcd_propagators.py:69-103 -> abcd.abcd_lens)."""
+    return np.array([[1.0, 0.0], [-1.0 / float(focal_length), 1.0]])
+
+
+def abcd_mirror(radius):
+    """Curved mirror of radius R (abcd_propagators.py:106-136 -> abcd.abcd_mirror)."""
+    return np.array([[1.0, 0.0], [-2.0 / float(radius), 1.0]])
+
+
+def abcd_fraunhofer(focal_length):
+    """Front-to-back focal-plane system (abcd_propagators.py:139-173 -> abcd.abcd_fraunhofer)."""
+    f = float(focal_length)
+    return np.array([[0.0, f], [-1.0 / f, 0.0]])
+
+
+def compose_abcd(matrices):
+    """Elements applied in order compose as M_n ... M_1 (abcd_propagators.py:236-245)."""
+    out = np.eye(2)
+    for m in matrices:
+        out = np.asarray(m, np.float64) @ out
+    return out
+
+
+def _lct_matrix(xs_in, xs_out, wavelength, M):
+    A, B, D = float(M[0, 0]), float(M[0, 1]), float(M[1, 1])
+    lb = float(wavelength) * B
+    dx = float(xs_in[1] - xs_in[0]) if len(xs_in) > 1 else 1.0
+    x = np.asarray(xs_in, np.float64)[None, :]
+    u = np.asarray(xs_out, np.float64)[:, None]
+    phase = (A * x * x - 2.0 * x * u + D * u * u) / (2.0 * lb)  # cycles
+    return np.exp(2j * np.pi * phase) * dx / np.sqrt(1j * lb)
+
+
+def lct_direct(u, xs_in, xs_out, wavelength, M):
+    """Collins integral of an ABCD system on explicit grids (MFTPropagator,
+    abcd_propagators.py:248-300 -> lct.lct_prop), both axes:
+    u_out(x', y') = (i lambda B)^-1 sum u(x, y) exp(i pi / (lambda B) *
+    (A (x^2 + y^2) - 2 (x x' + y y') + D (x'^2 + y'^2))) dx dy, in FP64."""
+    K = _lct_matrix(xs_in, xs_out, wavelength, M)
+    return K @ np.asarray(u, np.complex128) @ K.T
+
+
+def asm_prop(u, pixel_scale, wavelength, distance, n_pad):
+    """Angular-spectrum propagation (ASMPropagator, abcd_propagators.py:380-459
+    -> asm.asm_prop): centred zero padding to n_pad, centred FFT, transfer
+    function exp(2 pi i z sqrt(1/lambda^2 - f^2)) with evanescent decay,
+    inverse FFT; same pixel scale. FP64."""
+    u = np.asarray(u, np.complex128)
+    n = u.shape[-1]
+    lo = (n_pad - n) // 2
+    up = np.zeros((n_pad, n_pad), np.complex128)
+    up[lo:lo + n, lo:lo + n] = u
+    U = np.fft.fftshift(np.fft.fft2(np.fft.ifftshift(up)))
+    f = (np.arange(n_pad) - n_pad // 2) / (n_pad * float(pixel_scale))
+    s = float(wavelength) ** 2 * (f[None, :] ** 2 + f[:, None] ** 2)
+    zl = float(distance) / float(wavelength)
+    prop = s <= 1.0
+    H = np.where(prop, np.exp(2j * np.pi * zl * np.sqrt(np.where(prop, 1.0 - s, 0.0))),
+                 np.exp(-2.0 * np.pi * zl * np.sqrt(np.where(prop, 0.0, s - 1.0))))
+    return np.fft.fftshift(np.fft.ifft2(np.fft.ifftshift(U * H)))
