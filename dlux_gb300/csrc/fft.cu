@@ -92,8 +92,50 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
     x[smem_slot<LPB>(li, k, sh, P)] = v;
   }
   __syncthreads();
-  const int hp = log2p - 1;  // P / 2 = 1 << hp butterflies per line
-  for (int s = 1; s <= log2p; ++s) {
+  // Butterfly stages two at a time (radix-4 passes): the four elements
+  // k0 + {0, h, 2h, 3h} of stages s (half-length h) and s + 1 (2h) stay in
+  // registers between the stages, so each pass reads and writes shared memory
+  // once. Same butterflies and twiddles, in the same order, as two radix-2
+  // stages. An odd stage count ends with one radix-2 stage.
+  int s = 1;
+  if (log2p >= 2) {
+    const int qp = log2p - 2;  // P / 4 = 1 << qp quads per line
+    for (; s + 1 <= log2p; s += 2) {
+      const int h = 1 << (s - 1);
+      for (int t = threadIdx.x; t < LPB * (P / 4); t += blockDim.x) {
+        const int li = t >> qp;
+        const int i = t & ((P / 4) - 1);
+        const int grp = i >> (s - 1);
+        const int pos = i & (h - 1);
+        const int k0 = (grp << (s + 1)) + pos;
+        const int i0 = smem_slot<LPB>(li, k0, sh, P);
+        const int i1 = smem_slot<LPB>(li, k0 + h, sh, P);
+        const int i2 = smem_slot<LPB>(li, k0 + 2 * h, sh, P);
+        const int i3 = smem_slot<LPB>(li, k0 + 3 * h, sh, P);
+        const float2 w1 = tw[h - 1 + pos];
+        const float2 w2 = tw[2 * h - 1 + pos];
+        const float2 w3 = tw[2 * h - 1 + pos + h];
+        const float2 a0 = x[i0], a1 = x[i1], a2 = x[i2], a3 = x[i3];
+        // stage s: (k0, k0 + h) and (k0 + 2h, k0 + 3h), twiddle w1
+        float2 v = cmul(a1, w1);
+        const float2 b0 = make_float2(a0.x + v.x, a0.y + v.y);
+        const float2 b1 = make_float2(a0.x - v.x, a0.y - v.y);
+        v = cmul(a3, w1);
+        const float2 b2 = make_float2(a2.x + v.x, a2.y + v.y);
+        const float2 b3 = make_float2(a2.x - v.x, a2.y - v.y);
+        // stage s + 1: (k0, k0 + 2h) with w2 and (k0 + h, k0 + 3h) with w3
+        v = cmul(b2, w2);
+        x[i0] = make_float2(b0.x + v.x, b0.y + v.y);
+        x[i2] = make_float2(b0.x - v.x, b0.y - v.y);
+        v = cmul(b3, w3);
+        x[i1] = make_float2(b1.x + v.x, b1.y + v.y);
+        x[i3] = make_float2(b1.x - v.x, b1.y - v.y);
+      }
+      __syncthreads();
+    }
+  }
+  if (s == log2p) {
+    const int hp = log2p - 1;  // P / 2 = 1 << hp butterflies per line
     const int half = 1 << (s - 1);
     for (int t = threadIdx.x; t < LPB * (P / 2); t += blockDim.x) {
       const int li = t >> hp;
