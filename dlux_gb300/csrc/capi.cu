@@ -783,7 +783,14 @@ struct dlx_poly_plan_s {
   DevBuf planes;     // intensity [L*R][M][M] f32, or pre/pim [2][L*R][N][N] f32
   DevBuf partial;    // double reduction partials
   DevBuf pathff;     // [R][N][N] float4 (path, phase) pairs, then [R][3][N][N] pixel sums
+  DevBuf splitws;    // split-K partial sums of the GEMMs that split (see split_k)
   int nparts = kPolyParts;
+  // Split K for GEMMs whose tiles leave most SMs idle, decided from the
+  // plan's capacity (wavelengths x max_objects), not from the call's object
+  // count, so an object's result is the same alone and in a batch of the
+  // plan. Plans on a shared workspace (serving buckets, which fill the GPU by
+  // batching requests) do not split.
+  bool split_k = false;
   // Forward-to-backward reuse (dlx_poly_forward_token / dlx_poly_reuse_forward):
   // after a single-chunk forward, `field`, `mid` (the first-stage product D1)
   // and `pathff` hold that forward's state until the next call on the plan.
@@ -807,11 +814,12 @@ struct dlx_poly_plan_s {
   // Device bytes this plan owns: an attached workspace belongs to the caller.
   size_t footprint() const {
     return ts.footprint() + field.owned_bytes() + mid.owned_bytes() + fbar.owned_bytes() +
-           planes.owned_bytes() + partial.owned_bytes() + pathff.owned_bytes();
+           planes.owned_bytes() + partial.owned_bytes() + pathff.owned_bytes() +
+           splitws.owned_bytes();
   }
   void release() {
     ts.release(); field.release(); mid.release(); fbar.release(); planes.release();
-    partial.release(); pathff.release();
+    partial.release(); pathff.release(); splitws.release();
   }
 
   static void tables(const dlx_poly_object* objs, int n, ObjTable* t, OutTable* o) {
@@ -846,6 +854,14 @@ struct dlx_poly_plan_s {
     GemmArgs g = gemm_for(ts.variant, ts.batch * R, M, N, K, op, conj, B, e);
     g.a_batch_div = R;
     g.a_bs = (long long)M * K;
+    if (split_k && op.mat) {
+      const long long tiles = (long long)ts.batch * max_obj * ((M + 127) / 128) * ((N + 127) / 128);
+      const int sk = split_k_count(tiles, K);
+      if (sk > 1) {
+        g.splits = sk;
+        g.split_ws = splitws.as<float2>();
+      }
+    }
     return g;
   }
 
@@ -1008,9 +1024,11 @@ struct dlx_poly_plan_s {
   }
 };
 
-// Byte sizes of the per-call buffers of a plan: field, mid, fbar, planes, partial, pathff.
-constexpr int kPolyBuffers = 6;
-static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[kPolyBuffers]) {
+// Byte sizes of the per-call buffers of a plan: field, mid, fbar, planes,
+// partial, pathff and the split-K partials (split_on: the plan splits K).
+constexpr int kPolyBuffers = 7;
+static void poly_ws_sizes(int L, int N, int M, int R, int nparts, bool split_on,
+                          size_t sz[kPolyBuffers]) {
   const size_t lr = (size_t)L * R, n = N, m = M;
   sz[0] = lr * n * n * 8;
   sz[1] = lr * n * m * 8;
@@ -1019,7 +1037,23 @@ static void poly_ws_sizes(int L, int N, int M, int R, int nparts, size_t sz[kPol
   sz[3] = a > b ? a : b;
   sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
   sz[5] = (sizeof(float4) + 3 * sizeof(float)) * (size_t)R * n * n;  // (path, phase) + pixel sums
+  sz[6] = 0;
+  if (split_on) {
+    // the four GEMM shapes of a plan: rows x cols, inner size
+    const int shapes[4][3] = {{M, N, N}, {M, M, N}, {N, M, M}, {N, N, M}};
+    for (const auto& sh : shapes) {
+      const long long tiles = (long long)lr * ((sh[0] + 127) / 128) * ((sh[1] + 127) / 128);
+      const size_t bytes = split_k_bytes(split_k_count(tiles, sh[2]), (long long)lr, sh[0], sh[1]);
+      if (bytes > sz[6]) sz[6] = bytes;
+    }
+  }
   for (int i = 0; i < kPolyBuffers; ++i) sz[i] = (sz[i] + 255) / 256 * 256;
+}
+
+// Plans of the tensor-core form with cached operands split K where their
+// GEMMs leave most SMs idle (read once, at creation).
+static bool poly_split_on(const dlx_poly_desc& d) {
+  return d.variant == DLX_VARIANT_SPLIT_BF16 && d.operand_mode == 0 && split_k_enabled();
 }
 
 static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects,
@@ -1060,15 +1094,17 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
     return fail(DLX_ERR_ARG, "poly_plan_create: operand_mode must be 0 or 1");
   }
   int st = ts.build(ax, ax, alphas, d->operand_mode == 1);
+  p->split_k = own_workspace && poly_split_on(*d);
   if (st == DLX_OK && own_workspace) {
     size_t sz[kPolyBuffers];
-    poly_ws_sizes(L, N, M, max_objects, p->nparts, sz);
+    poly_ws_sizes(L, N, M, max_objects, p->nparts, p->split_k, sz);
     if (st == DLX_OK) st = p->field.alloc(sz[0]);
     if (st == DLX_OK) st = p->mid.alloc(sz[1]);
     if (st == DLX_OK) st = p->fbar.alloc(sz[2]);
     if (st == DLX_OK) st = p->planes.alloc(sz[3]);
     if (st == DLX_OK) st = p->partial.alloc(sz[4]);
     if (st == DLX_OK) st = p->pathff.alloc(sz[5]);
+    if (st == DLX_OK) st = p->splitws.alloc(sz[6]);
   }
   if (st != DLX_OK) {
     p->release();
@@ -1100,7 +1136,7 @@ int dlx_poly_workspace_bytes(const dlx_poly_desc* d, int max_objects, size_t* by
   if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0 || max_objects <= 0)
     return fail(DLX_ERR_SHAPE, "poly_workspace_bytes: sizes must be positive");
   size_t sz[kPolyBuffers];
-  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, kPolyParts, sz);
+  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, kPolyParts, false, sz);
   *bytes = 0;
   for (int i = 0; i < kPolyBuffers; ++i) *bytes += sz[i];
   return DLX_OK;
@@ -1112,7 +1148,8 @@ int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes)
   if ((uintptr_t)workspace % 256 != 0)
     return fail(DLX_ERR_ARG, "poly_attach_workspace: workspace must be 256-byte aligned");
   size_t sz[kPolyBuffers];
-  poly_ws_sizes(plan->ts.batch, plan->ts.n_in, plan->ts.n_out, plan->max_obj, plan->nparts, sz);
+  poly_ws_sizes(plan->ts.batch, plan->ts.n_in, plan->ts.n_out, plan->max_obj, plan->nparts,
+                plan->split_k, sz);
   size_t need = 0;
   for (int i = 0; i < kPolyBuffers; ++i) need += sz[i];
   if (bytes < need)
@@ -1130,6 +1167,8 @@ int dlx_poly_attach_workspace(dlx_poly_plan plan, void* workspace, size_t bytes)
   plan->partial.view(w, sz[4]);
   w += sz[4];
   plan->pathff.view(w, sz[5]);
+  w += sz[5];
+  plan->splitws.view(w, sz[6]);
   return DLX_OK;
 }
 

@@ -43,6 +43,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "epilogue.cuh"
@@ -281,11 +282,30 @@ __device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b) 
 struct TcParams {
   int batch, M, N, K;
   int a_batch_div, b_batch_div;
-  int mt, nt, total;
+  int mt, nt, total;   // total = batch * mt * nt * splits work items
+  int splits, kbps;    // split K: each work item covers kbps K blocks of one tile
   int conj_a;
   int* status;
   EpiArgs epi;
 };
+
+// Work item w of the loaded kernel: split ks of output tile (b, mt, nt), K
+// blocks [kb0, kb1). Every role decodes it the same way.
+struct TcWork {
+  int b, mt, nt, ks, kb0, kb1;
+};
+__device__ __forceinline__ TcWork tc_work(const TcParams& p, int w, int nkb) {
+  TcWork t;
+  t.ks = w % p.splits;
+  const int wt = w / p.splits;
+  t.b = wt / (p.mt * p.nt);
+  const int r = wt - t.b * p.mt * p.nt;
+  t.mt = r / p.nt;
+  t.nt = r - t.mt * p.nt;
+  t.kb0 = t.ks * p.kbps;
+  t.kb1 = min(nkb, t.kb0 + p.kbps);
+  return t;
+}
 
 template <int KIND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -335,11 +355,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       uint32_t issued_mask = 0, issued_ph = 0;
       bool ok = true;
       for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
-        const int b = w / (p.mt * p.nt);
-        const int r = w - b * p.mt * p.nt;
-        const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
+        const TcWork t = tc_work(p, w, nkb);
+        const int b = t.b, mt = t.mt, nt = t.nt;
         const int ab = b / p.a_batch_div;
-        for (int kb = 0; kb < nkb; ++kb) {
+        for (int kb = t.kb0; kb < t.kb1; ++kb) {
           if (!mbar_wait(&empty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
           mbar_expect_tx(&full[stage], STAGE_BYTES);
           uint8_t* base = smem + stage * STAGE_BYTES;
@@ -378,9 +397,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       uint32_t ph = 0, acc_ph = 0;
       bool ok = true;
       for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
+        const TcWork t = tc_work(p, w, nkb);
         if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
         tc_fence_after();
-        for (int kb = 0; kb < nkb; ++kb) {
+        for (int kb = t.kb0; kb < t.kb1; ++kb) {
           if (!mbar_wait(&full[stage], ph, abort_flag, p.status)) { ok = false; break; }
           tc_fence_after();
           const uint32_t sa = smem_u32(smem + stage * STAGE_BYTES);
@@ -396,7 +416,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint64_t brl = make_desc(sb + 1 * B_PLANE_BYTES + ko);
             const uint64_t bih = make_desc(sb + 2 * B_PLANE_BYTES + ko);
             const uint64_t bil = make_desc(sb + 3 * B_PLANE_BYTES + ko);
-            const uint32_t acc = (kb > 0 || j > 0) ? 1u : 0u;
+            const uint32_t acc = (kb > t.kb0 || j > 0) ? 1u : 0u;
             // Re += Ar Br -/+ Ai Bi
             mma_bf16(m_re, brh, arh, id_pos, acc);
             mma_bf16(m_re, bih, aih, id_rii, 1u);
@@ -435,9 +455,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
       if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
       tc_fence_after();
-      const int b = w / (p.mt * p.nt);
-      const int r = w - b * p.mt * p.nt;
-      const int mt = r / p.nt, nt = r - (r / p.nt) * p.nt;
+      const TcWork t = tc_work(p, w, nkb);
+      const int b = t.b, mt = t.mt, nt = t.nt;
       const int n = nt * TC_BN + q * 32 + lane;
       const int mbase = mt * TC_BM;
       const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16);
@@ -459,8 +478,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(tempty);
       if (n < p.N) {
-        if (has0) epi_col32<KIND>(p.epi, b, n, mbase + c0 * 32, p.M, p.N, re0, im0);
-        if (has1) epi_col32<KIND>(p.epi, b, n, mbase + c1 * 32, p.M, p.N, re1, im1);
+        if constexpr (KIND == EPI_PARTIAL) {
+          // raw partial sums of split t.ks, one column per thread
+          float2* o = p.epi.partial + ((long long)t.ks * p.batch + b) * p.M * p.N + n;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int m0 = mbase + c0 * 32 + j, m1 = mbase + c1 * 32 + j;
+            if (has0 && m0 < p.M) o[(long long)m0 * p.N] = make_float2(re0[j], im0[j]);
+            if (has1 && m1 < p.M) o[(long long)m1 * p.N] = make_float2(re1[j], im1[j]);
+          }
+        } else {
+          if (has0) epi_col32<KIND>(p.epi, b, n, mbase + c0 * 32, p.M, p.N, re0, im0);
+          if (has1) epi_col32<KIND>(p.epi, b, n, mbase + c1 * 32, p.M, p.N, re1, im1);
+        }
       }
       acc_ph ^= 1u;
     }
@@ -781,6 +811,7 @@ LoadedKernel loaded_kernel(int kind) {
     case EPI_PSF_GRADF: return tc_cgemm_kernel<EPI_PSF_GRADF>;
     case EPI_SPLIT2: return tc_cgemm_kernel<EPI_SPLIT2>;
     case EPI_DOT: return tc_cgemm_kernel<EPI_DOT>;
+    case EPI_PARTIAL: return tc_cgemm_kernel<EPI_PARTIAL>;
     default: return nullptr;
   }
 }
@@ -791,9 +822,30 @@ const void* const* loaded_kernels() {
       (const void*)tc_cgemm_kernel<EPI_INTENSITY>, (const void*)tc_cgemm_kernel<EPI_GRADF>,
       (const void*)tc_cgemm_kernel<EPI_PUPIL>,     (const void*)tc_cgemm_kernel<EPI_PSF_GRADF>,
       (const void*)tc_cgemm_kernel<EPI_SPLIT2>,    (const void*)tc_cgemm_kernel<EPI_DOT>,
-      nullptr};
+      (const void*)tc_cgemm_kernel<EPI_PARTIAL>,   nullptr};
   return all;
 }
+// Split-K reduction: D = sum of the partials in split order, then the GEMM's
+// own epilogue element by element (the FP32 form's epilogue code).
+__global__ void splitk_reduce_kernel(const float2* __restrict__ part, int splits, int batch,
+                                     int M, int N, const EpiArgs e) {
+  const long long total = (long long)batch * M * N;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  float2 v = part[i];
+  for (int s = 1; s < splits; ++s) {
+    const float2 q = part[(long long)s * total + i];
+    v.x += q.x;
+    v.y += q.y;
+  }
+  const long long mn = (long long)M * N;
+  const int b = (int)(i / mn);
+  const long long r = i - (long long)b * mn;
+  const int m = (int)(r / N);
+  const int n = (int)(r - (long long)m * N);
+  epi_apply(e, b, m, n, M, N, v);
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
 int g_cc = 0;
@@ -875,6 +927,30 @@ bool tc_supported() {
   return g_init_status == DLX_OK && g_cc == 103;
 }
 
+// Split K (see GemmArgs::splits). Creation-time switch for plans made after
+// the call (dlx_set_split_k); on by default.
+std::atomic<int> g_split_k_enabled{1};
+bool split_k_enabled() { return g_split_k_enabled.load() != 0; }
+
+int split_k_count(long long tiles, int K) {
+  std::call_once(g_once, init_once);
+  if (g_init_status != DLX_OK || g_cc != 103 || tiles <= 0) return 1;
+  const int nkb = (K + TC_BK - 1) / TC_BK;
+  if (nkb < 2 || tiles * 2 > g_num_sms) return 1;  // half the SMs or more are busy already
+  long long s = g_num_sms / tiles;
+  if (s > 8) s = 8;
+  if (s > nkb) s = nkb;
+  if (s < 2) return 1;
+  // the count the launch will use: every split gets at least one K block
+  const int kbps = (nkb + (int)s - 1) / (int)s;
+  return (nkb + kbps - 1) / kbps;
+}
+
+size_t split_k_bytes(int splits, long long batch, int M, int N) {
+  if (splits <= 1) return 0;
+  return (size_t)splits * (size_t)batch * (size_t)M * (size_t)N * sizeof(float2);
+}
+
 int* tc_status_word() {
   std::call_once(g_once, init_once);
   return g_status;
@@ -921,19 +997,42 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   p.b_batch_div = bdiv;
   p.mt = (g.M + TC_BM - 1) / TC_BM;
   p.nt = (g.N + TC_BN - 1) / TC_BN;
-  p.total = g.batch * p.mt * p.nt;
+  const int nkb = (g.K + TC_BK - 1) / TC_BK;
+  p.splits = 1;
+  p.kbps = nkb;
+  const bool split = g.splits > 1 && g.split_ws != nullptr && nkb > 1;
+  if (split) {
+    p.kbps = (nkb + g.splits - 1) / g.splits;
+    p.splits = (nkb + p.kbps - 1) / p.kbps;  // every split gets at least one K block
+  }
+  p.total = g.batch * p.mt * p.nt * p.splits;
   p.conj_a = g.conj_a ? 1 : 0;
   p.status = g_status;
   p.epi = g.epi;
+  if (split) {
+    p.epi.kind = EPI_PARTIAL;
+    p.epi.partial = g.split_ws;
+  }
   const int grid = p.total < g_num_sms ? p.total : g_num_sms;
-  LoadedKernel kern = loaded_kernel(g.epi.kind);
+  LoadedKernel kern = loaded_kernel(p.epi.kind);
   if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
   kern<<<grid, TC_THREADS, SMEM_BYTES, s>>>(ta, tb, p);
   DLX_LAUNCH_CHECK("tc_cgemm_kernel");
+  if (split) {
+    const long long n = (long long)g.batch * g.M * g.N;
+    splitk_reduce_kernel<<<ceil_div(n, 256), 256, 0, s>>>(g.split_ws, p.splits, g.batch, g.M,
+                                                          g.N, g.epi);
+    DLX_LAUNCH_CHECK("splitk_reduce_kernel");
+  }
   return DLX_OK;
 }
 
 }  // namespace dlx
+
+extern "C" int dlx_set_split_k(int enable) {
+  dlx::g_split_k_enabled.store(enable ? 1 : 0);
+  return DLX_OK;
+}
 
 extern "C" int dlx_device_status(void* stream, int* status) {
   using namespace dlx;

@@ -183,6 +183,8 @@ enum EpiKind {
   EPI_PSF_GRADF = 5, // both EPI_INTENSITY (out_f32) and EPI_GRADF (out_split / out_c64)
   EPI_SPLIT2 = 6,    // EPI_SPLIT / EPI_C64, plus the same values times colw[n] into out_*2
   EPI_DOT = 7,       // out_f32 = k_l alpha_l (Fb.im D.re - Fb.re D.im), Fb read from in_*
+  EPI_PARTIAL = 8,   // split K: raw FP32 partial sums [split][b][m][n] (tensor-core form,
+                     // internal: a reduction kernel then applies the GEMM's own epilogue)
 };
 
 struct EpiArgs {
@@ -211,6 +213,7 @@ struct EpiArgs {
   const __nv_bfloat16* in_split;  // EPI_DOT: F-bar [b][4][m][n] (tensor-core form)
   const float2* in_c64;      // EPI_DOT: F-bar [b][m][n] (FP32 form)
   const float* kf;           // EPI_DOT: [wavelength] 2 pi / lambda
+  float2* partial;           // EPI_PARTIAL: [split][b][m][n] FP32 partial sums
   const float2* coltilt;     // nullable [b][n]: phasor multiplying column n of the
                              // EPI_C64 / EPI_SPLIT / EPI_SPLIT2 outputs of batch element b
 };
@@ -232,7 +235,23 @@ struct GemmArgs {
   const DftAxis* a_axes;
   bool a_rows_are_out;
   EpiArgs epi;
+  // Split K (tensor-core form, loaded operands): `splits` > 1 CTAs share each
+  // output tile, each over a contiguous range of K, writing FP32 partials
+  // into split_ws [splits][batch][M][N]; a reduction kernel sums them in split
+  // order and applies `epi`. The caller fixes `splits` from the shape alone
+  // (split_k_count), so a result does not depend on what else is in the batch.
+  int splits;
+  float2* split_ws;
 };
+
+// Splits for a GEMM with `tiles` output tiles (over the largest batch the
+// caller will run) and inner size K: > 1 only when the tiles leave most SMs
+// idle. 1 on devices without the tensor-core form.
+int split_k_count(long long tiles, int K);
+// Whether plans created now may split K (dlx_set_split_k).
+bool split_k_enabled();
+// Bytes of split_ws for that GEMM (0 when not split).
+size_t split_k_bytes(int splits, long long batch, int M, int N);
 
 int launch_gemm_fp32(const GemmArgs& g, cudaStream_t s);
 // Either form by variant, bracketed by CUDA events while dlx_gemm_timing is on.

@@ -285,6 +285,14 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
  * values) differ. The caller orders the backward after the forward on the
  * device, as for any two calls on one plan. */
 int dlx_poly_forward_token(dlx_poly_plan plan, unsigned long long* token);
+/* Split K for the tensor-core GEMMs of poly plans created after the call
+ * with their own workspace (default on): a GEMM whose output tiles over the
+ * plan's capacity (wavelengths x max_objects) would leave most SMs idle runs
+ * each tile as up to 8 K ranges in parallel and sums the FP32 partials in a
+ * fixed order. The choice is made per plan, so an object's result is the
+ * same alone and in a batch of that plan. Plans on a shared workspace
+ * (dlx_poly_plan_create_shared) do not split. No dLux counterpart. */
+int dlx_set_split_k(int enable);
 int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token);
 /* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
  * is known before the forward pass (a serving request, a linear functional):

@@ -155,7 +155,14 @@ def test_shared_plan_workspace_and_generated_operand(cuda):
     amp = dev(o["T"])
     scale = kernels.amp_norm(amp)
     args = (amp, scale, dev(o["opd"]), None, dev(o["w"]))
-    own = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", max_objects=2)
+    # shared-workspace plans do not split K; compare with an owning plan that does not either
+    from dlux_gb300 import _lib
+    lib = _lib.load()
+    _lib.check(lib.dlx_set_split_k(0))
+    try:
+        own = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", max_objects=2)
+    finally:
+        _lib.check(lib.dlx_set_split_k(1))
     shared = kernels.PolyPlan(wls, n, 1.0 / n, m, ps, variant="split_bf16", max_objects=2,
                               own_workspace=False)
     assert shared.footprint < own.footprint
