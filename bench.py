@@ -162,6 +162,52 @@ def cpu_step_sample(n_lambda_sample=2):
     return dt * (N_WAVELENGTHS / n_lambda_sample), n_lambda_sample
 
 
+def parity_sample(variant, n_lambda_sample=2):
+    """Part of the CPU-baseline leg: the FP64 oracle (the checker) on the same
+    wavelength sample at full size, against the public-API step on the GPU for
+    those wavelengths and weights. Relative L2 errors of the 128^2 image and of
+    the coefficient gradient."""
+    import torch
+    from oracle import dlux_oracle as O
+
+    coeffs, wls, weights, R = make_inputs()
+    T, B = O.circular_aperture(N_PUPIL, 1.0, oversample=5, secondary_diameter=0.1,
+                               spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                               zernike_nolls=NOLLS)
+    ps_out = float(O.arcsec2rad(PSF_PIXEL_SCALE / OVERSAMPLE))
+    idx = np.linspace(0, N_WAVELENGTHS - 1, n_lambda_sample).astype(int)
+    opd = np.tensordot(B, coeffs, axes=(0, 0))
+    psf = O.poly_psf(T, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out)
+    img_ref = O.downsample(psf, OVERSAMPLE, mean=False)
+    Teff = T / np.sqrt((T ** 2).sum())
+    G = np.kron(R, np.ones((OVERSAMPLE, OVERSAMPLE)))
+    g = O.poly_psf_grad(Teff, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out, G)
+    gc_ref = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+
+    import dlux_gb300 as dl
+    dl.set_variant(variant)
+    f32 = dict(dtype=torch.float32, device="cuda")
+    c = torch.as_tensor(coeffs, **f32)
+    # the same aperture and basis arrays on both sides, through the public API
+    optics = dl.AngularOpticalSystem(
+        N_PUPIL, 1.0, [dl.TransmissiveLayer(torch.as_tensor(T, **f32), normalise=True),
+                       dl.BasisLayer(torch.as_tensor(B, **f32), c)],
+        N_FOCAL // OVERSAMPLE, PSF_PIXEL_SCALE, OVERSAMPLE)
+    detector = dl.LayeredDetector([dl.Downsample(OVERSAMPLE)])
+    _, gc, img = step(optics, detector, wls[idx], torch.as_tensor(weights[idx], **f32),
+                      torch.as_tensor(R, **f32), c)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+    return {"image_rel_l2": rel(img.cpu().numpy(), img_ref),
+            "grad_rel_l2": rel(gc.cpu().numpy(), gc_ref),
+            "reference": "FP64 NumPy restatement of dLux's op order (the oracle)",
+            "sample": f"{n_lambda_sample} of {N_WAVELENGTHS} wavelengths (first and last) at "
+                      "full size through the same public API; tests/test_gpu_headline_parity.py "
+                      "checks all 64"}
+
+
 def cpu_threads():
     try:
         from threadpoolctl import threadpool_info
@@ -781,12 +827,14 @@ def main():
                     "gemm_share_of_step": g["total_ms"] / res["ms_total"]}
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu:
         t, ns = cpu_step_sample(2)
         cpu = {"value": 1.0 / t, "unit": "evals/s", "cores": cpu_threads(), "kind": "port",
                "sample": f"{ns} of {N_WAVELENGTHS} wavelengths at full size, time scaled by "
                          f"{N_WAVELENGTHS // ns}; NumPy complex64 restatement of dLux's op "
                          "order"}
+        parity = parity_sample(args.variant, 2)
 
     if rank == 0:
         line = {
@@ -805,6 +853,7 @@ def main():
             "eager_value": eager_value,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "error_vs_fp64_oracle": parity,
             "clocks": clk,
             "fp32_form": fp32,
             "speedup_vs_fp32": (value / fp32["value"]) if fp32 else None,

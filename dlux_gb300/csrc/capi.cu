@@ -1001,6 +1001,7 @@ struct dlx_poly_plan_s {
       DLX_TRY(run_gemm(v, gemm(ts.opANy(), R, N, N, M, true, mid.p, ec), s));
       ra.ebar = planes.as<float2>();
       ra.path = pathff.as<float4>();
+      ra.split_form = v == DLX_VARIANT_SPLIT_BF16 ? 1 : 0;
       ra.inv_lambda_ff = ts.inv_lambda_ff.as<float2>();
       ra.pix_scratch = reinterpret_cast<float*>(pathff.as<float4>() + (size_t)R * N * N);
       return launch_obj_pupil_fused(ra, s);

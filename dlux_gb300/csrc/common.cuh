@@ -97,6 +97,22 @@ __device__ __forceinline__ float2 cis_ff(FF path, FF inv_lambda, FF phase_cycles
   return make_float2(c, s);
 }
 
+// cis_ff for the split-BF16 form: the same exact reduction to r in [-1/2, 1/2]
+// cycles, then the hardware sine/cosine of 2 pi r (absolute error below 1e-6
+// on [-pi, pi]), which is below the ~7.6e-6 resolution of the hi/lo bf16
+// operands that the result feeds. The FP32 form keeps cis_ff.
+__device__ __forceinline__ float2 cis_ff_split(FF path, FF inv_lambda, FF phase_cycles) {
+  const float p = path.hi * inv_lambda.hi;
+  const float e = fmaf(path.hi, inv_lambda.hi, -p);
+  const float small = e + fmaf(path.hi, inv_lambda.lo, path.lo * inv_lambda.hi);
+  float r = (p - rintf(p)) + phase_cycles.hi;
+  r = r + (small + phase_cycles.lo);
+  r = r - rintf(r);
+  float s, c;
+  __sincosf(6.28318530717958647692f * r, &s, &c);
+  return make_float2(c, s);
+}
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -64,6 +64,8 @@ int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool 
 // 319-327; optics.py:77-96; optical_systems.py:213-215).
 // One thread per pixel; the wavelength loop reuses amp/opd/phase.
 // ---------------------------------------------------------------------------
+// kSplit: the output is the split-BF16 operand only (cis_ff_split).
+template <bool kSplit>
 __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) {
   // cached: per-wavelength 1/lambda pairs and per-(object, wavelength)
   // sqrt(weight) staged once per block in shared memory
@@ -112,7 +114,8 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
       const int b = wl * R + r;
       const float2 il2 = cached ? c_il[wl]
                                 : (a.inv_lambda_ff ? a.inv_lambda_ff[wl] : inv_lambda_arg.v[wl]);
-      float2 u = cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
+      float2 u = kSplit ? cis_ff_split(path, FF{il2.x, il2.y}, ph_cyc)
+                        : cis_ff(path, FF{il2.x, il2.y}, ph_cyc);
       float sc = amp;
       if (cached) sc *= c_sw[r * L + wl];
       else if (o_w) sc *= sqrtf(o_w[wl]);
@@ -147,7 +150,12 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
   // stage the per-wavelength factors in shared memory when they fit in 32 KB
   const size_t smem = sizeof(float) * (size_t)(2 * L + R * L);
   const int cached = smem <= 32 * 1024 ? 1 : 0;
-  phasor_kernel<<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg, cached);
+  if (a.out_split && !a.out_c64 && !a.in)
+    phasor_kernel<true><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
+                                                                             cached);
+  else
+    phasor_kernel<false><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
+                                                                              cached);
   DLX_LAUNCH_CHECK("phasor_kernel");
   return DLX_OK;
 }
@@ -620,6 +628,7 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
 // and summing them at once: pixel gradients (g_amp = sum pre, g_phase = sum
 // pim, g_opd = sum k_l pim), tilt partials, and weight partials
 // sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
+template <bool kSplit>
 __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
   // dynamic shared memory: [L] float4 (1/lambda hi, lo, sqrt(w), k) then, when
   // weight gradients are wanted, [8 warps][L] double partials
@@ -677,7 +686,8 @@ __global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, i
         if (live) {
           const float2 eb = ebq[j];
           const float4 c = lam[l];
-          const float2 u = cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
+          const float2 u = kSplit ? cis_ff_split(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w})
+                                  : cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
           const float sw = c.z;
           const float pr = u.x * eb.x + u.y * eb.y;
           const float pi = u.x * eb.y - u.y * eb.x;
@@ -759,12 +769,16 @@ int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s) {
   const size_t smem = sizeof(float4) * (size_t)a.L + (want_w ? sizeof(double) * 8 * (size_t)a.L : 0);
   static std::atomic<bool> attr_done{false};  // host side, once per process
   if (smem > 48 * 1024 && !attr_done.load()) {
-    DLX_TRY_CUDA(cudaFuncSetAttribute(obj_pupil_fused_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)(sizeof(double) * 10 * kFusedPupilMaxL)));
+    for (const void* k : {(const void*)obj_pupil_fused_kernel<true>,
+                          (const void*)obj_pupil_fused_kernel<false>})
+      DLX_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(double) * 10 * kFusedPupilMaxL)));
     attr_done.store(true);
   }
-  obj_pupil_fused_kernel<<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
+  if (a.split_form)
+    obj_pupil_fused_kernel<true><<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
+  else
+    obj_pupil_fused_kernel<false><<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
   DLX_LAUNCH_CHECK("obj_pupil_fused_kernel");
   if (a.sum_pixels) {
     obj_pupil_sumr_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);

@@ -122,6 +122,7 @@ struct ObjReduceArgs {
   const float4* path;
   const float2* inv_lambda_ff;  // [L]
   float* pix_scratch;        // [R][3][npix] per-object pixel sums (sum_pixels only)
+  int split_form;            // the plan's split-BF16 form: phasors by cis_ff_split
 };
 int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s);
 int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s);
