@@ -137,6 +137,86 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
   }
 }
 
+struct alignas(8) Bf16Quad {
+  __nv_bfloat16 v[4];
+};
+
+// Split-BF16 output only, four adjacent pixels of one row per thread (n % 4
+// == 0): each of the four planes gets one 8-byte store per thread and
+// wavelength, and the per-pixel FP64 path set-up is amortised over a
+// wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg), so that
+// small pupils still fill the GPU). Same arithmetic per pixel as phasor_kernel.
+__global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
+  extern __shared__ float psm[];
+  const long long npix = (long long)a.n * a.n;
+  const int R = a.objs.n > 0 ? a.objs.n : 1;
+  const int L = a.batch / R;
+  float2* c_il = reinterpret_cast<float2*>(psm);
+  float* c_sw = psm + 2 * L;
+  if (cached) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x)
+      c_il[i] = a.inv_lambda_ff ? a.inv_lambda_ff[i] : inv_lambda_arg.v[i];
+    for (int i = threadIdx.x; i < R * L; i += blockDim.x) {
+      const int r = i / L, wl = i - (i / L) * L;
+      const float* o_w = a.objs.n > 0 ? a.objs.o[r].weights : a.weights;
+      c_sw[i] = o_w ? sqrtf(o_w[wl]) : 1.0f;
+    }
+    __syncthreads();
+  }
+  const long long p0 = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (p0 >= npix) return;
+  const int y = (int)(p0 / a.n);
+  const int x0 = (int)(p0 - (long long)y * a.n);
+  const double half = 0.5 * (a.n - 1);
+  const double Y = ((double)y - half) * a.pixel_scale;
+  for (int r = 0; r < R; ++r) {
+    const bool obj = a.objs.n > 0;
+    const float* o_amp = obj ? a.objs.o[r].amp : a.amp;
+    const float* o_scale = obj ? a.objs.o[r].amp_scale : a.amp_scale;
+    const float* o_opd = obj ? a.objs.o[r].opd : a.opd;
+    const float* o_phase = obj ? a.objs.o[r].phase : a.phase;
+    const float* o_w = obj ? a.objs.o[r].weights : a.weights;
+    const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
+    const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
+    const float scale = (o_scale ? *o_scale : 1.0f);
+    FF path[4], ph[4];
+    float amp[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const long long p = p0 + k;
+      const double X = ((double)(x0 + k) - half) * a.pixel_scale;
+      path[k] = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
+      ph[k] = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+      if (a.out_path && blockIdx.y == 0)
+        a.out_path[(long long)r * npix + p] =
+            make_float4(path[k].hi, path[k].lo, ph[k].hi, ph[k].lo);
+      float am = o_amp ? o_amp[p] : 1.0f;
+      if (o_scale) am *= scale;
+      amp[k] = am * (float)a.const_scale;
+    }
+    const int wl1 = min(L, (int)(blockIdx.y + 1) * lg);
+    for (int wl = blockIdx.y * lg; wl < wl1; ++wl) {
+      const int b = wl * R + r;
+      const float2 il2 = cached ? c_il[wl]
+                                : (a.inv_lambda_ff ? a.inv_lambda_ff[wl] : inv_lambda_arg.v[wl]);
+      float sw = 1.0f;
+      if (cached) sw = c_sw[r * L + wl];
+      else if (o_w) sw = sqrtf(o_w[wl]);
+      Bf16Quad q[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float2 u = cis_ff_split(path[k], FF{il2.x, il2.y}, ph[k]);
+        const float sc = amp[k] * sw;
+        split_bf16(u.x * sc, q[0].v[k], q[1].v[k]);
+        split_bf16(u.y * sc, q[2].v[k], q[3].v[k]);
+      }
+      __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p0;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Quad*>(base + c * npix) = q[c];
+    }
+  }
+}
+
 int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream_t s) {
   const long long npix = (long long)a.n * a.n;
   if (npix == 0 || a.batch == 0) return DLX_OK;
@@ -150,7 +230,13 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
   // stage the per-wavelength factors in shared memory when they fit in 32 KB
   const size_t smem = sizeof(float) * (size_t)(2 * L + R * L);
   const int cached = smem <= 32 * 1024 ? 1 : 0;
-  if (a.out_split && !a.out_c64 && !a.in)
+  if (a.out_split && !a.out_c64 && !a.in && a.n % 4 == 0) {
+    // One wavelength group: splitting the wavelengths over more blocks
+    // measured slower at 512^2 x 64 (42.9 vs 38.3 us), the FP64 path set-up
+    // being repeated per group.
+    phasor_split4_kernel<<<dim3(ceil_div(npix / 4, 256), 1), 256, cached ? smem : 0, s>>>(
+        a, *inv_lambda_arg, cached, L);
+  } else if (a.out_split && !a.out_c64 && !a.in)
     phasor_kernel<true><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
                                                                              cached);
   else
