@@ -170,6 +170,9 @@ _SIGNATURES = {
     "dlx_poly_forward_token": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     "dlx_poly_reuse_forward": (_c_int, [_c_vp, ctypes.c_ulonglong]),
     "dlx_set_split_k": (_c_int, [_c_int]),
+    "dlx_scene_forward_token": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "dlx_scene_reuse_forward": (_c_int, [_c_vp, ctypes.c_ulonglong]),
+    "dlx_scene_set_retain_limit": (_c_int, [_c_vp, ctypes.c_size_t]),
     "dlx_poly_forward_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "dlx_poly_backward_sum": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_vp, _c_vp, _c_vp]),
     "dlx_poly_plan_destroy": (_c_int, [_c_vp]),

@@ -166,7 +166,9 @@ class ScenePSF(torch.autograd.Function):
         w = weights.detach().to(torch.float32).contiguous()
         ctx.plan, ctx.pos_device = plan, positions.device
         ctx.save_for_backward(amp, amp_scale, opd, phase, w, pos)
-        return plan.forward(_d(amp), amp_scale, _d(opd), _d(phase), pos, w)
+        out = plan.forward(_d(amp), amp_scale, _d(opd), _d(phase), pos, w)
+        ctx.token = plan.forward_token()  # retained fields, if the plan kept them
+        return out
 
     @staticmethod
     def backward(ctx, g):
@@ -176,7 +178,7 @@ class ScenePSF(torch.autograd.Function):
         if not (want_w or want_pos):
             return None, None, None, None, None, None, None, None
         g_pos, g_w = ctx.plan.backward(_d(amp), amp_scale, _d(opd), _d(phase), pos, w,
-                                       g.contiguous(), want_pos, want_w)
+                                       g.contiguous(), want_pos, want_w, reuse_token=ctx.token)
         if g_pos is not None:
             g_pos = g_pos.to(device=ctx.pos_device, dtype=torch.float64)
         return None, None, None, None, None, g_w, g_pos, None

@@ -285,20 +285,31 @@ struct dlx_scene_plan_s {
   // workspace
   Buf e, ex, ax, d1, d1y, fbar, planes, tx, ty, bsum, bw;
   const double* pos = nullptr;  // device [S][2] positions of the current call
+  // Forward-to-backward retention (dlx_scene_forward_token / reuse_forward):
+  // a forward that fits retain_limit keeps every chunk's D1 and Y.D1 (the
+  // half-transformed fields, M x N per source and wavelength), so that the
+  // backward starts from them instead of repeating the first GEMM; it still
+  // recomputes the focal field from D1.
+  Buf retain;  // per chunk: D1 [R L][M][N] then Y.D1, complex (elem() bytes each)
+  size_t retain_limit = (size_t)48 << 30;
+  unsigned long long epoch = 0, fwd_token = 0, reuse_req = 0;
+  const void* fwd_in[6] = {};
+  int fwd_S = 0;
 
   bool split() const { return variant == DLX_VARIANT_SPLIT_BF16; }
   size_t elem() const { return 8; }  // bytes per complex element (split planes or c64)
 
   void release() {
     for (Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw, &a0,
-                   &a0s, &e, &ex, &ax, &d1, &d1y, &fbar, &planes, &tx, &ty, &bsum, &bw})
+                   &a0s, &e, &ex, &ax, &d1, &d1y, &fbar, &planes, &tx, &ty, &bsum, &bw,
+                   &retain})
       b->release();
   }
   size_t footprint() const {
     size_t t = 0;
     for (const Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw,
                          &a0, &a0s, &e, &ex, &ax, &d1, &d1y, &fbar, &planes, &tx, &ty, &bsum,
-                         &bw})
+                         &bw, &retain})
       t += b->bytes;
     return t;
   }
@@ -374,56 +385,103 @@ struct dlx_scene_plan_s {
   // The shared y-axis matrix of every wavelength (A operand, batch divisor Rc).
   const void* ay0() const { return split() ? a0s.p : a0.p; }
 
+  size_t chunk_bytes() const { return 2 * (size_t)R * L * M * N * elem(); }
+  void* keep_d1(int c) const { return retain.as<char>() + (size_t)c * chunk_bytes(); }
+  void* keep_d1y(int c) const { return static_cast<char*>(keep_d1(c)) + chunk_bytes() / 2; }
+
+  // Room for the retained fields of S sources: within retain_limit, and
+  // allocated only outside stream capture (a capture runs without retention).
+  bool ensure_retain(int S, cudaStream_t s) {
+    const size_t need = (size_t)((S + R - 1) / R) * chunk_bytes();
+    if (need == 0 || need > retain_limit) return false;
+    if (retain.bytes >= need) return true;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (cs != cudaStreamCaptureStatusNone) return false;
+    retain.release();
+    return retain.alloc(need) == DLX_OK;  // out of memory: run without retention
+  }
+
+  // D1 (and, when d1y_out is set, Y.D1) of chunk s0 into the given buffers.
+  int first_gemm(int Rc, void* d1_out, void* d1y_out, cudaStream_t s) {
+    const int B = Rc * L;
+    // D1[b][u][y] = sum_x A'x[b][u][x] E_l[y][x], times the y tilt ty[b][y]
+    EpiArgs e1 = epi(d1y_out ? EPI_SPLIT2 : (split() ? EPI_SPLIT : EPI_C64), Rc);
+    e1.alpha = nullptr;
+    e1.coltilt = ty.as<float2>();
+    if (d1y_out) {
+      e1.colw = yw.as<float>();  // Y along the y index = GEMM column n
+      if (split()) {
+        e1.out_split = static_cast<__nv_bfloat16*>(d1_out);
+        e1.out_split2 = static_cast<__nv_bfloat16*>(d1y_out);
+      } else {
+        e1.out_c64 = static_cast<float2*>(d1_out);
+        e1.out_c642 = static_cast<float2*>(d1y_out);
+      }
+    } else {
+      set_out(e1, d1_out);
+    }
+    return run(gemm(B, M, N, N, ax.p, 1, e.p, Rc, e1), s);
+  }
+
   int forward(const float* amp, const float* amp_scale, const float* opd, const float* phase,
               const double* positions, const float* weights, int S, float* image, int accumulate,
               cudaStream_t s) {
     pos = positions;
+    fwd_token = 0;
+    const bool keep = ensure_retain(S, s);
     DLX_TRY(build_field(amp, amp_scale, opd, phase, s));
     for (int s0 = 0; s0 < S; s0 += R) {
-      const int Rc = std::min(R, S - s0), B = Rc * L;
+      const int Rc = std::min(R, S - s0), B = Rc * L, c = s0 / R;
       DLX_TRY(build_matrices(s0, Rc, s));
-      // D1[b][u][y] = sum_x A'x[b][u][x] E_l[y][x]
-      // times the y tilt ty[b][y] (so D1 holds the y-tilted field)
-      EpiArgs e1 = epi(split() ? EPI_SPLIT : EPI_C64, Rc);
-      e1.alpha = nullptr;
-      e1.coltilt = ty.as<float2>();
-      set_out(e1, d1.p);
-      DLX_TRY(run(gemm(B, M, N, N, ax.p, 1, e.p, Rc, e1), s));
+      void* d1src = keep ? keep_d1(c) : d1.p;
+      DLX_TRY(first_gemm(Rc, d1src, keep ? keep_d1y(c) : nullptr, s));
       // |F[b][v][u]|^2, F = alpha_l sum_y A0[l][v][y] D1[b][u][y]
       EpiArgs e2 = epi(EPI_INTENSITY, Rc);
       e2.out_f32 = planes.as<float>();
-      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1.p, 1, e2), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1src, 1, e2), s));
       const long long npix = (long long)M * M;
       scene_image_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(planes.as<float>(), Rc, L, npix,
                                                              weights, s0,
                                                              (s0 > 0 || accumulate) ? 1 : 0, image);
       DLX_LAUNCH_CHECK("scene_image_kernel");
     }
+    if (keep) {
+      fwd_token = ++epoch;
+      const void* in[6] = {amp, amp_scale, opd, phase, positions, weights};
+      std::copy(in, in + 6, fwd_in);
+      fwd_S = S;
+    }
     return DLX_OK;
+  }
+
+  bool can_reuse(unsigned long long req, const void* const in[6], int S) const {
+    if (req == 0 || req != fwd_token || S != fwd_S) return false;
+    for (int i = 0; i < 6; ++i)
+      if (in[i] != fwd_in[i]) return false;
+    return true;
   }
 
   int backward(const float* amp, const float* amp_scale, const float* opd, const float* phase,
                const double* positions, const float* weights, int S, const float* g_image,
                float* g_pos, float* g_w, cudaStream_t s) {
+    const unsigned long long req = reuse_req;
+    reuse_req = 0;  // a request covers one backward call
+    const void* in[6] = {amp, amp_scale, opd, phase, positions, weights};
+    const bool reuse = can_reuse(req, in, S);
     pos = positions;
     DLX_TRY(build_field(amp, amp_scale, opd, phase, s));
     const long long npix = (long long)M * M;
     for (int s0 = 0; s0 < S; s0 += R) {
-      const int Rc = std::min(R, S - s0), B = Rc * L;
-      DLX_TRY(build_matrices(s0, Rc, s));
-      // D1 and D1Y = Y.D1 (Y along the y index = GEMM column n), both y-tilted
-      EpiArgs e1 = epi(EPI_SPLIT2, Rc);
-      e1.alpha = nullptr;
-      e1.colw = yw.as<float>();
-      e1.coltilt = ty.as<float2>();
-      if (split()) {
-        e1.out_split = d1.as<__nv_bfloat16>();
-        e1.out_split2 = d1y.as<__nv_bfloat16>();
-      } else {
-        e1.out_c64 = d1.as<float2>();
-        e1.out_c642 = d1y.as<float2>();
-      }
-      DLX_TRY(run(gemm(B, M, N, N, ax.p, 1, e.p, Rc, e1), s));
+      const int Rc = std::min(R, S - s0), B = Rc * L, c = s0 / R;
+      DLX_TRY(build_matrices(s0, Rc, s));  // A'x is needed for D1X either way
+      // D1 and D1Y = Y.D1, both y-tilted: retained by the forward, or recomputed
+      const void* d1src = reuse ? keep_d1(c) : d1.p;
+      const void* d1ysrc = reuse ? keep_d1y(c) : d1y.p;
+      if (!reuse) DLX_TRY(first_gemm(Rc, d1.p, d1y.p, s));
       // intensity planes and F-bar = 2 w alpha G D
       EpiArgs e2 = epi(EPI_PSF_GRADF, Rc, g_image);
       e2.out_f32 = planes.as<float>();
@@ -433,7 +491,7 @@ struct dlx_scene_plan_s {
                                                                     bw.as<float>());
       DLX_LAUNCH_CHECK("scene_gather_weights_kernel");
       e2.bweight = bw.as<float>();
-      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1.p, 1, e2), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1src, 1, e2), s));
       if (g_w) {
         scene_bsum_kernel<<<B, 256, 0, s>>>(planes.as<float>(), npix, g_image,
                                             bsum.as<double>());
@@ -448,7 +506,7 @@ struct dlx_scene_plan_s {
       ed.out_f32 = planes.as<float>();
       if (split()) ed.in_split = fbar.as<__nv_bfloat16>();
       else ed.in_c64 = fbar.as<float2>();
-      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1y.p, 1, ed), s));
+      DLX_TRY(run(gemm(B, M, M, N, ay0(), Rc, d1ysrc, 1, ed), s));
       DLX_TRY(pos_reduce(Rc, s0, g_pos, 1, s));
       // d/dtx: D1X = A'x (X.E)^T (into d1), then the same dot
       EpiArgs ex1 = epi(split() ? EPI_SPLIT : EPI_C64, Rc);
@@ -598,6 +656,27 @@ int dlx_scene_forward(dlx_scene_plan plan, const float* amp, const float* amp_sc
   if (n_sources <= 0) return fail(DLX_ERR_ARG, "scene_forward: n_sources must be positive");
   return plan->forward(amp, amp_scale, opd, phase, positions, weights, n_sources, image,
                        accumulate, static_cast<cudaStream_t>(stream));
+}
+
+int dlx_scene_forward_token(dlx_scene_plan plan, unsigned long long* token) {
+  if (!plan || !token) return fail(DLX_ERR_ARG, "scene_forward_token: null pointer");
+  *token = plan->fwd_token;
+  return DLX_OK;
+}
+
+int dlx_scene_reuse_forward(dlx_scene_plan plan, unsigned long long token) {
+  if (!plan) return fail(DLX_ERR_ARG, "scene_reuse_forward: null plan");
+  plan->reuse_req = token;
+  return DLX_OK;
+}
+
+int dlx_scene_set_retain_limit(dlx_scene_plan plan, size_t bytes) {
+  if (!plan) return fail(DLX_ERR_ARG, "scene_set_retain_limit: null plan");
+  cudaDeviceSynchronize();
+  plan->retain_limit = bytes;
+  plan->fwd_token = 0;
+  if (plan->retain.bytes > bytes) plan->retain.release();
+  return DLX_OK;
 }
 
 int dlx_scene_backward(dlx_scene_plan plan, const float* amp, const float* amp_scale,

@@ -492,11 +492,25 @@ class ScenePlan(_Plan):
              _stream())
         return out
 
+    def forward_token(self) -> int:
+        """Token of the retained forward state (0 if none)."""
+        t = ctypes.c_ulonglong(0)
+        call("dlx_scene_forward_token", self.handle, ctypes.byref(t))
+        return int(t.value)
+
+    def set_retain_limit(self, nbytes: int) -> None:
+        """Cap (bytes) on the fields a forward keeps for its backward; 0 disables."""
+        call("dlx_scene_set_retain_limit", self.handle, int(nbytes))
+
     def backward(self, amp, amp_scale, opd, phase, positions, weights, g_image, want_pos=True,
-                 want_w=True):
+                 want_w=True, reuse_token=0):
+        """Reverse pass. ``reuse_token`` (forward_token() after the matching
+        forward) lets it start from the retained fields when they are intact."""
         positions = positions.to(device="cuda", dtype=torch.float64).contiguous()
         weights = weights.to(device="cuda", dtype=torch.float32).contiguous()
         S = positions.shape[0]
+        if reuse_token:
+            call("dlx_scene_reuse_forward", self.handle, ctypes.c_ulonglong(reuse_token))
         g_pos = torch.empty((S, 2), dtype=torch.float32, device="cuda") if want_pos else None
         g_w = torch.empty(weights.shape, dtype=torch.float32, device="cuda") if want_w else None
         call("dlx_scene_backward", self.handle, ptr(_contig(amp)), ptr(amp_scale),

@@ -450,6 +450,18 @@ int dlx_scene_backward(dlx_scene_plan plan, const float* amp, const float* amp_s
                        const float* opd, const float* phase, const double* positions,
                        const float* weights, int n_sources, const float* g_image, float* g_pos,
                        float* g_weights, void* stream);
+/* Forward-to-backward retention, as for poly plans. A dlx_scene_forward
+ * whose retained fields fit the plan's limit (default 48 GiB; 0 disables)
+ * keeps every source chunk's half-transformed fields D1 and Y.D1, i.e.
+ * 2 x n_sources x n_wavelengths x n_out x n_in complex values. The buffer is
+ * allocated outside stream capture only. dlx_scene_forward_token returns a
+ * token for that state (0 if none). After dlx_scene_reuse_forward(token),
+ * the next dlx_scene_backward with the same input pointers starts from
+ * those fields instead of repeating the first GEMM, and still recomputes the
+ * focal fields. Otherwise it recomputes everything. */
+int dlx_scene_forward_token(dlx_scene_plan plan, unsigned long long* token);
+int dlx_scene_reuse_forward(dlx_scene_plan plan, unsigned long long token);
+int dlx_scene_set_retain_limit(dlx_scene_plan plan, size_t bytes);
 
 /* ---- Serving batch ----
  * No counterpart in dLux, which has no serving loop. One batch of requests

@@ -104,3 +104,47 @@ def test_point_sources_scene_gradients_vs_differences(cuda):
             d[s, k] = h
             gp[s, k] = (loss(p0 + d, f0) - loss(p0 - d, f0)) / (2 * h)
     assert rel(pos.grad.numpy(), gp) < 1e-3
+
+
+@pytest.mark.parametrize("variant", ["fp32", "split_bf16"])
+def test_retained_fields_give_the_recomputed_bits(cuda, variant):
+    """A backward that starts from the forward's retained D1 / Y.D1 (several
+    source chunks) gives the same image and gradients, bit for bit, as one
+    that recomputes them; a stale token or a different input falls back to
+    the recomputation."""
+    from dlux_gb300 import kernels
+    n, m, L, S = 128, 64, 3, 40
+    T, opd, wls, pos, w = scene(n, m, L, S, 9)
+    ps = float(O.arcsec2rad(0.02))
+    amp = dev(T)
+    scale = kernels.amp_norm(amp)
+    opd_d, pos_t, w_d = dev(opd), dev(pos, torch.float64), dev(w)
+    G = dev(np.random.default_rng(5).normal(size=(m, m)))
+    plan = kernels.ScenePlan(wls, n, 1.0 / n, m, ps, variant=variant, max_sources=16)
+
+    # reference: no retention
+    plan.set_retain_limit(0)
+    img0 = plan.forward(amp, scale, opd_d, None, pos_t, w_d).clone()
+    assert plan.forward_token() == 0
+    gp0, gw0 = plan.backward(amp, scale, opd_d, None, pos_t, w_d, G)
+    # retained: 3 chunks of at most 16 sources
+    plan.set_retain_limit(1 << 34)
+    img1 = plan.forward(amp, scale, opd_d, None, pos_t, w_d).clone()
+    tok = plan.forward_token()
+    assert tok != 0
+    gp1, gw1 = plan.backward(amp, scale, opd_d, None, pos_t, w_d, G, reuse_token=tok)
+    torch.cuda.synchronize()
+    assert torch.equal(img0, img1)
+    assert torch.equal(gp0, gp1) and torch.equal(gw0, gw1)
+    # a second backward may reuse the same retained state
+    gp2, gw2 = plan.backward(amp, scale, opd_d, None, pos_t, w_d, G, reuse_token=tok)
+    assert torch.equal(gp0, gp2) and torch.equal(gw0, gw2)
+    # stale token: another forward (other weights) replaced the retained state
+    w2 = dev(w * 1.5)
+    plan.forward(amp, scale, opd_d, None, pos_t, w2)
+    gp3, gw3 = plan.backward(amp, scale, opd_d, None, pos_t, w_d, G, reuse_token=tok)
+    assert torch.equal(gp0, gp3) and torch.equal(gw0, gw3)
+    # current token but different inputs (weights pointer): recomputed
+    gp4, gw4 = plan.backward(amp, scale, opd_d, None, pos_t, w_d, G,
+                             reuse_token=plan.forward_token())
+    assert torch.equal(gp0, gp4) and torch.equal(gw0, gw4)
