@@ -715,7 +715,7 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
 // pim, g_opd = sum k_l pim), tilt partials, and weight partials
 // sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
 template <bool kSplit>
-__global__ void __launch_bounds__(256) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
+__global__ void __launch_bounds__(256, 5) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
   // dynamic shared memory: [L] float4 (1/lambda hi, lo, sqrt(w), k) then, when
   // weight gradients are wanted, [8 warps][L] double partials
   extern __shared__ double dyn[];
