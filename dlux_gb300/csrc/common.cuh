@@ -40,6 +40,43 @@ void note_launch();
   } while (0)
 
 // ---------------------------------------------------------------------------
+// Programmatic dependent launch (PDL) for the kernels of the PSF + gradient
+// step, which run as a chain of dependent launches. A kernel launched with
+// launch_pdl may be scheduled before its predecessor in the stream has
+// finished; it calls pdl_enter() before touching global memory, which waits
+// for the predecessor to complete (its writes visible) and then lets the next
+// kernel of the stream be launched early. Both instructions are no-ops for
+// a kernel launched without the attribute.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+#define DLX_PDL_LAUNCH(what, kernel, grid, block, smem, stream, ...)                      \
+  do {                                                                                     \
+    cudaError_t _e = ::dlx::launch_pdl(kernel, grid, block, smem, stream, __VA_ARGS__);    \
+    if (_e != cudaSuccess) return ::dlx::check_cuda(_e, what);                             \
+    ::dlx::note_launch();                                                                  \
+  } while (0)
+
+// ---------------------------------------------------------------------------
 // DFT-type axis description. Element (i_in, j_out) of a generated matrix is
 //   exp(2 pi i * [ sigma * x_i * u_j + g_in * i + d_in + g_out * j + d_out
 //                  + q_in * x_i^2 + q_out * u_j^2 ])

@@ -147,6 +147,7 @@ struct alignas(8) Bf16Quad {
 // wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg), so that
 // small pupils still fill the GPU). Same arithmetic per pixel as phasor_kernel.
 __global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
+  pdl_enter();
   extern __shared__ float psm[];
   const long long npix = (long long)a.n * a.n;
   const int R = a.objs.n > 0 ? a.objs.n : 1;
@@ -234,8 +235,10 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     // One wavelength group: splitting the wavelengths over more blocks
     // measured slower at 512^2 x 64 (42.9 vs 38.3 us), the FP64 path set-up
     // being repeated per group.
-    phasor_split4_kernel<<<dim3(ceil_div(npix / 4, 256), 1), 256, cached ? smem : 0, s>>>(
-        a, *inv_lambda_arg, cached, L);
+    DLX_PDL_LAUNCH("phasor_split4_kernel", phasor_split4_kernel,
+                   dim3(ceil_div(npix / 4, 256), 1), dim3(256), cached ? smem : 0, s, a,
+                   *inv_lambda_arg, cached, L);
+    return DLX_OK;
   } else if (a.out_split && !a.out_c64 && !a.in)
     phasor_kernel<true><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
                                                                              cached);
@@ -339,6 +342,7 @@ int launch_power_scale(const float2* in, int batch, long long npix, double value
 // Two-level deterministic sum of amp^2 (partials then one block).
 __global__ void sumsq_partial_kernel(const float* __restrict__ x, long long npix, int nparts,
                                      double* __restrict__ partial) {
+  pdl_enter();
   __shared__ double smem[32];
   const long long chunk = (npix + nparts - 1) / nparts;
   const long long lo = (long long)blockIdx.x * chunk;
@@ -354,6 +358,7 @@ __global__ void sumsq_partial_kernel(const float* __restrict__ x, long long npix
 
 __global__ void norm_finish_kernel(const double* __restrict__ partial, int nparts, double value,
                                    float* __restrict__ out_scale) {
+  pdl_enter();
   __shared__ double smem[32];
   double acc = 0.0;
   for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += partial[i];
@@ -363,10 +368,10 @@ __global__ void norm_finish_kernel(const double* __restrict__ partial, int npart
 
 int launch_amp_norm(const float* amp, long long npix, double value, float* out_scale,
                     double* partial_ws, int nparts, cudaStream_t s) {
-  sumsq_partial_kernel<<<nparts, 256, 0, s>>>(amp, npix, nparts, partial_ws);
-  DLX_LAUNCH_CHECK("sumsq_partial_kernel");
-  norm_finish_kernel<<<1, 256, 0, s>>>(partial_ws, nparts, value, out_scale);
-  DLX_LAUNCH_CHECK("norm_finish_kernel");
+  DLX_PDL_LAUNCH("sumsq_partial_kernel", sumsq_partial_kernel, dim3(nparts), dim3(256), 0, s,
+                 amp, npix, nparts, partial_ws);
+  DLX_PDL_LAUNCH("norm_finish_kernel", norm_finish_kernel, dim3(1), dim3(256), 0, s,
+                 partial_ws, nparts, value, out_scale);
   return DLX_OK;
 }
 
@@ -434,6 +439,7 @@ __global__ void basis_eval_kernel(const float* __restrict__ basis,
                                   const float* __restrict__ coeffs,
                                   const float* __restrict__ base, int nterms, long long npix,
                                   float* __restrict__ out) {
+  pdl_enter();
   extern __shared__ float sc[];
   for (int k = threadIdx.x; k < nterms; k += blockDim.x) sc[k] = coeffs[k];
   __syncthreads();
@@ -447,15 +453,16 @@ __global__ void basis_eval_kernel(const float* __restrict__ basis,
 int launch_basis_eval(const float* basis, const float* coeffs, const float* base, int nterms,
                       long long npix, float* out, cudaStream_t s) {
   if (npix == 0) return DLX_OK;
-  basis_eval_kernel<<<ceil_div(npix, 256), 256, sizeof(float) * (nterms > 0 ? nterms : 1), s>>>(
-      basis, coeffs, base, nterms, npix, out);
-  DLX_LAUNCH_CHECK("basis_eval_kernel");
+  DLX_PDL_LAUNCH("basis_eval_kernel", basis_eval_kernel, dim3(ceil_div(npix, 256)), dim3(256),
+                 sizeof(float) * (nterms > 0 ? nterms : 1), s, basis, coeffs, base, nterms, npix,
+                 out);
   return DLX_OK;
 }
 
 __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
                                           const float* __restrict__ g, long long npix,
                                           int nparts, double* __restrict__ partial) {
+  pdl_enter();
   __shared__ double smem[32];
   const int k = blockIdx.y;
   const long long chunk = (npix + nparts - 1) / nparts;
@@ -482,6 +489,7 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
 
 __global__ void basis_grad_finish_kernel(const double* __restrict__ partial, int nparts,
                                          float* __restrict__ g_coeffs) {
+  pdl_enter();
   __shared__ double smem[32];
   const int k = blockIdx.x;
   double acc = 0.0;
@@ -494,10 +502,10 @@ int launch_basis_grad(const float* basis, const float* g, int nterms, long long 
                       float* g_coeffs, double* partial_ws, int nparts, cudaStream_t s) {
   if (nterms == 0) return DLX_OK;
   dim3 grid(nparts, nterms);
-  basis_grad_partial_kernel<<<grid, 256, 0, s>>>(basis, g, npix, nparts, partial_ws);
-  DLX_LAUNCH_CHECK("basis_grad_partial_kernel");
-  basis_grad_finish_kernel<<<nterms, 256, 0, s>>>(partial_ws, nparts, g_coeffs);
-  DLX_LAUNCH_CHECK("basis_grad_finish_kernel");
+  DLX_PDL_LAUNCH("basis_grad_partial_kernel", basis_grad_partial_kernel, grid, dim3(256), 0, s,
+                 basis, g, npix, nparts, partial_ws);
+  DLX_PDL_LAUNCH("basis_grad_finish_kernel", basis_grad_finish_kernel, dim3(nterms), dim3(256), 0,
+                 s, partial_ws, nparts, g_coeffs);
   return DLX_OK;
 }
 
@@ -507,6 +515,7 @@ int launch_basis_grad(const float* basis, const float* g, int nterms, long long 
 // ---------------------------------------------------------------------------
 __global__ void downsample_kernel(const float* __restrict__ in, int n_in, int k, int mean,
                                   const float* __restrict__ flat, float* __restrict__ out) {
+  pdl_enter();
   const int n_out = n_in / k;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const int a = blockIdx.y * blockDim.y + threadIdx.y;
@@ -529,13 +538,14 @@ int launch_downsample(const float* in, int n_in, int k, int mean, const float* f
   if (n_out == 0) return DLX_OK;
   dim3 block(32, 8);
   dim3 grid(ceil_div(n_out, 32), ceil_div(n_out, 8));
-  downsample_kernel<<<grid, block, 0, s>>>(in, n_in, k, mean, flat, out);
-  DLX_LAUNCH_CHECK("downsample_kernel");
+  DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel, grid, block, 0, s, in, n_in, k, mean,
+                 flat, out);
   return DLX_OK;
 }
 
 __global__ void downsample_bwd_kernel(const float* __restrict__ g_out, int n_in, int k, int mean,
                                       const float* __restrict__ flat, float* __restrict__ g_in) {
+  pdl_enter();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= n_in || y >= n_in) return;
@@ -553,8 +563,8 @@ int launch_downsample_backward(const float* in, const float* g_out, int n_in, in
   if (g_in) {
     dim3 block(32, 8);
     dim3 grid(ceil_div(n_in, 32), ceil_div(n_in, 8));
-    downsample_bwd_kernel<<<grid, block, 0, s>>>(g_out, n_in, k, mean, flat, g_in);
-    DLX_LAUNCH_CHECK("downsample_bwd_kernel");
+    DLX_PDL_LAUNCH("downsample_bwd_kernel", downsample_bwd_kernel, grid, block, 0, s, g_out,
+                   n_in, k, mean, flat, g_in);
   }
   if (g_flat) {
     // g_flat = g_out * downsample(in): reuse the forward kernel with flat = g_out.
@@ -571,6 +581,7 @@ int launch_downsample_backward(const float* in, const float* g_out, int n_in, in
 // reproducible and independent of which other objects share the batch.
 // ---------------------------------------------------------------------------
 __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
+  pdl_enter();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
   const int R = a.objs.n;
@@ -586,8 +597,8 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
 
 int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s) {
   if (a.npix == 0 || a.objs.n == 0) return DLX_OK;
-  obj_psf_reduce_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
-  DLX_LAUNCH_CHECK("obj_psf_reduce_kernel");
+  DLX_PDL_LAUNCH("obj_psf_reduce_kernel", obj_psf_reduce_kernel, dim3(ceil_div(a.npix, 256)),
+                 dim3(256), 0, s, a);
   return DLX_OK;
 }
 
@@ -671,6 +682,7 @@ __global__ void obj_w_partial_kernel(ObjReduceArgs a) {
 }
 
 __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
+  pdl_enter();
   __shared__ double smem[32];
   const int r = blockIdx.x;
   const int R = a.objs.n;
@@ -716,6 +728,7 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
 // sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
 template <bool kSplit>
 __global__ void __launch_bounds__(256, 5) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
+  pdl_enter();
   // dynamic shared memory: [L] float4 (1/lambda hi, lo, sqrt(w), k) then, when
   // weight gradients are wanted, [8 warps][L] double partials
   extern __shared__ double dyn[];
@@ -831,6 +844,7 @@ __global__ void __launch_bounds__(256, 5) obj_pupil_fused_kernel(ObjReduceArgs a
 
 // Sum of the per-object pixel gradients over the objects, in object order.
 __global__ void obj_pupil_sumr_kernel(ObjReduceArgs a) {
+  pdl_enter();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= a.npix) return;
   float sre = 0.f, sim = 0.f, sk = 0.f;
@@ -862,16 +876,16 @@ int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s) {
     attr_done.store(true);
   }
   if (a.split_form)
-    obj_pupil_fused_kernel<true><<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
+    DLX_PDL_LAUNCH("obj_pupil_fused_kernel", obj_pupil_fused_kernel<true>, dim3(a.nparts, R),
+                   dim3(256), smem, s, a, want_w ? 1 : 0);
   else
-    obj_pupil_fused_kernel<false><<<dim3(a.nparts, R), 256, smem, s>>>(a, want_w ? 1 : 0);
-  DLX_LAUNCH_CHECK("obj_pupil_fused_kernel");
-  if (a.sum_pixels) {
-    obj_pupil_sumr_kernel<<<ceil_div(a.npix, 256), 256, 0, s>>>(a);
-    DLX_LAUNCH_CHECK("obj_pupil_sumr_kernel");
-  }
-  obj_finish_kernel<<<R, 256, 0, s>>>(a, want_w ? 1 : 0);
-  DLX_LAUNCH_CHECK("obj_finish_kernel");
+    DLX_PDL_LAUNCH("obj_pupil_fused_kernel", obj_pupil_fused_kernel<false>, dim3(a.nparts, R),
+                   dim3(256), smem, s, a, want_w ? 1 : 0);
+  if (a.sum_pixels)
+    DLX_PDL_LAUNCH("obj_pupil_sumr_kernel", obj_pupil_sumr_kernel, dim3(ceil_div(a.npix, 256)),
+                   dim3(256), 0, s, a);
+  DLX_PDL_LAUNCH("obj_finish_kernel", obj_finish_kernel, dim3(R), dim3(256), 0, s, a,
+                 want_w ? 1 : 0);
   return DLX_OK;
 }
 
@@ -898,8 +912,8 @@ int launch_obj_pupil_reduce(const ObjReduceArgs& a, cudaStream_t s) {
     obj_w_partial_kernel<<<dim3(a.nparts, R * a.L), 256, 0, s>>>(a);
     DLX_LAUNCH_CHECK("obj_w_partial_kernel");
   }
-  obj_finish_kernel<<<R, 256, 0, s>>>(a, want_w ? 1 : 0);
-  DLX_LAUNCH_CHECK("obj_finish_kernel");
+  DLX_PDL_LAUNCH("obj_finish_kernel", obj_finish_kernel, dim3(R), dim3(256), 0, s, a,
+                 want_w ? 1 : 0);
   return DLX_OK;
 }
 

@@ -344,6 +344,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  // The prologue above overlaps the previous kernel of the stream (PDL);
+  // operands and outputs are touched only after it has completed.
+  pdl_enter();
 
   if (warp < TC_EPI_W0) {
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(REG_CTRL));
@@ -829,6 +832,7 @@ const void* const* loaded_kernels() {
 // own epilogue element by element (the FP32 form's epilogue code).
 __global__ void splitk_reduce_kernel(const float2* __restrict__ part, int splits, int batch,
                                      int M, int N, const EpiArgs e) {
+  pdl_enter();
   const long long total = (long long)batch * M * N;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
@@ -1016,13 +1020,11 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const int grid = p.total < g_num_sms ? p.total : g_num_sms;
   LoadedKernel kern = loaded_kernel(p.epi.kind);
   if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
-  kern<<<grid, TC_THREADS, SMEM_BYTES, s>>>(ta, tb, p);
-  DLX_LAUNCH_CHECK("tc_cgemm_kernel");
+  DLX_PDL_LAUNCH("tc_cgemm_kernel", kern, dim3(grid), dim3(TC_THREADS), SMEM_BYTES, s, ta, tb, p);
   if (split) {
     const long long n = (long long)g.batch * g.M * g.N;
-    splitk_reduce_kernel<<<ceil_div(n, 256), 256, 0, s>>>(g.split_ws, p.splits, g.batch, g.M,
-                                                          g.N, g.epi);
-    DLX_LAUNCH_CHECK("splitk_reduce_kernel");
+    DLX_PDL_LAUNCH("splitk_reduce_kernel", splitk_reduce_kernel, dim3(ceil_div(n, 256)),
+                   dim3(256), 0, s, g.split_ws, p.splits, g.batch, g.M, g.N, g.epi);
   }
   return DLX_OK;
 }
