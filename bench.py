@@ -411,13 +411,27 @@ def run_serving(args):
     import torch
     from dlux_gb300 import serving
 
+    from dlux_gb300.autotune import PlanTuner
+
     out = {}
-    variants = [args.variant] + (["fp32"] if args.variant == "split_bf16" and
-                                 not args.no_fp32_compare else [])
+    tuned = args.variant == "split_bf16" and not args.no_tune
+    main_leg = "autotuned" if tuned else args.variant
+    variants = [main_leg] + (["fp32"] if args.variant == "split_bf16" and
+                             not args.no_fp32_compare else [])
+    tuning = None
     for variant in variants:
+        tuner = None
+        if variant == "autotuned":
+            # form and DFT operand per (N, M), timed once before the stream
+            tuner = PlanTuner()
+            grid, secs = tuner.tune_grid((128, 256, 512, 1024), (64, 128, 256, 512))
+            tuning = {"seconds": secs, "cache": tuner.cache_path,
+                      "choices": {f"{n}x{m}": f"{c['variant']}/op{c['operand_mode']}"
+                                  for (n, m), c in sorted(grid.items())}}
         srv = serving.PSFServer(max_batch=8, n_slots=args.slots, hbm_budget=150e9, k_max=36,
-                                limits=(1024, 512, 64), variant=variant, timeout_s=120.0,
-                                graph_after=args.graph_after)
+                                limits=(1024, 512, 64),
+                                variant=None if tuner is not None else variant,
+                                tuner=tuner, timeout_s=120.0, graph_after=args.graph_after)
         times, reqs = serving.poisson_stream(args.requests, args.rate, seed=SEED)
         _, warm = serving.poisson_stream(max(args.requests // 4, 50), args.rate, seed=SEED + 1)
         keys = sorted({r.key for r in reqs} | {r.key for r in warm})
@@ -444,7 +458,7 @@ def run_serving(args):
         rep.update(variant=variant, buckets=len(keys), resident_buckets=resident,
                    prewarm_s=t_prewarm, clocks=clk)
         out[variant] = rep
-    main_rep = out[args.variant]
+    main_rep = out[main_leg]
     line = {
         "metric": "served requests/sec (mixed PSF and PSF+grad stream)",
         "value": main_rep.get("throughput_rps"), "unit": "req/s", "n_gpus": 1,
@@ -461,6 +475,7 @@ def run_serving(args):
         "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
         "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
         "clocks": main_rep["clocks"],
+        "autotune": tuning,
         "serving": out,
     }
     print(json.dumps(line))
@@ -749,6 +764,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--variant", default="split_bf16", choices=["split_bf16", "fp32"])
     ap.add_argument("--no-fp32-compare", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="serving: fixed split-BF16 plans instead of the per-(N, M) autotuner")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="psf_grad",
                     choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft"])

@@ -475,7 +475,8 @@ class CudaExecutor:
 
     def __init__(self, max_batch=8, k_max=36, limits=(1024, 512, 64), n_slots=4,
                  diameter=1.0, psf_pixel_scale=0.02, band=DEFAULT_BAND, variant=None,
-                 operand_mode=0, graphs=True, graph_after=2, max_graphs=512, device=None):
+                 operand_mode=0, graphs=True, graph_after=2, max_graphs=512, device=None,
+                 tuner=None):
         _lib.require_cuda()
         self.device = torch.device(device) if device is not None else \
             torch.device("cuda", torch.cuda.current_device())
@@ -486,6 +487,8 @@ class CudaExecutor:
         self.band = (float(band[0]), float(band[1]))
         self.variant = variant
         self.operand_mode = int(operand_mode)
+        # per-(n, m) form and DFT operand from the autotuner, when no form is forced
+        self.tuner = tuner if variant is None else None
         self.graphs_on = bool(graphs)
         self.graph_after = int(graph_after)
         self.max_graphs = int(max_graphs)
@@ -549,12 +552,20 @@ class CudaExecutor:
             torch.cuda.synchronize(self.device)
         self.models[n] = (amp, basis, scale)
 
+    def plan_config(self, n, m):
+        """(variant, operand_mode) of the bucket plans of shape (n, m)."""
+        if self.tuner is not None:
+            cfg = self.tuner.choose(n, m)
+            return cfg["variant"], int(cfg["operand_mode"])
+        return self.variant, self.operand_mode
+
     def create_plan(self, key):
         n, m, L = key
+        variant, mode = self.plan_config(n, m)
         with torch.cuda.device(self.device):
             return kernels.PolyPlan(self.wavelengths(L), n, self.diameter / n, m,
-                                    self.pixel_scale, None, self.variant, self.max_batch,
-                                    self.operand_mode, own_workspace=False)
+                                    self.pixel_scale, None, variant, self.max_batch,
+                                    mode, own_workspace=False)
 
     def release_plan(self, key, plan):
         for gk in [k for k in self.graphs if k[1] == key]:

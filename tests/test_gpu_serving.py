@@ -165,3 +165,49 @@ def test_serve_run_rejects_bad_batches(cuda):
     run()                                  # the unmodified batch is accepted
     torch.cuda.synchronize()
     s.close()
+
+
+def test_autotuned_server_alone_vs_mix_and_oracle(cuda, tmp_path):
+    """A server whose bucket plans take their form and DFT operand from the
+    autotuner: the tuner times every candidate and records a choice, results
+    stay bit-identical alone and in a mix, and match the oracle."""
+    from dlux_gb300.autotune import PlanTuner
+    tuner = PlanTuner(cache_path=str(tmp_path / "tune.json"), probe_wavelengths=2,
+                      probe_objects=2, iters=2)
+    base = requests(6)
+    shapes = {(r.n_pupil, r.n_focal) for r in base}
+    grid, secs = tuner.tune_grid(sorted({n for n, _ in shapes}), sorted({m for _, m in shapes}))
+    print("autotuned:", {k: (v["variant"], v["operand_mode"]) for k, v in grid.items()},
+          f"in {secs:.2f} s;", tuner.timings)
+    for cfg in grid.values():
+        assert cfg["variant"] in ("split_bf16", "fp32") and cfg["operand_mode"] in (0, 1)
+    assert all(len(t) >= 1 for t in tuner.timings.values())
+
+    alone_srv = make_server(max_batch=1, n_slots=1, graphs=False, tuner=tuner)
+    alone = clone(base)
+    for r in alone:
+        alone_srv.submit(r)
+        drive(alone_srv, [r])
+    alone_srv.close()
+    mix_srv = make_server(max_batch=4, n_slots=2, graphs=True, graph_after=1, tuner=tuner)
+    mix = clone(base)
+    for r in mix:
+        mix_srv.submit(r)
+    drive(mix_srv, mix)
+    mix_srv.close()
+    for a, b in zip(alone, mix):
+        assert np.array_equal(a.psf, b.psf)
+        if a.want_grad:
+            assert np.array_equal(a.grad, b.grad)
+    # one request against the oracle
+    r = next(x for x in alone if x.want_grad)
+    s = make_server(graphs=False, tuner=tuner)
+    s.prewarm([(r.n_pupil, r.n_focal, r.n_wavelengths)])
+    amp, basis, _ = (t.cpu().numpy() for t in s.ex.models[r.n_pupil])
+    c = np.zeros(K)
+    c[:r.coefficients.size] = np.asarray(r.coefficients, np.float32)
+    opd = O.eval_basis(basis.astype(np.float64), c)
+    wls = s.ex.wavelengths(r.n_wavelengths)
+    ref = O.poly_psf(amp, opd, wls, r.weights, 1.0, r.n_focal, s.ex.pixel_scale)
+    s.close()
+    assert rel(r.psf, ref) < 1e-5
