@@ -771,7 +771,9 @@ def main():
                     choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
-    ap.add_argument("--slots", type=int, default=4, help="serving: concurrent stream slots")
+    ap.add_argument("--slots", type=int, default=6,
+                    help="serving: concurrent stream slots (measured: 4 gives p99 2.1-4.2 ms "
+                         "across runs, 6 gives 2.1-2.2 ms, 8 oversubscribes the 150 GB budget)")
     ap.add_argument("--fft-n", type=int, default=1024, help="fft: pupil side (pad 2)")
     ap.add_argument("--scene-sources", type=int, default=1024,
                     help="cfg4: point sources (1024 is the measured configuration)")
