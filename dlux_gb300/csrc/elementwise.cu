@@ -727,7 +727,7 @@ __global__ void obj_finish_kernel(ObjReduceArgs a, int want_w) {
 // pim, g_opd = sum k_l pim), tilt partials, and weight partials
 // sum_p pre_l amp_p (per-warp float sums of one pixel each, then FP64).
 template <bool kSplit>
-__global__ void __launch_bounds__(256, 5) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
+__global__ void __launch_bounds__(256, 4) obj_pupil_fused_kernel(ObjReduceArgs a, int want_w) {
   pdl_enter();
   // dynamic shared memory: [L] float4 (1/lambda hi, lo, sqrt(w), k) then, when
   // weight gradients are wanted, [8 warps][L] double partials
@@ -768,9 +768,9 @@ __global__ void __launch_bounds__(256, 5) obj_pupil_fused_kernel(ObjReduceArgs a
       if (od.amp_scale) amp *= *od.amp_scale;
     }
     float sre = 0.f, sim = 0.f, sk = 0.f;
-    // The Ebar loads of four wavelengths are issued before their arithmetic,
+    // The Ebar loads of eight wavelengths are issued before their arithmetic,
     // so that their latencies overlap.
-    constexpr int kPre = 4;
+    constexpr int kPre = 8;  // measured: 8 beats 4 (-6.5 us per 64-wavelength step) and 2
     for (int l0 = 0; l0 < a.L; l0 += kPre) {
       float2 ebq[kPre];
 #pragma unroll
