@@ -137,16 +137,18 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
   }
 }
 
-struct alignas(8) Bf16Quad {
-  __nv_bfloat16 v[4];
+template <int V>
+struct alignas(2 * V) Bf16Vec {
+  __nv_bfloat16 v[V];
 };
 
-// Split-BF16 output only, four adjacent pixels of one row per thread (n % 4
-// == 0): each of the four planes gets one 8-byte store per thread and
+// Split-BF16 output only, V adjacent pixels of one row per thread (n % V ==
+// 0): each of the four planes gets one 2V-byte store per thread and
 // wavelength, and the per-pixel FP64 path set-up is amortised over a
-// wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg), so that
-// small pupils still fill the GPU). Same arithmetic per pixel as phasor_kernel.
-__global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
+// wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg)). Same
+// arithmetic per pixel as phasor_kernel.
+template <int V>
+__global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
   pdl_enter();
   extern __shared__ float psm[];
   const long long npix = (long long)a.n * a.n;
@@ -164,7 +166,7 @@ __global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
     }
     __syncthreads();
   }
-  const long long p0 = 4 * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  const long long p0 = V * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
   if (p0 >= npix) return;
   const int y = (int)(p0 / a.n);
   const int x0 = (int)(p0 - (long long)y * a.n);
@@ -180,10 +182,10 @@ __global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
     const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
     const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
     const float scale = (o_scale ? *o_scale : 1.0f);
-    FF path[4], ph[4];
-    float amp[4];
+    FF path[V], ph[V];
+    float amp[V];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < V; ++k) {
       const long long p = p0 + k;
       const double X = ((double)(x0 + k) - half) * a.pixel_scale;
       path[k] = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
@@ -203,9 +205,9 @@ __global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
       float sw = 1.0f;
       if (cached) sw = c_sw[r * L + wl];
       else if (o_w) sw = sqrtf(o_w[wl]);
-      Bf16Quad q[4];
+      Bf16Vec<V> q[4];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < V; ++k) {
         const float2 u = cis_ff_split(path[k], FF{il2.x, il2.y}, ph[k]);
         const float sc = amp[k] * sw;
         split_bf16(u.x * sc, q[0].v[k], q[1].v[k]);
@@ -213,7 +215,7 @@ __global__ void phasor_split4_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
       }
       __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p0;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Quad*>(base + c * npix) = q[c];
+      for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Vec<V>*>(base + c * npix) = q[c];
     }
   }
 }
@@ -235,8 +237,10 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     // One wavelength group: splitting the wavelengths over more blocks
     // measured slower at 512^2 x 64 (42.9 vs 38.3 us), the FP64 path set-up
     // being repeated per group.
-    DLX_PDL_LAUNCH("phasor_split4_kernel", phasor_split4_kernel,
-                   dim3(ceil_div(npix / 4, 256), 1), dim3(256), cached ? smem : 0, s, a,
+    // 4 pixels per thread (2 measured the same at 512^2 x 64)
+    constexpr int V = 4;
+    DLX_PDL_LAUNCH("phasor_splitv_kernel", phasor_splitv_kernel<V>,
+                   dim3(ceil_div(npix / V, 256), 1), dim3(256), cached ? smem : 0, s, a,
                    *inv_lambda_arg, cached, L);
     return DLX_OK;
   } else if (a.out_split && !a.out_c64 && !a.in)
