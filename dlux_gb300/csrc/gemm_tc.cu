@@ -44,6 +44,7 @@
 #include <cudaTypedefs.h>
 
 #include <atomic>
+#include <cstdlib>
 #include <mutex>
 
 #include "epilogue.cuh"
@@ -73,6 +74,19 @@ static_assert(128 * REG_CTRL + 256 * REG_EPI <= TC_THREADS * REG_LAUNCH,
               "register split exceeds the launch registers");
 static_assert(REG_LAUNCH * TC_THREADS <= 65536, "launch registers exceed the SM");
 constexpr uint32_t TMEM_COLS = 512;
+// Paired form (cta_group::2, opt-in). A cluster of two CTAs on adjacent
+// n-tiles issues M = 256 MMAs from the even CTA: each CTA holds its own 128 B
+// rows and half (64) of the A rows, and the tensor cores exchange the A
+// halves. Per SM that is 6 KB of operand reads per MMA and 48 KB of fills per
+// K block instead of 8 KB and 64 KB, a fourth pipeline stage in the same
+// shared memory, and a quarter less L2 traffic. Every output element is formed
+// from the same products in the same order, so results are bitwise those of
+// the single-CTA form.
+constexpr int TP_STAGES = 4;
+constexpr int TP_A_PLANE_BYTES = (TC_BM / 2) * TC_BK * 2;                 // 4 KB
+constexpr int TP_STAGE_BYTES = 4 * TP_A_PLANE_BYTES + 4 * B_PLANE_BYTES;  // 48 KB
+static_assert(TP_STAGES * TP_STAGE_BYTES == TC_STAGES * STAGE_BYTES,
+              "both forms use the same shared-memory layout size");
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
 
 // ------------------------------- PTX wrappers -------------------------------
@@ -155,21 +169,71 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// Paired form: the copy lands in this CTA's shared memory and completes on
+// the mbarrier at cluster address `bar` (the even CTA's).
+__device__ __forceinline__ void tma_load_3d_pair(void* dst, const CUtensorMap* map, uint32_t bar,
+                                                 int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      ".cta_group::2 [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Cluster address of the shared variable at the same offset in CTA `rank`.
+__device__ __forceinline__ uint32_t cluster_addr(const void* local, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(local)), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t cluster_bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_bar)
+               : "memory");
+}
+
+// Every thread of both CTAs.
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// PAIR: the cta_group::2 forms, issued by one warp in each CTA of the pair.
+template <bool PAIR = false>
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                   smem_u32(slot)),
-               "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  if constexpr (PAIR) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  } else {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
 }
 
+template <bool PAIR = false>
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
-               : "memory");
+  if constexpr (PAIR)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
+  else
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -179,20 +243,39 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
+template <bool PAIR = false>
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc,
                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
-      : "memory");
+  if constexpr (PAIR)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
 }
 
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(bar))
+      : "memory");
+}
+
+// Paired form: arrive on the mbarrier at this offset in every CTA of `mask`
+// once the pair's MMAs issued so far have completed.
+__device__ __forceinline__ void mma_commit_pair(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(smem_u32(bar)),
+      "h"(mask)
       : "memory");
 }
 
@@ -268,9 +351,10 @@ __device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
 // (MMA M = TC_BN rows -> TMEM lanes) and its second the A tile (MMA N = TC_BM
 // -> TMEM columns). Negating either factor negates the product, so the sign
 // bit serves the -Ai*Bi and conj(A) terms unchanged.
-__host__ __device__ constexpr uint32_t make_idesc(bool neg_a) {
+// `mrows` is the MMA M: TC_BN, or 2 TC_BN for the paired form.
+__host__ __device__ constexpr uint32_t make_idesc(bool neg_a, int mrows = TC_BN) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((neg_a ? 1u : 0u) << 13) |
-         ((uint32_t)(TC_BM >> 3) << 17) | ((uint32_t)(TC_BN >> 4) << 24);
+         ((uint32_t)(TC_BM >> 3) << 17) | ((uint32_t)(mrows >> 4) << 24);
 }
 
 // --------------------------- vectorised epilogue ----------------------------
@@ -306,17 +390,38 @@ __device__ __forceinline__ TcWork tc_work(const TcParams& p, int w, int nkb) {
   t.kb1 = min(nkb, t.kb0 + p.kbps);
   return t;
 }
+// Paired form: work item w is the n-tile pair (2 np, 2 np + 1) of (b, mt);
+// CTA `rank` of the cluster takes n-tile 2 np + rank. No split K.
+__device__ __forceinline__ TcWork tc_work_pair(const TcParams& p, int w, int nkb, int rank) {
+  TcWork t;
+  const int np = p.nt >> 1;
+  t.ks = 0;
+  t.b = w / (p.mt * np);
+  const int r = w - t.b * p.mt * np;
+  t.mt = r / np;
+  t.nt = 2 * (r - t.mt * np) + rank;
+  t.kb0 = 0;
+  t.kb1 = nkb;
+  return t;
+}
 
-template <int KIND>
+// PAIR: the paired form, launched in clusters of two CTAs (work items are
+// n-tile pairs, see tc_work_pair). The even CTA issues the MMAs; both CTAs
+// load their operand parts against the even CTA's `full` barriers, drain
+// their own TMEM and release it on the even CTA's `tempty` barrier.
+template <int KIND, bool PAIR = false>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_cgemm_kernel(const __grid_constant__ CUtensorMap tmA,
                     const __grid_constant__ CUtensorMap tmB, const TcParams p) {
+  constexpr int kStages = PAIR ? TP_STAGES : TC_STAGES;
+  constexpr int kStageBytes = PAIR ? TP_STAGE_BYTES : STAGE_BYTES;
+  constexpr int kAPlane = PAIR ? TP_A_PLANE_BYTES : A_PLANE_BYTES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + TC_STAGES * STAGE_BYTES);
-  uint64_t* empty = full + TC_STAGES;
-  uint64_t* tfull = empty + TC_STAGES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* tfull = empty + kStages;
   uint64_t* tempty = tfull + 1;
   uint64_t* mdone = tempty + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
@@ -325,23 +430,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   const int nkb = (p.K + TC_BK - 1) / TC_BK;
+  // work items: one per CTA, or one per cluster (PAIR)
+  const int rank = PAIR ? (int)cluster_rank() : 0;
+  const int unit0 = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+  const int ustep = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) {
+    for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
-    mbar_init(tempty, TC_EPI_WARPS);
+    mbar_init(tempty, PAIR ? 2 * TC_EPI_WARPS : TC_EPI_WARPS);
     mbar_init(mdone, 1);
     *abort_flag = 0;
     fence_barrier_init();
     prefetch_tmap(&tmA);
     prefetch_tmap(&tmB);
   }
-  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  if (warp == 1) tmem_alloc<PAIR>(tmem_slot, TMEM_COLS);
   tc_fence_before();
-  __syncthreads();
+  // PAIR: the peer's barriers must be initialised and its TMEM allocated
+  // before either CTA signals or writes across the pair.
+  __syncwarp();
+  if constexpr (PAIR) cluster_sync(); else __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   // The prologue above overlaps the previous kernel of the stream (PDL);
@@ -357,39 +469,54 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       uint32_t ph = 0;
       uint32_t issued_mask = 0, issued_ph = 0;
       bool ok = true;
-      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
-        const TcWork t = tc_work(p, w, nkb);
+      for (int w = unit0; w < p.total && ok; w += ustep) {
+        const TcWork t = PAIR ? tc_work_pair(p, w, nkb, rank) : tc_work(p, w, nkb);
         const int b = t.b, mt = t.mt, nt = t.nt;
         const int ab = b / p.a_batch_div;
         for (int kb = t.kb0; kb < t.kb1; ++kb) {
           if (!mbar_wait(&empty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
-          mbar_expect_tx(&full[stage], STAGE_BYTES);
-          uint8_t* base = smem + stage * STAGE_BYTES;
+          uint8_t* base = smem + stage * kStageBytes;
+          if constexpr (PAIR) {
+            // both CTAs' parts complete on the even CTA's barrier
+            const uint32_t fb = cluster_addr(&full[stage], 0);
+            if (rank == 0) mbar_expect_tx(&full[stage], 2 * kStageBytes);
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            tma_load_3d(base + q * A_PLANE_BYTES, &tmA, &full[stage], kb * TC_BK, mt * TC_BM,
-                        ab * 4 + q);
+            for (int q = 0; q < 4; ++q)
+              tma_load_3d_pair(base + q * kAPlane, &tmA, fb, kb * TC_BK,
+                               mt * TC_BM + rank * (TC_BM / 2), ab * 4 + q);
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            tma_load_3d(base + 4 * A_PLANE_BYTES + q * B_PLANE_BYTES, &tmB, &full[stage],
-                        kb * TC_BK, nt * TC_BN, (b / p.b_batch_div) * 4 + q);
+            for (int q = 0; q < 4; ++q)
+              tma_load_3d_pair(base + 4 * kAPlane + q * B_PLANE_BYTES, &tmB, fb, kb * TC_BK,
+                               nt * TC_BN, (b / p.b_batch_div) * 4 + q);
+          } else {
+            mbar_expect_tx(&full[stage], STAGE_BYTES);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              tma_load_3d(base + q * A_PLANE_BYTES, &tmA, &full[stage], kb * TC_BK, mt * TC_BM,
+                          ab * 4 + q);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              tma_load_3d(base + 4 * A_PLANE_BYTES + q * B_PLANE_BYTES, &tmB, &full[stage],
+                          kb * TC_BK, nt * TC_BN, (b / p.b_batch_div) * 4 + q);
+          }
           issued_mask |= 1u << stage;
           issued_ph = (issued_ph & ~(1u << stage)) | (ph << stage);
-          if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
+          if (++stage == kStages) { stage = 0; ph ^= 1u; }
         }
       }
-      if (!ok) {
-        // Drain every copy this thread issued before the CTA can exit.
-        for (int s = 0; s < TC_STAGES; ++s)
+      // Drain every copy this thread issued before the CTA can exit. In the
+      // paired form only the even CTA sees completions (on its barriers).
+      if (!ok && (!PAIR || rank == 0)) {
+        for (int s = 0; s < kStages; ++s)
           if (issued_mask & (1u << s))
             mbar_wait(&full[s], (issued_ph >> s) & 1u, abort_flag, p.status, false);
       }
     }
   } else if (warp == 1) {
     // ------------------------------- MMA issuer -------------------------------
-    if (lane == 0) {
-      const uint32_t id_pos = make_idesc(false);
-      const uint32_t id_neg = make_idesc(true);
+    if (lane == 0 && (!PAIR || rank == 0)) {
+      const uint32_t id_pos = make_idesc(false, PAIR ? 2 * TC_BN : TC_BN);
+      const uint32_t id_neg = make_idesc(true, PAIR ? 2 * TC_BN : TC_BN);
       // Sign of the Ai * Bi term in Re and of the Ai * Br term in Im.
       const uint32_t id_rii = p.conj_a ? id_pos : id_neg;
       const uint32_t id_iir = p.conj_a ? id_neg : id_pos;
@@ -399,51 +526,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int stage = 0;
       uint32_t ph = 0, acc_ph = 0;
       bool ok = true;
-      for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
-        const TcWork t = tc_work(p, w, nkb);
+      for (int w = unit0; w < p.total && ok; w += ustep) {
+        const TcWork t = PAIR ? tc_work_pair(p, w, nkb, rank) : tc_work(p, w, nkb);
         if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
         tc_fence_after();
         for (int kb = t.kb0; kb < t.kb1; ++kb) {
           if (!mbar_wait(&full[stage], ph, abort_flag, p.status)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t sa = smem_u32(smem + stage * STAGE_BYTES);
-          const uint32_t sb = sa + 4 * A_PLANE_BYTES;
+          const uint32_t sa = smem_u32(smem + stage * kStageBytes);
+          const uint32_t sb = sa + 4 * kAPlane;
 #pragma unroll
           for (int j = 0; j < TC_BK / 16; ++j) {
             const uint32_t ko = j * 32;  // 16 bf16 = 32 bytes along K
-            const uint64_t arh = make_desc(sa + 0 * A_PLANE_BYTES + ko);
-            const uint64_t arl = make_desc(sa + 1 * A_PLANE_BYTES + ko);
-            const uint64_t aih = make_desc(sa + 2 * A_PLANE_BYTES + ko);
-            const uint64_t ail = make_desc(sa + 3 * A_PLANE_BYTES + ko);
+            const uint64_t arh = make_desc(sa + 0 * kAPlane + ko);
+            const uint64_t arl = make_desc(sa + 1 * kAPlane + ko);
+            const uint64_t aih = make_desc(sa + 2 * kAPlane + ko);
+            const uint64_t ail = make_desc(sa + 3 * kAPlane + ko);
             const uint64_t brh = make_desc(sb + 0 * B_PLANE_BYTES + ko);
             const uint64_t brl = make_desc(sb + 1 * B_PLANE_BYTES + ko);
             const uint64_t bih = make_desc(sb + 2 * B_PLANE_BYTES + ko);
             const uint64_t bil = make_desc(sb + 3 * B_PLANE_BYTES + ko);
             const uint32_t acc = (kb > t.kb0 || j > 0) ? 1u : 0u;
             // Re += Ar Br -/+ Ai Bi
-            mma_bf16(m_re, brh, arh, id_pos, acc);
-            mma_bf16(m_re, bih, aih, id_rii, 1u);
-            mma_bf16(c_re, brl, arh, id_pos, acc);
-            mma_bf16(c_re, brh, arl, id_pos, 1u);
-            mma_bf16(c_re, bil, aih, id_rii, 1u);
-            mma_bf16(c_re, bih, ail, id_rii, 1u);
+            mma_bf16<PAIR>(m_re, brh, arh, id_pos, acc);
+            mma_bf16<PAIR>(m_re, bih, aih, id_rii, 1u);
+            mma_bf16<PAIR>(c_re, brl, arh, id_pos, acc);
+            mma_bf16<PAIR>(c_re, brh, arl, id_pos, 1u);
+            mma_bf16<PAIR>(c_re, bil, aih, id_rii, 1u);
+            mma_bf16<PAIR>(c_re, bih, ail, id_rii, 1u);
             // Im += Ar Bi +/- Ai Br
-            mma_bf16(m_im, bih, arh, id_pos, acc);
-            mma_bf16(m_im, brh, aih, id_iir, 1u);
-            mma_bf16(c_im, bil, arh, id_pos, acc);
-            mma_bf16(c_im, bih, arl, id_pos, 1u);
-            mma_bf16(c_im, brl, aih, id_iir, 1u);
-            mma_bf16(c_im, brh, ail, id_iir, 1u);
+            mma_bf16<PAIR>(m_im, bih, arh, id_pos, acc);
+            mma_bf16<PAIR>(m_im, brh, aih, id_iir, 1u);
+            mma_bf16<PAIR>(c_im, bil, arh, id_pos, acc);
+            mma_bf16<PAIR>(c_im, bih, arl, id_pos, 1u);
+            mma_bf16<PAIR>(c_im, brl, aih, id_iir, 1u);
+            mma_bf16<PAIR>(c_im, brh, ail, id_iir, 1u);
           }
-          mma_commit(&empty[stage]);
-          if (++stage == TC_STAGES) { stage = 0; ph ^= 1u; }
+          if constexpr (PAIR) mma_commit_pair(&empty[stage], 0x3); else mma_commit(&empty[stage]);
+          if (++stage == kStages) { stage = 0; ph ^= 1u; }
         }
         if (!ok) break;
-        mma_commit(tfull);
+        if constexpr (PAIR) mma_commit_pair(tfull, 0x3); else mma_commit(tfull);
         acc_ph ^= 1u;
       }
       // Wait for every MMA this thread issued before TMEM is released.
-      mma_commit(mdone);
+      if constexpr (PAIR) mma_commit_pair(mdone, 0x1); else mma_commit(mdone);
       mbar_wait(mdone, 0, abort_flag, p.status, false);
     }
   }
@@ -455,10 +582,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int half = (warp - TC_EPI_W0) >> 2;  // the two warps of a quarter take alternate chunks
     uint32_t acc_ph = 0;
-    for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
+    for (int w = unit0; w < p.total; w += ustep) {
       if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
       tc_fence_after();
-      const TcWork t = tc_work(p, w, nkb);
+      const TcWork t = PAIR ? tc_work_pair(p, w, nkb, rank) : tc_work(p, w, nkb);
       const int b = t.b, mt = t.mt, nt = t.nt;
       const int n = nt * TC_BN + q * 32 + lane;
       const int mbase = mt * TC_BM;
@@ -479,7 +606,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tempty);
+      if (lane == 0) {
+        if constexpr (PAIR) mbar_arrive_cluster(cluster_addr(tempty, 0));
+        else mbar_arrive(tempty);
+      }
       if (n < p.N) {
         if constexpr (KIND == EPI_PARTIAL) {
           // raw partial sums of split t.ks, one column per thread
@@ -500,11 +630,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 
   tc_fence_before();
-  __syncthreads();
+  // PAIR: neither CTA leaves (or frees TMEM) while the pair's MMAs, copies or
+  // arrivals may still touch it.
+  __syncwarp();
+  if constexpr (PAIR) cluster_sync(); else __syncthreads();
   tc_fence_after();
   if (warp == 1) {
     __syncwarp();
-    tmem_dealloc(tmem, TMEM_COLS);
+    tmem_dealloc<PAIR>(tmem, TMEM_COLS);
   }
 }
 
@@ -819,14 +952,54 @@ LoadedKernel loaded_kernel(int kind) {
   }
 }
 
+// The paired form per epilogue kind (split K never runs paired).
+LoadedKernel loaded_kernel_pair(int kind) {
+  switch (kind) {
+    case EPI_C64: return tc_cgemm_kernel<EPI_C64, true>;
+    case EPI_SPLIT: return tc_cgemm_kernel<EPI_SPLIT, true>;
+    case EPI_INTENSITY: return tc_cgemm_kernel<EPI_INTENSITY, true>;
+    case EPI_GRADF: return tc_cgemm_kernel<EPI_GRADF, true>;
+    case EPI_PUPIL: return tc_cgemm_kernel<EPI_PUPIL, true>;
+    case EPI_PSF_GRADF: return tc_cgemm_kernel<EPI_PSF_GRADF, true>;
+    case EPI_SPLIT2: return tc_cgemm_kernel<EPI_SPLIT2, true>;
+    case EPI_DOT: return tc_cgemm_kernel<EPI_DOT, true>;
+    default: return nullptr;
+  }
+}
+
 const void* const* loaded_kernels() {
   static const void* all[] = {
       (const void*)tc_cgemm_kernel<EPI_C64>,       (const void*)tc_cgemm_kernel<EPI_SPLIT>,
       (const void*)tc_cgemm_kernel<EPI_INTENSITY>, (const void*)tc_cgemm_kernel<EPI_GRADF>,
       (const void*)tc_cgemm_kernel<EPI_PUPIL>,     (const void*)tc_cgemm_kernel<EPI_PSF_GRADF>,
       (const void*)tc_cgemm_kernel<EPI_SPLIT2>,    (const void*)tc_cgemm_kernel<EPI_DOT>,
-      (const void*)tc_cgemm_kernel<EPI_PARTIAL>,   nullptr};
+      (const void*)tc_cgemm_kernel<EPI_PARTIAL>,
+      (const void*)tc_cgemm_kernel<EPI_C64, true>,       (const void*)tc_cgemm_kernel<EPI_SPLIT, true>,
+      (const void*)tc_cgemm_kernel<EPI_INTENSITY, true>, (const void*)tc_cgemm_kernel<EPI_GRADF, true>,
+      (const void*)tc_cgemm_kernel<EPI_PUPIL, true>,     (const void*)tc_cgemm_kernel<EPI_PSF_GRADF, true>,
+      (const void*)tc_cgemm_kernel<EPI_SPLIT2, true>,    (const void*)tc_cgemm_kernel<EPI_DOT, true>,
+      nullptr};
   return all;
+}
+
+// Paired launch: clusters of two CTAs, with programmatic dependent launch.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pair(void (*kernel)(KArgs...), int clusters, cudaStream_t s, Args&&... args) {
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[1].id = cudaLaunchAttributeClusterDimension;
+  at[1].val.clusterDim.x = 2;
+  at[1].val.clusterDim.y = 1;
+  at[1].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * clusters);
+  cfg.blockDim = dim3(TC_THREADS);
+  cfg.dynamicSmemBytes = SMEM_BYTES;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 // Split-K reduction: D = sum of the partials in split order, then the GEMM's
 // own epilogue element by element (the FP32 form's epilogue code).
@@ -852,6 +1025,15 @@ __global__ void splitk_reduce_kernel(const float2* __restrict__ part, int splits
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_num_sms = 0;
+int g_pair_clusters = 0;  // co-resident clusters of the paired form (0: unavailable)
+// Paired form of the loaded-operand GEMM (dlx_set_gemm_pair, or DLX_GEMM_PAIR=1
+// in the environment); off by default: on GB300 it measures the same as the
+// single-CTA form (within 1-3% either way on the batched workloads), whose
+// mainloop is bound by barrier hand-offs, TMA latency and the epilogue's
+// memory traffic rather than by shared-memory or L2 bandwidth. Read at every
+// launch, so a change also applies to existing plans (but not to CUDA graphs
+// already captured).
+std::atomic<int> g_pair_enabled{0};
 int g_cc = 0;
 int* g_status = nullptr;
 std::once_flag g_once;
@@ -879,6 +1061,7 @@ void init_once() {
     return;
   }
   g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  if (const char* e = getenv("DLX_GEMM_PAIR")) g_pair_enabled.store(atoi(e) != 0 ? 1 : 0);
   if (cudaMalloc(&g_status, sizeof(int)) != cudaSuccess ||
       cudaMemset(g_status, 0, sizeof(int)) != cudaSuccess) {
     g_init_status = fail(DLX_ERR_NOMEM, "status word allocation failed");
@@ -904,6 +1087,27 @@ void init_once() {
                            G_SMEM_BYTES) != cudaSuccess) {
     g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tensor-core GEMM) failed");
     return;
+  }
+  // How many two-CTA clusters fit at once: the paired form's persistent grid.
+  {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * (g_num_sms / 2));
+    cfg.blockDim = dim3(TC_THREADS);
+    cfg.dynamicSmemBytes = SMEM_BYTES;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (const void*)tc_cgemm_kernel<EPI_C64, true>, &cfg) !=
+        cudaSuccess) {
+      (void)cudaGetLastError();
+      n = 0;
+    }
+    g_pair_clusters = n;
   }
 }
 
@@ -935,6 +1139,8 @@ bool tc_supported() {
 // the call (dlx_set_split_k); on by default.
 std::atomic<int> g_split_k_enabled{1};
 bool split_k_enabled() { return g_split_k_enabled.load() != 0; }
+
+
 
 int split_k_count(long long tiles, int K) {
   std::call_once(g_once, init_once);
@@ -992,19 +1198,23 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   }
   if (!g.As || !g.Bs) return fail(DLX_ERR_ARG, "split-BF16 GEMM: null operand");
   const int nA = (g.batch + div - 1) / div;
+  const int nkb = (g.K + TC_BK - 1) / TC_BK;
+  const bool split = g.splits > 1 && g.split_ws != nullptr && nkb > 1;
+  const int nt_tiles = (g.N + TC_BN - 1) / TC_BN;
+  // Paired form: n-tiles in pairs, no split K.
+  const bool pair = !split && nt_tiles % 2 == 0 && g_pair_clusters > 0 &&
+                    g_pair_enabled.load() != 0;
   CUtensorMap ta, tb;
-  DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, TC_BM));
+  DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, pair ? TC_BM / 2 : TC_BM));
   DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, nB, TC_BN));
   TcParams p{};
   p.batch = g.batch; p.M = g.M; p.N = g.N; p.K = g.K;
   p.a_batch_div = div;
   p.b_batch_div = bdiv;
   p.mt = (g.M + TC_BM - 1) / TC_BM;
-  p.nt = (g.N + TC_BN - 1) / TC_BN;
-  const int nkb = (g.K + TC_BK - 1) / TC_BK;
+  p.nt = nt_tiles;
   p.splits = 1;
   p.kbps = nkb;
-  const bool split = g.splits > 1 && g.split_ws != nullptr && nkb > 1;
   if (split) {
     p.kbps = (nkb + g.splits - 1) / g.splits;
     p.splits = (nkb + p.kbps - 1) / p.kbps;  // every split gets at least one K block
@@ -1016,6 +1226,16 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   if (split) {
     p.epi.kind = EPI_PARTIAL;
     p.epi.partial = g.split_ws;
+  }
+  if (pair) {
+    p.total = g.batch * p.mt * (p.nt / 2);  // n-tile pairs
+    LoadedKernel kern = loaded_kernel_pair(p.epi.kind);
+    if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
+    const int clusters = p.total < g_pair_clusters ? p.total : g_pair_clusters;
+    const cudaError_t e = launch_pair(kern, clusters, s, ta, tb, p);
+    if (e != cudaSuccess) return check_cuda(e, "tc_cgemm_kernel (paired)");
+    note_launch();
+    return DLX_OK;
   }
   const int grid = p.total < g_num_sms ? p.total : g_num_sms;
   LoadedKernel kern = loaded_kernel(p.epi.kind);
@@ -1033,6 +1253,18 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
 
 extern "C" int dlx_set_split_k(int enable) {
   dlx::g_split_k_enabled.store(enable ? 1 : 0);
+  return DLX_OK;
+}
+
+extern "C" int dlx_set_gemm_pair(int enable) {
+  dlx::g_pair_enabled.store(enable ? 1 : 0);
+  return DLX_OK;
+}
+
+extern "C" int dlx_gemm_pair_clusters(int* clusters) {
+  if (!clusters) return DLX_ERR_ARG;
+  std::call_once(dlx::g_once, dlx::init_once);
+  *clusters = dlx::g_init_status == DLX_OK ? dlx::g_pair_clusters : 0;
   return DLX_OK;
 }
 

@@ -293,6 +293,16 @@ int dlx_poly_forward_token(dlx_poly_plan plan, unsigned long long* token);
  * same alone and in a batch of that plan. Plans on a shared workspace
  * (dlx_poly_plan_create_shared) do not split. No dLux counterpart. */
 int dlx_set_split_k(int enable);
+/* Paired form of the loaded-operand tensor-core GEMM (default off; also
+ * DLX_GEMM_PAIR=1 in the environment): a GEMM with an even number of
+ * 128-column output tiles and no split K runs in clusters of two CTAs that
+ * issue 256-row MMAs (cta_group::2), each CTA loading half of the A tile.
+ * Results are bitwise the single-CTA form's. Read at every launch (CUDA
+ * graphs keep the form they were captured with). No dLux counterpart. */
+int dlx_set_gemm_pair(int enable);
+/* Two-CTA clusters of the paired GEMM that fit on the device at once (0: the
+ * paired form is unavailable). No dLux counterpart. */
+int dlx_gemm_pair_clusters(int* clusters);
 int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token);
 /* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
  * is known before the forward pass (a serving request, a linear functional):
