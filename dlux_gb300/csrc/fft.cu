@@ -9,8 +9,8 @@
 // sits at slot (j + npad - c) mod P and whose output element k is read at slot
 // (k - c) mod P. One kernel covers every pass. It loads n_in elements of each
 // line through an input ramp, scatters them into bit-reversed slots, runs
-// log2(P) in-place butterfly stages and gathers n_out elements through an
-// output ramp and a scale:
+// log2(P) in-place butterfly stages (four per shared-memory pass) and gathers
+// n_out elements through an output ramp and a scale:
 //   forward   rows:    N lines of N -> P   (x), into tmp [N][P]
 //             columns: P lines of N -> P   (y), from tmp into out [P][P]
 //   adjoint   rows:    P lines of P -> N   (x, conjugate), into tmp [P][N]
@@ -42,29 +42,73 @@ struct LineIO {
 };
 
 // Shared-memory slot of element k of line li (P elements per line). The low
-// four index bits are XORed with four high bits and with a per-line pattern,
-// so that one wavefront of 16 threads (8-byte words) lands in 16 distinct bank
-// pairs for the bit-reversed scatter (consecutive slots -> k differing in the
-// high bits), for the butterflies (consecutive k) and for the gathers, also
-// when a wavefront spans several lines (the column passes):
+// four index bits are XORed with every higher nibble of k and with a
+// per-line pattern, so that one wavefront of 16 threads (8-byte words) lands
+// in 16 distinct bank pairs in the radix-16 passes (16 consecutive k, or k 16
+// apart in the first pass) and in the gathers, also when a wavefront spans
+// several lines (the column passes). The second radix-8 pass (two groups of
+// 8 k, 64 apart) sees 2-way conflicts; removing them (bit 6 folded into bit
+// 3 as well) measured no faster. Per-line patterns:
 //   2 lines x 8 elements:  pattern 9 flips bits 0 and 3 of the second line;
 //   4 lines x 4 elements:  pattern 5 li gives distinct low and high bit pairs.
-// Every map is a bijection on [0, P) (only the low nibble changes, by a value
-// that depends on the other bits); for P < 16 it is the identity.
+// The bit-reversed scatter sees at most 2-way conflicts at the sizes used
+// (4-way at P = 512 and 8192 with 2 lines per block). Every map is a
+// bijection on [0, P): only the low nibble changes, by a value that depends
+// on the other bits. For P < 16 it is the identity.
 template <int LPB>
-__device__ __forceinline__ int smem_slot(int li, int k, int sh, int P) {
-  const int g = P < 16 ? 0 : (LPB == 2 ? 9 * li : (LPB == 4 ? 5 * li : li)) & 15;
-  return li * P + (k ^ (((k >> sh) & 15) ^ g));
+__device__ __forceinline__ int smem_slot(int li, int k, int P) {
+  if (P < 16) return li * P + k;
+  const int g = LPB == 2 ? 9 * li : (LPB == 4 ? 5 * li : li);
+  return li * P + (k ^ (((k >> 4) ^ (k >> 8) ^ (k >> 12) ^ g) & 15));
 }
 
-template <int LPB>
+// Butterfly stages s .. s + R - 1 of every line (half-lengths h = 2^lh, 2h,
+// ..., 2^(R-1) h) as one pass: the 2^R elements k0 + m h of a group stay in
+// registers across the R stages, so shared memory is read and written once
+// per R stages. These are the same butterflies and twiddles, in the same
+// order, as R radix-2 stages: at half-length H = 2^j h, element m (bit j
+// clear) pairs with m + 2^j and takes the twiddle of position
+// pos + (m mod 2^j) h.
+template <int LPB, int R>
+__device__ __forceinline__ void radix_pass(float2* x, const float2* tw, int log2p, int lh,
+                                           int P) {
+  constexpr int M = 1 << R;
+  const int h = 1 << lh;
+  const int gq = log2p - R;  // P / 2^R groups per line
+  for (int t = threadIdx.x; t < (LPB << gq); t += blockDim.x) {
+    const int li = t >> gq;
+    const int i = t & ((1 << gq) - 1);
+    const int grp = i >> lh;
+    const int pos = i & (h - 1);
+    const int k0 = (grp << (lh + R)) + pos;
+    float2 v[M];
+#pragma unroll
+    for (int m = 0; m < M; ++m) v[m] = x[smem_slot<LPB>(li, k0 + m * h, P)];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int H = h << j;
+#pragma unroll
+      for (int m = 0; m < M; ++m) {
+        if (m & (1 << j)) continue;
+        const float2 w = tw[H - 1 + pos + (m & ((1 << j) - 1)) * h];
+        const float2 u = v[m];
+        const float2 q = cmul(v[m + (1 << j)], w);
+        v[m] = make_float2(u.x + q.x, u.y + q.y);
+        v[m + (1 << j)] = make_float2(u.x - q.x, u.y - q.y);
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < M; ++m) x[smem_slot<LPB>(li, k0 + m * h, P)] = v[m];
+  }
+}
+
+template <int LPB, int RMAX>
 __global__ void __launch_bounds__(256) fft_lines_kernel(
     const float2* __restrict__ in, LineIO io_in, int n_in, int off_in,
     float2* __restrict__ out, LineIO io_out, int n_out, int off_out, int lines, int log2p,
     float sign, const LineRamp* __restrict__ ramps, const float2* __restrict__ twg) {
   extern __shared__ float2 sm[];
   const int P = 1 << log2p;
-  const int sh = log2p - 4 > 4 ? log2p - 4 : 4;  // >= 4: the XOR never reads the low nibble
   float2* tw = sm;             // [P - 1]: stage of half-length h at [h - 1, 2h - 1)
   float2* x = sm + (P - 1);    // [LPB][P], slots by smem_slot
   const int b = blockIdx.y;
@@ -89,69 +133,21 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
       v = cmul(v, cis_ff(FF{(float)e, 0.f}, FF{rp.g_in.x, rp.g_in.y}, FF{rp.d_in.x, rp.d_in.y}));
     const int slot = (e + off_in) & (P - 1);  // P is a power of two: also for e + off_in < 0
     const int k = log2p > 0 ? (int)(__brev((unsigned)slot) >> (32 - log2p)) : 0;
-    x[smem_slot<LPB>(li, k, sh, P)] = v;
+    x[smem_slot<LPB>(li, k, P)] = v;
   }
   __syncthreads();
-  // Butterfly stages two at a time (radix-4 passes): the four elements
-  // k0 + {0, h, 2h, 3h} of stages s (half-length h) and s + 1 (2h) stay in
-  // registers between the stages, so each pass reads and writes shared memory
-  // once. Same butterflies and twiddles, in the same order, as two radix-2
-  // stages. An odd stage count ends with one radix-2 stage.
-  int s = 1;
-  if (log2p >= 2) {
-    const int qp = log2p - 2;  // P / 4 = 1 << qp quads per line
-    for (; s + 1 <= log2p; s += 2) {
-      const int h = 1 << (s - 1);
-      for (int t = threadIdx.x; t < LPB * (P / 4); t += blockDim.x) {
-        const int li = t >> qp;
-        const int i = t & ((P / 4) - 1);
-        const int grp = i >> (s - 1);
-        const int pos = i & (h - 1);
-        const int k0 = (grp << (s + 1)) + pos;
-        const int i0 = smem_slot<LPB>(li, k0, sh, P);
-        const int i1 = smem_slot<LPB>(li, k0 + h, sh, P);
-        const int i2 = smem_slot<LPB>(li, k0 + 2 * h, sh, P);
-        const int i3 = smem_slot<LPB>(li, k0 + 3 * h, sh, P);
-        const float2 w1 = tw[h - 1 + pos];
-        const float2 w2 = tw[2 * h - 1 + pos];
-        const float2 w3 = tw[2 * h - 1 + pos + h];
-        const float2 a0 = x[i0], a1 = x[i1], a2 = x[i2], a3 = x[i3];
-        // stage s: (k0, k0 + h) and (k0 + 2h, k0 + 3h), twiddle w1
-        float2 v = cmul(a1, w1);
-        const float2 b0 = make_float2(a0.x + v.x, a0.y + v.y);
-        const float2 b1 = make_float2(a0.x - v.x, a0.y - v.y);
-        v = cmul(a3, w1);
-        const float2 b2 = make_float2(a2.x + v.x, a2.y + v.y);
-        const float2 b3 = make_float2(a2.x - v.x, a2.y - v.y);
-        // stage s + 1: (k0, k0 + 2h) with w2 and (k0 + h, k0 + 3h) with w3
-        v = cmul(b2, w2);
-        x[i0] = make_float2(b0.x + v.x, b0.y + v.y);
-        x[i2] = make_float2(b0.x - v.x, b0.y - v.y);
-        v = cmul(b3, w3);
-        x[i1] = make_float2(b1.x + v.x, b1.y + v.y);
-        x[i3] = make_float2(b1.x - v.x, b1.y - v.y);
-      }
-      __syncthreads();
-    }
-  }
-  if (s == log2p) {
-    const int hp = log2p - 1;  // P / 2 = 1 << hp butterflies per line
-    const int half = 1 << (s - 1);
-    for (int t = threadIdx.x; t < LPB * (P / 2); t += blockDim.x) {
-      const int li = t >> hp;
-      const int i = t & ((P / 2) - 1);
-      const int grp = i >> (s - 1);
-      const int pos = i & (half - 1);
-      const int k0 = (grp << s) + pos;
-      const int i0 = smem_slot<LPB>(li, k0, sh, P);
-      const int i1 = smem_slot<LPB>(li, k0 + half, sh, P);
-      const float2 w = tw[half - 1 + pos];
-      const float2 u = x[i0];
-      const float2 v = cmul(x[i1], w);
-      x[i0] = make_float2(u.x + v.x, u.y + v.y);
-      x[i1] = make_float2(u.x - v.x, u.y - v.y);
+  // Butterfly stages RMAX at a time (radix-2^RMAX passes), then one pass of
+  // the remaining stages.
+  for (int st = 1; st <= log2p;) {
+    const int R = log2p - st + 1 < RMAX ? log2p - st + 1 : RMAX;
+    switch (R) {
+      case 4: if constexpr (RMAX >= 4) radix_pass<LPB, 4>(x, tw, log2p, st - 1, P); break;
+      case 3: radix_pass<LPB, 3>(x, tw, log2p, st - 1, P); break;
+      case 2: radix_pass<LPB, 2>(x, tw, log2p, st - 1, P); break;
+      default: radix_pass<LPB, 1>(x, tw, log2p, st - 1, P); break;
     }
     __syncthreads();
+    st += R;
   }
   const bool oline_fast = io_out.ls == 1;
   for (int t = threadIdx.x; t < LPB * n_out; t += blockDim.x) {
@@ -160,7 +156,7 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
     const int l = l0 + li;
     if (l >= lines) continue;
     const int slot = (o + off_out) & (P - 1);
-    float2 v = x[smem_slot<LPB>(li, slot, sh, P)];
+    float2 v = x[smem_slot<LPB>(li, slot, P)];
     if (rp.ramp_out)
       v = cmul(v, cis_ff(FF{(float)o, 0.f}, FF{rp.g_out.x, rp.g_out.y},
                          FF{rp.d_out.x, rp.d_out.y}));
@@ -187,38 +183,42 @@ __global__ void fft_twiddle_kernel(int P, float2* __restrict__ tw) {
 // stages are latency-bound); two lines keep column loads at 16-byte segments.
 int lines_per_block(int P) { return P <= 1024 ? 4 : 2; }
 
+// Stages per shared-memory pass. Radix-16 passes need 103 registers per
+// thread, radix-8 passes 63, which keeps twice the blocks resident. Measured
+// forward + adjoint of 16 planes: radix-8 wins up to P = 2048 (1.93 against
+// 2.67 ms), radix-16 from P = 4096 (10.6 against 11.3 ms).
+int max_radix_log2(int P) { return P >= 4096 ? 4 : 3; }
+
 int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* out, LineIO io_out,
                  int n_out, int off_out, int lines, int batch, int log2p, float sign,
                  const LineRamp* ramps, const float2* tw, cudaStream_t s) {
   const int P = 1 << log2p;
   const int lpb = lines_per_block(P);
+  const int rmax = max_radix_log2(P);
   const size_t smem = sizeof(float2) * ((size_t)P - 1 + (size_t)lpb * P);
   static std::atomic<bool> attr_done{false};  // host side, once per process
   if (!attr_done.load()) {
     const int lim = 200 * 1024;  // covers P <= 8192 at the lines-per-block choice above
-    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<8>,
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4, 3>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4>,
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4, 4>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<2>,
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<2, 3>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
+    DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<2, 4>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     attr_done.store(true);
   }
   dim3 grid((lines + lpb - 1) / lpb, batch);
-  switch (lpb) {
-    case 8:
-      fft_lines_kernel<8><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps, tw);
-      break;
-    case 4:
-      fft_lines_kernel<4><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps, tw);
-      break;
-    default:
-      fft_lines_kernel<2><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out,
-                                                  off_out, lines, log2p, sign, ramps, tw);
-      break;
+#define DLX_FFT_LAUNCH(L, R)                                                                \
+  fft_lines_kernel<L, R><<<grid, 256, smem, s>>>(in, io_in, n_in, off_in, out, io_out, n_out, \
+                                                 off_out, lines, log2p, sign, ramps, tw)
+  if (lpb == 4) {
+    if (rmax >= 4) DLX_FFT_LAUNCH(4, 4); else DLX_FFT_LAUNCH(4, 3);
+  } else {
+    if (rmax >= 4) DLX_FFT_LAUNCH(2, 4); else DLX_FFT_LAUNCH(2, 3);
   }
+#undef DLX_FFT_LAUNCH
   DLX_LAUNCH_CHECK("fft_lines_kernel");
   return DLX_OK;
 }
