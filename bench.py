@@ -364,37 +364,29 @@ def time_graphed(args, gstep, c0, world):
 
 
 def time_e2e(args, gstep, world):
-    """The graphed step with the coefficients copied from pinned host memory and the
-    loss, gradient and image read back every step."""
+    """The step driven from host memory: the coefficients come from pinned host
+    memory and the loss, gradient and image go back to pinned host memory every
+    step. The same step is captured with its copies inside the graph
+    (GraphedStep(host_io=True)), so a step is one graph launch and one wait."""
     import torch
+    from dlux_gb300.graphs import GraphedStep
 
-    optics_coeffs = gstep.static_in[0]
-    host_c = optics_coeffs.detach().cpu().pin_memory()
-    out_img = torch.empty((128, 128), dtype=torch.float32).pin_memory()
-    out_g = torch.empty((len(NOLLS),), dtype=torch.float32).pin_memory()
-    out_l = torch.empty((), dtype=torch.float32).pin_memory()
-    c = torch.empty((len(NOLLS),), dtype=torch.float32, device="cuda")
+    host_c = gstep.static_in[0].detach().cpu().pin_memory()
+    gio = GraphedStep(gstep.fn, host_c, warmup=1, host_io=True)
     for _ in range(2):
-        c.copy_(host_c, non_blocking=True)
-        gstep(c)
-    torch.cuda.synchronize()
+        gio(host_c)
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        c.copy_(host_c, non_blocking=True)
-        loss, g, img = gstep(c)
-        out_l.copy_(loss, non_blocking=True)
-        out_g.copy_(g, non_blocking=True)
-        out_img.copy_(img, non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        loss, g, img = gio(host_c)
     dt = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([dt], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dt = float(t.item())
-    h2d = host_c.numel() * 4
-    d2h = 4 + out_g.numel() * 4 + out_img.numel() * 4
+    h2d = host_c.numel() * host_c.element_size()
+    d2h = sum(o.numel() * o.element_size() for o in (loss, g, img))
     return dt, h2d, d2h
 
 
@@ -684,26 +676,26 @@ def run_config(args):
             except RuntimeError as e:  # a step that cannot be captured stays eager
                 gstep, graphed = None, {"capture_error": str(e)[:200]}
         if hasattr(run, "step") and gstep is not None:
-            outs0 = [o for o in gstep.static_out if o is not None]
             host_c = run.c0.detach().cpu().pin_memory()
-            host_outs = [torch.empty(o.shape, dtype=o.dtype).pin_memory() for o in outs0]
-            dev_c = torch.empty_like(run.c0)
+            # end to end: the same step with its host copies captured in the graph
+            gio = GraphedStep(run.step, host_c, warmup=1, host_io=True)
+            dev_c = run.c0.detach().clone()
             gt, et = [], []
-            for i in range(args.steps + 3):
+            for i in range(args.steps + 3):   # device time of the replay
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 torch.cuda.synchronize()
-                h0 = time.perf_counter()
-                dev_c.copy_(host_c, non_blocking=True)
                 e0.record()
-                outs = [o for o in gstep(dev_c) if o is not None]
+                gstep(dev_c)
                 e1.record()
-                for h, o in zip(host_outs, outs):
-                    h.copy_(o, non_blocking=True)
                 torch.cuda.synchronize()
                 if i >= 3:
-                    et.append((time.perf_counter() - h0) * 1e3)
                     gt.append(e0.elapsed_time(e1))
+            for i in range(args.steps + 3):   # host in -> host out
+                h0 = time.perf_counter()
+                outs = [o for o in gio(host_c) if o is not None]
+                if i >= 3:
+                    et.append((time.perf_counter() - h0) * 1e3)
             gt, et = np.array(gt), np.array(et)
             graphed = {"device_ms_p50": float(np.percentile(gt, 50)),
                        "device_ms_p99": float(np.percentile(gt, 99)),
@@ -712,7 +704,7 @@ def run_config(args):
                        "e2e_ms_p99": float(np.percentile(et, 99)),
                        "e2e_ms_mean": float(et.mean()),
                        "h2d_bytes": host_c.numel() * host_c.element_size(),
-                       "d2h_bytes": sum(o.numel() * o.element_size() for o in outs0)}
+                       "d2h_bytes": sum(o.numel() * o.element_size() for o in outs)}
         out[variant] = {"ms_mean": float(t.mean()), "ms_p50": float(np.percentile(t, 50)),
                         "ms_p99": float(np.percentile(t, 99)),
                         "evals_per_s": 1e3 / float(t.mean()),

@@ -81,3 +81,38 @@ def test_graphed_phase_retrieval_step_matches_eager(cuda):
         torch.cuda.synchronize()
         for a, b in zip(got, ref):
             assert torch.equal(a, b)
+
+
+def test_graphed_step_host_io_matches_device_graph(cuda):
+    """GraphedStep(host_io=True) holds the host copies inside the graph: host
+    coefficients in, pinned host outputs back, the same bits as the device-mode
+    graph for new coefficients each call."""
+    import dlux_gb300 as dl
+    import dlux_gb300.utils as dlu
+    from dlux_gb300.graphs import GraphedStep
+
+    rng = np.random.default_rng(9)
+    T, B = dlu.circular_aperture(128, 1.0, oversample=1, secondary_diameter=0.1,
+                                 zernike_nolls=list(range(4, 14)))
+    c0 = torch.as_tensor(rng.normal(0, 50e-9, 10), dtype=torch.float32, device="cuda")
+    R = torch.as_tensor(rng.normal(size=(64, 64)), dtype=torch.float32, device="cuda")
+    optics = dl.AngularOpticalSystem(128, 1.0, [dl.TransmissiveLayer(T, normalise=True),
+                                                dl.BasisLayer(B, c0)], 64, 0.04, 1)
+
+    def step(c_in):
+        c = c_in.detach().requires_grad_(True)
+        psf = optics.set("layers.BasisLayer.coefficients", c).propagate([1e-6, 1.2e-6])
+        loss = (psf * R).sum()
+        loss.backward()
+        return loss.detach(), c.grad, None
+
+    g = GraphedStep(step, c0)
+    gh = GraphedStep(step, c0.cpu(), host_io=True)
+    for seed in (3, 4):
+        c = torch.as_tensor(np.random.default_rng(seed).normal(0, 50e-9, 10),
+                            dtype=torch.float32)
+        loss_d, grad_d, _ = g(c.cuda())
+        loss_d, grad_d = loss_d.cpu(), grad_d.cpu()
+        loss_h, grad_h, none_h = gh(c)
+        assert not loss_h.is_cuda and loss_h.is_pinned() and none_h is None
+        assert torch.equal(loss_h, loss_d) and torch.equal(grad_h, grad_d)
