@@ -17,7 +17,9 @@
 //             columns: N lines of P -> N   (y, conjugate), into gin [N][N]
 // Ramps exp(2 pi i (g j + d)) are reduced exactly in FP32 pairs (cis_ff), and
 // the twiddles exp(2 pi i s k / P) come from sincospif of an exact argument,
-// one table per plan with every stage's twiddles contiguous.
+// one table per plan with every stage's twiddles contiguous. The butterflies
+// read the table from global memory through L1 (32 KB at P = 4096), which
+// keeps the shared memory of a block to its lines.
 #include <atomic>
 #include <cmath>
 #include <string>
@@ -70,8 +72,8 @@ __device__ __forceinline__ int smem_slot(int li, int k, int P) {
 // clear) pairs with m + 2^j and takes the twiddle of position
 // pos + (m mod 2^j) h.
 template <int LPB, int R>
-__device__ __forceinline__ void radix_pass(float2* x, const float2* tw, int log2p, int lh,
-                                           int P) {
+__device__ __forceinline__ void radix_pass(float2* x, const float2* __restrict__ tw, float sign,
+                                           int log2p, int lh, int P) {
   constexpr int M = 1 << R;
   const int h = 1 << lh;
   const int gq = log2p - R;  // P / 2^R groups per line
@@ -90,7 +92,8 @@ __device__ __forceinline__ void radix_pass(float2* x, const float2* tw, int log2
 #pragma unroll
       for (int m = 0; m < M; ++m) {
         if (m & (1 << j)) continue;
-        const float2 w = tw[H - 1 + pos + (m & ((1 << j) - 1)) * h];
+        float2 w = __ldg(tw + H - 1 + pos + (m & ((1 << j) - 1)) * h);
+        w.y *= sign;
         const float2 u = v[m];
         const float2 q = cmul(v[m + (1 << j)], w);
         v[m] = make_float2(u.x + q.x, u.y + q.y);
@@ -102,22 +105,20 @@ __device__ __forceinline__ void radix_pass(float2* x, const float2* tw, int log2
   }
 }
 
+// Registers are capped so that the shared memory sets the residency: radix-16
+// passes (RMAX 4) at 80 registers, three blocks per SM (64 KB each at
+// P = 4096); radix-8 passes at 64, four blocks.
 template <int LPB, int RMAX>
-__global__ void __launch_bounds__(256) fft_lines_kernel(
+__global__ void __launch_bounds__(256, RMAX >= 4 ? 3 : 4) fft_lines_kernel(
     const float2* __restrict__ in, LineIO io_in, int n_in, int off_in,
     float2* __restrict__ out, LineIO io_out, int n_out, int off_out, int lines, int log2p,
     float sign, const LineRamp* __restrict__ ramps, const float2* __restrict__ twg) {
   extern __shared__ float2 sm[];
   const int P = 1 << log2p;
-  float2* tw = sm;             // [P - 1]: stage of half-length h at [h - 1, 2h - 1)
-  float2* x = sm + (P - 1);    // [LPB][P], slots by smem_slot
+  float2* x = sm;  // [LPB][P], slots by smem_slot
   const int b = blockIdx.y;
   const int l0 = blockIdx.x * LPB;
   const LineRamp rp = ramps[b];
-  for (int k = threadIdx.x; k < P - 1; k += blockDim.x) {
-    const float2 w = twg[k];
-    tw[k] = make_float2(w.x, sign * w.y);
-  }
   for (int i = threadIdx.x; i < LPB * P; i += blockDim.x) x[i] = make_float2(0.f, 0.f);
   __syncthreads();
   // load: consecutive threads take consecutive addresses (line-major when the
@@ -141,10 +142,10 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(
   for (int st = 1; st <= log2p;) {
     const int R = log2p - st + 1 < RMAX ? log2p - st + 1 : RMAX;
     switch (R) {
-      case 4: if constexpr (RMAX >= 4) radix_pass<LPB, 4>(x, tw, log2p, st - 1, P); break;
-      case 3: radix_pass<LPB, 3>(x, tw, log2p, st - 1, P); break;
-      case 2: radix_pass<LPB, 2>(x, tw, log2p, st - 1, P); break;
-      default: radix_pass<LPB, 1>(x, tw, log2p, st - 1, P); break;
+      case 4: if constexpr (RMAX >= 4) radix_pass<LPB, 4>(x, twg, sign, log2p, st - 1, P); break;
+      case 3: radix_pass<LPB, 3>(x, twg, sign, log2p, st - 1, P); break;
+      case 2: radix_pass<LPB, 2>(x, twg, sign, log2p, st - 1, P); break;
+      default: radix_pass<LPB, 1>(x, twg, sign, log2p, st - 1, P); break;
     }
     __syncthreads();
     st += R;
@@ -183,10 +184,9 @@ __global__ void fft_twiddle_kernel(int P, float2* __restrict__ tw) {
 // stages are latency-bound); two lines keep column loads at 16-byte segments.
 int lines_per_block(int P) { return P <= 1024 ? 4 : 2; }
 
-// Stages per shared-memory pass. Radix-16 passes need 103 registers per
-// thread, radix-8 passes 63, which keeps twice the blocks resident. Measured
-// forward + adjoint of 16 planes: radix-8 wins up to P = 2048 (1.93 against
-// 2.67 ms), radix-16 from P = 4096 (10.6 against 11.3 ms).
+// Stages per shared-memory pass. Measured forward + adjoint of 16 planes:
+// radix-8 passes win up to P = 2048 (1.93 against 2.04 ms for radix-16 at
+// P = 2048), radix-16 passes from P = 4096 (8.0 ms).
 int max_radix_log2(int P) { return P >= 4096 ? 4 : 3; }
 
 int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* out, LineIO io_out,
@@ -195,7 +195,7 @@ int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* o
   const int P = 1 << log2p;
   const int lpb = lines_per_block(P);
   const int rmax = max_radix_log2(P);
-  const size_t smem = sizeof(float2) * ((size_t)P - 1 + (size_t)lpb * P);
+  const size_t smem = sizeof(float2) * (size_t)lpb * P;
   static std::atomic<bool> attr_done{false};  // host side, once per process
   if (!attr_done.load()) {
     const int lim = 200 * 1024;  // covers P <= 8192 at the lines-per-block choice above
