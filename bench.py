@@ -633,6 +633,114 @@ def run_fft(args):
     return 0
 
 
+def run_ops(args):
+    """The path's other operations, each forward + reverse at a representative size:
+    - LCT of an ABCD system (dLux layers/abcd_propagators.py:245-370, MFTPropagator /
+      FFTPropagator): 16 wavelengths, 512 -> 512, split-BF16 and FP32 GEMM forms;
+    - angular-spectrum propagation (ASMPropagator, :380-459): 16 wavelengths, 512
+      padded to 1024;
+    - PSF convolution, mode "same" (PSF.convolve psfs.py:93-110, ApplyJitter, resolved
+      sources): 16 images of 512^2 and a 33 x 33 kernel, forward and both gradients;
+    - dynamic aperture (AberratedAperture on a CoordTransform): 1024^2 transmission and
+      OPD of 21 Zernikes, and the coefficient gradient.
+    The line's value is the time of one step of all four. Each item reports its time and
+    its rate: GEMM flops for the transforms (the launches' own CUDA-event timing),
+    direct-convolution flops for the convolution, pixels for the aperture."""
+    import ctypes
+    import torch
+    from dlux_gb300 import _lib as L
+    from dlux_gb300 import kernels
+    from dlux_gb300.layers.abcd_propagators import lct_axes
+
+    lib = L.load()
+    rng = np.random.default_rng(11)
+    Lw, n = 16, 512
+    wls = np.linspace(0.8e-6, 1.2e-6, Lw)
+    dev = dict(device="cuda")
+
+    def field(b, m):
+        return torch.as_tensor((rng.normal(size=(b, m, m)) + 1j * rng.normal(size=(b, m, m)))
+                               / m, dtype=torch.complex64, **dev)
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        L.check(lib.dlx_gemm_timing_begin())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        tot, cnt, fl = ctypes.c_double(0), ctypes.c_int(0), ctypes.c_double(0)
+        L.check(lib.dlx_gemm_timing_end(ctypes.byref(tot), ctypes.byref(cnt), ctypes.byref(fl)))
+        ms = e0.elapsed_time(e1) / args.steps
+        gemm = None
+        if cnt.value > 0 and tot.value > 0:
+            gemm = {"launches_per_step": cnt.value / args.steps,
+                    "gemm_ms_per_step": tot.value / args.steps,
+                    "gemm_tflops": fl.value / (tot.value * 1e-3) / 1e12}
+        return ms, gemm
+
+    hbm, bf16, src = load_peaks()
+    items = {}
+    # LCT: a lens of focal length 1 m followed by 1 m of free space, 1 mm -> 1 mm grids
+    M = np.array([[0.0, 1.0], [-1.0, 1.0]])
+    ax = lct_axes(M, wls, n, 1e-3 / n, 0.0, n, 1e-3 / n, 0.0)
+    x, y = field(Lw, n), field(Lw, n)
+    for form in ("split_bf16", "fp32"):
+        plan = kernels.XformPlan(ax, ax, n, n, variant=form)
+        ms, gemm = timed(lambda: (plan.forward(x), plan.adjoint(y)))
+        items[f"lct_{form}"] = {"ms_per_step": ms, "gemm": gemm,
+                                "planes_per_s": Lw / (ms * 1e-3)}
+        plan.close()
+    # ASM: 512 padded to 1024, 0.5 m
+    xa, ya = field(Lw, n), field(Lw, 2 * n)
+    plan = kernels.ASMPlan(wls, n, 2 * n, 1e-3 / n, 0.5, variant="split_bf16")
+    ms, gemm = timed(lambda: (plan.forward(xa), plan.adjoint(ya)))
+    items["asm_split_bf16"] = {"ms_per_step": ms, "gemm": gemm, "planes_per_s": Lw / (ms * 1e-3)}
+    plan.close()
+    # PSF convolution: forward and both gradients
+    imgs = torch.as_tensor(rng.random((Lw, n, n)), dtype=torch.float32, **dev)
+    ker = torch.as_tensor(rng.random((33, 33)), dtype=torch.float32, **dev)
+    gimg = torch.as_tensor(rng.normal(size=(Lw, n, n)), dtype=torch.float32, **dev)
+    ms, _ = timed(lambda: (kernels.conv2d_same(imgs, ker),
+                           kernels.conv2d_same_backward(imgs, ker, gimg)))
+    fl = 3 * 2.0 * Lw * n * n * 33 * 33   # forward, input gradient, kernel gradient
+    ms_f, _ = timed(lambda: kernels.conv2d_same(imgs, ker))
+    items["conv_33x33"] = {"ms_per_step": ms, "tflops": fl / (ms * 1e-3) / 1e12,
+                           "flops_per_step": fl, "forward_ms": ms_f,
+                           "forward_tflops": fl / 3 / (ms_f * 1e-3) / 1e12}
+    # dynamic aperture, 1024^2, Noll 1..21
+    na = 1024
+    desc = kernels.aperture_desc(na, 1.0 / na, 0.5, softening=1.0)
+    noll = list(range(1, 22))
+    coeffs = torch.as_tensor(rng.normal(0, 30e-9, 21), dtype=torch.float32, **dev)
+    g_opd = torch.as_tensor(rng.normal(size=(na, na)), dtype=torch.float32, **dev)
+    ms, _ = timed(lambda: (kernels.aberrated_aperture(desc, noll, coeffs),
+                           kernels.aberrated_aperture_grad(desc, noll, g_opd)))
+    items["aperture_1024_21z"] = {"ms_per_step": ms, "pixels_per_s": na * na / (ms * 1e-3)}
+    total = sum(v["ms_per_step"] for v in items.values() if v is not items["lct_fp32"])
+    lct = items["lct_split_bf16"]["gemm"] or {}
+    line = {"metric": "path operations (LCT, ASM, convolution, aperture) ms per step",
+            "value": total, "unit": "ms", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3-split / fp32",
+            "data": "synthetic (seeded PCG64)",
+            "config": {"workload": f"LCT and ASM of {Lw} wavelengths at {n}^2 (ASM padded to "
+                                   f"{2 * n}), forward + adjoint; 33x33 PSF convolution of {Lw} "
+                                   f"x {n}^2, forward + gradients; {na}^2 dynamic aperture, 21 "
+                                   "Zernikes, + gradient"},
+            "roofline": {"bound": "tensor", "kernel": "tc_cgemm (LCT)",
+                         "achieved": lct.get("gemm_tflops"), "peak": bf16, "unit": "TFLOP/s",
+                         "frac": (lct["gemm_tflops"] / bf16) if lct else None, "traffic": None,
+                         "peak_source": f"{src} bf16 dense (burst)"},
+            "items": items}
+    print(json.dumps(line))
+    return 0
+
+
 def run_config(args):
     import torch
     import dlux_gb300._lib as L
@@ -760,7 +868,7 @@ def main():
                     help="serving: fixed split-BF16 plans instead of the per-(N, M) autotuner")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="psf_grad",
-                    choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft"])
+                    choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft", "ops"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
     ap.add_argument("--slots", type=int, default=6,
@@ -793,6 +901,8 @@ def main():
         return run_config(args) if rank == 0 else 0
     if args.workload == "fft":
         return run_fft(args) if rank == 0 else 0
+    if args.workload == "ops":
+        return run_ops(args) if rank == 0 else 0
     if world > 1:
         torch.distributed.init_process_group("nccl")
 

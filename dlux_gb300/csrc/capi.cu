@@ -1309,6 +1309,7 @@ struct dlx_asm_plan_s {
   TwoStepPlan fwd;   // centred DFT of the zero-padded field: N -> P
   TwoStepPlan inv;   // centred inverse DFT: P -> P
   DevBuf spec;       // [b][P][P] c64 spectrum
+  DevBuf H;          // [b][P][P] c64 transfer function, tabulated at creation
   DevBuf zl, lam2;   // double [b]: distance / lambda, lambda^2
   double df = 0;     // frequency step 1 / (P dx)
   int P = 0;
@@ -1430,8 +1431,18 @@ int dlx_asm_plan_create(const dlx_asm_desc* d, const double* wavelengths_host,
   };
   if (st == DLX_OK) st = upload(p->zl, zl);
   if (st == DLX_OK) st = upload(p->lam2, l2);
+  if (st == DLX_OK) st = p->H.alloc(sizeof(float2) * (size_t)B * P * P);
+  if (st == DLX_OK)
+    st = launch_asm_table(p->H.as<float2>(), B, P, p->df, p->zl.as<double>(),
+                          p->lam2.as<double>(), 0);
+  if (st == DLX_OK) {
+    // the table is read from the caller's streams, which need not wait for this one
+    const cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) st = check_cuda(e, "asm transfer table");
+  }
   if (st != DLX_OK) {
-    p->fwd.release(); p->inv.release(); p->spec.release(); p->zl.release(); p->lam2.release();
+    p->fwd.release(); p->inv.release(); p->spec.release(); p->H.release(); p->zl.release();
+    p->lam2.release();
     delete p;
     return st;
   }
@@ -1442,8 +1453,8 @@ int dlx_asm_plan_create(const dlx_asm_desc* d, const double* wavelengths_host,
 int dlx_asm_plan_destroy(dlx_asm_plan plan) {
   if (!plan) return DLX_OK;
   cudaDeviceSynchronize();
-  plan->fwd.release(); plan->inv.release(); plan->spec.release(); plan->zl.release();
-  plan->lam2.release();
+  plan->fwd.release(); plan->inv.release(); plan->spec.release(); plan->H.release();
+  plan->zl.release(); plan->lam2.release();
   delete plan;
   return DLX_OK;
 }
@@ -1452,8 +1463,8 @@ int dlx_asm_forward(dlx_asm_plan plan, const void* in, void* out, void* stream) 
   if (!plan || !in || !out) return fail(DLX_ERR_ARG, "asm_forward: null pointer");
   cudaStream_t s = as_stream(stream);
   DLX_TRY(plan->fwd.forward(in, plan->spec.p, s));
-  DLX_TRY(launch_asm_transfer(plan->spec.as<float2>(), plan->fwd.ts.batch, plan->P, plan->df,
-                              plan->zl.as<double>(), plan->lam2.as<double>(), 0, s));
+  DLX_TRY(launch_asm_apply(plan->spec.as<float2>(), plan->H.as<float2>(), plan->fwd.ts.batch,
+                           plan->P, 0, s));
   return plan->inv.forward(plan->spec.p, out, s);
 }
 
@@ -1461,8 +1472,8 @@ int dlx_asm_adjoint(dlx_asm_plan plan, const void* gout, void* gin, void* stream
   if (!plan || !gout || !gin) return fail(DLX_ERR_ARG, "asm_adjoint: null pointer");
   cudaStream_t s = as_stream(stream);
   DLX_TRY(plan->inv.adjoint(gout, plan->spec.p, s));
-  DLX_TRY(launch_asm_transfer(plan->spec.as<float2>(), plan->fwd.ts.batch, plan->P, plan->df,
-                              plan->zl.as<double>(), plan->lam2.as<double>(), 1, s));
+  DLX_TRY(launch_asm_apply(plan->spec.as<float2>(), plan->H.as<float2>(), plan->fwd.ts.batch,
+                           plan->P, 1, s));
   return plan->fwd.adjoint(plan->spec.p, gin, s);
 }
 

@@ -932,38 +932,58 @@ namespace dlx {
 //   H = exp(2 pi i z sqrt(1/lambda^2 - fx^2 - fy^2))      (propagating waves)
 //   H = exp(-2 pi z sqrt(fx^2 + fy^2 - 1/lambda^2))        (evanescent waves)
 // with f = (k - floor(P/2)) / (P dx). The phase z/lambda sqrt(1 - lambda^2 f^2)
-// is formed and reduced in FP64 (it reaches ~1e6 cycles at z = 1 m); conj = 1
-// applies conj(H), the adjoint.
+// is formed and reduced in FP64 (it reaches ~1e6 cycles at z = 1 m). H depends
+// only on the plan (wavelengths, distance, grid), so it is tabulated once in
+// complex64 when the plan is made; a call multiplies by the table (conj = 1:
+// by conj(H), the adjoint). FP64 runs at about 1/64 of the FP32 rate here, and
+// evaluating H on every call cost 1.5 ms of a 2.9 ms forward + adjoint at 16
+// wavelengths of 1024^2.
 // ---------------------------------------------------------------------------
-__global__ void asm_transfer_kernel(float2* __restrict__ f, int P, double df,
-                                    const double* __restrict__ zl,
-                                    const double* __restrict__ lam2, int conj) {
+__device__ __forceinline__ float2 asm_h(int kx, int ky, int P, double df, double zl,
+                                        double lam2) {
+  const int c = P / 2;
+  const double fx = (kx - c) * df, fy = (ky - c) * df;
+  const double s = lam2 * (fx * fx + fy * fy);
+  if (s <= 1.0) return cis_cycles(zl * sqrt(1.0 - s));
+  return make_float2((float)exp(-2.0 * CUDART_PI * zl * sqrt(s - 1.0)), 0.0f);
+}
+
+__global__ void asm_table_kernel(float2* __restrict__ H, int P, double df,
+                                 const double* __restrict__ zl,
+                                 const double* __restrict__ lam2) {
   const long long npix = (long long)P * P;
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   if (p >= npix) return;
   const int ky = (int)(p / P);
   const int kx = (int)(p - (long long)ky * P);
-  const int c = P / 2;
-  const double fx = (kx - c) * df, fy = (ky - c) * df;
-  const double s = lam2[b] * (fx * fx + fy * fy);
-  float2 h;
-  if (s <= 1.0) {
-    h = cis_cycles(zl[b] * sqrt(1.0 - s));
-    if (conj) h.y = -h.y;
-  } else {
-    h = make_float2((float)exp(-2.0 * CUDART_PI * zl[b] * sqrt(s - 1.0)), 0.0f);
-  }
-  float2* q = f + (long long)b * npix + p;
-  *q = cmul(*q, h);
+  H[(long long)b * npix + p] = asm_h(kx, ky, P, df, zl[b], lam2[b]);
 }
 
-int launch_asm_transfer(float2* spec, int batch, int P, double df, const double* zl,
-                        const double* lam2, int conj, cudaStream_t s) {
+__global__ void asm_apply_kernel(float2* __restrict__ f, const float2* __restrict__ H,
+                                 long long n, int conj) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float2 h = H[i];
+  if (conj) h.y = -h.y;
+  f[i] = cmul(f[i], h);
+}
+
+int launch_asm_table(float2* H, int batch, int P, double df, const double* zl,
+                     const double* lam2, cudaStream_t s) {
   if (batch <= 0 || P <= 0) return DLX_OK;
   dim3 grid(ceil_div((long long)P * P, 256), batch);
-  asm_transfer_kernel<<<grid, 256, 0, s>>>(spec, P, df, zl, lam2, conj);
-  DLX_LAUNCH_CHECK("asm_transfer_kernel");
+  asm_table_kernel<<<grid, 256, 0, s>>>(H, P, df, zl, lam2);
+  DLX_LAUNCH_CHECK("asm_table_kernel");
+  return DLX_OK;
+}
+
+int launch_asm_apply(float2* spec, const float2* H, int batch, int P, int conj,
+                     cudaStream_t s) {
+  const long long n = (long long)batch * P * P;
+  if (n <= 0) return DLX_OK;
+  asm_apply_kernel<<<ceil_div(n, 256), 256, 0, s>>>(spec, H, n, conj);
+  DLX_LAUNCH_CHECK("asm_apply_kernel");
   return DLX_OK;
 }
 

@@ -16,10 +16,12 @@ struct BatchFF {
 };
 
 // --- elementwise.cu --------------------------------------------------------
-// Angular-spectrum transfer function applied in place to centred spectra
-// [batch][P][P] (conj != 0: its conjugate, the adjoint).
-int launch_asm_transfer(float2* spec, int batch, int P, double df, const double* zl,
-                        const double* lam2, int conj, cudaStream_t s);
+// Angular-spectrum transfer function: tabulated once per plan into H
+// [batch][P][P] (complex64), then applied in place to centred spectra
+// (conj != 0: its conjugate, the adjoint).
+int launch_asm_table(float2* H, int batch, int P, double df, const double* zl,
+                     const double* lam2, cudaStream_t s);
+int launch_asm_apply(float2* spec, const float2* H, int batch, int P, int conj, cudaStream_t s);
 int launch_dft_gen(const DftAxis* axes_dev, int batch, int rows, int cols, bool rows_are_out,
                    float2* out_c64, long long out_batch_stride, __nv_bfloat16* out_split,
                    cudaStream_t s);
