@@ -63,42 +63,102 @@ __global__ void conv2d_same_kernel(const float* __restrict__ in, int H, int W,
 }
 
 // g_k[a][b] = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - b] over every batch
-// element; one block per kernel element, float-pair accumulation per thread.
-__global__ void conv2d_kgrad_kernel(const float* __restrict__ in, const float* __restrict__ g,
-                                    int H, int W, int batch, int K0, int K1,
-                                    float* __restrict__ g_k) {
-  __shared__ double smem[32];
-  const int a = blockIdx.x / K1, bb = blockIdx.x % K1;
+// element, in two stages.
+// Stage 1: a block takes kernel row a, a chunk of KC kernel columns and a band
+// of image rows, over every batch element. Each thread keeps KC float-pair
+// sums: one g_out value meets the KC shifted input values of its row, which
+// are read through L1. The block's sums go to part[band][a][b] in double.
+// Compared with one block per kernel element, g_out and the input are read
+// from L2 once per chunk instead of once per kernel element.
+// Stage 2: g_k[a][b] sums the bands in order, so the result is deterministic.
+constexpr int KC = 16;
+
+__global__ void __launch_bounds__(256) conv2d_kgrad_rows_kernel(
+    const float* __restrict__ in, const float* __restrict__ g, int H, int W, int batch, int K0,
+    int K1, int rows_per_band, double* __restrict__ part) {
+  __shared__ double red[8][KC];
+  const int a = blockIdx.x;
+  const int c0 = blockIdx.y * KC;  // first kernel column of the chunk
+  const int band = blockIdx.z;
   const int s0 = (K0 - 1) / 2, s1 = (K1 - 1) / 2;
-  float hi = 0.f, lo = 0.f;
+  // rows i of the band with i + s0 - a in [0, H)
+  const int i0 = max(band * rows_per_band, max(0, a - s0));
+  const int i1 = min(min(H, (band + 1) * rows_per_band), H + a - s0);
+  float hi[KC], lo[KC];
+#pragma unroll
+  for (int q = 0; q < KC; ++q) hi[q] = lo[q] = 0.f;
   const long long npix = (long long)H * W;
   for (int b = 0; b < batch; ++b) {
-    const float* inb = in + b * npix;
-    const float* gb = g + b * npix;
-    for (long long p = threadIdx.x; p < npix; p += blockDim.x) {
-      const int i = (int)(p / W), j = (int)(p % W);
-      const int r = i + s0 - a, c = j + s1 - bb;
-      if (r < 0 || r >= H || c < 0 || c >= W) continue;
-      const float x = gb[p], y = inb[(long long)r * W + c];
-      const float pr = x * y;
-      const float pe = fmaf(x, y, -pr);
-      const float t = hi + pr;
-      const float bv = t - hi;
-      lo += ((hi - (t - bv)) + (pr - bv)) + pe;
-      hi = t;
+    for (int i = i0; i < i1; ++i) {
+      const float* grow = g + b * npix + (long long)i * W;
+      const float* xrow = in + b * npix + (long long)(i + s0 - a) * W;
+      for (int j = threadIdx.x; j < W; j += blockDim.x) {
+        const float x = grow[j];
+#pragma unroll
+        for (int q = 0; q < KC; ++q) {
+          const int c = j + s1 - (c0 + q);  // input column of kernel column c0 + q
+          if (c0 + q < K1 && c >= 0 && c < W) {
+            const float y = __ldg(xrow + c);
+            const float pr = x * y;
+            const float pe = fmaf(x, y, -pr);
+            const float t = hi[q] + pr;
+            const float bv = t - hi[q];
+            lo[q] += ((hi[q] - (t - bv)) + (pr - bv)) + pe;
+            hi[q] = t;
+          }
+        }
+      }
     }
   }
-  double v = (double)hi + (double)lo;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) smem[warp] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += smem[w];
-    g_k[blockIdx.x] = (float)t;
+#pragma unroll
+  for (int q = 0; q < KC; ++q) {
+    double v = (double)hi[q] + (double)lo[q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][q] = v;
   }
+  __syncthreads();
+  if (threadIdx.x < KC && c0 + (int)threadIdx.x < K1) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][threadIdx.x];
+    part[((long long)band * K0 + a) * K1 + c0 + threadIdx.x] = t;
+  }
+}
+
+__global__ void conv2d_kgrad_sum_kernel(const double* __restrict__ part, int nband, int nk,
+                                        float* __restrict__ g_k) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  double t = 0.0;
+  for (int band = 0; band < nband; ++band) t += part[(long long)band * nk + k];
+  g_k[k] = (float)t;
+}
+
+int launch_conv_kgrad(const float* in, const float* g, int H, int W, int batch, int K0, int K1,
+                      float* g_k, cudaStream_t s) {
+  const int nchunk = (K1 + KC - 1) / KC;
+  // about two blocks per SM in all
+  int nband = (2 * 152 + K0 * nchunk - 1) / (K0 * nchunk);
+  if (nband > H) nband = H;
+  if (nband < 1) nband = 1;
+  const int rows = (H + nband - 1) / nband;
+  nband = (H + rows - 1) / rows;
+  const int nk = K0 * K1;
+  double* part = nullptr;
+  DLX_TRY_CUDA(cudaMallocAsync((void**)&part, sizeof(double) * (size_t)nband * nk, s));
+  conv2d_kgrad_rows_kernel<<<dim3(K0, nchunk, nband), 256, 0, s>>>(in, g, H, W, batch, K0, K1,
+                                                                    rows, part);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    conv2d_kgrad_sum_kernel<<<(nk + 255) / 256, 256, 0, s>>>(part, nband, nk, g_k);
+    e = cudaGetLastError();
+  }
+  cudaFreeAsync(part, s);
+  if (e != cudaSuccess) return check_cuda(e, "conv2d kernel gradient");
+  note_launch();
+  note_launch();
+  return DLX_OK;
 }
 
 int check_conv(int batch, int H, int W, int K0, int K1) {
@@ -144,11 +204,7 @@ int dlx_conv2d_same_backward(const float* in, int batch, int height, int width,
     return fail(DLX_ERR_ARG, "conv2d_backward: null pointer");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (g_in) DLX_TRY(launch_conv(g_out, batch, height, width, kernel, k0, k1, 1, g_in, s));
-  if (g_kernel) {
-    conv2d_kgrad_kernel<<<k0 * k1, 256, 0, s>>>(in, g_out, height, width, batch, k0, k1,
-                                                g_kernel);
-    DLX_LAUNCH_CHECK("conv2d_kgrad_kernel");
-  }
+  if (g_kernel) DLX_TRY(launch_conv_kgrad(in, g_out, height, width, batch, k0, k1, g_kernel, s));
   return DLX_OK;
 }
 
