@@ -62,15 +62,15 @@ __global__ void conv2d_same_kernel(const float* __restrict__ in, int H, int W,
   }
 }
 
-// g_k[a][b] = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - b] over every batch
-// element, in two stages.
+// g_k[a][c] = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - c] over every batch
+// element (kernel row a, kernel column c), in two stages.
 // Stage 1: a block takes kernel row a, a chunk of KC kernel columns and a band
 // of image rows, over every batch element. Each thread keeps KC float-pair
 // sums: one g_out value meets the KC shifted input values of its row, which
-// are read through L1. The block's sums go to part[band][a][b] in double.
+// are read through L1. The block's sums go to part[band][a][c] in double.
 // Compared with one block per kernel element, g_out and the input are read
 // from L2 once per chunk instead of once per kernel element.
-// Stage 2: g_k[a][b] sums the bands in order, so the result is deterministic.
+// Stage 2: g_k[a][c] sums the bands in order, so the result is deterministic.
 constexpr int KC = 16;
 
 __global__ void __launch_bounds__(256) conv2d_kgrad_rows_kernel(
