@@ -11,7 +11,28 @@ k0 + m h of each group. For every P the kernel supports (16 ... 8192):
   gathers 2-way.
 """
 
+import pathlib
+import re
+
 import pytest
+
+_SRC = (pathlib.Path(__file__).resolve().parents[1] / "dlux_gb300" / "csrc" / "fft.cu").read_text()
+
+
+def _threshold(pattern):
+    m = re.search(pattern, _SRC)
+    assert m, f"fft.cu no longer has the form this model restates: {pattern}"
+    return int(m.group(1))
+
+
+# the kernel's own choices, read from its source so that the model follows it
+_LPB4_MAX_P = _threshold(r"int lines_per_block\(int P\) \{ return P <= (\d+) \? 4 : 2; \}")
+_RADIX16_MIN_P = _threshold(r"int max_radix_log2\(int P\) \{ return P >= (\d+) \? 4 : 3; \}")
+
+
+def test_model_matches_the_kernel_source():
+    assert "(k ^ (((k >> 4) ^ (k >> 8) ^ (k >> 12) ^ g) & 15))" in _SRC
+    assert "LPB == 2 ? 9 * li : (LPB == 4 ? 5 * li : li)" in _SRC
 
 
 def slot(k, li, lpb, P):
@@ -42,12 +63,8 @@ def passes(log2p, rmax):
     return out
 
 
-def max_radix_log2(P):
-    return 4 if P >= 4096 else 3
-
-
 def lines_per_block(P):
-    return 4 if P <= 1024 else 2
+    return 4 if P <= _LPB4_MAX_P else 2
 
 
 @pytest.mark.parametrize("log2p", range(4, 14))
@@ -57,8 +74,10 @@ def test_slot_map_is_a_bijection_and_passes_are_conflict_free(log2p):
         for li in range(lpb):
             assert sorted(slot(k, li, lpb, P) - li * P for k in range(P)) == list(range(P))
     lpb = lines_per_block(P)
-    for rmax in (3, 4):
+    for rmax in (3, 4):   # both schedules; the kernel uses 4 from P = _RADIX16_MIN_P on
         bound = 1 if (P >= 256 and rmax == 4) else 2
+        if rmax == 4 and P >= _RADIX16_MIN_P:
+            assert bound == 1   # the kernel's radix-16 sizes are conflict-free
         for R, lh in passes(log2p, rmax):
             gq = log2p - R
             for m in range(1 << R):
