@@ -50,6 +50,10 @@ N_WAVELENGTHS = 64
 NOLLS = list(range(4, 25))
 SEED = 2
 METRIC = "PSF+grad evals/sec"
+# Individually timed steps for the p50/p99 latencies (outside the K-step timed region).
+LATENCY_SAMPLES = 200
+# Whole steps of the CPU restatement timed for the GPU line's cpu_baseline.
+CPU_BASELINE_STEPS = 3
 # DRAM bytes (read + write) of one tensor-core GEMM launch per wavelength, from an ncu
 # capture of a 16-wavelength launch of this workload (71.0 MB / 16). Traffic grows in
 # proportion to the wavelength count (each wavelength is an independent GEMM on its own
@@ -137,29 +141,92 @@ class ClockSampler:
 # ----------------------------------------------------------------------------
 # CPU arm: the oracle's complex64 restatement of dLux's op order
 # ----------------------------------------------------------------------------
-def cpu_step_sample(n_lambda_sample=2):
-    """Times one PSF+grad evaluation on the host for a sample of the wavelengths."""
-    from oracle import dlux_oracle as O
+_CPU = {}
 
-    coeffs, wls, weights, R = make_inputs()
-    T, B = O.circular_aperture(N_PUPIL, 1.0, oversample=5, secondary_diameter=0.1,
-                               spider_width=0.01, spider_angles=(0, 90, 180, 270),
-                               zernike_nolls=NOLLS)
-    ps_out = float(O.arcsec2rad(PSF_PIXEL_SCALE / OVERSAMPLE))
-    idx = np.linspace(0, N_WAVELENGTHS - 1, n_lambda_sample).astype(int)
-    Bf = B.astype(np.float32)
-    t0 = time.perf_counter()
-    opd = np.tensordot(Bf, coeffs.astype(np.float32), axes=(0, 0))
-    Teff = (T / np.sqrt((T ** 2).sum())).astype(np.float32)
-    psf = O.poly_psf(T, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out, precision="c64")
-    img = O.downsample(psf, OVERSAMPLE, mean=False)
-    G = np.kron(R.astype(np.float32), np.ones((OVERSAMPLE, OVERSAMPLE), np.float32))
-    g = O.poly_psf_grad(Teff, opd, wls[idx], weights[idx], 1.0, N_FOCAL, ps_out, G,
+
+def _cpu_worker_init(T, Teff, ps_out):
+    _CPU.update(T=T, Teff=Teff, ps_out=ps_out)
+
+
+def _cpu_worker(job):
+    """PSF and opd-gradient partial sums of one block of wavelengths (complex64 port)."""
+    from oracle import dlux_oracle as O
+    opd, wls, weights, G = job
+    psf = O.poly_psf(_CPU["T"], opd, wls, weights, 1.0, N_FOCAL, _CPU["ps_out"],
+                     precision="c64")
+    g = O.poly_psf_grad(_CPU["Teff"], opd, wls, weights, 1.0, N_FOCAL, _CPU["ps_out"], G,
                         precision="c64")
-    gc = np.tensordot(Bf, g["g_opd"], axes=((1, 2), (0, 1)))
-    dt = time.perf_counter() - t0
-    assert np.isfinite(img).all() and np.isfinite(gc).all()
-    return dt * (N_WAVELENGTHS / n_lambda_sample), n_lambda_sample
+    return psf.astype(np.float32), g["g_opd"].astype(np.float32)
+
+
+class CpuStep:
+    """The benchmark step restated on the host: the oracle's complex64 port of
+    dLux's op order (the stand-in for dLux's JAX CPU path, which cannot be
+    installed here), every wavelength of the step, split in contiguous blocks
+    over a process pool with one single-threaded worker per host core (started
+    with spawn). One call = one PSF + coefficient-gradient evaluation."""
+
+    def __init__(self, workers=None):
+        import multiprocessing as mp
+        from oracle import dlux_oracle as O
+
+        self.coeffs, self.wls, self.weights, R = make_inputs()
+        T, B = O.circular_aperture(N_PUPIL, 1.0, oversample=5, secondary_diameter=0.1,
+                                   spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                                   zernike_nolls=NOLLS)
+        self.Bf = B.astype(np.float32)
+        Teff = (T / np.sqrt((T ** 2).sum())).astype(np.float32)
+        self.G = np.kron(R.astype(np.float32), np.ones((OVERSAMPLE, OVERSAMPLE), np.float32))
+        ps_out = float(O.arcsec2rad(PSF_PIXEL_SCALE / OVERSAMPLE))
+        self.workers = int(workers or os.cpu_count() or 1)
+        self.blocks = [b for b in np.array_split(np.arange(N_WAVELENGTHS), self.workers)
+                       if len(b)]
+        saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS",
+                                                "MKL_NUM_THREADS")}
+        for k in saved:
+            os.environ[k] = "1"
+        try:
+            self.pool = mp.get_context("spawn").Pool(
+                self.workers, initializer=_cpu_worker_init,
+                initargs=(T.astype(np.float32), Teff, ps_out))
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+
+    def __call__(self):
+        from oracle import dlux_oracle as O
+        opd = np.tensordot(self.Bf, self.coeffs.astype(np.float32), axes=(0, 0))
+        jobs = [(opd, self.wls[b], self.weights[b], self.G) for b in self.blocks]
+        parts = self.pool.map(_cpu_worker, jobs)
+        psf = np.sum([p[0] for p in parts], axis=0)
+        g_opd = np.sum([p[1] for p in parts], axis=0)
+        img = O.downsample(psf, OVERSAMPLE, mean=False)
+        gc = np.tensordot(self.Bf, g_opd, axes=((1, 2), (0, 1)))
+        assert np.isfinite(img).all() and np.isfinite(gc).all()
+        return img, gc
+
+    def time(self, steps, warmup):
+        for _ in range(warmup):
+            self()
+        times = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            self()
+            times.append(time.perf_counter() - t0)
+        return times
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
+
+    def sample(self):
+        return (f"all {N_WAVELENGTHS} wavelengths of the step at full 512^2 pupil / 512^2 focal "
+                f"size, in {len(self.blocks)} blocks over {self.workers} single-threaded "
+                "worker processes; NumPy complex64 restatement of dLux's op order (dLux/JAX "
+                "is not installable here)")
 
 
 def parity_sample(variant, n_lambda_sample=2):
@@ -208,39 +275,25 @@ def parity_sample(variant, n_lambda_sample=2):
                       "checks all 64"}
 
 
-def cpu_threads():
-    try:
-        from threadpoolctl import threadpool_info
-        info = threadpool_info()
-        return max([i.get("num_threads", 1) for i in info] + [1])
-    except Exception:
-        return os.cpu_count() or 1
-
-
 def run_reference(args, rank, world):
-    """--impl reference: the CPU restatement timed on the host cores."""
+    """--impl reference: the CPU restatement of the whole step timed on the host cores."""
     if rank != 0:
         return 0
-    times = []
-    nsample = 2
-    for _ in range(max(args.warmup, 0) and 1):
-        cpu_step_sample(nsample)
-    for _ in range(args.steps):
-        t, nsample = cpu_step_sample(nsample)
-        times.append(t)
-    t = statistics.median(times)
+    cpu = CpuStep()
+    try:
+        times = cpu.time(args.steps, max(args.warmup, 0))
+    finally:
+        cpu.close()
+    t = sum(times) / len(times)
     value = 1.0 / t
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
         "data": "synthetic (seeded PCG64)", "config": config_dict(),
-        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cpu_threads(),
-                         "kind": "port",
-                         "sample": f"{nsample} of {N_WAVELENGTHS} wavelengths per step at full "
-                                   f"512^2 pupil / 512^2 focal size, time scaled by "
-                                   f"{N_WAVELENGTHS // nsample}; NumPy complex64 restatement of "
-                                   "dLux's op order (dLux/JAX is not installable here)"},
+        "p50_ms": statistics.median(times) * 1e3, "p99_ms": float(np.percentile(times, 99)) * 1e3,
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cpu.workers,
+                         "kind": "port", "sample": cpu.sample()},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -363,6 +416,21 @@ def time_graphed(args, gstep, c0, world):
     return ms
 
 
+def step_latencies(gstep, c0, n):
+    """Per-step device latency of the graphed step: CUDA events around each of n
+    replays (after the timed region, so its K-step number is unaffected)."""
+    import torch
+
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(n)]
+    for e0, e1 in evs:
+        e0.record()
+        gstep(c0)
+        e1.record()
+    torch.cuda.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+
 def time_e2e(args, gstep, world):
     """The step driven from host memory: the coefficients come from pinned host
     memory and the loss, gradient and image go back to pinned host memory every
@@ -387,7 +455,13 @@ def time_e2e(args, gstep, world):
         dt = float(t.item())
     h2d = host_c.numel() * host_c.element_size()
     d2h = sum(o.numel() * o.element_size() for o in (loss, g, img))
-    return dt, h2d, d2h
+    # per-step latency through the same host-driven graph (each step waits for its results)
+    lat = []
+    for _ in range(max(args.steps, LATENCY_SAMPLES)):
+        t1 = time.perf_counter()
+        gio(host_c)
+        lat.append((time.perf_counter() - t1) * 1e3)
+    return dt, h2d, d2h, lat
 
 
 def run_serving(args):
@@ -916,7 +990,8 @@ def main():
     clk = clocks.stop()
     ms_step = ms_total / args.steps
     value = world * args.steps / (ms_total / 1e3)
-    e2e_dt, h2d, d2h = time_e2e(args, gstep, world)
+    lat_dev = step_latencies(gstep, c0, max(args.steps, LATENCY_SAMPLES))
+    e2e_dt, h2d, d2h, lat_e2e = time_e2e(args, gstep, world)
     e2e_value = world * args.steps / e2e_dt
 
     fp32 = None
@@ -945,16 +1020,22 @@ def main():
                     "algorithmic_flops_per_launch": flops_launch,
                     "avg_launch_ms": avg_ms,
                     "frac_of_split_ceiling": achieved / (tflops / 3.0),
-                    "gemm_share_of_step": g["total_ms"] / res["ms_total"]}
+                    # GEMM time per step (eager launches, each bracketed by events) over
+                    # the graphed step that `value` times
+                    "gemm_share_of_step": (g["total_ms"] / args.steps) / ms_step,
+                    "gemm_launches_per_step": g["launches"] / args.steps}
 
     cpu = None
     parity = None
-    if rank == 0 and not args.no_cpu:
-        t, ns = cpu_step_sample(2)
-        cpu = {"value": 1.0 / t, "unit": "evals/s", "cores": cpu_threads(), "kind": "port",
-               "sample": f"{ns} of {N_WAVELENGTHS} wavelengths at full size, time scaled by "
-                         f"{N_WAVELENGTHS // ns}; NumPy complex64 restatement of dLux's op "
-                         "order"}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cs = CpuStep()
+        try:
+            times = cs.time(CPU_BASELINE_STEPS, 1)
+        finally:
+            cs.close()
+        cpu = {"value": len(times) / sum(times), "unit": "evals/s", "cores": cs.workers,
+               "kind": "port",
+               "sample": f"{len(times)} whole steps after one warm-up: " + cs.sample()}
         parity = parity_sample(args.variant, 2)
 
     if rank == 0:
@@ -964,8 +1045,19 @@ def main():
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
             "data": "synthetic (seeded PCG64)",
-            "config": config_dict({"variant": args.variant,
-                                   "parallelism": f"replicas x{world}"}),
+            "config": config_dict(),
+            "variant": args.variant,
+            "parallelism": f"replicas x{world}",
+            "p50_ms": statistics.median(lat_dev),
+            "p99_ms": float(np.percentile(lat_dev, 99)),
+            "latency": {"device_p50_ms": statistics.median(lat_dev),
+                        "device_p99_ms": float(np.percentile(lat_dev, 99)),
+                        "e2e_p50_ms": statistics.median(lat_e2e),
+                        "e2e_p99_ms": float(np.percentile(lat_e2e, 99)),
+                        "samples": len(lat_dev),
+                        "how": "graphed step replayed one at a time: CUDA events around each "
+                               "replay (device), host wall time of each host-driven replay "
+                               "with its pinned copies and wait (e2e)"},
             "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": res["launches"],

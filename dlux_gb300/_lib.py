@@ -172,6 +172,8 @@ _SIGNATURES = {
     "dlx_set_split_k": (_c_int, [_c_int]),
     "dlx_set_gemm_pair": (_c_int, [_c_int]),
     "dlx_gemm_pair_clusters": (_c_int, [ctypes.POINTER(_c_int)]),
+    "dlx_set_wait_limit_ns": (_c_int, [ctypes.c_ulonglong]),
+    "dlx_test_gemm_withhold_copies": (_c_int, [_c_int]),
     "dlx_scene_forward_token": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     "dlx_scene_reuse_forward": (_c_int, [_c_vp, ctypes.c_ulonglong]),
     "dlx_scene_set_retain_limit": (_c_int, [_c_vp, ctypes.c_size_t]),

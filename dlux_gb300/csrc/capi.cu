@@ -35,6 +35,34 @@ int check_cuda(cudaError_t e, const char* what) {
   return DLX_ERR_CUDA;
 }
 
+int current_device(int* dev) {
+  DLX_TRY_CUDA(cudaGetDevice(dev));
+  if (*dev < 0 || *dev >= kMaxDevices)
+    return fail(DLX_ERR_UNSUPPORTED, "device index " + std::to_string(*dev) +
+                                         " is beyond the library's per-device tables");
+  return DLX_OK;
+}
+
+int check_focal(double focal_length, const char* who) {
+  if (focal_length >= 0) return DLX_OK;
+  return fail(DLX_ERR_ARG, std::string(who) +
+                               ": focal_length must be positive (0 selects the angular form)");
+}
+
+static std::atomic<int> g_sm_count[kMaxDevices];
+int device_sm_count(int* sms) {
+  int dev = 0;
+  DLX_TRY(current_device(&dev));
+  int n = g_sm_count[dev].load();
+  if (n <= 0) {
+    DLX_TRY_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    if (n <= 0) return fail(DLX_ERR_CUDA, "device reports no multiprocessors");
+    g_sm_count[dev].store(n);
+  }
+  *sms = n;
+  return DLX_OK;
+}
+
 namespace {
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
@@ -474,6 +502,7 @@ int dlx_transfer_matrix(const double* wavelengths_host, int batch, int n_in,
     return fail(DLX_ERR_SHAPE, "transfer_matrix: batch >= 0, n_in > 0 and n_out > 0 required");
   if (batch == 0) return DLX_OK;
   if (!wavelengths_host || !out_c64) return fail(DLX_ERR_ARG, "transfer_matrix: null pointer");
+  DLX_TRY(check_focal(focal_length, "transfer_matrix"));
   cudaStream_t s = as_stream(stream);
   std::vector<DftAxis> ax(batch);
   for (int b = 0; b < batch; ++b) {
@@ -507,6 +536,7 @@ int dlx_mft_plan_create(const dlx_mft_desc* d, const double* wl, dlx_mft_plan* p
     return fail(DLX_ERR_SHAPE, "mft_plan_create: batch, n_in and n_out must be positive");
   if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
     return fail(DLX_ERR_ARG, "mft_plan_create: pixel scales must be positive");
+  DLX_TRY(check_focal(d->focal_length, "mft_plan_create"));
   DLX_TRY(validate_variant(d->variant));
   DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
   auto* p = new (std::nothrow) dlx_mft_plan_s();
@@ -564,6 +594,7 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
   if (d->batch <= 0 || d->n_in <= 0 || d->pad <= 0)
     return fail(DLX_ERR_SHAPE, "fft_plan_create: batch, n_in and pad must be positive");
   if (!(d->pixel_scale_in > 0)) return fail(DLX_ERR_ARG, "fft_plan_create: pixel scale <= 0");
+  DLX_TRY(check_focal(d->focal_length, "fft_plan_create"));
   if (d->variant == DLX_VARIANT_RADIX) {
     auto* p = new (std::nothrow) dlx_fft_plan_s();
     if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
@@ -1068,6 +1099,7 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
                                  std::to_string(kMaxObj) + "]");
   if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
     return fail(DLX_ERR_ARG, "poly_plan_create: pixel scales must be positive");
+  DLX_TRY(check_focal(d->focal_length, "poly_plan_create"));
   DLX_TRY(validate_variant(d->variant));
   DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
   auto* p = new (std::nothrow) dlx_poly_plan_s();

@@ -32,6 +32,15 @@ int check_cuda(cudaError_t e, const char* what);
 // Counts every kernel launch of the library (dlx_launch_count).
 void note_launch();
 
+// Host-side state that depends on the device (kernel attributes, SM counts,
+// status words) is kept once per device: a process may drive several
+// devices, making each current in turn. Device indices are below kMaxDevices.
+constexpr int kMaxDevices = 64;
+// Writes the current device's index; DLX_ERR_CUDA / DLX_ERR_UNSUPPORTED otherwise.
+int current_device(int* dev);
+// Multiprocessor count of the current device (looked up once per device).
+int device_sm_count(int* sms);
+
 #define DLX_LAUNCH_CHECK(what)                                          \
   do {                                                                  \
     cudaError_t _e = cudaGetLastError();                                \

@@ -139,15 +139,8 @@ int launch_conv_kgrad(const float* in, const float* g, int H, int W, int batch, 
                       float* g_k, cudaStream_t s) {
   const int nchunk = (K1 + KC - 1) / KC;
   // about two blocks per SM in all
-  static int sms = 0;
-  if (sms == 0) {
-    int dev = 0, n = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
-      sms = n;
-    else
-      sms = 152;
-  }
+  int sms = 0;
+  DLX_TRY(device_sm_count(&sms));
   int nband = (2 * sms + K0 * nchunk - 1) / (K0 * nchunk);
   if (nband > H) nband = H;
   if (nband < 1) nband = 1;

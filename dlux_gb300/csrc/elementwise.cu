@@ -871,13 +871,15 @@ int launch_obj_pupil_fused(const ObjReduceArgs& a, cudaStream_t s) {
   bool want_w = false;
   for (int r = 0; r < R; ++r) want_w |= a.outs.o[r].g_w != nullptr;
   const size_t smem = sizeof(float4) * (size_t)a.L + (want_w ? sizeof(double) * 8 * (size_t)a.L : 0);
-  static std::atomic<bool> attr_done{false};  // host side, once per process
-  if (smem > 48 * 1024 && !attr_done.load()) {
+  static std::atomic<bool> attr_done[kMaxDevices];  // host side, once per device
+  int dev = 0;
+  DLX_TRY(current_device(&dev));
+  if (smem > 48 * 1024 && !attr_done[dev].load()) {
     for (const void* k : {(const void*)obj_pupil_fused_kernel<true>,
                           (const void*)obj_pupil_fused_kernel<false>})
       DLX_TRY_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(sizeof(double) * 10 * kFusedPupilMaxL)));
-    attr_done.store(true);
+    attr_done[dev].store(true);
   }
   if (a.split_form)
     DLX_PDL_LAUNCH("obj_pupil_fused_kernel", obj_pupil_fused_kernel<true>, dim3(a.nparts, R),

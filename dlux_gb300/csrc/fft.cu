@@ -196,8 +196,10 @@ int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* o
   const int lpb = lines_per_block(P);
   const int rmax = max_radix_log2(P);
   const size_t smem = sizeof(float2) * (size_t)lpb * P;
-  static std::atomic<bool> attr_done{false};  // host side, once per process
-  if (!attr_done.load()) {
+  static std::atomic<bool> attr_done[kMaxDevices];  // host side, once per device
+  int dev = 0;
+  DLX_TRY(current_device(&dev));
+  if (!attr_done[dev].load()) {
     const int lim = 200 * 1024;  // covers P <= 8192 at the lines-per-block choice above
     DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<4, 3>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
@@ -207,7 +209,7 @@ int launch_lines(const float2* in, LineIO io_in, int n_in, int off_in, float2* o
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
     DLX_TRY_CUDA(cudaFuncSetAttribute(fft_lines_kernel<2, 4>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, lim));
-    attr_done.store(true);
+    attr_done[dev].store(true);
   }
   dim3 grid((lines + lpb - 1) / lpb, batch);
 #define DLX_FFT_LAUNCH(L, R)                                                                \

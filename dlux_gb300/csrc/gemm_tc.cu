@@ -87,7 +87,11 @@ constexpr int TP_A_PLANE_BYTES = (TC_BM / 2) * TC_BK * 2;                 // 4 K
 constexpr int TP_STAGE_BYTES = 4 * TP_A_PLANE_BYTES + 4 * B_PLANE_BYTES;  // 48 KB
 static_assert(TP_STAGES * TP_STAGE_BYTES == TC_STAGES * STAGE_BYTES,
               "both forms use the same shared-memory layout size");
+// Wall-clock limit of each mbarrier wait: the default, and the one used while
+// draining after an abort (copies and MMAs already issued always complete,
+// so the drain keeps the long limit whatever the caller set).
 constexpr unsigned long long kTimeoutNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kDrainNs = kTimeoutNs;
 
 // ------------------------------- PTX wrappers -------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -131,13 +135,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // (then the abort flag and the device status word are set). Inlined: a call
 // inside a setmaxnreg region makes ptxas run out of memory.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
-                                       int* status, bool honour_abort = true) {
+                                       int* status, unsigned long long limit_ns,
+                                       bool honour_abort = true) {
   const unsigned long long t0 = globaltimer();
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 63u) == 63u) {
       if (honour_abort && *abort_flag) return false;
-      if (globaltimer() - t0 > kTimeoutNs) {
+      if (globaltimer() - t0 > limit_ns) {
         *abort_flag = 1;
         if (status) atomicExch(status, DLX_ERR_TIMEOUT);
         return false;
@@ -149,9 +154,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
 // Warp-uniform bounded wait: lane 0 polls, the verdict is broadcast, so the
 // whole warp leaves together (required before .sync.aligned tcgen05 ops).
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity,
-                                          volatile int* abort_flag, int* status) {
+                                          volatile int* abort_flag, int* status,
+                                          unsigned long long limit_ns) {
   int ok = 0;
-  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag, status) ? 1 : 0;
+  if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort_flag, status, limit_ns) ? 1 : 0;
   ok = __shfl_sync(0xffffffffu, ok, 0);
   return ok != 0;
 }
@@ -370,6 +376,8 @@ struct TcParams {
   int splits, kbps;    // split K: each work item covers kbps K blocks of one tile
   int conj_a;
   int* status;
+  unsigned long long wait_ns;  // limit of each mbarrier wait
+  int withhold_copies;         // test hook: the copy warp issues nothing (waits run out)
   EpiArgs epi;
 };
 
@@ -464,7 +472,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(REG_CTRL));
   if (warp == 0) {
     // ------------------------------ TMA producer ------------------------------
-    if (lane == 0) {
+    // withhold_copies (tests of the bounded waits, single-CTA form only):
+    // nothing is issued, so the consumers' waits run into their limit with no
+    // copy in flight.
+    if (lane == 0 && !p.withhold_copies) {
       int stage = 0;
       uint32_t ph = 0;
       uint32_t issued_mask = 0, issued_ph = 0;
@@ -474,7 +485,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int b = t.b, mt = t.mt, nt = t.nt;
         const int ab = b / p.a_batch_div;
         for (int kb = t.kb0; kb < t.kb1; ++kb) {
-          if (!mbar_wait(&empty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+          if (!mbar_wait(&empty[stage], ph ^ 1u, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
           uint8_t* base = smem + stage * kStageBytes;
           if constexpr (PAIR) {
             // both CTAs' parts complete on the even CTA's barrier
@@ -509,7 +520,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       if (!ok && (!PAIR || rank == 0)) {
         for (int s = 0; s < kStages; ++s)
           if (issued_mask & (1u << s))
-            mbar_wait(&full[s], (issued_ph >> s) & 1u, abort_flag, p.status, false);
+            mbar_wait(&full[s], (issued_ph >> s) & 1u, abort_flag, p.status, kDrainNs, false);
       }
     }
   } else if (warp == 1) {
@@ -528,10 +539,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool ok = true;
       for (int w = unit0; w < p.total && ok; w += ustep) {
         const TcWork t = PAIR ? tc_work_pair(p, w, nkb, rank) : tc_work(p, w, nkb);
-        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int kb = t.kb0; kb < t.kb1; ++kb) {
-          if (!mbar_wait(&full[stage], ph, abort_flag, p.status)) { ok = false; break; }
+          if (!mbar_wait(&full[stage], ph, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
           tc_fence_after();
           const uint32_t sa = smem_u32(smem + stage * kStageBytes);
           const uint32_t sb = sa + 4 * kAPlane;
@@ -571,7 +582,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       // Wait for every MMA this thread issued before TMEM is released.
       if constexpr (PAIR) mma_commit_pair(mdone, 0x1); else mma_commit(mdone);
-      mbar_wait(mdone, 0, abort_flag, p.status, false);
+      mbar_wait(mdone, 0, abort_flag, p.status, kDrainNs, false);
     }
   }
   } else {
@@ -583,7 +594,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int half = (warp - TC_EPI_W0) >> 2;  // the two warps of a quarter take alternate chunks
     uint32_t acc_ph = 0;
     for (int w = unit0; w < p.total; w += ustep) {
-      if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
+      if (!warp_wait(tfull, acc_ph, abort_flag, p.status, p.wait_ns)) break;
       tc_fence_after();
       const TcWork t = PAIR ? tc_work_pair(p, w, nkb, rank) : tc_work(p, w, nkb);
       const int b = t.b, mt = t.mt, nt = t.nt;
@@ -668,6 +679,7 @@ struct TcGenParams {
   int rows_are_out;
   const DftAxis* axes;
   int* status;
+  unsigned long long wait_ns;  // limit of each mbarrier wait
   EpiArgs epi;
 };
 
@@ -738,7 +750,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         const int r = w - b * p.mt * p.nt;
         const int nt = r - (r / p.nt) * p.nt;
         for (int kb = 0; kb < nkb; ++kb) {
-          if (!mbar_wait(&bempty[stage], ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+          if (!mbar_wait(&bempty[stage], ph ^ 1u, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
           mbar_expect_tx(&bfull[stage], G_B_BYTES);
           uint8_t* base = bbuf + stage * G_B_BYTES;
 #pragma unroll
@@ -753,7 +765,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       if (!ok)
         for (int s = 0; s < GB_STAGES; ++s)
           if (issued_mask & (1u << s))
-            mbar_wait(&bfull[s], (issued_ph >> s) & 1u, abort_flag, p.status, false);
+            mbar_wait(&bfull[s], (issued_ph >> s) & 1u, abort_flag, p.status, kDrainNs, false);
     }
   } else if (warp == 1) {
     // ------------------------------- MMA issuer -------------------------------
@@ -768,11 +780,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       uint32_t phb = 0, pha = 0, acc_ph = 0;
       bool ok = true;
       for (int w = blockIdx.x; w < p.total && ok; w += gridDim.x) {
-        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        if (!mbar_wait(tempty, acc_ph ^ 1u, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
         tc_fence_after();
         for (int kb = 0; kb < nkb; ++kb) {
-          if (!mbar_wait(&bfull[sb], phb, abort_flag, p.status)) { ok = false; break; }
-          if (!mbar_wait(&afull[sa], pha, abort_flag, p.status)) { ok = false; break; }
+          if (!mbar_wait(&bfull[sb], phb, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
+          if (!mbar_wait(&afull[sa], pha, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
           tc_fence_after();
           const uint32_t s_a = smem_u32(abuf + sa * G_A_BYTES);
           const uint32_t s_b = smem_u32(bbuf + sb * G_B_BYTES);
@@ -811,14 +823,14 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         acc_ph ^= 1u;
       }
       mma_commit(mdone);
-      mbar_wait(mdone, 0, abort_flag, p.status, false);
+      mbar_wait(mdone, 0, abort_flag, p.status, kDrainNs, false);
     }
   } else if (warp < 6) {
     // -------------------------------- epilogue --------------------------------
     const int q = warp & 3;  // column-per-thread drain, as in tc_cgemm_kernel
     uint32_t acc_ph = 0;
     for (int w = blockIdx.x; w < p.total; w += gridDim.x) {
-      if (!warp_wait(tfull, acc_ph, abort_flag, p.status)) break;
+      if (!warp_wait(tfull, acc_ph, abort_flag, p.status, p.wait_ns)) break;
       tc_fence_after();
       const int b = w / (p.mt * p.nt);
       const int r = w - b * p.mt * p.nt;
@@ -879,7 +891,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
       for (int t = 0; t < 32; ++t) step[t] = cis_affine((float)t, dff, zero);
       for (int kb = 0; kb < nkb; ++kb) {
-        if (!warp_wait(&aempty[sa], pha ^ 1u, abort_flag, p.status)) { ok = false; break; }
+        if (!warp_wait(&aempty[sa], pha ^ 1u, abort_flag, p.status, p.wait_ns)) { ok = false; break; }
         const float2 base = cis_affine((float)(kb * TC_BK), dff, tff);
         uint8_t* tile = abuf + sa * G_A_BYTES + r * 64;
         const int kvalid = p.K - kb * TC_BK;  // columns beyond K must be zero
@@ -1024,8 +1036,19 @@ __global__ void splitk_reduce_kernel(const float2* __restrict__ part, int splits
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-int g_num_sms = 0;
-int g_pair_clusters = 0;  // co-resident clusters of the paired form (0: unavailable)
+std::once_flag g_encode_once;
+int g_encode_status = DLX_OK;
+void init_encode() {
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                       &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    g_encode_status = fail(DLX_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    return;
+  }
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+}
 // Paired form of the loaded-operand GEMM (dlx_set_gemm_pair, or DLX_GEMM_PAIR=1
 // in the environment); off by default: on GB300 it measures the same as the
 // single-CTA form (within 1-3% either way on the batched workloads), whose
@@ -1033,59 +1056,74 @@ int g_pair_clusters = 0;  // co-resident clusters of the paired form (0: unavail
 // memory traffic rather than by shared-memory or L2 bandwidth. Read at every
 // launch, so a change also applies to existing plans (but not to CUDA graphs
 // already captured).
-std::atomic<int> g_pair_enabled{0};
-int g_cc = 0;
-int* g_status = nullptr;
-std::once_flag g_once;
-int g_init_status = DLX_OK;
+std::atomic<int> g_pair_enabled{-1};  // -1: not yet read from the environment
+// Limit of each mbarrier wait (dlx_set_wait_limit_ns), read at every launch.
+std::atomic<unsigned long long> g_wait_ns{kTimeoutNs};
+// Test hook (dlx_test_gemm_withhold_copies): the copy warp issues nothing.
+std::atomic<int> g_withhold{0};
 
-void init_once() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) {
-    g_init_status = fail(DLX_ERR_CUDA, "cudaGetDevice failed");
+bool pair_enabled() {
+  int v = g_pair_enabled.load();
+  if (v < 0) {
+    const char* e = getenv("DLX_GEMM_PAIR");
+    int want = (e && atoi(e) != 0) ? 1 : 0;
+    int expect = -1;
+    g_pair_enabled.compare_exchange_strong(expect, want);
+    v = g_pair_enabled.load();
+  }
+  return v != 0;
+}
+
+// State of one device: set up on first use with that device current.
+struct TcDevice {
+  std::once_flag once;
+  int init_status = DLX_OK;
+  int num_sms = 0;
+  int cc = 0;
+  int pair_clusters = 0;  // co-resident clusters of the paired form (0: unavailable)
+  int* status = nullptr;  // DLX_ERR_TIMEOUT word read by dlx_device_status
+};
+TcDevice g_dev[kMaxDevices];
+
+void init_device(TcDevice* d, int dev) {
+  std::call_once(g_encode_once, init_encode);
+  if (g_encode_status != DLX_OK) {
+    d->init_status = g_encode_status;
     return;
   }
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-    g_init_status = fail(DLX_ERR_CUDA, "cudaGetDeviceProperties failed");
+    d->init_status = fail(DLX_ERR_CUDA, "cudaGetDeviceProperties failed");
     return;
   }
-  g_num_sms = prop.multiProcessorCount;
-  g_cc = prop.major * 10 + prop.minor;
-  void* fn = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
-                                       &q) != cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !fn) {
-    g_init_status = fail(DLX_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+  d->num_sms = prop.multiProcessorCount;
+  d->cc = prop.major * 10 + prop.minor;
+  if (cudaMalloc(&d->status, sizeof(int)) != cudaSuccess ||
+      cudaMemset(d->status, 0, sizeof(int)) != cudaSuccess) {
+    d->status = nullptr;
+    d->init_status = fail(DLX_ERR_NOMEM, "status word allocation failed");
     return;
   }
-  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  if (const char* e = getenv("DLX_GEMM_PAIR")) g_pair_enabled.store(atoi(e) != 0 ? 1 : 0);
-  if (cudaMalloc(&g_status, sizeof(int)) != cudaSuccess ||
-      cudaMemset(g_status, 0, sizeof(int)) != cudaSuccess) {
-    g_init_status = fail(DLX_ERR_NOMEM, "status word allocation failed");
-    return;
-  }
-  bool attr_ok = true;
+  if (d->cc != 103) return;  // no tensor-core form on this device
   // The register split of the loaded kernels needs REG_LAUNCH registers per
   // thread at launch; refuse a build that came out with fewer.
   for (const void* const* k = loaded_kernels(); *k; ++k) {
     cudaFuncAttributes fa{};
     if (cudaFuncGetAttributes(&fa, *k) != cudaSuccess || fa.numRegs < REG_LAUNCH) {
-      g_init_status = fail(DLX_ERR_UNSUPPORTED,
-                           "tensor-core GEMM: the build's register count does not cover its "
-                           "warpgroup register split");
+      d->init_status = fail(DLX_ERR_UNSUPPORTED,
+                            "tensor-core GEMM: the build's register count does not cover its "
+                            "warpgroup register split");
       return;
     }
   }
+  bool attr_ok = true;
   for (const void* const* k = loaded_kernels(); *k; ++k)
     attr_ok = attr_ok && cudaFuncSetAttribute(*k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               SMEM_BYTES) == cudaSuccess;
   if (!attr_ok ||
       cudaFuncSetAttribute(tc_cgemm_gen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            G_SMEM_BYTES) != cudaSuccess) {
-    g_init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tensor-core GEMM) failed");
+    d->init_status = fail(DLX_ERR_CUDA, "cudaFuncSetAttribute(tensor-core GEMM) failed");
     return;
   }
   // How many two-CTA clusters fit at once: the paired form's persistent grid.
@@ -1096,7 +1134,7 @@ void init_once() {
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(2 * (g_num_sms / 2));
+    cfg.gridDim = dim3(2 * (d->num_sms / 2));
     cfg.blockDim = dim3(TC_THREADS);
     cfg.dynamicSmemBytes = SMEM_BYTES;
     cfg.attrs = at;
@@ -1107,8 +1145,18 @@ void init_once() {
       (void)cudaGetLastError();
       n = 0;
     }
-    g_pair_clusters = n;
+    d->pair_clusters = n;
   }
+}
+
+// The current device's state, set up on first use; nullptr (error recorded)
+// if the device cannot be queried.
+TcDevice* tc_device() {
+  int dev = 0;
+  if (current_device(&dev) != DLX_OK) return nullptr;
+  TcDevice* d = &g_dev[dev];
+  std::call_once(d->once, init_device, d, dev);
+  return d;
 }
 
 // Operand tiles are 64-byte rows (32 K elements); L2 promotion of 128 bytes
@@ -1133,8 +1181,8 @@ int encode_split(CUtensorMap* map, const __nv_bfloat16* base, int rows, int K, i
 }  // namespace
 
 bool tc_supported() {
-  std::call_once(g_once, init_once);
-  return g_init_status == DLX_OK && g_cc == 103;
+  const TcDevice* d = tc_device();
+  return d && d->init_status == DLX_OK && d->cc == 103;
 }
 
 // Split K (see GemmArgs::splits). Creation-time switch for plans made after
@@ -1142,14 +1190,12 @@ bool tc_supported() {
 std::atomic<int> g_split_k_enabled{1};
 bool split_k_enabled() { return g_split_k_enabled.load() != 0; }
 
-
-
 int split_k_count(long long tiles, int K) {
-  std::call_once(g_once, init_once);
-  if (g_init_status != DLX_OK || g_cc != 103 || tiles <= 0) return 1;
+  const TcDevice* d = tc_device();
+  if (!d || d->init_status != DLX_OK || d->cc != 103 || tiles <= 0) return 1;
   const int nkb = (K + TC_BK - 1) / TC_BK;
-  if (nkb < 2 || tiles * 2 > g_num_sms) return 1;  // half the SMs or more are busy already
-  long long s = g_num_sms / tiles;
+  if (nkb < 2 || tiles * 2 > d->num_sms) return 1;  // half the SMs or more are busy already
+  long long s = d->num_sms / tiles;
   if (s > 8) s = 8;
   if (s > nkb) s = nkb;
   if (s < 2) return 1;
@@ -1164,13 +1210,17 @@ size_t split_k_bytes(int splits, long long batch, int M, int N) {
 }
 
 int* tc_status_word() {
-  std::call_once(g_once, init_once);
-  return g_status;
+  TcDevice* d = tc_device();
+  return d ? d->status : nullptr;
 }
 
 int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
-  std::call_once(g_once, init_once);
-  if (g_init_status != DLX_OK) return g_init_status;
+  const TcDevice* dev = tc_device();
+  if (!dev) return DLX_ERR_CUDA;
+  if (dev->init_status != DLX_OK) return dev->init_status;
+  if (dev->cc != 103) return fail(DLX_ERR_UNSUPPORTED, "split-BF16 GEMM needs an sm_103 device");
+  const int num_sms = dev->num_sms;
+  const unsigned long long wait_ns = g_wait_ns.load();
   if (g.batch <= 0 || g.M <= 0 || g.N <= 0) return DLX_OK;
   if (g.K % 8 != 0 || g.N % 8 != 0)
     return fail(DLX_ERR_SHAPE, "split-BF16 GEMM needs K and N to be multiples of 8");
@@ -1191,9 +1241,10 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
     p.conj_a = g.conj_a ? 1 : 0;
     p.rows_are_out = g.a_rows_are_out ? 1 : 0;
     p.axes = g.a_axes;
-    p.status = g_status;
+    p.status = dev->status;
+    p.wait_ns = wait_ns;
     p.epi = g.epi;
-    const int grid = p.total < g_num_sms ? p.total : g_num_sms;
+    const int grid = p.total < num_sms ? p.total : num_sms;
     tc_cgemm_gen_kernel<<<grid, G_THREADS, G_SMEM_BYTES, s>>>(tb, p);
     DLX_LAUNCH_CHECK("tc_cgemm_gen_kernel");
     return DLX_OK;
@@ -1204,8 +1255,9 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const bool split = g.splits > 1 && g.split_ws != nullptr && nkb > 1;
   const int nt_tiles = (g.N + TC_BN - 1) / TC_BN;
   // Paired form: n-tiles in pairs, no split K.
-  const bool pair = !split && nt_tiles % 2 == 0 && g_pair_clusters > 0 &&
-                    g_pair_enabled.load() != 0;
+  const int withhold = g_withhold.load();
+  const bool pair = !split && nt_tiles % 2 == 0 && dev->pair_clusters > 0 && !withhold &&
+                    pair_enabled();
   CUtensorMap ta, tb;
   DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, pair ? TC_BM / 2 : TC_BM));
   DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, nB, TC_BN));
@@ -1223,7 +1275,9 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   }
   p.total = g.batch * p.mt * p.nt * p.splits;
   p.conj_a = g.conj_a ? 1 : 0;
-  p.status = g_status;
+  p.status = dev->status;
+  p.wait_ns = wait_ns;
+  p.withhold_copies = withhold;
   p.epi = g.epi;
   if (split) {
     p.epi.kind = EPI_PARTIAL;
@@ -1233,13 +1287,13 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
     p.total = g.batch * p.mt * (p.nt / 2);  // n-tile pairs
     LoadedKernel kern = loaded_kernel_pair(p.epi.kind);
     if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
-    const int clusters = p.total < g_pair_clusters ? p.total : g_pair_clusters;
+    const int clusters = p.total < dev->pair_clusters ? p.total : dev->pair_clusters;
     const cudaError_t e = launch_pair(kern, clusters, s, ta, tb, p);
     if (e != cudaSuccess) return check_cuda(e, "tc_cgemm_kernel (paired)");
     note_launch();
     return DLX_OK;
   }
-  const int grid = p.total < g_num_sms ? p.total : g_num_sms;
+  const int grid = p.total < num_sms ? p.total : num_sms;
   LoadedKernel kern = loaded_kernel(p.epi.kind);
   if (!kern) return fail(DLX_ERR_ARG, "split-BF16 GEMM: unknown epilogue kind");
   DLX_PDL_LAUNCH("tc_cgemm_kernel", kern, dim3(grid), dim3(TC_THREADS), SMEM_BYTES, s, ta, tb, p);
@@ -1265,8 +1319,18 @@ extern "C" int dlx_set_gemm_pair(int enable) {
 
 extern "C" int dlx_gemm_pair_clusters(int* clusters) {
   if (!clusters) return DLX_ERR_ARG;
-  std::call_once(dlx::g_once, dlx::init_once);
-  *clusters = dlx::g_init_status == DLX_OK ? dlx::g_pair_clusters : 0;
+  const dlx::TcDevice* d = dlx::tc_device();
+  *clusters = (d && d->init_status == DLX_OK) ? d->pair_clusters : 0;
+  return DLX_OK;
+}
+
+extern "C" int dlx_set_wait_limit_ns(unsigned long long limit_ns) {
+  dlx::g_wait_ns.store(limit_ns ? limit_ns : dlx::kTimeoutNs);
+  return DLX_OK;
+}
+
+extern "C" int dlx_test_gemm_withhold_copies(int enable) {
+  dlx::g_withhold.store(enable ? 1 : 0);
   return DLX_OK;
 }
 

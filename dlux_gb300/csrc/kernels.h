@@ -5,6 +5,11 @@
 
 namespace dlx {
 
+// focal_length of the C ABI: 0 selects the angular form (dLux's
+// focal_length=None), a positive value the Cartesian form. A negative value is
+// refused: dLux's own MFT takes log(nfringes), which is NaN for it.
+int check_focal(double focal_length, const char* who);
+
 // Per-batch double scalars passed by value (chunks of up to kMaxBatchArg).
 constexpr int kMaxBatchArg = 256;
 struct BatchD {

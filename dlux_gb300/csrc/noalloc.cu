@@ -16,8 +16,11 @@
 // Costs and rules:
 //   * every GPU that loads the library holds kNoAllocScratchBytes (8 MiB)
 //     for the life of the process;
-//   * sizes needing more than that are rejected (DLX_ERR_SHAPE): the limit
-//     is 3 * n_in * n_out * 8 bytes, e.g. n_in = n_out = 512 fits;
+//   * sizes needing more than that are rejected (DLX_ERR_SHAPE): a call
+//     needs 3 * roundup(n_in * n_out * 8, 256) + 256 bytes (three complex64
+//     matrices, each rounded up to 256 bytes, plus the normalisation scalar),
+//     e.g. n_in = n_out = 512 fits and 592 x 592 does not;
+//   * focal_length 0 selects the angular form; a negative one is refused;
 //   * all calls share the one array, so calls that may overlap on the GPU
 //     (different streams, no ordering between them) race and must be
 //     serialised by the caller; calls on one stream are ordered;
@@ -32,7 +35,7 @@ namespace dlx {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
-constexpr int kMaxDevices = 64;
+constexpr size_t kNoAllocAlign = 256;
 
 // The scratch itself. Host code must not use this name as a pointer: on the
 // host it is only a stand-in for the symbol, so its device address is looked
@@ -45,8 +48,7 @@ void* g_addr[kMaxDevices] = {};
 // Device address of g_noalloc_scratch on the current device (set-up on first use).
 int scratch_address(void** out) {
   int dev = 0;
-  DLX_TRY_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(DLX_ERR_UNSUPPORTED, "device index too large");
+  DLX_TRY(current_device(&dev));
   std::lock_guard<std::mutex> lock(g_addr_mutex);
   if (!g_addr[dev]) {
     void* p = nullptr;
@@ -64,7 +66,7 @@ DftAxis axis_for(double wl, int n_in, double ps_in, int n_out, double ps_out, do
                  double focal, bool inverse) {
   DftAxis a{};
   double s_out = ps_out / (wl / (ps_in * n_in));
-  if (focal > 0) s_out /= focal;
+  if (focal != 0) s_out /= focal;  // 0: angular (focal_length=None)
   a.a_in = 1.0 / n_in;
   a.b_in = -(0.5 * (n_in - 1) + shift) / n_in;
   a.a_out = s_out;
@@ -103,16 +105,16 @@ extern "C" int dlx_mft_forward_noalloc(const void* in_c64, int batch, int n_in,
     return fail(DLX_ERR_ARG, "mft_forward_noalloc: null pointer");
   if (!(pixel_scale_in > 0) || !(pixel_scale_out > 0))
     return fail(DLX_ERR_ARG, "mft_forward_noalloc: pixel scales must be positive");
+  DLX_TRY(check_focal(focal_length, "mft_forward_noalloc"));
   const size_t mat = (size_t)n_in * n_out;
-  const size_t align = 256;
-  const size_t mat_bytes = (mat * sizeof(float2) + align - 1) / align * align;
-  const size_t need = 3 * mat_bytes + align;  // AxT, AyT, half-transformed field, alpha
+  const size_t mat_bytes = (mat * sizeof(float2) + kNoAllocAlign - 1) / kNoAllocAlign * kNoAllocAlign;
+  const size_t need = 3 * mat_bytes + kNoAllocAlign;  // AxT, AyT, half-transformed field, alpha
   if (need > kNoAllocScratchBytes)
     return fail(DLX_ERR_SHAPE,
                 "mft_forward_noalloc: n_in = " + std::to_string(n_in) + ", n_out = " +
                     std::to_string(n_out) + " needs " + std::to_string(need) +
-                    " bytes of scratch; the fixed scratch holds " +
-                    std::to_string(kNoAllocScratchBytes) + " (3 * n_in * n_out * 8 bytes max)");
+                    " bytes of scratch (3 * roundup(n_in * n_out * 8, 256) + 256); the fixed "
+                    "scratch holds " + std::to_string(kNoAllocScratchBytes));
   for (int b = 0; b < batch; ++b)
     if (!(wavelengths_host[b] > 0))
       return fail(DLX_ERR_ARG, "mft_forward_noalloc: wavelengths must be positive");
@@ -140,7 +142,7 @@ extern "C" int dlx_mft_forward_noalloc(const void* in_c64, int batch, int n_in,
                  inverse != 0), n_out, n_in, aty);
     DLX_LAUNCH_CHECK("noalloc_dft_kernel");
     double out_size = n_out * pixel_scale_out;
-    if (focal_length > 0) out_size /= focal_length;
+    if (focal_length != 0) out_size /= focal_length;
     const double nf = out_size / (wl / (n_in * pixel_scale_in));
     noalloc_set_kernel<<<1, 1, 0, st>>>(alpha, (float)(nf / ((double)n_in * n_out)));
     DLX_LAUNCH_CHECK("noalloc_set_kernel");

@@ -613,6 +613,7 @@ int dlx_scene_plan_create(const dlx_scene_desc* d, const double* wavelengths,
                                  std::to_string(kMaxObj) + "]");
   if (!(d->pixel_scale_in > 0) || !(d->pixel_scale_out > 0))
     return fail(DLX_ERR_ARG, "scene_plan_create: pixel scales must be positive");
+  DLX_TRY(check_focal(d->focal_length, "scene_plan_create"));
   if (d->variant != DLX_VARIANT_FP32 && d->variant != DLX_VARIANT_SPLIT_BF16)
     return fail(DLX_ERR_ARG, "scene_plan_create: unknown variant");
   if (d->variant == DLX_VARIANT_SPLIT_BF16) {

@@ -43,8 +43,20 @@ const char* dlx_last_error(void);
 int dlx_version(void);
 /* Synchronises `stream`, then reports (and clears) the device status word that
  * the tensor-core kernels set when a bounded wait expires: *status is DLX_OK
- * or DLX_ERR_TIMEOUT. No dLux counterpart (dLux has no device-side waits). */
+ * or DLX_ERR_TIMEOUT. The status word is kept per device (the current one is
+ * read). No dLux counterpart (dLux has no device-side waits). */
 int dlx_device_status(void* stream, int* status);
+/* Wall-clock limit of each wait inside the tensor-core GEMMs, in ns, read at
+ * every launch (0 restores the default of 2 s). On expiry a GEMM sets the
+ * device status word to DLX_ERR_TIMEOUT, lets the copies and MMAs it already
+ * issued complete, frees its tensor memory and returns; its output is then
+ * undefined. No dLux counterpart. */
+int dlx_set_wait_limit_ns(unsigned long long limit_ns);
+/* Test hook for the bounded waits: while enabled, the copy warp of the
+ * loaded-operand tensor-core GEMM (single-CTA form) issues no copies, so its
+ * consumers' waits run into the limit of dlx_set_wait_limit_ns with nothing in
+ * flight. Results are undefined while it is on. No dLux counterpart. */
+int dlx_test_gemm_withhold_copies(int enable);
 /* Number of kernel launches the library has issued in this process. */
 long long dlx_launch_count(void);
 /* Brackets every complex-GEMM launch with CUDA events on its own stream until
@@ -60,7 +72,9 @@ int dlx_gemm_timing_end(double* total_ms, int* launches, double* flops);
  *   exp(-+2 pi i in_vec (x) out_vec)
  * (or its [n_out][n_in] transpose when transpose != 0), with the phase
  * argument formed and range-reduced in FP64 on the device.
- * focal_length <= 0 means angular (dLux focal_length=None).
+ * focal_length 0 means angular (dLux focal_length=None); a negative
+ * focal_length is refused with DLX_ERR_ARG in every entry point (dLux's MFT
+ * takes the log of the then negative fringe count and returns NaN).
  */
 int dlx_transfer_matrix(const double* wavelengths_host, int batch, int n_in,
                         double pixel_scale_in, int n_out, double pixel_scale_out,
@@ -80,7 +94,7 @@ typedef struct {
   int n_out;              /* output side M */
   double pixel_scale_in;  /* input pixel scale (m/pixel) */
   double pixel_scale_out; /* output pixel scale (rad/pixel, or m/pixel with focal_length) */
-  double focal_length;    /* <= 0: angular propagation */
+  double focal_length;    /* 0: angular propagation; < 0 is refused */
   double shift_x;         /* output-plane shift in output pixels (dLux pixel=True) */
   double shift_y;
   int inverse;            /* dLux inverse=True */
@@ -101,8 +115,8 @@ int dlx_mft_adjoint(dlx_mft_plan plan, const void* gout_c64, void* gin_c64, void
  * allocation after start-up. No counterpart in the reference (dLux allocates
  * through XLA). Needs no plan: the DFT matrices and the intermediate field
  * live in a fixed 8 MiB device array inside the library, so
- * 3 * n_in * n_out * 8 bytes must fit (n_in = n_out = 512 does); larger sizes
- * return DLX_ERR_SHAPE. The caller passes input [batch][n_in][n_in] and
+ * 3 * roundup(n_in * n_out * 8, 256) + 256 bytes must fit (n_in = n_out = 512
+ * does); larger sizes return DLX_ERR_SHAPE. The caller passes input [batch][n_in][n_in] and
  * output [batch][n_out][n_out] complex64 device buffers. All calls share the
  * array: calls that can overlap on the GPU (unordered streams) race. The first
  * call on a device looks the array up (cudaGetSymbolAddress); make it before
@@ -125,7 +139,7 @@ typedef struct {
   int n_in;               /* input side N */
   int pad;                /* output side is n_in * pad */
   double pixel_scale_in;
-  double focal_length;    /* <= 0: angular */
+  double focal_length;    /* 0: angular; < 0 is refused */
   int inverse;
   int apply_ramps;        /* 0: no ramps (spec_out None); 1: ramps from centers below */
   double center_in;       /* input grid centre (m) */
@@ -214,7 +228,7 @@ typedef struct {
   int n_out;              /* focal side M (psf_npixels * oversample) */
   double pixel_scale_in;  /* diameter / N */
   double pixel_scale_out; /* rad/pixel (angular) or m/pixel */
-  double focal_length;    /* <= 0: angular */
+  double focal_length;    /* 0: angular; < 0 is refused */
   int variant;            /* DLX_VARIANT_* */
   int operand_mode;       /* split form only: 0 = cached DFT matrices streamed by TMA,
                              1 = DFT operand generated inside the GEMM (no cached matrices) */
@@ -444,7 +458,7 @@ typedef struct {
   int n_out;               /* PSF side M */
   double pixel_scale_in;   /* pupil pixel (m) */
   double pixel_scale_out;  /* PSF pixel (rad, or m with focal_length) */
-  double focal_length;     /* <= 0: angular */
+  double focal_length;     /* 0: angular; < 0 is refused */
   int variant;             /* DLX_VARIANT_* */
   int max_sources;         /* sources per launch, 1..32 */
 } dlx_scene_desc;
