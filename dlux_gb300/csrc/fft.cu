@@ -1,16 +1,20 @@
 // fft.cu -- the padded, centred 2-D FFT of dLux (utils/propagation.py:8-64,
-// utils/fourier.py:14-78, wavefronts.py:654-727) as radix-2 FFTs of lines in
-// shared memory, for large pad * N where the exact DFT-GEMM pair costs
-// O(P^2 N).
+// utils/fourier.py:14-78, wavefronts.py:654-727) as power-of-two FFTs of
+// lines in shared memory, for large pad * N where the exact DFT-GEMM pair
+// costs O(P^2 N).
 //
 // The DFT-GEMM form uses A[k][j] = exp(2 pi i s (j + npad - c)(k - c) / P)
 // times the input and output phase ramps. Since exp(2 pi i s j' k' / P) is
 // P-periodic in j' and k', that is a plain length-P FFT whose input element j
 // sits at slot (j + npad - c) mod P and whose output element k is read at slot
 // (k - c) mod P. One kernel covers every pass. It loads n_in elements of each
-// line through an input ramp, scatters them into bit-reversed slots, runs
-// log2(P) in-place butterfly stages (four per shared-memory pass) and gathers
-// n_out elements through an output ramp and a scale:
+// line through an input ramp, scatters them into bit-reversed slots, runs the
+// log2(P) radix-2 butterfly stages in place and gathers n_out elements through
+// an output ramp and a scale. The stages are grouped into radix-2^R passes: a
+// thread keeps 2^R elements in registers for R consecutive stages, so shared
+// memory is touched once per R stages; R is 3 up to P = 2048 and 4 from
+// P = 4096 (max_radix_log2). A block holds 4 lines up to P = 1024 and 2 above
+// (lines_per_block). The passes are:
 //   forward   rows:    N lines of N -> P   (x), into tmp [N][P]
 //             columns: P lines of N -> P   (y), from tmp into out [P][P]
 //   adjoint   rows:    P lines of P -> N   (x, conjugate), into tmp [P][N]

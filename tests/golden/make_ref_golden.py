@@ -1,0 +1,282 @@
+"""Golden fixtures made by dLux itself (tests/golden/ref_*.npz).
+
+Runs dLux's own, unmodified source (the ``src`` directory of dLux v0.16.0,
+passed as the first argument) on the host under the NumPy stand-ins of
+ref_standin.py, in float64 -- dLux as it runs with jax_enable_x64 -- and
+saves its outputs on the seeded inputs of ref_inputs.py:
+
+  ref_utils.npz  utils functions: transfer_matrix, calc_nfringes and MFT
+                 (utils/propagation.py:67-256), FFT (:8-64), fft_spec and
+                 fft_phase_ramp (utils/fourier.py:14-78), zernike_basis
+                 (utils/zernikes.py:297-315), circular_aperture
+                 (utils/apertures.py:153-242), downsample
+                 (utils/array_ops.py:124-162), eval_basis (utils/math.py:177-196);
+  ref_cfg1.npz   config 1 through AngularOpticalSystem.propagate
+                 (optical_systems.py:147-223): PSF and the gradient of
+                 sum(R * PSF) with respect to the coefficients;
+  ref_cfg2.npz   config 2 (the benchmark workload) through
+                 AngularOpticalSystem + LayeredDetector([Downsample(4)]):
+                 image and coefficient gradient of sum(R * image);
+  ref_cfg3.npz   config 3: image through ApplyPixelResponse, the Poisson data
+                 and NLL, the coefficient gradient and directional derivatives
+                 with respect to the pupil amplitude and the flat field;
+  ref_cfg4.npz   config 4 at its sizes with 4 sources, PointSources.model
+                 (sources.py:392-411): image, and directional derivatives of
+                 sum(R * image) with respect to positions and fluxes.
+
+dLux's gradients come from JAX autodiff, which cannot run here, so every
+gradient is taken by fourth-order central differences of dLux's own forward in
+float64 (step h: truncation ~h^4, far below the 1e-5 tolerance of the tests).
+The script also checks the oracle (oracle/dlux_oracle.py, FP64) against every
+fixture before saving and prints the differences.
+
+    python tests/golden/make_ref_golden.py <dLux src dir> [utils cfg1 cfg2 cfg3 cfg4]
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+import ref_inputs as RI  # noqa: E402
+import ref_standin  # noqa: E402
+from ref_standin import J  # noqa: E402
+
+
+def rel(a, b):
+    a = np.asarray(a, np.complex128)
+    b = np.asarray(b, np.complex128)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def fd4(f, x, v, h):
+    """Fourth-order central difference of f at x along v."""
+    return (-f(x + 2 * h * v) + 8 * f(x + h * v) - 8 * f(x - h * v) + f(x - 2 * h * v)) / (12 * h)
+
+
+def fd4_grad(f, x, h):
+    g = np.zeros(len(x))
+    for i in range(len(x)):
+        e = np.zeros(len(x))
+        e[i] = 1.0
+        g[i] = fd4(f, x, e, h)
+    return g
+
+
+def make_utils(dl, O):
+    dlu = dl.utils
+    out = {}
+    for name, n_in, n_out, ps_in, ps_out, fl, shift, pixel, inv, wl in RI.MFT_CASES:
+        E = RI.case_field(name, n_in)
+        sh = np.array(shift, float)
+        got = dlu.MFT(J(E.copy()), wl, ps_in, n_out, ps_out, focal_length=fl, shift=J(sh.copy()),
+                      pixel=pixel, inverse=inv)
+        ora = O.mft(E, wl, ps_in, n_out, ps_out, fl, shift, pixel, inv)
+        print(f"MFT {name}: oracle vs dLux {rel(ora, got):.2e}")
+        out[f"mft_{name}"] = got.astype(np.complex64)
+        out[f"nfringes_{name}"] = np.float64(dlu.propagation.calc_nfringes(
+            wl, n_in, ps_in, n_out, ps_out, focal_length=fl))
+        tm = dlu.propagation.transfer_matrix(wl, n_in, ps_in, n_out, ps_out, shift=sh[0], focal_length=fl,
+                                 inverse=inv)
+        tora = O.transfer_matrix(wl, n_in, ps_in, n_out, ps_out, sh[0], fl, 0.0, inv)
+        print(f"  transfer_matrix: oracle vs dLux {rel(tora, tm):.2e}")
+        if n_in * n_out <= 256 * 128:
+            out[f"tm_{name}"] = tm.astype(np.complex64)
+    for name, n, ps, wl, fl, pad, inv in RI.FFT_CASES:
+        E = RI.case_field(name, n, salt=7)
+        got, ps_out = dlu.FFT(J(E.copy()), wl, ps, focal_length=fl, pad=pad, inverse=inv)
+        ora, ops = O.fft_prop(E, wl, ps, fl, pad, inv)
+        print(f"FFT {name}: oracle vs dLux {rel(ora, got):.2e}, pixel scale "
+              f"{abs(ops - ps_out) / abs(ps_out):.1e}")
+        out[f"fft_{name}"] = got.astype(np.complex64)
+        out[f"fft_ps_{name}"] = np.float64(ps_out)
+        d, c = dlu.fft_spec(n * pad, ps, wl, focal_length=fl)
+        out[f"fft_spec_{name}"] = np.array([d, c], float)
+    xs = np.linspace(-0.5, 0.5, 17)
+    for inv in (False, True):
+        out[f"ramp_{int(inv)}"] = dlu.fft_phase_ramp(xs, 1e-6, 0.3e-6, focal_length=2.0,
+                                                     inverse=inv)
+    coords = dlu.pixel_coords(48, 1.0)
+    zb = dlu.zernike_basis(list(range(1, 40)), coords, 1.0)
+    out["zernike_basis_48"] = zb.astype(np.float32)
+    print(f"zernike_basis: oracle vs dLux "
+          f"{rel(O.zernike_basis(list(range(1, 40)), coords, 1.0), zb):.2e}")
+    apertures = {
+        "cfg1": dict(npixels=256, oversample=1, secondary_diameter=0.1,
+                     zernike_nolls=list(range(4, 14))),
+        "cfg2": dict(npixels=512, oversample=5, secondary_diameter=0.1, spider_width=0.01,
+                     spider_angles=(0, 90, 180, 270), zernike_nolls=list(range(4, 25))),
+    }
+    for name, kw in apertures.items():
+        n = kw.pop("npixels")
+        T, B = dlu.circular_aperture(n, 1.0, **kw)
+        To, Bo = O.circular_aperture(n, 1.0, **kw)
+        print(f"circular_aperture {name}: T {rel(To, T):.2e}, B {rel(Bo, B):.2e}")
+        step = n // 64
+        out[f"aperture_T_{name}"] = T.astype(np.float32)
+        out[f"aperture_Bsub_{name}"] = B[:, ::step, ::step].astype(np.float32)
+        out[f"aperture_Bsum_{name}"] = B.sum((1, 2))
+        out[f"aperture_Bsq_{name}"] = (B ** 2).sum((1, 2))
+    x = RI.normal(np.random.default_rng(9), (64, 64))
+    out["downsample_sum"] = dlu.downsample(x, 4, mean=False)
+    out["downsample_mean"] = dlu.downsample(x, 4, mean=True)
+    basis = RI.normal(np.random.default_rng(10), (5, 16, 16))
+    coeffs = RI.normal(np.random.default_rng(11), 5)
+    out["eval_basis"] = dlu.eval_basis(basis, coeffs)
+    return out
+
+
+def _cfg1_system(dl, T, B, c):
+    L = dl.layers
+    return dl.optical_systems.AngularOpticalSystem(
+        256, 1.0, [L.TransmissiveLayer(T, normalise=True), L.BasisLayer(B, c)], 128, 0.02, 1)
+
+
+def make_cfg1(dl, O):
+    inp = RI.cfg1()
+    T, B = dl.utils.circular_aperture(256, 1.0, oversample=1, secondary_diameter=0.1,
+                                      zernike_nolls=inp["nolls"])
+    wls = inp["wavelengths"]
+
+    def psf_of(c):
+        return _cfg1_system(dl, T, B, c).propagate(wls)
+
+    psf = psf_of(inp["coeffs"])
+    loss = lambda c: float((psf_of(c) * inp["R"]).sum())  # noqa: E731
+    grad = fd4_grad(loss, inp["coeffs"], 2e-10)
+    ora = O.poly_psf(T, np.tensordot(B, inp["coeffs"], axes=(0, 0)), wls, [1.0], 1.0, 128,
+                     0.02 * RI.ARCSEC)
+    Teff = T / np.sqrt((T ** 2).sum())
+    g = O.poly_psf_grad(Teff, np.tensordot(B, inp["coeffs"], axes=(0, 0)), wls, [1.0], 1.0,
+                        128, 0.02 * RI.ARCSEC, inp["R"])
+    gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+    print(f"cfg1: PSF oracle vs dLux {rel(ora, psf):.2e}, gradient oracle vs dLux FD "
+          f"{rel(gc, grad):.2e}")
+    return {"psf": psf, "loss": loss(inp["coeffs"]), "grad": grad}
+
+
+def make_cfg2(dl, O):
+    inp = RI.cfg2()
+    L = dl.layers
+    T, B = dl.utils.circular_aperture(512, 1.0, oversample=5, secondary_diameter=0.1,
+                                      spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                                      zernike_nolls=inp["nolls"])
+    wls, w = inp["wavelengths"], inp["weights"]
+    det = dl.detectors.LayeredDetector([L.Downsample(4)])
+
+    def image_of(c):
+        optics = dl.optical_systems.AngularOpticalSystem(
+            512, 1.0, [L.TransmissiveLayer(T, normalise=True), L.BasisLayer(B, c)], 128,
+            0.02, 4)
+        return det.model(optics.propagate(wls, weights=w, return_psf=True))
+
+    t0 = time.time()
+    img = image_of(inp["coeffs"])
+    print(f"cfg2 forward {time.time() - t0:.1f} s")
+    loss = lambda c: float((image_of(c) * inp["R"]).sum())  # noqa: E731
+    grad = fd4_grad(loss, inp["coeffs"], 2e-10)
+    opd = np.tensordot(B, inp["coeffs"], axes=(0, 0))
+    ps = 0.02 / 4 * RI.ARCSEC
+    ora = O.downsample(O.poly_psf(T, opd, wls, w, 1.0, 512, ps), 4, mean=False)
+    Teff = T / np.sqrt((T ** 2).sum())
+    G = np.kron(inp["R"], np.ones((4, 4)))
+    g = O.poly_psf_grad(Teff, opd, wls, w, 1.0, 512, ps, G)
+    gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+    print(f"cfg2: image oracle vs dLux {rel(ora, img):.2e}, gradient oracle vs dLux FD "
+          f"{rel(gc, grad):.2e}")
+    return {"image": img, "loss": loss(inp["coeffs"]), "grad": grad}
+
+
+def make_cfg3(dl, O):
+    inp = RI.cfg3()
+    L = dl.layers
+    T, B = dl.utils.circular_aperture(512, 1.0, oversample=1, secondary_diameter=0.1,
+                                      zernike_nolls=inp["nolls"])
+    A0 = T * (1.0 + inp["amp_pert"])
+    wls = inp["wavelengths"]
+
+    def image_of(c, A, flat):
+        optics = dl.optical_systems.AngularOpticalSystem(
+            512, 1.0, [L.TransmissiveLayer(A, normalise=True), L.BasisLayer(B, c)], 256,
+            0.02, 1)
+        det = dl.detectors.LayeredDetector([L.ApplyPixelResponse(flat)])
+        return det.model(optics.propagate(wls, return_psf=True))
+
+    img = image_of(inp["coeffs"], A0, inp["flat"])
+    scale = 1e6 / img.sum()
+    lam = img * scale
+    # data: a seeded Gaussian stand-in for the Poisson draw, rounded to counts
+    z = RI.normal(np.random.default_rng(303), lam.shape)
+    data = np.maximum(0.0, np.round(lam + np.sqrt(lam) * z))
+
+    def nll(c, A, flat):
+        m = image_of(c, A, flat) * scale
+        return float((m - data * np.log(m)).sum())
+
+    c0, f0 = inp["coeffs"], inp["flat"]
+    grad_c = fd4_grad(lambda c: nll(c, A0, f0), c0, 2e-10)
+    d_amp = [fd4(lambda A: nll(c0, A, f0), A0, v * T, 1e-6) for v in inp["dir_amp"]]
+    d_flat = [fd4(lambda f: nll(c0, A0, f), f0, v, 1e-6) for v in inp["dir_flat"]]
+    opd = np.tensordot(B, c0, axes=(0, 0))
+    ora = O.poly_psf(A0, opd, wls, np.full(len(wls), 1.0 / len(wls)), 1.0, 256,
+                     0.02 * RI.ARCSEC) * f0
+    print(f"cfg3: image oracle vs dLux {rel(ora, img):.2e}")
+    return {"image": img.astype(np.float32), "data": data.astype(np.float32),
+            "scale": scale, "loss": nll(c0, A0, f0), "grad_c": grad_c,
+            "dd_amp": np.array(d_amp), "dd_flat": np.array(d_flat)}
+
+
+def make_cfg4(dl, O):
+    inp = RI.cfg4()
+    L = dl.layers
+    T, B = dl.utils.circular_aperture(1024, 1.0, oversample=1, secondary_diameter=0.1,
+                                      zernike_nolls=inp["nolls"])
+    optics = dl.optical_systems.AngularOpticalSystem(
+        1024, 1.0, [L.TransmissiveLayer(T, normalise=True), L.BasisLayer(B, inp["coeffs"])],
+        128, 0.02, 1)
+    wls = inp["wavelengths"]
+
+    def image_of(pos, flux):
+        return dl.sources.PointSources(wls, position=pos, flux=flux).model(optics)
+
+    t0 = time.time()
+    img = image_of(inp["positions"], inp["fluxes"])
+    print(f"cfg4 forward {time.time() - t0:.1f} s")
+    loss_pos = lambda p: float((image_of(p, inp["fluxes"]) * inp["R"]).sum())  # noqa: E731
+    loss_flux = lambda f: float((image_of(inp["positions"], f) * inp["R"]).sum())  # noqa: E731
+    dd_pos = [fd4(loss_pos, inp["positions"], v, 1e-9) for v in inp["dir_pos"] / RI.ARCSEC]
+    dd_flux = [fd4(loss_flux, inp["fluxes"], v, 1.0) for v in inp["dir_flux"]]
+    opd = np.tensordot(B, inp["coeffs"], axes=(0, 0))
+    w = np.full(len(wls), 1.0 / len(wls))
+    ora = sum(f * O.poly_psf(T, opd, wls, w, 1.0, 128, 0.02 * RI.ARCSEC, offset=tuple(p))
+              for p, f in zip(inp["positions"], inp["fluxes"]))
+    print(f"cfg4: image oracle vs dLux {rel(ora, img):.2e}")
+    return {"image": img, "loss": float((img * inp["R"]).sum()), "dd_pos": np.array(dd_pos),
+            "dd_flux": np.array(dd_flux)}
+
+
+def main():
+    src = sys.argv[1]
+    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4"]
+    dl = ref_standin.load_dlux(src)
+    from oracle import dlux_oracle as O
+    makers = {"utils": make_utils, "cfg1": make_cfg1, "cfg2": make_cfg2, "cfg3": make_cfg3,
+              "cfg4": make_cfg4}
+    for name in which:
+        t0 = time.time()
+        data = makers[name](dl, O)
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, **data)
+        print(f"wrote {path} ({os.path.getsize(path) / 1e6:.2f} MB, {time.time() - t0:.0f} s)")
+
+
+if __name__ == "__main__":
+    main()

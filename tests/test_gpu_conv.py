@@ -1,6 +1,8 @@
 """PSF convolution (mode "same") on the device: PSF.convolve, ApplyJitter, ResolvedSource,
 PointResolvedSource against the FP64 oracle, with gradients. Tolerances: relative L2 <= 1e-5
-for values and gradients (FP32 sums of at most a few thousand products)."""
+for values and gradients (FP32 sums of at most a few thousand products). Batches of images
+share one kernel: its gradient is the sum over the batch. A kernel nearly as tall as the
+image leaves some row bands of the kernel-gradient reduction without valid rows."""
 
 import numpy as np
 import pytest
@@ -21,31 +23,37 @@ def dev(x):
     return torch.as_tensor(np.ascontiguousarray(x), dtype=torch.float32, device="cuda")
 
 
-@pytest.mark.parametrize("H,W,K0,K1", [(64, 64, 3, 3), (100, 70, 8, 5), (128, 128, 33, 33),
-                                       (40, 40, 1, 7)])
-def test_conv_same_and_gradients(cuda, H, W, K0, K1):
+@pytest.mark.parametrize("Bt,H,W,K0,K1", [(1, 64, 64, 3, 3), (1, 100, 70, 8, 5),
+                                          (1, 128, 128, 33, 33), (1, 40, 40, 1, 7),
+                                          (3, 64, 48, 5, 7), (3, 40, 40, 33, 9),
+                                          (2, 16, 20, 15, 3)])
+def test_conv_same_and_gradients(cuda, Bt, H, W, K0, K1):
     from dlux_gb300 import autograd
-    rng = np.random.default_rng(H + K0)
-    a = rng.random((H, W))
+    rng = np.random.default_rng(H + K0 + 100 * Bt)
+    a = rng.random((Bt, H, W))
     k = rng.random((K0, K1))
-    G = rng.normal(size=(H, W))
-    x = dev(a).requires_grad_(True)
+    G = rng.normal(size=(Bt, H, W))
+    x = dev(a if Bt > 1 else a[0]).requires_grad_(True)
     kt = dev(k).requires_grad_(True)
     out = autograd.conv2d_same(x, kt)
-    (out * dev(G)).sum().backward()
-    ref = O.convolve_same(a, k)
-    # <conv(a, k), G> is linear in k: d/dk[i][j] = <conv(a, e_ij), G>
-    g_k = np.array([[(O.convolve_same(a, np.eye(1, K0 * K1, i * K1 + j).reshape(K0, K1)) * G).sum()
+    (out * dev(G if Bt > 1 else G[0])).sum().backward()
+    ref = np.stack([O.convolve_same(a[b], k) for b in range(Bt)])
+    # <conv(a, k), G> is linear in k: d/dk[i][j] = sum_b <conv(a_b, e_ij), G_b>
+    g_k = np.array([[sum((O.convolve_same(a[b], np.eye(1, K0 * K1, i * K1 + j)
+                                           .reshape(K0, K1)) * G[b]).sum() for b in range(Bt))
                      for j in range(K1)] for i in range(K0)])
-    # and in a: d/da is the correlation of G with k
+    # and in a: d/da_b is the correlation of G_b with k
     g_a = np.zeros_like(a)
     s0, s1 = (K0 - 1) // 2, (K1 - 1) // 2
-    Gp = np.pad(G, ((K0, K0), (K1, K1)))
-    for p in range(K0):
-        for q in range(K1):
-            g_a += k[p, q] * Gp[K0 - s0 + p:K0 - s0 + p + H, K1 - s1 + q:K1 - s1 + q + W]
-    e_o, e_a, e_k = rel(out.detach().cpu(), ref), rel(x.grad.cpu(), g_a), rel(kt.grad.cpu(), g_k)
-    print(f"conv {H}x{W} * {K0}x{K1}: out {e_o:.2e}, d/din {e_a:.2e}, d/dk {e_k:.2e}")
+    for b in range(Bt):
+        Gp = np.pad(G[b], ((K0, K0), (K1, K1)))
+        for p in range(K0):
+            for q in range(K1):
+                g_a[b] += k[p, q] * Gp[K0 - s0 + p:K0 - s0 + p + H, K1 - s1 + q:K1 - s1 + q + W]
+    out_np = out.detach().cpu().numpy().reshape(Bt, H, W)
+    ga_np = x.grad.cpu().numpy().reshape(Bt, H, W)
+    e_o, e_a, e_k = rel(out_np, ref), rel(ga_np, g_a), rel(kt.grad.cpu(), g_k)
+    print(f"conv {Bt}x{H}x{W} * {K0}x{K1}: out {e_o:.2e}, d/din {e_a:.2e}, d/dk {e_k:.2e}")
     assert e_o < 1e-5 and e_a < 1e-5 and e_k < 1e-5
 
 
@@ -83,13 +91,16 @@ def test_jitter_and_resolved_sources(cuda):
     # d/d dist through the normalisation: finite differences of the oracle
     def loss(dd):
         return (O.convolve_same(2.0 * base, dd / dd.sum()) * G).sum()
+    # (fourth-order central differences in FP64: accurate to ~1e-10 here)
     gd = np.zeros_like(dist)
+    h = 1e-4
     for i in range(5):
         for j in range(5):
             e = np.zeros_like(dist)
-            e[i, j] = 1e-6
-            gd[i, j] = (loss(dist + e) - loss(dist - e)) / 2e-6
-    assert rel(d.grad.cpu(), gd) < 1e-4
+            e[i, j] = h
+            gd[i, j] = (-loss(dist + 2 * e) + 8 * loss(dist + e) - 8 * loss(dist - e)
+                        + loss(dist - 2 * e)) / (12 * h)
+    assert rel(d.grad.cpu(), gd) < 1e-5
     # point + resolved with a contrast
     prs = dl.PointResolvedSource(wls, position=pos, flux=3.0, distribution=dist, contrast=0.5)
     img2 = prs.model(optics)
