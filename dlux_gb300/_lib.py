@@ -154,6 +154,14 @@ _SIGNATURES = {
     "dlx_basis_eval": (_c_int, [_c_vp, _c_vp, _c_vp, _c_int, _c_ll, _c_vp, _c_vp]),
     "dlx_basis_grad": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_vp, _c_vp]),
     "dlx_psf_sum": (_c_int, [_c_vp, _c_int, _c_ll, _c_vp, _c_vp]),
+    "dlx_psf_sum_weighted": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_vp, _c_vp]),
+    "dlx_psf_sum_weighted_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_ll, _c_vp, _c_vp,
+                                               _c_vp, _c_vp]),
+    "dlx_phasor_backward": (_c_int, [_c_vp, _c_vp, _c_vp, _c_vp, _c_vp, _c_int, _c_int, _c_vp,
+                                     _c_vp, _c_vp, _c_vp, _c_vp, _c_vp]),
+    "dlx_normalise": (_c_int, [_c_vp, _c_int, _c_ll, _c_int, _c_dbl, _c_vp, _c_vp, _c_vp]),
+    "dlx_normalise_backward": (_c_int, [_c_vp, _c_int, _c_ll, _c_int, _c_dbl, _c_vp, _c_vp,
+                                        _c_vp]),
     "dlx_downsample": (_c_int, [_c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp, _c_vp]),
     "dlx_downsample_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_int, _c_int, _c_vp, _c_vp,
                                          _c_vp, _c_vp]),

@@ -282,9 +282,10 @@ def downsample(psf, k, mean=False, flat=None):
 class PhasorMul(torch.autograd.Function):
     """field * amp * exp(i (2 pi opd / lambda_b + phase)) for a batch of wavelengths.
 
-    The forward runs the phasor kernel. The backward (used only by the
-    layer-by-layer path, not by the fused system path) is written with torch
-    complex elementwise operations.
+    The forward runs the phasor kernel, the backward its hand-written reverse
+    kernel (dlx_phasor_backward), which rebuilds the phasors with the forward's
+    own error-free reduction. Used by the layer-by-layer path; the fused system
+    path has its own reverse kernels.
     """
 
     @staticmethod
@@ -299,21 +300,55 @@ class PhasorMul(torch.autograd.Function):
     @staticmethod
     def backward(ctx, g):
         field, amp, opd, phase = ctx.saved_tensors
-        wl = torch.as_tensor(ctx.wavelengths, dtype=torch.float64, device=g.device).reshape(-1, 1, 1)
-        k = (2 * torch.pi / wl).to(torch.float32)
-        ph = torch.zeros((), device=g.device)
-        if opd is not None:
-            ph = ph + k * opd
-        if phase is not None:
-            ph = ph + phase
-        u = torch.polar(torch.ones_like(ph), ph) if torch.is_tensor(ph) and ph.dim() else \
-            torch.ones((), dtype=torch.complex64, device=g.device)
-        a = amp if amp is not None else torch.ones((), device=g.device)
-        fac = a * u
-        g_field = g * fac.conj() if ctx.needs_input_grad[2] else None
-        inner = (field * u).conj() * g  # d/d(real amp)
-        g_amp = inner.real.sum(0) if (amp is not None and ctx.needs_input_grad[3]) else None
-        dphi = ((field * fac).conj() * g).imag
-        g_opd = (k * dphi).sum(0) if (opd is not None and ctx.needs_input_grad[4]) else None
-        g_phase = dphi.sum(0) if (phase is not None and ctx.needs_input_grad[5]) else None
+        need = ctx.needs_input_grad
+        g_field, g_amp, g_opd, g_phase = kernels.phasor_backward(
+            ctx.wavelengths, field.detach().contiguous(), _d(amp), _d(opd), _d(phase), g,
+            want_field=need[2], want_amp=amp is not None and need[3],
+            want_opd=opd is not None and need[4], want_phase=phase is not None and need[5])
         return None, None, g_field, g_amp, g_opd, g_phase
+
+
+class PsfSum(torch.autograd.Function):
+    """PSF = sum_b w_b |F_b|^2 of unweighted focal fields (optical_systems.py:211-223):
+    the weighted intensity kernel and its reverse kernel."""
+
+    @staticmethod
+    def forward(ctx, field, weights):
+        f = field.detach().contiguous()
+        w = None if weights is None else weights.detach()
+        ctx.save_for_backward(f, w)
+        return kernels.psf_sum_weighted(f, w)
+
+    @staticmethod
+    def backward(ctx, g):
+        f, w = ctx.saved_tensors
+        gf, gw = kernels.psf_sum_weighted_backward(
+            f, w, g, want_field=ctx.needs_input_grad[0],
+            want_weights=w is not None and ctx.needs_input_grad[1])
+        if gw is not None:
+            gw = gw.to(w.dtype)
+        return gf, gw
+
+
+def psf_sum(field, weights=None):
+    return PsfSum.apply(field, weights)
+
+
+class Normalise(torch.autograd.Function):
+    """Wavefront.normalise (wavefronts.py:397-424) per plane, with its reverse kernel."""
+
+    @staticmethod
+    def forward(ctx, field, mode, value):
+        f = field.detach().contiguous()
+        ctx.save_for_backward(f)
+        ctx.mode, ctx.value = mode, value
+        return kernels.normalise(f, mode, value)
+
+    @staticmethod
+    def backward(ctx, g):
+        (f,) = ctx.saved_tensors
+        return kernels.normalise_backward(f, g, ctx.mode, ctx.value), None, None
+
+
+def normalise(field, mode="power", value=1.0):
+    return Normalise.apply(field, mode, float(value))

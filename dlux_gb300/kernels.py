@@ -705,6 +705,68 @@ def psf_sum(field):
     return out
 
 
+def psf_sum_weighted(field, weights=None):
+    """sum_b w_b |field_b|^2 of [B, N, N] focal fields (weights None: 1)."""
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    w = None if weights is None else weights.to(device=f.device, dtype=torch.float32).contiguous()
+    out = torch.empty(f.shape[-2:], dtype=torch.float32, device=f.device)
+    call("dlx_psf_sum_weighted", ptr(f), ptr(w), f.shape[0], f.shape[-1] * f.shape[-2],
+         ptr(out), _stream())
+    return out
+
+
+def psf_sum_weighted_backward(field, weights, g, want_field=True, want_weights=True):
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    w = None if weights is None else weights.to(device=f.device, dtype=torch.float32).contiguous()
+    gf = torch.empty_like(f) if want_field else None
+    gw = torch.empty((f.shape[0],), dtype=torch.float32, device=f.device) if want_weights \
+        else None
+    call("dlx_psf_sum_weighted_backward", ptr(f), ptr(w), f.shape[0],
+         f.shape[-1] * f.shape[-2], ptr(g.contiguous()), ptr(gf), ptr(gw), _stream())
+    return gf, gw
+
+
+def phasor_backward(wavelengths, field, amp, opd, phase, g, want_field=True, want_amp=True,
+                    want_opd=True, want_phase=True):
+    """Reverse pass of the phasor multiply (see dlx_phasor_backward)."""
+    wl = [float(w) for w in torch.as_tensor(wavelengths, dtype=torch.float64).reshape(-1)]
+    gg = g.contiguous()
+    n = gg.shape[-1]
+    pix = (n, n)
+    dev = gg.device
+    gf = torch.empty_like(gg) if want_field else None
+    g_amp = torch.empty(pix, dtype=torch.float32, device=dev) if want_amp else None
+    g_opd = torch.empty(pix, dtype=torch.float32, device=dev) if want_opd else None
+    g_ph = torch.empty(pix, dtype=torch.float32, device=dev) if want_phase else None
+    call("dlx_phasor_backward", ptr(field), ptr(amp), ptr(opd), ptr(phase),
+         _lib.dbl_array(wl), len(wl), n, ptr(gg), ptr(gf), ptr(g_amp), ptr(g_opd), ptr(g_ph),
+         _stream())
+    return gf, g_amp, g_opd, g_ph
+
+
+_NORM_MODES = {"power": 0, "peak": 1}
+
+
+def normalise(field, mode="power", value=1.0):
+    """Each [N, N] plane of `field` scaled to unit power or unit peak (times value)."""
+    if mode not in _NORM_MODES:
+        raise ValueError("mode must be 'power' or 'peak'")
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    out = torch.empty_like(f)
+    call("dlx_normalise", ptr(f), f.shape[0], f.shape[-1] * f.shape[-2], _NORM_MODES[mode],
+         float(value), ptr(out), None, _stream())
+    return out.reshape(field.shape)
+
+
+def normalise_backward(field, g, mode="power", value=1.0):
+    f = field.reshape(-1, field.shape[-2], field.shape[-1]).contiguous()
+    gg = g.reshape(f.shape).contiguous()
+    gin = torch.empty_like(f)
+    call("dlx_normalise_backward", ptr(f), f.shape[0], f.shape[-1] * f.shape[-2],
+         _NORM_MODES[mode], float(value), ptr(gg), ptr(gin), _stream())
+    return gin.reshape(field.shape)
+
+
 def downsample(psf, k, mean=False, flat=None):
     n = psf.shape[-1]
     if psf.shape[-2] != n:

@@ -53,7 +53,7 @@ class PupilAccumulator:
         self.phase = None
         self.opd_static = []
         self.phase_static = []
-        self.tilt = [0.0, 0.0]
+        self.tilt = torch.zeros(2, dtype=torch.float64)  # radians; may carry a gradient
 
     def amplitude(self, t):
         if t is None:
@@ -235,7 +235,8 @@ class Tilt(OpticalLayer):
     """Tilt by (x, y) radians (optical_layers.py:330-359)."""
 
     def __init__(self, angles):
-        a = torch.as_tensor(angles, dtype=torch.float64)
+        a = angles if isinstance(angles, torch.Tensor) else torch.as_tensor(angles,
+                                                                             dtype=torch.float64)
         if a.shape != (2,):
             raise ValueError("angles must be a 1d array of shape (2,).")
         self.angles = a
@@ -244,8 +245,8 @@ class Tilt(OpticalLayer):
         return wavefront.tilt(self.angles)
 
     def fuse(self, acc):
-        acc.tilt[0] += float(self.angles[0])
-        acc.tilt[1] += float(self.angles[1])
+        a = self.angles.to(torch.float64)
+        acc.tilt = acc.tilt.to(a.device) + a
 
 
 class Normalise(OpticalLayer):

@@ -86,11 +86,10 @@ class OpticalSystem(BaseOpticalSystem):
         raise NotImplementedError
 
     def _propagate_psf(self, wl, offset, weights):
-        wf = self._propagate_fields(wl, offset, weights)
-        f = wf.phasor
-        if f.requires_grad:
-            return (f.real ** 2 + f.imag ** 2).sum(0)
-        return kernels.psf_sum(f.contiguous())
+        """sum_l w_l |F_l|^2 of the unweighted focal fields (weighted intensity kernel)."""
+        wf = self._propagate_fields(wl, offset, None)
+        f = wf.phasor if wf.phasor.dim() == 3 else wf.phasor[None]
+        return autograd.psf_sum(f, weights)
 
     def _psf_pixel_scale(self):  # pragma: no cover - abstract
         raise NotImplementedError
@@ -145,9 +144,12 @@ class LayeredOpticalSystem(OpticalSystem):
         return wf
 
     def _propagate_fields(self, wl, offset, weights):
+        """Focal fields of every wavelength, times sqrt(weight) when weights are given."""
         wlt = torch.tensor(wl, dtype=torch.float64)
         wf = self.initialise_wavefront(wlt, offset.detach())
         wf = self._focus(self._run_layers(wf))
+        if weights is None:
+            return wf
         return wf.set(phasor=wf.phasor * torch.sqrt(weights)[:, None, None])
 
     def propagate_mono(self, wavelength, offset=None, return_wf=False):
@@ -222,7 +224,7 @@ class ParametricLayeredOpticalSystem(ParametricOpticalSystem, LayeredOpticalSyst
             return OpticalSystem._propagate_psf(self, wl, offset, weights)
         amp, flag, opd, phase, tilt = fused
         plan = self.fused_plan(wl)
-        tilt_t = offset.to(torch.float64) + torch.tensor(tilt, dtype=torch.float64)
+        tilt_t = offset.to(dtype=torch.float64, device=tilt.device) + tilt
         return autograd.poly_psf(plan, amp, opd, phase, weights, flag, tilt_t)
 
 

@@ -121,6 +121,7 @@ class PointSources(Source):
         if fused is None:
             return None
         amp, flag, opd, phase, tilt = fused
+        tilt = (float(tilt[0]), float(tilt[1]))
         wl = [float(v) for v in torch.as_tensor(src.spectrum.wavelengths,
                                                dtype=torch.float64).reshape(-1)]
         n_src = src.position.shape[0]

@@ -164,30 +164,25 @@ class Wavefront(Base):
         return self._mul_phasor(opd=opd)
 
     def tilt(self, angles, unit="rad"):
-        """Tilt by (x, y) angles (wavefronts.py:370-395)."""
+        """Tilt by (x, y) angles (wavefronts.py:370-395); differentiable in the angles."""
         a = torch.as_tensor(angles, dtype=torch.float64)
         if a.shape != (2,):
             raise ValueError("angles must be a 1d array of shape (2,).")
         f = unit_factor_to_rad(unit)
         coords = self.coordinates()
-        opd = (float(a[0]) * f) * coords[0] + (float(a[1]) * f) * coords[1]
+        if isinstance(angles, torch.Tensor) and angles.requires_grad:
+            at = (angles.to(torch.float64) * f).to(device=coords.device, dtype=torch.float32)
+            opd = at[0] * coords[0] + at[1] * coords[1]
+        else:
+            opd = (float(a[0]) * f) * coords[0] + (float(a[1]) * f) * coords[1]
         return self.add_opd(opd)
 
     def normalise(self, mode="power", value=1.0):
-        """Scale to unit power or unit peak (wavefronts.py:397-424)."""
-        if mode == "power":
-            field = self.phasor if self.batched else self.phasor[None]
-            scale = kernels.power_scale(field.detach().contiguous(), value)
-            if self.phasor.requires_grad:
-                p = (field.real ** 2 + field.imag ** 2).sum((-2, -1))
-                scale = torch.sqrt(value / p)
-            out = field * scale[:, None, None]
-            return self.set(phasor=out if self.batched else out[0])
-        if mode == "peak":
-            p = (self.phasor.real ** 2 + self.phasor.imag ** 2)
-            scale = torch.sqrt(value / p.amax((-2, -1), keepdim=True))
-            return self.set(phasor=self.phasor * scale)
-        raise ValueError("mode must be 'power' or 'peak'")
+        """Scale each wavelength's field to unit power or unit peak (wavefronts.py:397-424):
+        the normalisation kernel and its hand-written reverse pass."""
+        if mode not in ("power", "peak"):
+            raise ValueError("mode must be 'power' or 'peak'")
+        return self.set(phasor=autograd.normalise(self.phasor, mode, value))
 
     def flip(self, axis):
         return self.set(phasor=torch.flip(self.phasor, dims=(axis,) if isinstance(axis, int)

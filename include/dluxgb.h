@@ -168,6 +168,19 @@ int dlx_phasor(const void* in_c64, const float* amp, const float* opd, const flo
                const float* amp_scale, const float* weights, double const_scale,
                const double* wavelengths_host, int batch, int n, double pixel_scale,
                double tilt_x, double tilt_y, void* out_c64, void* stream);
+/* Reverse pass of dlx_phasor as the layer-by-layer path calls it (no tilt,
+ * amp_scale, weights or const_scale): for out_b = in_b * amp * u_b with
+ * u_b = exp(i (2 pi opd / lambda_b + phase)),
+ *   g_in_b = g_b conj(amp u_b),   g_amp = sum_b Re(conj(in_b u_b) g_b),
+ *   g_phase = sum_b Im(conj(out_b) g_b),   g_opd = sum_b (2 pi / lambda_b) Im(...).
+ * Replaces JAX's reverse mode of Wavefront.add_opd / add_phase
+ * (wavefronts.py:332-368) and of the real multiply (wavefronts.py:834-906).
+ * u_b is rebuilt with the forward's own reduction, bit for bit. in, amp, opd,
+ * phase and every output may be NULL (in NULL: a field of ones). */
+int dlx_phasor_backward(const void* in_c64, const float* amp, const float* opd,
+                        const float* phase, const double* wavelengths_host, int batch, int n,
+                        const void* g_c64, void* g_in_c64, float* g_amp, float* g_opd,
+                        float* g_phase, void* stream);
 
 /* ---- a8: power and normalisation ----------------------------------------
  * Wavefront.normalise (wavefronts.py:397-424), mode "power":
@@ -175,6 +188,17 @@ int dlx_phasor(const void* in_c64, const float* amp, const float* opd, const flo
  */
 int dlx_power_scale(const void* in_c64, int batch, int n, double value,
                     float* out_scale, void* stream);
+/* Wavefront.normalise (wavefronts.py:397-424) on each plane of a batch:
+ * out[b] = in[b] * s_b with s_b = sqrt(value / P_b), P_b = sum |in[b]|^2
+ * (mode 0, "power") or max |in[b]|^2 (mode 1, "peak"); out_scale[b] = s_b
+ * (NULL: not written). Another mode is refused with dLux's message. */
+int dlx_normalise(const void* in_c64, int batch, long long npix, int mode, double value,
+                  void* out_c64, float* out_scale, void* stream);
+/* Its reverse pass: g_in = s g - in s D / P with D = sum Re(conj(g) in), on
+ * every pixel (power) or on the pixels at the peak, shared equally among ties
+ * (peak), as JAX's reverse mode of max shares it. */
+int dlx_normalise_backward(const void* in_c64, int batch, long long npix, int mode,
+                           double value, const void* g_c64, void* g_in_c64, void* stream);
 /* Same for a real amplitude: out_scale = sqrt(value / sum amp^2). */
 int dlx_amp_norm(const float* amp, int n, double value, float* out_scale, void* stream);
 /* Reverse of a_eff = amp * sqrt(value / sum amp^2): g_amp from g_eff. */
@@ -196,6 +220,16 @@ int dlx_basis_grad(const float* basis, const float* g, int nterms, long long npi
  * (optical_systems.py:222-223): psf[p] = sum_b |in[b][p]|^2.
  */
 int dlx_psf_sum(const void* in_c64, int batch, long long npix, float* psf, void* stream);
+/* The PSF of OpticalSystem.propagate (optical_systems.py:211-223) from the
+ * unweighted focal fields: psf[p] = sum_b w_b |in[b][p]|^2 (weights NULL: 1),
+ * i.e. the field times sqrt(w_b) in dLux's vmap body, then the sum of |E|^2. */
+int dlx_psf_sum_weighted(const void* in_c64, const float* weights, int batch, long long npix,
+                         float* psf, void* stream);
+/* Its reverse pass: g_in[b][p] = 2 w_b g[p] in[b][p] and
+ * g_weights[b] = sum_p g[p] |in[b][p]|^2 (each output may be NULL). */
+int dlx_psf_sum_weighted_backward(const void* in_c64, const float* weights, int batch,
+                                  long long npix, const float* g, void* g_in_c64,
+                                  float* g_weights, void* stream);
 
 /* ---- a17/a18: detector ---------------------------------------------------
  * downsample(mean=False) (utils/array_ops.py:124-162, psfs.py:74-91) fused

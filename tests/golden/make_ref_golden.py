@@ -22,7 +22,14 @@ saves its outputs on the seeded inputs of ref_inputs.py:
                  with respect to the pupil amplitude and the flat field;
   ref_cfg4.npz   config 4 at its sizes with 4 sources, PointSources.model
                  (sources.py:392-411): image, and directional derivatives of
-                 sum(R * image) with respect to positions and fluxes.
+                 sum(R * image) with respect to positions and fluxes;
+  ref_layers.npz each layer type of the layer-by-layer path at small size:
+                 Optic and BasisOptic (layers/optics.py:17-175), AberratedLayer,
+                 BasisLayer effects "phase" and "amplitude", Tilt and Normalise
+                 (layers/optical_layers.py:189-371), CartesianOpticalSystem
+                 (optical_systems.py:683-775), a LayeredOpticalSystem with an MFT
+                 layer, and Wavefront.normalise "power"/"peak"
+                 (wavefronts.py:397-424): PSFs, losses and gradients.
 
 dLux's gradients come from JAX autodiff, which cannot run here, so every
 gradient is taken by fourth-order central differences of dLux's own forward in
@@ -263,13 +270,85 @@ def make_cfg4(dl, O):
             "dd_flux": np.array(dd_flux)}
 
 
+def make_layers(dl, O):
+    """Each layer type of the layer-by-layer path, through dLux's own classes."""
+    inp = RI.layers()
+    L = dl.layers
+    OS = dl.optical_systems
+    T, B = dl.utils.circular_aperture(64, 1.0, oversample=3, secondary_diameter=0.1,
+                                      zernike_nolls=inp["nolls"])
+    A = T * (1.0 + inp["amp_pert"])
+    wls, w, R = inp["wavelengths"], inp["weights"], inp["R"]
+    opd0, ph0, c0 = inp["opd"], inp["phase"], inp["coeffs"]
+    ang = lambda layers: OS.AngularOpticalSystem(64, 1.0, layers, 32, 0.04, 1)  # noqa: E731
+
+    def loss_of(make):
+        return lambda x: float((make(x).propagate(wls, weights=w) * R).sum())
+
+    out = {}
+    systems = {
+        # name: (builder of the system from its differentiated input, x0, kind, h)
+        "optic": (lambda o: ang([L.Optic(A, o, ph0, normalise=True)]), opd0, "dir_opd", 1e-9),
+        "optic_phase": (lambda p: ang([L.Optic(A, opd0, p, normalise=True)]), ph0, "dir_phase",
+                        1e-3),
+        "optic_amp": (lambda a: ang([L.Optic(a, opd0, None, normalise=True)]), A, "dir_amp", 1e-4),
+        "basis_optic": (lambda c: ang([L.BasisOptic(B, A, c, normalise=True)]), c0, "grad",
+                        2e-10),
+        "aberrated_opd": (lambda o: ang([L.TransmissiveLayer(A, normalise=True),
+                                         L.AberratedLayer(opd=o)]), opd0, "dir_opd", 1e-9),
+        "aberrated_phase": (lambda p: ang([L.TransmissiveLayer(A, normalise=True),
+                                           L.AberratedLayer(phase=p)]), ph0, "dir_phase", 1e-3),
+        "basis_phase": (lambda c: ang([L.TransmissiveLayer(A, normalise=True),
+                                       L.BasisLayer(B, c * 1e7, effect="phase")]), c0, "grad",
+                        2e-10),
+        "basis_amplitude": (lambda c: ang([L.TransmissiveLayer(A),
+                                           L.BasisLayer(B, c * 1e6, effect="amplitude"),
+                                           L.Normalise()]), c0, "grad", 2e-10),
+        "tilt_layer": (lambda t: ang([L.TransmissiveLayer(A, normalise=True), L.Tilt(t),
+                                      L.BasisLayer(B, c0)]), inp["tilt"], "grad", 1e-9),
+        "normalise_layer": (lambda c: ang([L.TransmissiveLayer(A), L.BasisLayer(B, c),
+                                           L.Normalise()]), c0, "grad", 2e-10),
+        "cartesian": (lambda c: OS.CartesianOpticalSystem(
+            64, 1.0, [L.TransmissiveLayer(A, normalise=True), L.BasisLayer(B, c)], 5.0, 32,
+            0.8, 1), c0, "grad", 2e-10),
+        "layered_mft": (lambda c: OS.LayeredOpticalSystem(
+            64, 1.0, [L.TransmissiveLayer(A, normalise=True), L.BasisLayer(B, c),
+                      L.MFT(32, 0.04 * RI.ARCSEC)]), c0, "grad", 2e-10),
+    }
+    for name, (make, x0, kind, h) in systems.items():
+        f = loss_of(make)
+        out[f"{name}_psf"] = make(x0).propagate(wls, weights=w)
+        out[f"{name}_loss"] = f(x0)
+        if kind == "grad":
+            out[f"{name}_grad"] = fd4_grad(f, np.asarray(x0, float), h)
+        else:
+            out[f"{name}_dd"] = fd4(f, x0, inp[kind] * (T if kind == "dir_amp" else 1.0), h)
+        print(f"layers {name}: loss {out[f'{name}_loss']:.6e}")
+
+    # Wavefront.normalise("peak") between the aperture and the MFT, one wavelength
+    def peak_psf(o):
+        wf = dl.wavefronts.Wavefront(1.0e-6, 64, diameter=1.0)
+        wf = wf * A
+        wf = wf.add_opd(o)
+        wf = wf.normalise("peak")
+        wf = wf.propagate(32, 0.04 * RI.ARCSEC)
+        return wf.psf
+    out["peak_psf"] = peak_psf(opd0)
+    out["peak_dd"] = fd4(lambda o: float((peak_psf(o) * R).sum()), opd0, inp["dir_opd"], 1e-9)
+    # power normalisation of a wavefront, for comparison
+    wf = dl.wavefronts.Wavefront(1.0e-6, 64, diameter=1.0) * A
+    out["power_phasor"] = wf.add_opd(opd0).normalise("power").phasor
+    out["peak_phasor"] = wf.add_opd(opd0).normalise("peak", 2.0).phasor
+    return out
+
+
 def main():
     src = sys.argv[1]
-    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4"]
+    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4", "layers"]
     dl = ref_standin.load_dlux(src)
     from oracle import dlux_oracle as O
     makers = {"utils": make_utils, "cfg1": make_cfg1, "cfg2": make_cfg2, "cfg3": make_cfg3,
-              "cfg4": make_cfg4}
+              "cfg4": make_cfg4, "layers": make_layers}
     for name in which:
         t0 = time.time()
         data = makers[name](dl, O)

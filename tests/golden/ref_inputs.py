@@ -111,3 +111,18 @@ def cfg4():
             "fluxes": 10.0 ** (2.0 + 4.0 * uniform(rng, 4)), "R": normal(rng, (128, 128)),
             "wavelengths": np.linspace(0.8e-6, 1.2e-6, 16), "nolls": list(range(4, 25)),
             "dir_pos": normal(rng, (2, 4, 2)) * ARCSEC, "dir_flux": normal(rng, (1, 4))}
+
+
+def layers():
+    """Small systems for the layer-type fixtures: 64^2 pupil (1 m, 10% obscuration),
+    Noll 4-11 basis, 2 wavelengths, 32^2 focal grid at 0.04"; loss sum(R * PSF).
+    OPD, phase and transmission perturbations and the derivative directions are
+    seeded fields."""
+    rng = np.random.default_rng(105)
+    return {"coeffs": 40e-9 * normal(rng, 8), "R": normal(rng, (32, 32)),
+            "wavelengths": np.array([0.9e-6, 1.1e-6]), "weights": np.array([0.4, 0.6]),
+            "nolls": list(range(4, 12)), "opd": 30e-9 * normal(rng, (64, 64)),
+            "phase": 0.2 * normal(rng, (64, 64)), "amp_pert": 0.05 * normal(rng, (64, 64)),
+            "tilt": np.array([0.03, -0.02]) * ARCSEC,
+            "dir_opd": 1e-8 * normal(rng, (64, 64)), "dir_phase": normal(rng, (64, 64)),
+            "dir_amp": normal(rng, (64, 64))}

@@ -92,7 +92,7 @@ def test_fusion_description_of_layers():
                   dl.Tilt([1e-7, 0.0])]:
         layer.fuse(acc)
     assert acc.normalised and len(acc.pre) == 1 and not acc.post
-    assert acc.tilt == [1e-7, 0.0] and len(acc.opd_static) == 1
+    assert acc.tilt.tolist() == [1e-7, 0.0] and len(acc.opd_static) == 1
     with pytest.raises(dl.layers.optical_layers.NotFusable):
         dl.MFT(16, 1e-7).fuse(acc)
 
