@@ -464,51 +464,45 @@ def time_e2e(args, gstep, world):
     return dt, h2d, d2h, lat
 
 
-def run_serving(args):
-    """Seeded Poisson stream of mixed-shape requests through dlux_gb300.serving.
+def _serving_tuner():
+    """The per-(N, M) plan autotuner, tuned once over the stream's shape grid."""
+    from dlux_gb300.autotune import PlanTuner
 
-    N in {128, 256, 512, 1024}, M in {64, 128, 256, 512}, L uniform on 1..64 over
-    0.8-1.2 um, 4..36 Zernike coefficients from N(0, 50 nm), 30 % of requests ask for
-    the coefficient gradient of <G, PSF> with G ~ N(0, 1). Arrivals are Poisson at
-    --rate requests/s. Plans of every bucket in the stream are made resident first
-    (within the 150 GB budget); a warm-up stream of a different seed runs before the
-    timed one. Latency is submit -> result on the host (pinned copies included).
-    """
+    tuner = PlanTuner()
+    grid, secs = tuner.tune_grid((128, 256, 512, 1024), (64, 128, 256, 512))
+    return tuner, {"seconds": secs, "cache": tuner.cache_path,
+                   "choices": {f"{n}x{m}": f"{c['variant']}/op{c['operand_mode']}"
+                               for (n, m), c in sorted(grid.items())}}
+
+
+def serve_streams(args, variant, rates, n_requests, tuner=None):
+    """One server (form `variant`, or the autotuner's per-shape choice), made
+    resident for every bucket of the streams, then one seeded Poisson stream per
+    arrival rate in `rates`, timed one after the other. Returns a report per rate."""
     import torch
     from dlux_gb300 import serving
 
-    from dlux_gb300.autotune import PlanTuner
-
+    srv = serving.PSFServer(max_batch=8, n_slots=args.slots, hbm_budget=150e9, k_max=36,
+                            limits=(1024, 512, 64),
+                            variant=None if tuner is not None else variant,
+                            tuner=tuner, timeout_s=120.0, graph_after=args.graph_after)
+    streams = [serving.poisson_stream(n_requests, rate, seed=SEED + 10 * i)
+               for i, rate in enumerate(rates)]
+    _, warm = serving.poisson_stream(max(n_requests // 4, 50), rates[0], seed=SEED + 1)
+    keys = sorted({r.key for _, reqs in streams for r in reqs} | {r.key for r in warm})
+    t0 = time.perf_counter()
+    resident = srv.prewarm(keys)
+    t_prewarm = time.perf_counter() - t0
+    srv.start()
+    serving.replay(srv, np.zeros(len(warm)), warm)      # warm-up: back to back
+    for r in warm:
+        r.result(120.0)
     out = {}
-    tuned = args.variant == "split_bf16" and not args.no_tune
-    main_leg = "autotuned" if tuned else args.variant
-    variants = [main_leg] + (["fp32"] if args.variant == "split_bf16" and
-                             not args.no_fp32_compare else [])
-    tuning = None
-    for variant in variants:
-        tuner = None
-        if variant == "autotuned":
-            # form and DFT operand per (N, M), timed once before the stream
-            tuner = PlanTuner()
-            grid, secs = tuner.tune_grid((128, 256, 512, 1024), (64, 128, 256, 512))
-            tuning = {"seconds": secs, "cache": tuner.cache_path,
-                      "choices": {f"{n}x{m}": f"{c['variant']}/op{c['operand_mode']}"
-                                  for (n, m), c in sorted(grid.items())}}
-        srv = serving.PSFServer(max_batch=8, n_slots=args.slots, hbm_budget=150e9, k_max=36,
-                                limits=(1024, 512, 64),
-                                variant=None if tuner is not None else variant,
-                                tuner=tuner, timeout_s=120.0, graph_after=args.graph_after)
-        times, reqs = serving.poisson_stream(args.requests, args.rate, seed=SEED)
-        _, warm = serving.poisson_stream(max(args.requests // 4, 50), args.rate, seed=SEED + 1)
-        keys = sorted({r.key for r in reqs} | {r.key for r in warm})
-        t0 = time.perf_counter()
-        resident = srv.prewarm(keys)
-        t_prewarm = time.perf_counter() - t0
-        srv.start()
-        serving.replay(srv, np.zeros(len(warm)), warm)      # warm-up: back to back
-        for r in warm:
-            r.result(120.0)
+    for rate, (times, reqs) in zip(rates, streams):
         srv.completed.clear()
+        srv.stats.clear()
+        srv.max_queue = 0
+        srv.ex.counts.clear()
         clocks = ClockSampler(torch.cuda.current_device())
         clocks.start()
         gc.collect()
@@ -518,13 +512,41 @@ def run_serving(args):
         finally:
             gc.enable()
         clk = clocks.stop()
-        srv.stop()
         rep = srv.report(reqs)
-        srv.close()
-        rep.update(variant=variant, buckets=len(keys), resident_buckets=resident,
+        rep.update(variant=variant if tuner is None else "autotuned", rate_hz=rate,
+                   requests=n_requests, buckets=len(keys), resident_buckets=resident,
                    prewarm_s=t_prewarm, clocks=clk)
-        out[variant] = rep
-    main_rep = out[main_leg]
+        out[rate] = rep
+    srv.stop()
+    srv.close()
+    return out
+
+
+def run_serving(args):
+    """Seeded Poisson streams of mixed-shape requests through dlux_gb300.serving.
+
+    N in {128, 256, 512, 1024}, M in {64, 128, 256, 512}, L uniform on 1..64 over
+    0.8-1.2 um, 4..36 Zernike coefficients from N(0, 50 nm), 30 % of requests ask for
+    the coefficient gradient of <G, PSF> with G ~ N(0, 1). Arrivals are Poisson at
+    each of --rates requests/s (default: --rate), one stream per rate. Plans of every
+    bucket in the streams are made resident first (within the 150 GB budget); a
+    warm-up stream of a different seed runs before the timed ones. Latency is
+    submit -> result on the host (pinned copies included).
+    """
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    out = {}
+    tuned = args.variant == "split_bf16" and not args.no_tune
+    main_leg = "autotuned" if tuned else args.variant
+    variants = [main_leg] + (["fp32"] if args.variant == "split_bf16" and
+                             not args.no_fp32_compare else [])
+    tuning = None
+    for variant in variants:
+        tuner = None
+        if variant == "autotuned":
+            tuner, tuning = _serving_tuner()
+        out[variant] = {f"{r:g}": rep for r, rep in
+                        serve_streams(args, variant, rates, args.requests, tuner).items()}
+    main_rep = out[main_leg][f"{rates[0]:g}"]
     line = {
         "metric": "served requests/sec (mixed PSF and PSF+grad stream)",
         "value": main_rep.get("throughput_rps"), "unit": "req/s", "n_gpus": 1,
@@ -534,9 +556,9 @@ def run_serving(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
         "data": "synthetic (seeded Poisson stream)",
-        "config": {"workload": f"serving: Poisson {args.rate:g} req/s, N in 128-1024, M in "
+        "config": {"workload": f"serving: Poisson {rates[0]:g} req/s, N in 128-1024, M in "
                                "64-512, L in 1..64, K in 4..36, 30% gradients",
-                   "requests": args.requests, "rate_hz": args.rate, "max_batch": 8,
+                   "requests": args.requests, "rates_hz": rates, "max_batch": 8,
                    "slots": args.slots, "graph_after": args.graph_after, "hbm_budget_gb": 150},
         "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
         "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
@@ -546,6 +568,20 @@ def run_serving(args):
     }
     print(json.dumps(line))
     return 0
+
+
+def serving_leg(args):
+    """The serving metric beside the headline line: a short stream (--serving-requests at
+    --rate) through the autotuned server and the FP32 server; throughput, p50/p99,
+    mean batch and CUDA-graph hit rate of each."""
+    keys = ("throughput_rps", "p50_ms", "p99_ms", "p99_ms_by_pupil", "mean_batch",
+            "graph_hit_rate", "completed", "failed")
+    tuner, _ = _serving_tuner()
+    out = {"rate_hz": args.rate, "requests": args.serving_requests}
+    for name, variant, t in (("split_bf16_autotuned", None, tuner), ("fp32", "fp32", None)):
+        rep = serve_streams(args, variant, [args.rate], args.serving_requests, t)[args.rate]
+        out[name] = {k: rep.get(k) for k in keys}
+    return out
 
 
 # ----------------------------------------------------------------------------
@@ -945,6 +981,10 @@ def main():
                     choices=["psf_grad", "serving", "cfg1", "cfg3", "cfg4", "fft", "ops"])
     ap.add_argument("--requests", type=int, default=4000, help="serving: timed requests")
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: arrivals per s")
+    ap.add_argument("--rates", default=None,
+                    help="serving: comma-separated arrival rates, one timed stream each")
+    ap.add_argument("--serving-requests", type=int, default=2000,
+                    help="requests of the serving leg of the default line (0: no leg)")
     ap.add_argument("--slots", type=int, default=6,
                     help="serving: concurrent stream slots (measured: 4 gives p99 2.1-4.2 ms "
                          "across runs, 6 gives 2.1-2.2 ms, 8 oversubscribes the 150 GB budget)")
@@ -1037,6 +1077,9 @@ def main():
                "kind": "port",
                "sample": f"{len(times)} whole steps after one warm-up: " + cs.sample()}
         parity = parity_sample(args.variant, 2)
+    serve = None
+    if rank == 0 and world == 1 and args.serving_requests > 0 and args.variant == "split_bf16":
+        serve = serving_leg(args)
 
     if rank == 0:
         line = {
@@ -1070,6 +1113,7 @@ def main():
             "clocks": clk,
             "fp32_form": fp32,
             "speedup_vs_fp32": (value / fp32["value"]) if fp32 else None,
+            "serving": serve,
         }
         print(json.dumps(line))
     if world > 1:

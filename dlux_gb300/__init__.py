@@ -12,7 +12,8 @@ from .base import Base  # noqa: F401
 from .coordinates import CoordSpec, PadSpec  # noqa: F401
 from .wavefronts import Wavefront  # noqa: F401
 from .psfs import PSF  # noqa: F401
-from .layers import CoordTransform, CircularAperture, AberratedAperture  # noqa: F401
+from .layers import (CoordTransform, CircularAperture, SquareAperture,  # noqa: F401
+                     RectangularAperture, RegPolyAperture, AberratedAperture)
 from .layers import (OpticalLayer, TransmissiveLayer, AberratedLayer, BasisLayer,  # noqa: F401
                      Tilt, Normalise, Optic, BasisOptic, MFT, FFT, DetectorLayer,
                      ApplyPixelResponse, Downsample, AddConstant, ApplySaturation,

@@ -91,11 +91,12 @@ class PolyObject(ctypes.Structure):
 
 
 class ApertureDesc(ctypes.Structure):
-    """dlx_aperture_desc: a dynamic circular aperture and its coordinate transformation."""
+    """dlx_aperture_desc: a dynamic aperture and its coordinate transformation."""
     _fields_ = [
         ("npixels", _c_int), ("pixel_scale", _c_dbl), ("translation", _c_dbl * 2),
         ("rotation", _c_dbl), ("compression", _c_dbl * 2), ("shear", _c_dbl * 2),
         ("radius", _c_dbl), ("softening", _c_dbl), ("occulting", _c_int),
+        ("shape", _c_int), ("width", _c_dbl), ("height", _c_dbl), ("nsides", _c_int),
     ]
 
 

@@ -147,12 +147,20 @@ struct ZernTable {                 // passed by value
   float norm[kMaxZern];
   float c[kMaxZern][kMaxZernCoeff];  // highest power of rho^2 first
 };
+constexpr int kMaxPolySides = 32;  // sides of a regular-polygon aperture
+enum ApertureShape { AP_CIRCLE = 0, AP_SQUARE = 1, AP_RECTANGLE = 2, AP_POLYGON = 3 };
 struct ZernAperture {
   int n;                  // pixels per side
   float pixel_scale;      // m
   float translation[2], shear[2], compression[2];
   float rot_c, rot_s;     // cos(-rotation), sin(-rotation)
-  float radius;           // m (also the Zernike normalisation extent)
+  int shape;              // ApertureShape
+  float radius;           // circle radius / polygon circumradius, m
+  float half_w, half_h;   // square and rectangle half widths, m
+  float extent;           // m: the Zernikes are evaluated at coordinates / extent
+  int nsides;             // 0: Zernikes; >= 3: polygon-stretched Zernikes with that many sides
+  int n_edges;            // polygon edges: signed distance a x + b y + c, the largest wins
+  float edge_a[kMaxPolySides], edge_b[kMaxPolySides], edge_c[kMaxPolySides];
   float clip;             // soft-edge half width, m
   int occulting;
 };

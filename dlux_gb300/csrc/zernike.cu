@@ -1,21 +1,31 @@
-// zernike.cu -- dynamic circular aperture with Zernike aberrations on the device
-// (AberratedAperture over a CircularAperture, layers/apertures.py:240-312 and
-// :643-800; DynamicZernike, polynomials.py:20-51; utils/zernikes.py:122-294;
-// soft edges utils/geometry.py:49-91, 229-255; CoordTransform
-// coordinates.py:240-320 with utils/coordinates.py:23-101).
+// zernike.cu -- dynamic apertures with Zernike aberrations on the device
+// (AberratedAperture over a Circular, Square, Rectangular or RegPoly aperture,
+// layers/apertures.py:240-555 and :643-800; DynamicZernike, polynomials.py:20-51;
+// utils/zernikes.py:122-419; soft edges and distances utils/geometry.py:49-91,
+// 229-351, 402-579; CoordTransform coordinates.py:240-320 with
+// utils/coordinates.py:23-101).
 //
 // Every pixel is evaluated from its coordinates, so no K x N x N basis is
 // stored or read:
 //   (x, y)  = pixel centre (i - (N-1)/2) * dx, transformed in dLux's order:
 //             translate, shear (with dLux's transposed-plane form), compress,
 //             rotate (clockwise by `rotation`)
-//   T       = soft circle: d = clip(radius - r, -c, c) (negated when
-//             occulting) rescaled by the global min/max of d to [0, 1]
-//   opd     = sum_j c_j Z_j(x / radius, y / radius), Z_j = [rho <= 1]
-//             norm_j R_nm(rho) {cos, sin}(|m| theta)
+//   T       = soft mask of the shape's distance d (circle: radius - r; square:
+//             w/2 - max(|x|, |y|); rectangle: -max(|x| - w/2, |y| - h/2);
+//             polygon: -max over its edges of the signed edge distance),
+//             clip(d, -c, c) (negated when occulting) rescaled by the global
+//             min/max of d to [0, 1]
+//   opd     = sum_j c_j Z_j at (x, y) / extent (radius, sqrt(2) w, hypot(h/2,
+//             w/2) or rmax), where Z_j = [rho <= 1] norm_j R_nm(rho) {cos,
+//             sin}(|m| theta) for a circle, and for an n-sided shape the
+//             polygon-stretched form (1 / r_a) Z_j((u, v) / r_a) with
+//             r_a = cos(pi / n) / cos(u_a), u_a the angle from the nearest
+//             edge normal (utils/zernikes.py:318-352).
 // The radial part is Horner in t = rho^2 times rho^|m|, and rho^|m| {cos,
-// sin}(|m| theta) is Re/Im of (u + i v)^|m|, so there is no atan2, pow or
-// trig call.
+// sin}(|m| theta) is Re/Im of (u + i v)^|m|, so only the polygon stretch
+// takes an angle.
+#include <math_constants.h>
+
 #include <atomic>
 #include <cmath>
 #include <string>
@@ -25,9 +35,11 @@
 namespace dlx {
 namespace {
 
-// d of one pixel after the coordinate transformation; also returns (u, v).
+// d of one pixel after the coordinate transformation; also returns the
+// Zernike coordinates (u, v) and the factor `zs` multiplying every Zernike
+// value there (1 for a circle; 1 / r_a for a polygon-stretched basis).
 __device__ __forceinline__ float aperture_point(const ZernAperture& a, int i, int j, float* u,
-                                                float* v) {
+                                                float* v, float* zs) {
   const float half = 0.5f * (float)(a.n - 1);
   const float x0 = ((float)i - half) * a.pixel_scale;
   const float y0 = ((float)j - half) * a.pixel_scale;
@@ -42,9 +54,34 @@ __device__ __forceinline__ float aperture_point(const ZernAperture& a, int i, in
   y = ys * a.compression[1];
   const float xr = a.rot_c * x + a.rot_s * y;   // cos(-r) x + sin(-r) y
   const float yr = -a.rot_s * x + a.rot_c * y;  // -sin(-r) x + cos(-r) y
-  *u = xr / a.radius;
-  *v = yr / a.radius;
-  float d = a.radius - sqrtf(xr * xr + yr * yr);
+  float uu = xr / a.extent, vv = yr / a.extent, scale = 1.0f;
+  if (a.nsides > 0) {
+    // polygon stretch: the wedge of the nearest edge and its radial factor
+    const float alpha = CUDART_PI_F / (float)a.nsides;
+    const float phi = atan2f(vv, uu) + alpha;
+    const float wedge = floorf((phi + alpha) / (2.0f * alpha));
+    const float ua = phi - wedge * (2.0f * alpha);
+    const float ra = cosf(alpha) / cosf(ua);
+    uu /= ra;
+    vv /= ra;
+    scale = 1.0f / ra;
+  }
+  *u = uu;
+  *v = vv;
+  *zs = scale;
+  float d;
+  if (a.shape == AP_SQUARE) {
+    d = a.half_w - fmaxf(fabsf(xr), fabsf(yr));
+  } else if (a.shape == AP_RECTANGLE) {
+    d = -fmaxf(fabsf(xr) - a.half_w, fabsf(yr) - a.half_h);
+  } else if (a.shape == AP_POLYGON) {
+    float e = -INFINITY;
+    for (int k = 0; k < a.n_edges; ++k)
+      e = fmaxf(e, fmaf(a.edge_a[k], xr, fmaf(a.edge_b[k], yr, a.edge_c[k])));
+    d = -e;
+  } else {
+    d = a.radius - sqrtf(xr * xr + yr * yr);
+  }
   if (a.occulting) d = -d;
   return fminf(fmaxf(d, -a.clip), a.clip);
 }
@@ -81,8 +118,8 @@ __global__ void aperture_minmax_kernel(ZernAperture a, unsigned* mm) {
   const long long npix = (long long)a.n * a.n;
   float lo = INFINITY, hi = -INFINITY;
   if (p < npix) {
-    float u, v;
-    const float d = aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v);
+    float u, v, zs;
+    const float d = aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v, &zs);
     lo = hi = d;
   }
 #pragma unroll
@@ -102,8 +139,8 @@ __global__ void aperture_eval_kernel(ZernAperture a, ZernTable z, const float* _
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long npix = (long long)a.n * a.n;
   if (p >= npix) return;
-  float u, v;
-  const float d = aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v);
+  float u, v, zs;
+  const float d = aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v, &zs);
   if (trans) {
     const float dmin = ordered2f(mm[0]), dmax = ordered2f(mm[1]);
     // soften(): constant support when every distance is equal, else (d - min) / (max - min)
@@ -112,7 +149,7 @@ __global__ void aperture_eval_kernel(ZernAperture a, ZernTable z, const float* _
   if (opd) {
     float acc = 0.0f;
     for (int j = 0; j < z.K; ++j) acc = fmaf(coeffs[j], zernike_at(z, j, u, v), acc);
-    opd[p] = acc;
+    opd[p] = acc * zs;
   }
 }
 
@@ -130,9 +167,9 @@ __global__ void zernike_grad_partial_kernel(ZernAperture a, ZernTable z, const f
 #pragma unroll
   for (int t = 0; t < kZernTermsPerBlock; ++t) sh[t] = sl[t] = 0.0f;
   for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-    float u, v;
-    aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v);
-    const float gp = g[p];
+    float u, v, zs;
+    aperture_point(a, (int)(p % a.n), (int)(p / a.n), &u, &v, &zs);
+    const float gp = g[p] * zs;
 #pragma unroll
     for (int t = 0; t < kZernTermsPerBlock; ++t) {
       if (j0 + t >= z.K) break;
@@ -172,7 +209,7 @@ __global__ void zernike_grad_finish_kernel(const double* __restrict__ partial, i
 
 int validate(const ZernAperture& a, const ZernTable& z) {
   if (a.n <= 0) return fail(DLX_ERR_SHAPE, "aperture: npixels must be positive");
-  if (!(a.radius > 0)) return fail(DLX_ERR_ARG, "aperture: radius must be positive");
+  if (!(a.extent > 0)) return fail(DLX_ERR_ARG, "aperture: its size must be positive");
   if (!(a.clip > 0)) return fail(DLX_ERR_ARG, "softening must be greater than 0.");
   if (z.K < 0 || z.K > kMaxZern) return fail(DLX_ERR_ARG, "aperture: too many Zernike terms");
   for (int j = 0; j < z.K; ++j)
@@ -274,7 +311,70 @@ int build_aperture(const dlx_aperture_desc* d, ZernAperture* a) {
   }
   a->rot_c = (float)std::cos(-d->rotation);
   a->rot_s = (float)std::sin(-d->rotation);
+  a->shape = d->shape;
   a->radius = (float)d->radius;
+  a->half_w = (float)(0.5 * d->width);
+  a->half_h = (float)(0.5 * d->height);
+  switch (d->shape) {
+    case AP_CIRCLE:
+      if (!(d->radius > 0)) return fail(DLX_ERR_ARG, "aperture: radius must be positive");
+      a->extent = (float)d->radius;
+      a->nsides = 0;
+      break;
+    case AP_SQUARE:
+      if (!(d->width > 0)) return fail(DLX_ERR_ARG, "aperture: width must be positive");
+      a->extent = (float)(std::sqrt(2.0) * d->width);
+      a->nsides = 4;
+      break;
+    case AP_RECTANGLE:
+      if (!(d->width > 0) || !(d->height > 0))
+        return fail(DLX_ERR_ARG, "aperture: width and height must be positive");
+      a->extent = (float)std::hypot(0.5 * d->height, 0.5 * d->width);
+      a->nsides = 4;
+      break;
+    case AP_POLYGON: {
+      const int n = d->nsides;
+      if (n < 3 || n > kMaxPolySides)
+        return fail(DLX_ERR_ARG, "aperture: a regular polygon needs 3 to " +
+                                     std::to_string(kMaxPolySides) + " sides");
+      if (!(d->radius > 0)) return fail(DLX_ERR_ARG, "aperture: rmax must be positive");
+      a->extent = (float)d->radius;
+      a->nsides = n;
+      a->n_edges = n;
+      // Edges from vertex i to i + 1, vertices at angles linspace(-pi, pi, n,
+      // endpoint=False) (utils/geometry.py:519-552). Signed distance of edge
+      // i as a x + b y + c (utils/geometry.py:486-516): horizontal (slope 0),
+      // vertical (run exactly 0: slope inf) or general, with the sign that
+      // makes the inside negative.
+      const double pi = 3.14159265358979323846;
+      for (int i = 0; i < n; ++i) {
+        const int k = (i + 1) % n;
+        const double ti = -pi + 2.0 * pi * i / n, tk = -pi + 2.0 * pi * k / n;
+        const double xi = d->radius * std::cos(ti), yi = d->radius * std::sin(ti);
+        const double xk = d->radius * std::cos(tk), yk = d->radius * std::sin(tk);
+        const double dx = xk - xi, dy = yk - yi;
+        auto sign = [](double v) { return v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); };
+        double ea, eb, ec;
+        if (dx == 0) {                     // vertical: -sgn (x_i - x)
+          const double sg = sign(xi);
+          ea = sg; eb = 0.0; ec = -sg * xi;
+        } else if (dy / dx == 0) {         // horizontal: -sgn (y_i - y)
+          const double sg = sign(yi);
+          ea = 0.0; eb = sg; ec = -sg * yi;
+        } else {                           // -sgn (m x - y + y_i - m x_i) / sqrt(m^2 + 1)
+          const double m = dy / dx;
+          const double sg = sign(yi - m * xi), s = std::sqrt(m * m + 1.0);
+          ea = -sg * m / s; eb = sg / s; ec = -sg * (yi - m * xi) / s;
+        }
+        a->edge_a[i] = (float)ea;
+        a->edge_b[i] = (float)eb;
+        a->edge_c[i] = (float)ec;
+      }
+      break;
+    }
+    default:
+      return fail(DLX_ERR_ARG, "aperture: unknown shape " + std::to_string(d->shape));
+  }
   if (!(d->softening > 0)) return fail(DLX_ERR_ARG, "softening must be greater than 0.");
   a->clip = (float)(d->pixel_scale * d->softening / 2.0);
   a->occulting = d->occulting ? 1 : 0;

@@ -519,10 +519,18 @@ class ScenePlan(_Plan):
         return g_pos, g_w
 
 
+APERTURE_SHAPES = {"circle": 0, "square": 1, "rectangle": 2, "polygon": 3}
+
+
 def aperture_desc(npixels, pixel_scale, radius, softening=1.0, occulting=False,
-                  translation=None, rotation=None, compression=None, shear=None):
-    """dlx_aperture_desc of a dynamic circular aperture under a CoordTransform."""
+                  translation=None, rotation=None, compression=None, shear=None,
+                  shape="circle", width=0.0, height=0.0, nsides=0):
+    """dlx_aperture_desc of a dynamic aperture under a CoordTransform: a circle of
+    `radius`, a square of side `width`, a `width` x `height` rectangle, or a regular
+    polygon of `nsides` with circumradius `radius`."""
     d = _lib.ApertureDesc()
+    d.shape = APERTURE_SHAPES[shape]
+    d.width, d.height, d.nsides = float(width), float(height), int(nsides)
     d.npixels = int(npixels)
     d.pixel_scale = float(pixel_scale)
     t = (0.0, 0.0) if translation is None else tuple(float(v) for v in translation)

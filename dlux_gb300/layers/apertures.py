@@ -1,18 +1,19 @@
 """Dynamic apertures evaluated on the device (layers/apertures.py of dLux).
 
-``CircularAperture`` is a soft-edged disk under an optional ``CoordTransform``
-(layers/apertures.py:240-312, utils/geometry.py:49-91 and :229-255).
-``AberratedAperture`` adds Zernike aberrations defined on that aperture
-(layers/apertures.py:643-800; polynomials.py:20-51). Both are computed per
-pixel by ``dlx_aberrated_aperture``, with no stored basis. The OPD is
-differentiable with respect to the coefficients; the aperture geometry is a
-constant here.
-
-Only circular apertures are implemented. dLux's polygonal apertures use
-polygon-orthogonalised Zernikes (``polike``).
+``CircularAperture``, ``SquareAperture``, ``RectangularAperture`` and
+``RegPolyAperture`` are soft-edged masks under an optional ``CoordTransform``
+(layers/apertures.py:240-555, utils/geometry.py:49-91, 229-351 and 402-579).
+``AberratedAperture`` adds Zernike aberrations defined on any of them
+(layers/apertures.py:643-800; polynomials.py:20-51): Zernikes for a circle,
+polygon-stretched Zernikes (utils/zernikes.py:318-419) with the shape's side
+count otherwise. Both are computed per pixel by ``dlx_aberrated_aperture``,
+with no stored basis. The OPD is differentiable with respect to the
+coefficients; the aperture geometry is a constant here.
 """
 
 from __future__ import annotations
+
+import math
 
 import numpy as np
 import torch
@@ -21,7 +22,8 @@ from .. import autograd, kernels
 from ..base import Base
 from .optical_layers import OpticalLayer
 
-__all__ = ["CoordTransform", "CircularAperture", "AberratedAperture"]
+__all__ = ["CoordTransform", "CircularAperture", "SquareAperture", "RectangularAperture",
+           "RegPolyAperture", "AberratedAperture"]
 
 
 class CoordTransform(Base):
@@ -43,38 +45,31 @@ class CoordTransform(Base):
         self.rotation = None if rotation is None else float(rotation)
 
 
-class CircularAperture(OpticalLayer):
-    """Soft-edged circle of ``radius`` (m) (layers/apertures.py:240-312)."""
+class DynamicAperture(OpticalLayer):
+    """Soft-edged aperture under a CoordTransform (layers/apertures.py:155-237)."""
 
-    def __init__(self, radius, transformation=None, occulting=False, softening=1.0,
-                 normalise=False):
+    def __init__(self, transformation=None, occulting=False, softening=1.0, normalise=False):
         if transformation is not None and not isinstance(transformation, CoordTransform):
             raise TypeError("transformation must be a BaseCoordTransform instance, got "
                             f"{type(transformation).__name__}.")
         if float(softening) <= 0:
             raise ValueError("softening must be greater than 0.")
-        self.radius = float(radius)
         self.transformation = transformation
         self.occulting = bool(occulting)
         self.softness = float(softening)
         self.normalise = bool(normalise)
 
-    @property
-    def extent(self):
-        return self.radius
-
-    @property
-    def nsides(self):
-        return 0
+    def _shape(self):  # pragma: no cover - abstract
+        raise NotImplementedError
 
     def desc(self, npixels, pixel_scale):
         t = self.transformation
-        return kernels.aperture_desc(npixels, pixel_scale, self.radius, self.softness,
-                                     self.occulting,
-                                     None if t is None else t.translation,
-                                     None if t is None else t.rotation,
-                                     None if t is None else t.compression,
-                                     None if t is None else t.shear)
+        return kernels.aperture_desc(npixels, pixel_scale, softening=self.softness,
+                                     occulting=self.occulting,
+                                     translation=None if t is None else t.translation,
+                                     rotation=None if t is None else t.rotation,
+                                     compression=None if t is None else t.compression,
+                                     shear=None if t is None else t.shear, **self._shape())
 
     def transmission(self, npixels, pixel_scale):
         trans, _ = kernels.aberrated_aperture(self.desc(npixels, pixel_scale), [], None,
@@ -93,13 +88,97 @@ class CircularAperture(OpticalLayer):
             acc.normalise()
 
 
+class CircularAperture(DynamicAperture):
+    """Soft-edged circle of ``radius`` (m) (layers/apertures.py:240-312)."""
+
+    def __init__(self, radius, transformation=None, occulting=False, softening=1.0,
+                 normalise=False):
+        super().__init__(transformation, occulting, softening, normalise)
+        self.radius = float(radius)
+
+    def _shape(self):
+        return dict(shape="circle", radius=self.radius)
+
+    @property
+    def extent(self):
+        return self.radius
+
+    @property
+    def nsides(self):
+        return 0
+
+
+class SquareAperture(DynamicAperture):
+    """Soft-edged square of side ``width`` (m) (layers/apertures.py:315-388)."""
+
+    def __init__(self, width, transformation=None, occulting=False, softening=1.0,
+                 normalise=False):
+        super().__init__(transformation, occulting, softening, normalise)
+        self.width = float(width)
+
+    def _shape(self):
+        return dict(shape="square", radius=0.0, width=self.width)
+
+    @property
+    def extent(self):
+        return math.sqrt(2) * self.width
+
+    @property
+    def nsides(self):
+        return 4
+
+
+class RectangularAperture(DynamicAperture):
+    """Soft-edged ``width`` (x) by ``height`` (y) rectangle (layers/apertures.py:391-472)."""
+
+    def __init__(self, height, width, transformation=None, occulting=False, softening=1.0,
+                 normalise=False):
+        self.height = float(height)
+        self.width = float(width)
+        super().__init__(transformation, occulting, softening, normalise)
+
+    def _shape(self):
+        return dict(shape="rectangle", radius=0.0, width=self.width, height=self.height)
+
+    @property
+    def extent(self):
+        return math.hypot(self.height / 2.0, self.width / 2.0)
+
+    @property
+    def nsides(self):
+        return 4
+
+
+class RegPolyAperture(DynamicAperture):
+    """Soft-edged regular polygon of ``nsides`` and circumradius ``rmax``
+    (layers/apertures.py:475-555)."""
+
+    def __init__(self, nsides, rmax, transformation=None, occulting=False, softening=1.0,
+                 normalise=False):
+        super().__init__(transformation, occulting, softening, normalise)
+        self._nsides = int(nsides)
+        self.rmax = float(rmax)
+
+    def _shape(self):
+        return dict(shape="polygon", radius=self.rmax, nsides=self._nsides)
+
+    @property
+    def extent(self):
+        return self.rmax
+
+    @property
+    def nsides(self):
+        return self._nsides
+
+
 class AberratedAperture(OpticalLayer):
     """Zernike aberrations on a dynamic aperture (layers/apertures.py:643-800)."""
 
     def __init__(self, aperture, noll_inds, coefficients=None, effect="opd"):
-        if not isinstance(aperture, CircularAperture):
+        if not isinstance(aperture, DynamicAperture):
             raise TypeError("AberratedApertures cannot contain Static, Compound or Multi "
-                            "Apertures (only circular dynamic apertures are supported here).")
+                            "Apertures. AberratedApertures can be placed in Compound or Multi "
+                            "Apertures, which can then be promoted to Static.")
         if effect not in ("opd", "phase", "amplitude"):
             raise ValueError("effect must be 'opd', 'phase', or 'amplitude'.")
         if aperture.occulting:

@@ -30,8 +30,13 @@ Execution (``CudaExecutor``):
   pinned staging buffers.
 - A batch is one ``dlx_serve_run`` call: H2D copies, Zernike OPDs, fused
   PSF, reverse pass, coefficient gradient, D2H copies.
-- After ``graph_after`` launches of the same (slot, bucket, R, n_grad), that
-  call is captured as a CUDA graph and replayed from then on.
+- With graphs on, a batch of R requests (n_grad of them with gradients) is
+  padded to R' = the next power of two and n_grad to the next power of two
+  (at most R'), with zero-weight, zero-cotangent filler objects whose results
+  are dropped. After ``graph_after`` launches of the same (slot, bucket, R',
+  n_grad'), that call is captured as a CUDA graph and replayed from then on.
+  Each bucket has a home slot (a hash of its shape), used whenever it is
+  free, so that a bucket's graphs are found again.
 - A request's numbers are bit-for-bit the same alone and inside any batch.
   The kernels give each object identical arithmetic and fixed-order
   reductions.
@@ -325,9 +330,11 @@ class PSFServer:
     def _dispatch(self):
         launched = False
         skip = set()
-        for si, busy in enumerate(self.slots):
-            if busy is not None:
-                continue
+        while True:
+            free = [i for i, busy in enumerate(self.slots) if busy is None]
+            if not free:
+                return launched
+            si = free[0]
             while True:
                 key = self._oldest_bucket(skip)
                 if key is None:
@@ -335,6 +342,9 @@ class PSFServer:
                 if self._admit(key):
                     break
                 skip.add(key)        # memory is held by running batches: try another bucket
+            home = self.ex.home_slot(key)
+            if home in free:
+                si = home
             dq = self.pending[key]
             reqs = []
             while dq and len(reqs) < self.max_batch:
@@ -364,7 +374,6 @@ class PSFServer:
             self.stats["batches"] += 1
             self.stats["launched"] += len(reqs)
             launched = True
-        return launched
 
     def _retire(self):
         done_any = False
@@ -476,7 +485,7 @@ class CudaExecutor:
     def __init__(self, max_batch=8, k_max=36, limits=(1024, 512, 64), n_slots=4,
                  diameter=1.0, psf_pixel_scale=0.02, band=DEFAULT_BAND, variant=None,
                  operand_mode=0, graphs=True, graph_after=2, max_graphs=512, device=None,
-                 tuner=None):
+                 tuner=None, pad_batches=None):
         _lib.require_cuda()
         self.device = torch.device(device) if device is not None else \
             torch.device("cuda", torch.cuda.current_device())
@@ -490,6 +499,8 @@ class CudaExecutor:
         # per-(n, m) form and DFT operand from the autotuner, when no form is forced
         self.tuner = tuner if variant is None else None
         self.graphs_on = bool(graphs)
+        # pad batches to power-of-two shapes (the captured graphs' shapes); on with graphs
+        self.pad_batches = self.graphs_on if pad_batches is None else bool(pad_batches)
         self.graph_after = int(graph_after)
         self.max_graphs = int(max_graphs)
         N, M, L = self.limits
@@ -573,6 +584,25 @@ class CudaExecutor:
         plan.close()
 
     # ---- batches ----
+    def home_slot(self, key):
+        """The slot a bucket prefers (a fixed hash of its shape)."""
+        n, m, L = key
+        return (n * 7919 + m * 104729 + L * 1299709) % self.n_slots
+
+    def padded_shape(self, R, G):
+        """(R', G') of a batch of R requests, G of them with gradients."""
+        if not self.pad_batches:
+            return R, G
+
+        def up(v):
+            p = 1
+            while p < v:
+                p *= 2
+            return p
+        Rp = min(up(R), self.max_batch)
+        Gp = 0 if G == 0 else min(up(G), Rp)
+        return Rp, Gp
+
     def _batch_struct(self, slot, key, R, G):
         n, m, L = key
         amp, basis, scale = self.models[n]
@@ -589,21 +619,27 @@ class CudaExecutor:
         return b
 
     def launch(self, si, key, plan, reqs):
+        """Enqueue a batch on slot si; reqs hold the gradient requests first."""
         slot = self.slots[si]
         n, m, L = key
-        R = len(reqs)
-        G = sum(1 for r in reqs if r.want_grad)
+        G_req = sum(1 for r in reqs if r.want_grad)
+        R, G = self.padded_shape(len(reqs), G_req)
         K = self.k_max
         c = slot.coeffs[:R * K].reshape(R, K)
         c[:] = 0.0
         w = slot.weights[:R * L].reshape(R, L)
+        w[:] = 0.0              # filler objects: zero weights, so a zero field
         for i, r in enumerate(reqs):
             c[i, :r.coefficients.size] = r.coefficients
             w[i] = r.weights
         if G:
             g = slot.gpsf[:G * m * m].reshape(G, m, m)
             for i in range(G):
-                g[i] = reqs[i].g_psf
+                if i < G_req:
+                    g[i] = reqs[i].g_psf
+                else:           # a forward-only request or a filler in the gradient group
+                    g[i] = 0.0
+        self.counts["padded_objects"] += R - len(reqs)
         gk = (si, key, R, G)
         stream = slot.stream
         graph = self.graphs.get(gk)
@@ -633,7 +669,7 @@ class CudaExecutor:
                     _lib.call("dlx_serve_run", plan.handle, ctypes.byref(b), stream.cuda_stream)
                     self.counts["direct_launches"] += 1
             slot.event.record(stream)
-        slot.current = (key, R, G)
+        slot.current = (key, R, G_req)
 
     def poll(self, si):
         return self.slots[si].event.query()
@@ -653,9 +689,11 @@ class CudaExecutor:
         torch.cuda.synchronize(self.device)
 
     def stats(self):
-        total = self.counts["graph_replays"] + self.counts["direct_launches"]
+        total = self.counts["graph_replays"] + self.counts["direct_launches"] + \
+            self.counts["graph_captures"]
         return {"graph_hit_rate": self.counts["graph_replays"] / max(total, 1),
-                "graphs": len(self.graphs), "graph_captures": self.counts["graph_captures"]}
+                "graphs": len(self.graphs), "graph_captures": self.counts["graph_captures"],
+                "padded_objects": self.counts["padded_objects"]}
 
     def close(self):
         self.synchronize()

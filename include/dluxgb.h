@@ -430,11 +430,15 @@ int dlx_asm_plan_destroy(dlx_asm_plan plan);
 int dlx_asm_forward(dlx_asm_plan plan, const void* in_c64, void* out_c64, void* stream);
 int dlx_asm_adjoint(dlx_asm_plan plan, const void* gout_c64, void* gin_c64, void* stream);
 
-/* ---- a12: dynamic aberrated circular aperture ----------------------------
- * Replaces AberratedAperture over a CircularAperture (layers/apertures.py:
- * 240-312, 643-800): the soft-edged transmission (utils/geometry.py:49-91,
- * 229-255) and OPD = sum_j coeffs[j] Z_noll[j] (polynomials.py:20-51,
- * utils/zernikes.py:122-294) evaluated per pixel on the device after dLux's
+/* ---- a12: dynamic aberrated apertures --------------------------------------
+ * Replaces AberratedAperture over a CircularAperture, SquareAperture,
+ * RectangularAperture or RegPolyAperture (layers/apertures.py:240-555,
+ * 643-800): the soft-edged transmission (utils/geometry.py:49-91, 229-351,
+ * 402-579) and OPD = sum_j coeffs[j] Z_noll[j] (polynomials.py:20-51,
+ * utils/zernikes.py:122-294) at the coordinates divided by the aperture's
+ * extent -- for the polygonal shapes the polygon-stretched Zernikes of
+ * utils/zernikes.py:318-419 with the shape's side count (4 for squares and
+ * rectangles) -- evaluated per pixel on the device after dLux's
  * CoordTransform (coordinates.py:240-320: translate, shear, compress,
  * rotate). No basis array is read or stored. Up to 64 terms, radial order
  * <= 16 (both outputs may be NULL). dlx_aberrated_aperture_grad returns
@@ -442,6 +446,10 @@ int dlx_asm_adjoint(dlx_asm_plan plan, const void* gout_c64, void* gin_c64, void
  * Noll index and its radial coefficients (9 per term, highest power of
  * rho^2 first).
  */
+#define DLX_APERTURE_CIRCLE 0    /* radius */
+#define DLX_APERTURE_SQUARE 1    /* width */
+#define DLX_APERTURE_RECTANGLE 2 /* width (x) and height (y) */
+#define DLX_APERTURE_POLYGON 3   /* nsides (3..32) and radius = rmax */
 typedef struct {
   int npixels;             /* wavefront side N */
   double pixel_scale;      /* m per pixel */
@@ -449,9 +457,13 @@ typedef struct {
   double rotation;         /* rad, clockwise */
   double compression[2];
   double shear[2];
-  double radius;           /* m; also the extent the Zernikes are normalised to */
+  double radius;           /* m: circle radius, or polygon circumradius (rmax) */
   double softening;        /* soft edge width in pixels (> 0) */
   int occulting;
+  int shape;               /* DLX_APERTURE_* */
+  double width;            /* m: square side, rectangle x side */
+  double height;           /* m: rectangle y side */
+  int nsides;              /* regular polygon sides */
 } dlx_aperture_desc;
 int dlx_zernike_table(const int* noll, int n_terms, int* n_out, int* m_out, float* coeffs_out);
 int dlx_aberrated_aperture(const dlx_aperture_desc* desc, const int* noll_host, int n_terms,

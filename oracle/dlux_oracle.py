@@ -491,6 +491,100 @@ def aberrated_circular_aperture(npixels, diameter, radius, noll, coefficients,
     return trans, opd, basis
 
 
+def square_distance(coords, width):
+    """utils/geometry.py:421-437."""
+    return np.max(np.abs(coords), axis=0) - width / 2
+
+
+def rectangle_distance(coords, width, height):
+    """utils/geometry.py:440-460."""
+    return np.maximum(np.abs(coords[0]) - width / 2, np.abs(coords[1]) - height / 2)
+
+
+def reg_polygon_edges(n, radius):
+    """Slope and a point of each edge of a regular polygon (utils/geometry.py:519-552):
+    vertices at angles linspace(-pi, pi, n, endpoint=False); a vertical edge's slope is
+    the fill value inf of utils/math.py nandiv."""
+    ang = np.linspace(-np.pi, np.pi, n, endpoint=False)
+    x, y = radius * np.cos(ang), radius * np.sin(ang)
+    j = np.roll(np.arange(n), -1)
+    dx, dy = x[j] - x, y[j] - y
+    m = np.where(dx == 0, np.inf, dy / np.where(dx == 0, 1.0, dx))
+    return m, np.stack([x, y], 1)
+
+
+def line_distance(coords, m, xy):
+    """Signed distance from an edge line (utils/geometry.py:486-516)."""
+    x, y = coords
+    if m == 0:
+        sgn, dist = np.sign(xy[1]), xy[1] - y
+    elif m == np.inf:
+        sgn, dist = np.sign(xy[0]), xy[0] - x
+    else:
+        sgn = np.sign(xy[1] - m * xy[0])
+        dist = (m * x - y + xy[1] - m * xy[0]) / np.sqrt(m ** 2 + 1)
+    return -sgn * dist
+
+
+def reg_polygon_distance(coords, nsides, radius):
+    """utils/geometry.py:560-579: the largest edge distance."""
+    m, xy = reg_polygon_edges(nsides, radius)
+    return np.max([line_distance(coords, mi, p) for mi, p in zip(m, xy)], axis=0)
+
+
+def polike(nsides, j, coordinates, diameter=2.0):
+    """Zernike j stretched onto a regular nsides-gon (utils/zernikes.py:318-352):
+    in the angular wedge of each edge, radii are scaled by r_alpha = cos(alpha) /
+    cos(u_alpha) and the value by 1 / r_alpha."""
+    if nsides < 3:
+        raise ValueError(f"nsides must be >= 3, not {nsides}.")
+    c = np.asarray(coordinates, np.float64) / (diameter / 2)
+    theta = np.arctan2(c[1], c[0])
+    alpha = np.pi / nsides
+    phi = theta + alpha
+    wedge = np.floor((phi + alpha) / (2.0 * alpha))
+    u_alpha = phi - wedge * (2 * alpha)
+    r_alpha = np.cos(alpha) / np.cos(u_alpha)
+    return 1 / r_alpha * zernike(j, c / r_alpha, 2.0)
+
+
+def aberrated_aperture(shape, npixels, diameter, noll, coefficients, transformation=None,
+                       softening=1.0, occulting=False):
+    """AberratedAperture over a dynamic aperture of any shape on a wavefront of
+    ``npixels`` over ``diameter``: (transmission, opd, basis).
+
+    ``shape`` is ("circle", radius), ("square", width), ("rectangle", width, height) or
+    ("polygon", nsides, rmax) (layers/apertures.py:240-555). The transmission is the
+    shape's soft mask with clip = pixel_scale * softening / 2 (utils/geometry.py:229-351);
+    the OPD evaluates the dynamic Zernikes at the transformed coordinates divided by the
+    aperture's extent -- radius, sqrt(2) width, hypot(h / 2, w / 2) or rmax -- as Zernikes
+    (circle) or polygon-stretched Zernikes with the aperture's side count (4 for squares
+    and rectangles) (layers/apertures.py:754-771, polynomials.py:20-51).
+    """
+    coords = pixel_coords(npixels, diameter)
+    pixel_scale = diameter / npixels
+    t = transformation or {}
+    c = coord_transform(coords, **t)
+    kind = shape[0]
+    if kind == "circle":
+        dist, extent, nsides = np.hypot(c[0], c[1]) - shape[1], shape[1], 0
+    elif kind == "square":
+        dist, extent, nsides = square_distance(c, shape[1]), np.sqrt(2) * shape[1], 4
+    elif kind == "rectangle":
+        dist = rectangle_distance(c, shape[1], shape[2])
+        extent, nsides = np.hypot(shape[2] / 2.0, shape[1] / 2.0), 4
+    elif kind == "polygon":
+        dist, extent, nsides = reg_polygon_distance(c, shape[1], shape[2]), shape[2], shape[1]
+    else:
+        raise ValueError(f"unknown aperture shape {kind!r}")
+    trans = soften(-dist, pixel_scale * softening / 2, occulting)
+    cz = c / extent
+    basis = np.array([zernike(j, cz, 2.0) if nsides == 0 else polike(nsides, j, cz, 2.0)
+                      for j in noll])
+    opd = np.tensordot(basis, np.asarray(coefficients, np.float64), axes=(0, 0))
+    return trans, opd, basis
+
+
 def convolve_same(array, kernel):
     """jax.scipy.signal.convolve(array, kernel, mode="same") (psfs.py:93-110; sources.py:516,
     :745): the full 2-d convolution, cropped at offset (K - 1) // 2 per axis."""

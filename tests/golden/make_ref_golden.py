@@ -29,7 +29,12 @@ saves its outputs on the seeded inputs of ref_inputs.py:
                  (layers/optical_layers.py:189-371), CartesianOpticalSystem
                  (optical_systems.py:683-775), a LayeredOpticalSystem with an MFT
                  layer, and Wavefront.normalise "power"/"peak"
-                 (wavefronts.py:397-424): PSFs, losses and gradients.
+                 (wavefronts.py:397-424): PSFs, losses and gradients;
+  ref_apertures.npz AberratedAperture over Circular, Square, Rectangular and
+                 RegPoly apertures (layers/apertures.py:240-800) under a
+                 CoordTransform: transmission, OPD (polygon-stretched Zernikes,
+                 utils/zernikes.py:318-419, for the polygons) and a system PSF
+                 with its coefficient gradient.
 
 dLux's gradients come from JAX autodiff, which cannot run here, so every
 gradient is taken by fourth-order central differences of dLux's own forward in
@@ -342,13 +347,48 @@ def make_layers(dl, O):
     return out
 
 
+def make_apertures(dl, O):
+    """AberratedAperture over each dynamic aperture shape, through dLux's own classes:
+    transmission and OPD on a transformed grid, and a system PSF with its coefficient
+    gradient."""
+    inp = RI.apertures()
+    L = dl.layers
+    out = {}
+    wf = dl.wavefronts.Wavefront(1e-6, 128, diameter=1.0)
+    coords, ps = wf.coordinates(), wf.pixel_scale
+    for name, cls, args, oshape in RI.APERTURE_SHAPES:
+        def make(c):
+            tf = dl.coordinates.CoordTransform(**{k: np.asarray(v, float) if k != "rotation"
+                                                  else v for k, v in
+                                                  RI.APERTURE_TRANSFORM.items()})
+            ap = getattr(L, cls)(*args, transformation=tf, softening=1.5)
+            return L.AberratedAperture(ap, RI.APERTURE_NOLLS, J(np.array(c, float)))
+        ab = make(inp["coeffs"])
+        trans = ab.transmission(coords, ps)
+        opd = ab.eval_basis(coords)
+        ot, oo, _ = O.aberrated_aperture(oshape, 128, 1.0, RI.APERTURE_NOLLS, inp["coeffs"],
+                                         RI.APERTURE_TRANSFORM, 1.5)
+        print(f"aperture {name}: transmission oracle vs dLux {rel(ot, trans):.2e}, "
+              f"OPD {rel(oo, opd):.2e}")
+        out[f"{name}_trans"] = trans.astype(np.float32)
+        out[f"{name}_opd"] = opd.astype(np.float32)
+
+        def psf_of(c):
+            return dl.optical_systems.AngularOpticalSystem(
+                128, 1.0, [make(c)], 64, 0.03, 1).propagate(inp["wavelengths"])
+        out[f"{name}_psf"] = psf_of(inp["coeffs"])
+        out[f"{name}_grad"] = fd4_grad(lambda c: float((psf_of(c) * inp["R"]).sum()),
+                                       inp["coeffs"], 2e-10)
+    return out
+
+
 def main():
     src = sys.argv[1]
-    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4", "layers"]
+    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4", "layers", "apertures"]
     dl = ref_standin.load_dlux(src)
     from oracle import dlux_oracle as O
     makers = {"utils": make_utils, "cfg1": make_cfg1, "cfg2": make_cfg2, "cfg3": make_cfg3,
-              "cfg4": make_cfg4, "layers": make_layers}
+              "cfg4": make_cfg4, "layers": make_layers, "apertures": make_apertures}
     for name in which:
         t0 = time.time()
         data = makers[name](dl, O)

@@ -126,3 +126,26 @@ def layers():
             "tilt": np.array([0.03, -0.02]) * ARCSEC,
             "dir_opd": 1e-8 * normal(rng, (64, 64)), "dir_phase": normal(rng, (64, 64)),
             "dir_amp": normal(rng, (64, 64))}
+
+
+# Dynamic aperture shapes: (name, class name, positional arguments) of dLux's
+# layers/apertures.py, all under APERTURE_TRANSFORM, softening 1.5 pixels,
+# aberrated by Noll 4-14 (APERTURE_NOLLS) on a 128^2 grid over 1 m.
+APERTURE_SHAPES = [
+    ("circle", "CircularAperture", (0.42,), ("circle", 0.42)),
+    ("square", "SquareAperture", (0.6,), ("square", 0.6)),
+    ("rectangle", "RectangularAperture", (0.5, 0.7), ("rectangle", 0.7, 0.5)),
+    ("hexagon", "RegPolyAperture", (6, 0.45), ("polygon", 6, 0.45)),
+    ("pentagon", "RegPolyAperture", (5, 0.44), ("polygon", 5, 0.44)),
+]
+APERTURE_TRANSFORM = dict(translation=(0.02, -0.015), rotation=0.3, compression=(1.05, 0.97),
+                          shear=(0.03, -0.02))
+APERTURE_NOLLS = list(range(4, 15))
+
+
+def apertures():
+    """Coefficients (N(0, 40 nm)), cotangent image and wavelengths of the aperture fixtures:
+    the aberrated aperture alone on 128^2 pixels, and in a system to a 64^2 PSF at 0.03"."""
+    rng = np.random.default_rng(106)
+    return {"coeffs": 40e-9 * normal(rng, len(APERTURE_NOLLS)), "R": normal(rng, (64, 64)),
+            "wavelengths": np.array([0.9e-6, 1.1e-6])}

@@ -2,7 +2,7 @@
 
 Transmission and OPD: relative L2 <= 1e-5 (FP32 evaluation of FP64 restatements).
 Coefficient gradient: relative L2 <= 1e-5. Through an optical system: PSF <= 1e-5,
-coefficient gradient <= 1e-4 against the oracle's analytic reverse pass.
+coefficient gradient <= 1e-5 against the oracle's analytic reverse pass.
 """
 
 import numpy as np
@@ -65,7 +65,7 @@ def test_aberrated_aperture_in_a_system(cuda):
     g_ref = np.tensordot(basis, g_opd, axes=((1, 2), (0, 1)))
     e_psf, e_g = rel(psf.detach().cpu(), ref), rel(c.grad.cpu(), g_ref)
     print(f"system with AberratedAperture: psf {e_psf:.2e}, coefficient grad {e_g:.2e}")
-    assert e_psf < 1e-5 and e_g < 1e-4
+    assert e_psf < 1e-5 and e_g < 1e-5
     # the layer-by-layer path (no fusion) gives the same image
     wf_psf = optics.propagate(wls, return_wf=True)
     assert wf_psf is not None

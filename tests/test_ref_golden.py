@@ -144,3 +144,14 @@ def test_oracle_cfg2_image_and_gradient_match_dlux():
     g = O.poly_psf_grad(Teff, opd, wls, w, 1.0, 512, ps, np.kron(inp["R"], np.ones((4, 4))))
     gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
     assert rel(gc, r["grad"]) < 1e-7
+
+
+@pytest.mark.parametrize("case", RI.APERTURE_SHAPES, ids=[c[0] for c in RI.APERTURE_SHAPES])
+def test_oracle_aperture_shapes_match_dlux(case):
+    r = _load("apertures")
+    name, _, _, oshape = case
+    inp = RI.apertures()
+    trans, opd, _ = O.aberrated_aperture(oshape, 128, 1.0, RI.APERTURE_NOLLS, inp["coeffs"],
+                                         RI.APERTURE_TRANSFORM, 1.5)
+    assert rel(trans, r[f"{name}_trans"]) < 1e-6
+    assert rel(opd, r[f"{name}_opd"]) < 1e-6

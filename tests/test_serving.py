@@ -59,6 +59,9 @@ class FakeExecutor:
         plan.closed = True
         self.closed_plans.append(key)
 
+    def home_slot(self, key):
+        return sum(key) % self.n_slots
+
     def launch(self, si, key, plan, reqs):
         assert not plan.closed
         if key in self.fail_on:
@@ -349,3 +352,34 @@ def test_poisson_stream_is_seeded():
     assert abs(len(r1) / t1[-1] - 2000.0) < 1000.0
     ks = collections.Counter(r.n_pupil for r in r1)
     assert set(ks) <= {128, 256, 512, 1024}
+
+
+def test_bucket_goes_to_its_home_slot_when_free():
+    ex = FakeExecutor(n_slots=3, auto_complete=False)
+    srv = PSFServer(executor=ex, max_batch=4, hbm_budget=1e9)
+    a, b = req(n=8, m=4, L=2), req(n=8, m=4, L=3)      # homes (14 % 3, 15 % 3) = (2, 0)
+    srv.submit(a)
+    srv.submit(b)
+    srv.step()
+    slots = {tuple(ids): si for si, key, ids in ex.batches}
+    assert slots[(a.id,)] == 2 and slots[(b.id,)] == 0
+    # with its home slot busy, a bucket takes another free slot
+    c = req(n=8, m=4, L=2, seed=1)
+    srv.submit(c)
+    srv.step()
+    assert ex.batches[-1][0] == 1 and ex.batches[-1][2] == [c.id]
+    ex.release()
+    srv.step()
+    srv.close()
+
+
+def test_padded_batch_shapes():
+    from dlux_gb300.serving import CudaExecutor
+    ex = CudaExecutor.__new__(CudaExecutor)
+    ex.pad_batches, ex.max_batch = True, 8
+    assert [ex.padded_shape(r, 0) for r in range(1, 9)] == \
+        [(1, 0), (2, 0), (4, 0), (4, 0), (8, 0), (8, 0), (8, 0), (8, 0)]
+    assert ex.padded_shape(3, 1) == (4, 1) and ex.padded_shape(3, 3) == (4, 4)
+    assert ex.padded_shape(5, 3) == (8, 4) and ex.padded_shape(8, 8) == (8, 8)
+    ex.pad_batches = False
+    assert ex.padded_shape(5, 3) == (5, 3)
