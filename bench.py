@@ -470,9 +470,10 @@ def _serving_tuner():
 
     tuner = PlanTuner()
     grid, secs = tuner.tune_grid((128, 256, 512, 1024), (64, 128, 256, 512))
+    from dlux_gb300.autotune import config_label
     return tuner, {"seconds": secs, "cache": tuner.cache_path,
-                   "choices": {f"{n}x{m}": f"{c['variant']}/op{c['operand_mode']}"
-                               for (n, m), c in sorted(grid.items())}}
+                   "choices": {f"{n}x{m}": config_label(c) for (n, m), c in sorted(grid.items())},
+                   "timings": {k: v for k, v in tuner.timings.items()}}
 
 
 def serve_streams(args, variant, rates, n_requests, tuner=None):
@@ -725,6 +726,28 @@ def run_fft(args):
         ms = e0.elapsed_time(e1) / args.steps
         out[form] = {"ms_per_step": ms, "planes_per_s": L / (ms * 1e-3)}
         plan.close()
+    # Comparison only (not the product path): cuFFT through torch.fft on the same
+    # pruned passes -- rows N -> P (zero-padded), then columns N -> P, and the
+    # adjoint's inverse transforms of the columns and rows cropped back to N.
+    def cufft_step():
+        t = torch.fft.fft(x, n=P, dim=-1)
+        torch.fft.fft(t, n=P, dim=-2)
+        u = torch.fft.ifft(y, dim=-2)[..., :n, :]
+        torch.fft.ifft(u, dim=-1)[..., :n]
+    for _ in range(max(3, args.warmup)):
+        cufft_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        cufft_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    out["cufft_comparison"] = {"ms_per_step": ms, "planes_per_s": L / (ms * 1e-3),
+                               "note": "torch.fft (cuFFT), same pruned row/column passes, "
+                                       "no centring ramps; a library comparison, not a "
+                                       "product path"}
     hbm, _, src = load_peaks()
     bytes_step = L * 2 * ((n * n + n * P) * 8 + (n * P + P * P) * 8)
     achieved = bytes_step / (out["radix"]["ms_per_step"] * 1e-3) / 1e9

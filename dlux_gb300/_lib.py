@@ -182,6 +182,7 @@ _SIGNATURES = {
     "dlx_set_gemm_pair": (_c_int, [_c_int]),
     "dlx_gemm_pair_clusters": (_c_int, [ctypes.POINTER(_c_int)]),
     "dlx_set_wait_limit_ns": (_c_int, [ctypes.c_ulonglong]),
+    "dlx_poly_plan_set_gemm_form": (_c_int, [_c_vp, _c_int, _c_int]),
     "dlx_test_gemm_withhold_copies": (_c_int, [_c_int]),
     "dlx_scene_forward_token": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     "dlx_scene_reuse_forward": (_c_int, [_c_vp, ctypes.c_ulonglong]),

@@ -9,7 +9,13 @@ its GEMMs run:
   leave most SMs idle;
 - ``operand_mode``: the DFT operand streamed from cached matrices by TMA
   (0), or generated inside the GEMM's CTAs (1), which halves the operand
-  bytes and the plan's memory.
+  bytes and the plan's memory;
+- ``pair``: for the streamed operand, 256 x 128 tiles on clusters of two
+  CTAs (cta_group::2 MMAs, each CTA loading half of the A tile) instead of
+  128 x 128 tiles on one CTA -- a candidate only where a GEMM of the plan
+  has an even number of 128-column tiles;
+- ``split_k`` (plans with their own workspace only): whether GEMMs whose
+  tiles leave most SMs idle split K, at the count fixed at plan creation.
 
 ``PlanTuner.choose(n, m)`` times each candidate on a probe batch (the
 one-sweep PSF + gradient of ``probe_objects`` objects at ``probe_wavelengths``
@@ -29,16 +35,34 @@ import time
 
 import numpy as np
 
-__all__ = ["PlanTuner", "candidate_configs"]
+__all__ = ["PlanTuner", "candidate_configs", "config_label"]
 
 
-def candidate_configs(n, m, tensor_cores=True):
+def _tiles(side):
+    return (int(side) + 127) // 128
+
+
+def candidate_configs(n, m, tensor_cores=True, own_workspace=False):
     """Configurations worth timing for an (n_in, n_out) plan."""
-    out = [{"variant": "fp32", "operand_mode": 0}]
-    if tensor_cores and n % 8 == 0 and m % 8 == 0:
-        out = [{"variant": "split_bf16", "operand_mode": 0},
-               {"variant": "split_bf16", "operand_mode": 1}] + out
-    return out
+    fp32 = {"variant": "fp32", "operand_mode": 0, "pair": 0, "split_k": 1}
+    if not (tensor_cores and n % 8 == 0 and m % 8 == 0):
+        return [fp32]
+    out = [{"variant": "split_bf16", "operand_mode": 0, "pair": 0, "split_k": 1}]
+    if _tiles(n) % 2 == 0 or _tiles(m) % 2 == 0:
+        out.append({"variant": "split_bf16", "operand_mode": 0, "pair": 1, "split_k": 1})
+    out.append({"variant": "split_bf16", "operand_mode": 1, "pair": 0, "split_k": 1})
+    if own_workspace:
+        out.append({"variant": "split_bf16", "operand_mode": 0, "pair": 0, "split_k": 0})
+    return out + [fp32]
+
+
+def config_label(cfg):
+    label = f"{cfg['variant']}/op{cfg['operand_mode']}"
+    if cfg.get("pair"):
+        label += "/pair"
+    if not cfg.get("split_k", 1):
+        label += "/nosplit"
+    return label
 
 
 def _default_cache_path():
@@ -52,7 +76,8 @@ class PlanTuner:
     """Chooses a poly plan's arithmetic form and DFT operand per (n_in, n_out)."""
 
     def __init__(self, cache_path=None, probe_wavelengths=8, probe_objects=4, iters=5,
-                 diameter=1.0, psf_pixel_scale_rad=1e-7, timer=None, device_name=None):
+                 diameter=1.0, psf_pixel_scale_rad=1e-7, timer=None, device_name=None,
+                 own_workspace=False):
         self.cache_path = cache_path if cache_path is not None else _default_cache_path()
         self.probe_wavelengths = int(probe_wavelengths)
         self.probe_objects = int(probe_objects)
@@ -60,6 +85,8 @@ class PlanTuner:
         self.diameter = float(diameter)
         self.pixel_scale = float(psf_pixel_scale_rad)
         self._timer = timer            # (n, m, config) -> seconds; None: time on the GPU
+        # plans with their own workspace may split K; shared-workspace (serving) plans do not
+        self.own_workspace = bool(own_workspace)
         self._device = device_name
         self._lock = threading.Lock()
         self._mem = {}
@@ -73,7 +100,8 @@ class PlanTuner:
         return self._device
 
     def _key(self, n, m):
-        return f"{self.device_name()}|{int(n)}|{int(m)}"
+        ws = "own" if self.own_workspace else "shared"
+        return f"{self.device_name()}|{ws}|{int(n)}|{int(m)}"
 
     def _load_file(self):
         try:
@@ -99,13 +127,14 @@ class PlanTuner:
 
     # ---- choice ----
     def choose(self, n, m):
-        """{"variant": ..., "operand_mode": ...} for a poly plan of this shape."""
+        """{"variant", "operand_mode", "pair", "split_k"} for a poly plan of this shape."""
         key = self._key(n, m)
         with self._lock:
             if key in self._mem:
                 return dict(self._mem[key])
             cached = self._load_file().get(key)
-            if isinstance(cached, dict) and "variant" in cached and "operand_mode" in cached:
+            if isinstance(cached, dict) and all(k in cached for k in
+                                                ("variant", "operand_mode", "pair", "split_k")):
                 self._mem[key] = cached
                 return dict(cached)
             cfg = self._tune(n, m)
@@ -119,20 +148,20 @@ class PlanTuner:
             tc = kernels.tensor_core_available()
         else:
             tc = True
-        results = {}
-        for cfg in candidate_configs(n, m, tc):
-            label = f"{cfg['variant']}/op{cfg['operand_mode']}"
+        results, configs = {}, {}
+        for cfg in candidate_configs(n, m, tc, self.own_workspace):
+            label = config_label(cfg)
             try:
                 t = self._timer(n, m, cfg) if self._timer else self._time_gpu(n, m, cfg)
             except Exception:  # a candidate that cannot run here is skipped
                 continue
             results[label] = float(t)
+            configs[label] = cfg
         if not results:
             raise RuntimeError(f"no plan configuration runs for n={n}, m={m}")
         self.timings[self._key(n, m)] = results
         best = min(results, key=results.get)
-        variant, op = best.split("/op")
-        return {"variant": variant, "operand_mode": int(op), "seconds": results[best]}
+        return dict(configs[best], seconds=results[best])
 
     def _time_gpu(self, n, m, cfg):
         import torch
@@ -142,15 +171,19 @@ class PlanTuner:
 
         L, R = self.probe_wavelengths, self.probe_objects
         wls = np.linspace(0.8e-6, 1.2e-6, L)
-        # serving plans run on shared workspaces, which do not split K: probe likewise
+        # shared-workspace (serving) plans do not split K: probe those likewise
         lib = _lib.load()
-        _lib.check(lib.dlx_set_split_k(0))
+        if not self.own_workspace:
+            _lib.check(lib.dlx_set_split_k(0))
         try:
             plan = kernels.PolyPlan(wls, n, self.diameter / n, m, self.pixel_scale,
                                     variant=cfg["variant"], max_objects=R,
-                                    operand_mode=cfg["operand_mode"])
+                                    operand_mode=cfg["operand_mode"],
+                                    gemm_pair=bool(cfg.get("pair", 0)),
+                                    split_k=bool(cfg.get("split_k", 1)))
         finally:
-            _lib.check(lib.dlx_set_split_k(1))
+            if not self.own_workspace:
+                _lib.check(lib.dlx_set_split_k(1))
         try:
             rng = np.random.default_rng(n * 7919 + m)
             dev = dict(dtype=torch.float32, device="cuda")

@@ -99,11 +99,16 @@ void fft_spec(int n, double ps, double wl, double focal, double* d, double* c) {
   *c = (n % 2 != 0) ? 0.0 : -0.5 * d_out;
 }
 
+// Output side of dLux's padded FFT: N zero-padded by (N (pad - 1)) // 2 on
+// each side (utils/propagation.py:52-53), i.e. N pad, or N pad - 1 when
+// N (pad - 1) is odd.
+int fft_out_side(int n_in, int pad) { return n_in + 2 * ((n_in * (pad - 1)) / 2); }
+
 // One axis of the padded centred FFT (utils/propagation.py:8-64) with the
 // propagate_FFT ramps (wavefronts.py:683-712, utils/fourier.py:48-78).
 DftAxis fft_axis(const dlx_fft_desc& d, double wl) {
   DftAxis a{};
-  const int N = d.n_in, P = d.n_in * d.pad;
+  const int N = d.n_in, P = fft_out_side(d.n_in, d.pad);
   const int npad = (N * (d.pad - 1)) / 2;
   const int c = P / 2;
   a.a_in = 1.0;
@@ -595,12 +600,18 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
     return fail(DLX_ERR_SHAPE, "fft_plan_create: batch, n_in and pad must be positive");
   if (!(d->pixel_scale_in > 0)) return fail(DLX_ERR_ARG, "fft_plan_create: pixel scale <= 0");
   DLX_TRY(check_focal(d->focal_length, "fft_plan_create"));
+  if (d->apply_ramps && fft_out_side(d->n_in, d->pad) != d->n_in * d->pad)
+    return fail(DLX_ERR_SHAPE, "fft_plan_create: the output phase ramps span n_in * pad "
+                               "pixels, but the padded FFT of an odd n_in (pad - 1) has one "
+                               "fewer");
   if (d->variant == DLX_VARIANT_RADIX) {
+    if (fft_out_side(d->n_in, d->pad) != d->n_in * d->pad)
+      return fail(DLX_ERR_SHAPE, "fft_plan_create: the radix form needs n_in (pad - 1) even");
     auto* p = new (std::nothrow) dlx_fft_plan_s();
     if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
     p->radix = true;
     std::vector<DftAxis> ax(d->batch);
-    std::vector<float> alphas(d->batch, 1.0f / (float)(d->n_in * d->pad));
+    std::vector<float> alphas(d->batch, 1.0f / (float)fft_out_side(d->n_in, d->pad));
     for (int b = 0; b < d->batch; ++b) {
       if (!(wl[b] > 0)) {
         delete p;
@@ -619,14 +630,15 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
     return DLX_OK;
   }
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_in * d->pad));
+  DLX_TRY(check_split_shape(d->variant, d->n_in, fft_out_side(d->n_in, d->pad)));
   auto* p = new (std::nothrow) dlx_fft_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   TwoStep& ts = p->p.ts;
-  ts.batch = d->batch; ts.n_in = d->n_in; ts.n_out = d->n_in * d->pad; ts.variant = d->variant;
+  ts.batch = d->batch; ts.n_in = d->n_in; ts.n_out = fft_out_side(d->n_in, d->pad);
+  ts.variant = d->variant;
   ts.wl.assign(wl, wl + d->batch);
   std::vector<DftAxis> ax(d->batch);
-  std::vector<float> alphas(d->batch, 1.0f / (float)(d->n_in * d->pad));
+  std::vector<float> alphas(d->batch, 1.0f / (float)fft_out_side(d->n_in, d->pad));
   for (int b = 0; b < d->batch; ++b) {
     if (!(wl[b] > 0)) {
       delete p;
@@ -822,6 +834,11 @@ struct dlx_poly_plan_s {
   // plan. Plans on a shared workspace (serving buckets, which fill the GPU by
   // batching requests) do not split.
   bool split_k = false;
+  // Launch form chosen for this plan (dlx_poly_plan_set_gemm_form): the
+  // paired GEMM mode of GemmArgs::pair_mode, and whether the K split decided
+  // at creation is used.
+  int pair_mode = 0;
+  bool split_allowed = true;
   // Forward-to-backward reuse (dlx_poly_forward_token / dlx_poly_reuse_forward):
   // after a single-chunk forward, `field`, `mid` (the first-stage product D1)
   // and `pathff` hold that forward's state until the next call on the plan.
@@ -885,7 +902,8 @@ struct dlx_poly_plan_s {
     GemmArgs g = gemm_for(ts.variant, ts.batch * R, M, N, K, op, conj, B, e);
     g.a_batch_div = R;
     g.a_bs = (long long)M * K;
-    if (split_k && op.mat) {
+    g.pair_mode = pair_mode;
+    if (split_k && split_allowed && op.mat) {
       const long long tiles = (long long)ts.batch * max_obj * ((M + 127) / 128) * ((N + 127) / 128);
       const int sk = split_k_count(tiles, K);
       if (sk > 1) {
@@ -1149,6 +1167,15 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
 }
 
 extern "C" {
+
+int dlx_poly_plan_set_gemm_form(dlx_poly_plan plan, int pair_mode, int split_k) {
+  if (!plan) return fail(DLX_ERR_ARG, "poly_plan_set_gemm_form: null plan");
+  if (pair_mode < 0 || pair_mode > 2)
+    return fail(DLX_ERR_ARG, "poly_plan_set_gemm_form: pair_mode must be 0, 1 or 2");
+  plan->pair_mode = pair_mode;
+  plan->split_allowed = split_k != 0;
+  return DLX_OK;
+}
 
 int dlx_poly_plan_create(const dlx_poly_desc* d, const double* wl, dlx_poly_plan* plan) {
   return poly_create(d, wl, 1, plan);

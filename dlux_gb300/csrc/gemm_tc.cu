@@ -1256,8 +1256,9 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const int nt_tiles = (g.N + TC_BN - 1) / TC_BN;
   // Paired form: n-tiles in pairs, no split K.
   const int withhold = g_withhold.load();
+  const bool want_pair = g.pair_mode == 2 || (g.pair_mode == 0 && pair_enabled());
   const bool pair = !split && nt_tiles % 2 == 0 && dev->pair_clusters > 0 && !withhold &&
-                    pair_enabled();
+                    want_pair;
   CUtensorMap ta, tb;
   DLX_TRY(encode_split(&ta, g.As, g.M, g.K, nA, pair ? TC_BM / 2 : TC_BM));
   DLX_TRY(encode_split(&tb, g.Bs, g.N, g.K, nB, TC_BN));

@@ -258,6 +258,10 @@ struct GemmArgs {
   // (split_k_count), so a result does not depend on what else is in the batch.
   int splits;
   float2* split_ws;
+  // Paired (cta_group::2) form of the loaded-operand tensor-core GEMM:
+  // 0 follows the process-wide switch (dlx_set_gemm_pair), 1 never, 2 where
+  // the shape allows it (an even number of 128-column tiles, no split K).
+  int pair_mode;
 };
 
 // Splits for a GEMM with `tiles` output tiles (over the largest batch the

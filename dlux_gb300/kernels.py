@@ -41,6 +41,12 @@ def get_variant() -> str | None:
     return _default_variant
 
 
+def fft_out_side(n_in: int, pad: int) -> int:
+    """Side of dLux's padded FFT output: n_in zero-padded by (n_in (pad - 1)) // 2 on
+    each side (utils/propagation.py:52-53)."""
+    return int(n_in) + 2 * ((int(n_in) * (int(pad) - 1)) // 2)
+
+
 def resolve_variant(n_in: int, n_out: int, variant: str | None = None) -> int:
     """Integer variant for a transform of the given sides.
 
@@ -281,8 +287,8 @@ RADIX_FFT_MIN = 2048
 def resolve_fft_variant(n_in, pad, variant=None):
     """Integer form of an FFT plan: "radix" (power-of-two pad * N <= 8192), or the
     MFT forms. Automatic: radix from RADIX_FFT_MIN on, otherwise as resolve_variant."""
-    p = int(n_in) * int(pad)
-    pow2 = p & (p - 1) == 0 and p <= 8192
+    p = fft_out_side(n_in, pad)
+    pow2 = p == int(n_in) * int(pad) and p & (p - 1) == 0 and p <= 8192
     if variant == "radix" or variant == _lib.VARIANT_RADIX:
         if not pow2:
             raise ValueError("the radix FFT form needs pad * npixels to be a power of two <= 8192")
@@ -305,7 +311,7 @@ class FFTPlan(_Plan):
         _lib.require_cuda()
         self.wavelengths = tuple(float(w) for w in wavelengths)
         self.n_in, self.pad = int(n_in), int(pad)
-        self.n_out = self.n_in * self.pad
+        self.n_out = fft_out_side(self.n_in, self.pad)
         self.variant = resolve_fft_variant(self.n_in, self.pad, variant)
         apply, c_in, c_out = (0, 0.0, 0.0) if ramps is None else (1, float(ramps[0]),
                                                                  float(ramps[1]))
@@ -337,7 +343,10 @@ class PolyPlan(_Plan):
 
     def __init__(self, wavelengths, n_in, pixel_scale_in, n_out, pixel_scale_out,
                  focal_length=None, variant=None, max_objects=1, operand_mode=0,
-                 own_workspace=True):
+                 own_workspace=True, gemm_pair=None, split_k=True):
+        """gemm_pair: None follows the process-wide paired-GEMM switch, False never
+        pairs, True pairs where the shape allows; split_k False keeps every GEMM
+        whole (see dlx_poly_plan_set_gemm_form)."""
         super().__init__()
         _lib.require_cuda()
         self.wavelengths = tuple(float(w) for w in wavelengths)
@@ -353,6 +362,10 @@ class PolyPlan(_Plan):
         fn = "dlx_poly_plan_create_batched" if own_workspace else "dlx_poly_plan_create_shared"
         call(fn, ctypes.byref(self.desc), _lib.dbl_array(self.wavelengths), self.max_objects,
              ctypes.byref(self.handle))
+        self.gemm_pair, self.split_k = gemm_pair, bool(split_k)
+        if gemm_pair is not None or not split_k:
+            call("dlx_poly_plan_set_gemm_form", self.handle,
+                 0 if gemm_pair is None else (2 if gemm_pair else 1), int(bool(split_k)))
 
     def workspace_bytes(self) -> int:
         n = ctypes.c_size_t(0)

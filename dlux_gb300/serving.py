@@ -564,19 +564,20 @@ class CudaExecutor:
         self.models[n] = (amp, basis, scale)
 
     def plan_config(self, n, m):
-        """(variant, operand_mode) of the bucket plans of shape (n, m)."""
+        """(variant, operand_mode, pair) of the bucket plans of shape (n, m); pair None
+        follows the process-wide paired-GEMM switch."""
         if self.tuner is not None:
             cfg = self.tuner.choose(n, m)
-            return cfg["variant"], int(cfg["operand_mode"])
-        return self.variant, self.operand_mode
+            return cfg["variant"], int(cfg["operand_mode"]), bool(cfg.get("pair", 0))
+        return self.variant, self.operand_mode, None
 
     def create_plan(self, key):
         n, m, L = key
-        variant, mode = self.plan_config(n, m)
+        variant, mode, pair = self.plan_config(n, m)
         with torch.cuda.device(self.device):
             return kernels.PolyPlan(self.wavelengths(L), n, self.diameter / n, m,
                                     self.pixel_scale, None, variant, self.max_batch,
-                                    mode, own_workspace=False)
+                                    mode, own_workspace=False, gemm_pair=pair)
 
     def release_plan(self, key, plan):
         for gk in [k for k in self.graphs if k[1] == key]:

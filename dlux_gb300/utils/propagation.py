@@ -82,5 +82,6 @@ def FFT(phasor, wavelength, pixel_scale, focal_length=None, pad=2, inverse=False
         new_ps = new_ps * focal_length
     plan = kernels.get_fft_plan(wl, n, float(pixel_scale), int(pad), focal_length, inverse)
     out = autograd.apply_plan(plan, xb)
-    out = out[0] if squeeze else out.reshape(*x.shape[:-2], n * pad, n * pad)
+    p = kernels.fft_out_side(n, pad)
+    out = out[0] if squeeze else out.reshape(*x.shape[:-2], p, p)
     return out, (float(new_ps) if new_ps.dim() == 0 else new_ps)

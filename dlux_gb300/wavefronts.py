@@ -215,6 +215,11 @@ class Wavefront(Base):
         wl = self.wavelengths
         d_fft, c_fft = fft_spec(n_out, self.pixel_scale, wl[0], focal_length)
         if spec_out is not None:
+            if kernels.fft_out_side(self.npixels, pad) != n_out:
+                # dLux's ramp of n_out pixels does not broadcast against its FFT output
+                raise ValueError(f"the FFT of {self.npixels} pixels padded by {pad} has "
+                                 f"{kernels.fft_out_side(self.npixels, pad)} pixels, not "
+                                 f"{n_out}: output ramps need npixels * (pad - 1) even")
             if spec_out.d is not None:
                 raise ValueError("Output spec cannot specify d; FFT output d is fixed.")
             if spec_out.n is not None:

@@ -351,6 +351,14 @@ int dlx_set_gemm_pair(int enable);
 /* Two-CTA clusters of the paired GEMM that fit on the device at once (0: the
  * paired form is unavailable). No dLux counterpart. */
 int dlx_gemm_pair_clusters(int* clusters);
+/* Launch form of one poly plan's tensor-core GEMMs, for the autotuner:
+ * pair_mode 0 follows dlx_set_gemm_pair, 1 never pairs, 2 pairs wherever the
+ * shape allows (an even number of 128-column tiles and no split K);
+ * split_k 0 keeps every GEMM whole, 1 uses the K split the plan chose at
+ * creation (if any). Applies to the plan's later calls (CUDA graphs keep the
+ * form they were captured with); each choice is fixed per plan, so an
+ * object's result stays the same alone and in a batch. No dLux counterpart. */
+int dlx_poly_plan_set_gemm_form(dlx_poly_plan plan, int pair_mode, int split_k);
 int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token);
 /* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
  * is known before the forward pass (a serving request, a linear functional):

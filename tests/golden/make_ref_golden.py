@@ -235,8 +235,10 @@ def make_cfg3(dl, O):
 
     c0, f0 = inp["coeffs"], inp["flat"]
     grad_c = fd4_grad(lambda c: nll(c, A0, f0), c0, 2e-10)
-    d_amp = [fd4(lambda A: nll(c0, A, f0), A0, v * T, 1e-6) for v in inp["dir_amp"]]
-    d_flat = [fd4(lambda f: nll(c0, A0, f), f0, v, 1e-6) for v in inp["dir_flat"]]
+    # steps of 1e-4 along N(0, 1) directions: the NLL is ~4e6, so smaller steps lose
+    # digits to rounding; the fourth-order truncation at 1e-4 is far below that
+    d_amp = [fd4(lambda A: nll(c0, A, f0), A0, v * T, 1e-4) for v in inp["dir_amp"]]
+    d_flat = [fd4(lambda f: nll(c0, A0, f), f0, v, 1e-4) for v in inp["dir_flat"]]
     opd = np.tensordot(B, c0, axes=(0, 0))
     ora = O.poly_psf(A0, opd, wls, np.full(len(wls), 1.0 / len(wls)), 1.0, 256,
                      0.02 * RI.ARCSEC) * f0
@@ -293,14 +295,14 @@ def make_layers(dl, O):
     out = {}
     systems = {
         # name: (builder of the system from its differentiated input, x0, kind, h)
-        "optic": (lambda o: ang([L.Optic(A, o, ph0, normalise=True)]), opd0, "dir_opd", 1e-9),
+        "optic": (lambda o: ang([L.Optic(A, o, ph0, normalise=True)]), opd0, "dir_opd", 0.05),
         "optic_phase": (lambda p: ang([L.Optic(A, opd0, p, normalise=True)]), ph0, "dir_phase",
                         1e-3),
         "optic_amp": (lambda a: ang([L.Optic(a, opd0, None, normalise=True)]), A, "dir_amp", 1e-4),
         "basis_optic": (lambda c: ang([L.BasisOptic(B, A, c, normalise=True)]), c0, "grad",
                         2e-10),
         "aberrated_opd": (lambda o: ang([L.TransmissiveLayer(A, normalise=True),
-                                         L.AberratedLayer(opd=o)]), opd0, "dir_opd", 1e-9),
+                                         L.AberratedLayer(opd=o)]), opd0, "dir_opd", 0.05),
         "aberrated_phase": (lambda p: ang([L.TransmissiveLayer(A, normalise=True),
                                            L.AberratedLayer(phase=p)]), ph0, "dir_phase", 1e-3),
         "basis_phase": (lambda c: ang([L.TransmissiveLayer(A, normalise=True),
@@ -320,6 +322,9 @@ def make_layers(dl, O):
             64, 1.0, [L.TransmissiveLayer(A, normalise=True), L.BasisLayer(B, c),
                       L.MFT(32, 0.04 * RI.ARCSEC)]), c0, "grad", 2e-10),
     }
+    # Steps h along each direction: the OPD directions are 1e-8 m fields (h = 0.05:
+    # ~5e-10 m, a few milliradians of phase), phase directions N(0, 1) rad (h = 1e-3),
+    # transmission directions N(0, 1) T (h = 1e-4), coefficients (h = 2e-10 m).
     for name, (make, x0, kind, h) in systems.items():
         f = loss_of(make)
         out[f"{name}_psf"] = make(x0).propagate(wls, weights=w)
@@ -339,7 +344,7 @@ def make_layers(dl, O):
         wf = wf.propagate(32, 0.04 * RI.ARCSEC)
         return wf.psf
     out["peak_psf"] = peak_psf(opd0)
-    out["peak_dd"] = fd4(lambda o: float((peak_psf(o) * R).sum()), opd0, inp["dir_opd"], 1e-9)
+    out["peak_dd"] = fd4(lambda o: float((peak_psf(o) * R).sum()), opd0, inp["dir_opd"], 0.05)
     # power normalisation of a wavefront, for comparison
     wf = dl.wavefronts.Wavefront(1.0e-6, 64, diameter=1.0) * A
     out["power_phasor"] = wf.add_opd(opd0).normalise("power").phasor

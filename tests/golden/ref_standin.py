@@ -19,7 +19,8 @@ What the stand-ins provide, and nothing more:
   * ``jax.scipy``: the SciPy functions of the same names;
   * ``equinox``: Module, field (static fields become plain attributes),
     filter_jit (identity), filter_vmap, partition;
-  * ``zodiax.Base``: get / set / add / multiply by attribute path, returning
+  * ``zodiax.Base``: get / set / add / subtract / multiply / divide / power by
+    attribute path, returning
     shallow copies, as zodiax does for its immutable modules;
   * ``abcdLux`` and ``interpax``: empty modules (dLux imports them at module
     level; the paths fixtures are made for never call into them).
@@ -30,7 +31,6 @@ holds dLux's source tree.
 
 from __future__ import annotations
 
-import copy
 import functools
 import importlib
 import os
@@ -134,6 +134,13 @@ class Module:
     """Stand-in for equinox.Module: a plain object whose attributes are its fields."""
 
 
+def _shallow(obj):
+    """A copy of a module sharing its fields (no __getattr__ lookups on the way)."""
+    new = object.__new__(type(obj))
+    new.__dict__.update(obj.__dict__)
+    return new
+
+
 def _is_node(x):
     return isinstance(x, (list, tuple, dict, Module)) or x is None
 
@@ -161,7 +168,7 @@ def _rebuild(meta, kids):
         return out
     if kind == "seq":
         return t(kids)
-    new = copy.copy(t)
+    new = _shallow(t)
     for k, v in zip(keys, kids):
         object.__setattr__(new, k, v)
     return new
@@ -298,7 +305,7 @@ class Base(Module):
             new = type(self)(self)
             child = self[key]
         else:
-            new = copy.copy(self)
+            new = _shallow(self)
             child = getattr(self, key)
         if len(keys) > 1:
             value = Base._set_path(child, keys[1:], value)
@@ -326,6 +333,15 @@ class Base(Module):
 
     def multiply(self, path, value):
         return self.set(path, self.get(path) * value)
+
+    def divide(self, path, value):
+        return self.set(path, self.get(path) / value)
+
+    def subtract(self, path, value):
+        return self.set(path, self.get(path) - value)
+
+    def power(self, path, value):
+        return self.set(path, self.get(path) ** value)
 
 
 # ----------------------------------------------------------------------------

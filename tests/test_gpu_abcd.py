@@ -184,6 +184,7 @@ def test_gradient_through_the_propagators(cuda):
         def f(e):
             v = ref_fn(amp * np.exp(1j * (phi0 + e * dphi)))
             return float((np.abs(v) ** 2 * R).sum())
-        h = 1e-4
-        fd = (f(h) - f(-h)) / (2 * h)
-        assert abs(t.grad.item() - fd) / abs(fd) < 1e-3, (t.grad.item(), fd)
+        # fourth-order central difference in FP64 (truncation ~h^4 = 1e-12)
+        h = 1e-3
+        fd = (-f(2 * h) + 8 * f(h) - 8 * f(-h) + f(-2 * h)) / (12 * h)
+        assert abs(t.grad.item() - fd) / abs(fd) < 1e-5, (t.grad.item(), fd)

@@ -54,7 +54,7 @@ def test_config1_psf_and_gradient(cuda, variant):
         gc_ref = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
         err = rel(coeffs.grad.cpu().numpy(), gc_ref)
         print(f"config 1 {variant}: d loss / d c rel L2 {err:.2e}")
-        assert err < 1e-4
+        assert err < 1e-5
     finally:
         dl.set_variant(None)
 
@@ -77,7 +77,9 @@ def test_transmission_gradient_through_normalise(cuda):
                         float(O.arcsec2rad(0.04)), G)
     ge = g["g_amp"]
     gT = ge / np.sqrt(S) - T * (T * ge).sum() / S ** 1.5
-    assert rel(Tt.grad.cpu().numpy(), gT) < 1e-4
+    e = rel(Tt.grad.cpu().numpy(), gT)
+    print(f"transmission gradient through the normalisation: {e:.2e}")
+    assert e < 1e-5
 
 
 def test_telescope_with_detector(cuda):
@@ -151,14 +153,16 @@ def test_point_sources_position_gradient(cuda):
                                          offset=(x, y))).sum()
         return tot
     p0 = pos.detach().numpy()
-    h = 1e-10
+    # fourth-order central differences in FP64 (step 2e-9 rad: truncation ~1e-9)
+    h = 2e-9
     fd = np.zeros_like(p0)
     for i in range(2):
         for j in range(2):
             d = np.zeros_like(p0)
             d[i, j] = h
-            fd[i, j] = (loss(p0 + d) - loss(p0 - d)) / (2 * h)
-    assert rel(pos.grad.numpy(), fd) < 1e-3
+            fd[i, j] = (-loss(p0 + 2 * d) + 8 * loss(p0 + d) - 8 * loss(p0 - d)
+                        + loss(p0 - 2 * d)) / (12 * h)
+    assert rel(pos.grad.numpy(), fd) < 1e-5
 
 
 def test_reference_error_paths():

@@ -133,15 +133,17 @@ def test_point_sources_flux_and_position_gradients(cuda):
     assert rel(img.detach().cpu().numpy(), ref_img) < 1e-5
     gf = np.array([(loss(p0, f0 + 1e-3 * np.eye(S)[s]) - loss(p0, f0 - 1e-3 * np.eye(S)[s]))
                    / 2e-3 for s in range(S)])
-    assert rel(flux.grad.cpu().numpy(), gf) < 1e-4
-    h = 1e-10
+    assert rel(flux.grad.cpu().numpy(), gf) < 1e-5
+    # fourth-order central differences in FP64 (step 2e-9 rad: truncation ~1e-9)
+    h = 2e-9
     gp = np.zeros_like(p0)
     for s in range(S):
         for k in range(2):
             d = np.zeros_like(p0)
             d[s, k] = h
-            gp[s, k] = (loss(p0 + d, f0) - loss(p0 - d, f0)) / (2 * h)
-    assert rel(pos.grad.numpy(), gp) < 1e-3
+            gp[s, k] = (-loss(p0 + 2 * d, f0) + 8 * loss(p0 + d, f0) - 8 * loss(p0 - d, f0)
+                        + loss(p0 - 2 * d, f0)) / (12 * h)
+    assert rel(pos.grad.numpy(), gp) < 1e-5
 
 
 def test_shared_plan_workspace_and_generated_operand(cuda):

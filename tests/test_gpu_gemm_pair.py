@@ -97,3 +97,40 @@ def test_pair_matches_single_cta_and_oracle(cuda, n, m, L):
     assert rel(psf1, ref) < 1e-5
     g = O.poly_psf_grad(Teff, x["opd"], x["wls"], x["w"], 1.0, m, ps, x["G"])
     assert rel(go1, g["g_opd"]) < 1e-5
+
+
+def test_per_plan_gemm_form_is_bitwise_the_global_one(cuda):
+    """dlx_poly_plan_set_gemm_form (the autotuner's per-plan launch form): a plan made
+    with gemm_pair=True gives the bits of the global switch's paired form, one with
+    gemm_pair=False those of the single-CTA form, whatever the global switch says; a plan
+    with split_k=False keeps every GEMM whole and still matches the oracle."""
+    from dlux_gb300 import kernels
+    n, m, L = 256, 256, 4
+    x = case(n, m, L, 21)
+    ps = float(O.arcsec2rad(0.02))
+    clusters = ctypes.c_int(0)
+    from dlux_gb300 import _lib
+    _lib.check(_lib.load().dlx_gemm_pair_clusters(ctypes.byref(clusters)))
+    if clusters.value == 0:
+        pytest.skip("paired form unavailable")
+    try:
+        set_pair(True)
+        ref_pair = run(kernels.PolyPlan(x["wls"], n, 1.0 / n, m, ps, variant="split_bf16"), x)
+        set_pair(False)
+        ref_single = run(kernels.PolyPlan(x["wls"], n, 1.0 / n, m, ps, variant="split_bf16"), x)
+        # per-plan forms against the opposite global setting
+        on = run(kernels.PolyPlan(x["wls"], n, 1.0 / n, m, ps, variant="split_bf16",
+                                  gemm_pair=True), x)
+        set_pair(True)
+        off = run(kernels.PolyPlan(x["wls"], n, 1.0 / n, m, ps, variant="split_bf16",
+                                   gemm_pair=False), x)
+    finally:
+        set_pair(False)
+    for a, b in zip(on, ref_pair):
+        assert np.array_equal(a, b)
+    for a, b in zip(off, ref_single):
+        assert np.array_equal(a, b)
+    whole = run(kernels.PolyPlan(x["wls"], n, 1.0 / n, m, ps, variant="split_bf16",
+                                 split_k=False), x)
+    ref = O.poly_psf(x["T"], x["opd"], x["wls"], x["w"], 1.0, m, ps)
+    assert rel(whole[0], ref) < 1e-5

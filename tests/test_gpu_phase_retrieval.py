@@ -1,13 +1,15 @@
-"""Phase-retrieval gradients (Poisson NLL) through the public API vs FP64 central differences.
+"""Phase-retrieval gradients (Poisson NLL) through the public API vs the FP64 oracle.
 
 The phase-retrieval configuration: per-pixel pupil amplitude 1 + N(0, 0.01)
 inside the aperture, Zernike coefficients N(0, 40 nm), a detector with a
 per-pixel flat field 1 + N(0, 0.02), data = a Poisson draw of the PSF scaled
 to 1e6 photons, loss = sum(m - d log m). It runs here at a reduced size
-(128^2 pupil, 64^2 detector, 4 wavelengths) so the FP64 oracle's central
-differences finish in seconds. Tolerance: relative error <= 1e-3 against the
-central differences (their own truncation error is ~1e-6), <= 1e-4 against
-the analytic FP64 reverse pass.
+(128^2 pupil, 64^2 detector, 4 wavelengths); tests/test_gpu_ref_golden.py runs
+the full-size configuration against dLux's own outputs. Every gradient is
+compared with the oracle's analytic reverse pass (coefficients, amplitude and
+flat field over all pixels, relative L2 <= 1e-5), and the coefficient
+gradient also with fourth-order central differences of the oracle in FP64
+(relative L2 <= 1e-5; their truncation is ~1e-9).
 """
 
 import numpy as np
@@ -67,26 +69,37 @@ def test_poisson_nll_gradients(cuda, variant):
         loss.backward()
         # value
         assert abs(loss.item() - oracle_loss(s)) < 1e-5 * abs(oracle_loss(s)) + 1e-2
-        # coefficients: central differences in FP64
-        h = 1e-10
+        # analytic FP64 reverse pass: dL/dpsf = scale (1 - d / m) flat, then the chain
+        # through the amplitude normalisation A / ||A||
+        wls, L, m_ = s["wls"], s["L"], s["m"]
+        opd = O.eval_basis(s["B"], s["c"])
+        w = np.ones(L) / L
+        psf = O.poly_psf(s["A"], opd, wls, w, 1.0, m_, s["ps"])
+        mod_ref = s["scale"] * psf * s["flat"]
+        G = s["scale"] * (1.0 - s["data"] / mod_ref) * s["flat"]
+        nrm = np.sqrt((s["A"] ** 2).sum())
+        g = O.poly_psf_grad(s["A"] / nrm, opd, wls, w, 1.0, m_, s["ps"], G)
+        gc_ref = np.tensordot(s["B"], g["g_opd"], axes=((1, 2), (0, 1)))
+        gA_ref = g["g_amp"] / nrm - s["A"] * (g["g_amp"] * s["A"]).sum() / nrm ** 3
+        gF_ref = s["scale"] * (1.0 - s["data"] / mod_ref) * psf
+        gc = c.grad.cpu().numpy()
+        errs = {"coefficients": np.linalg.norm(gc - gc_ref) / np.linalg.norm(gc_ref),
+                "amplitude": np.linalg.norm(A.grad.cpu().numpy() - gA_ref) /
+                np.linalg.norm(gA_ref),
+                "flat": np.linalg.norm(flat.grad.cpu().numpy() - gF_ref) / np.linalg.norm(gF_ref)}
+        # coefficients again: fourth-order central differences of the oracle in FP64
+        h = 2e-10
         fd = []
         for k in range(len(s["c"])):
             e = np.zeros_like(s["c"])
             e[k] = h
-            fd.append((oracle_loss(s, c=s["c"] + e) - oracle_loss(s, c=s["c"] - e)) / (2 * h))
+            fd.append((-oracle_loss(s, c=s["c"] + 2 * e) + 8 * oracle_loss(s, c=s["c"] + e)
+                       - 8 * oracle_loss(s, c=s["c"] - e) + oracle_loss(s, c=s["c"] - 2 * e))
+                      / (12 * h))
         fd = np.array(fd)
-        gc = c.grad.cpu().numpy()
-        assert np.linalg.norm(gc - fd) / np.linalg.norm(fd) < 1e-3
-        # amplitude and flat: a few pixels
-        for (i, j) in [(64, 64 + 20), (30, 70), (100, 60)]:
-            e = np.zeros_like(s["A"])
-            e[i, j] = 1e-5
-            fd_a = (oracle_loss(s, A=s["A"] + e) - oracle_loss(s, A=s["A"] - e)) / 2e-5
-            assert abs(A.grad[i, j].item() - fd_a) < 2e-3 * abs(fd_a) + 1e-6 * np.abs(fd).max()
-        for (i, j) in [(32, 32), (20, 40)]:
-            e = np.zeros_like(s["flat"])
-            e[i, j] = 1e-6
-            fd_f = (oracle_loss(s, flat=s["flat"] + e) - oracle_loss(s, flat=s["flat"] - e)) / 2e-6
-            assert abs(flat.grad[i, j].item() - fd_f) < 1e-3 * abs(fd_f) + 1e-3
+        errs["coefficients_fd"] = np.linalg.norm(gc - fd) / np.linalg.norm(fd)
+        print(f"phase retrieval {variant}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+        for k, v in errs.items():
+            assert v < 1e-5, (k, v)
     finally:
         dl.set_variant(None)

@@ -1,7 +1,7 @@
 """Serving loop on the GPU: parity with the oracle, and each request's result is bit for bit
 the same alone and inside mixed batches (direct launches and CUDA-graph replays).
 
-Tolerances against the FP64 oracle: PSF relative L2 <= 1e-5, coefficient gradient <= 1e-4.
+Tolerances against the FP64 oracle: PSF and coefficient gradient relative L2 <= 1e-5.
 """
 
 import ctypes
@@ -86,7 +86,7 @@ def test_serving_matches_oracle(cuda):
     gref = basis.reshape(K, -1).astype(np.float64) @ g_opd.reshape(-1)
     e_psf, e_grad = rel(psf, ref), rel(grad, gref)
     print(f"serving vs oracle: psf {e_psf:.2e}, grad {e_grad:.2e}")
-    assert e_psf < 1e-5 and e_grad < 1e-4
+    assert e_psf < 1e-5 and e_grad < 1e-5
     s.close()
 
 
