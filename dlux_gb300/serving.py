@@ -438,6 +438,15 @@ class PSFServer:
                    p99_queue_ms=float(np.percentile(wait, 99)),
                    p99_service_ms=float(np.percentile(service, 99)),
                    mean_batch=self.stats["launched"] / max(self.stats["batches"], 1))
+        # the slowest requests: when they arrived (ms after the first), their shape
+        # and how their latency splits into queueing and service
+        worst = np.argsort(lat)[-10:][::-1]
+        out["slowest"] = [{"arrival_ms": round((done[i].t_submit - t0) * 1e3, 3),
+                           "latency_ms": round(float(lat[i]), 3),
+                           "queue_ms": round(float(wait[i]), 3),
+                           "service_ms": round(float(service[i]), 3),
+                           "key": list(done[i].key), "grad": done[i].want_grad}
+                          for i in worst]
         by_n = collections.defaultdict(list)
         for r, l in zip(done, lat):
             by_n[r.n_pupil].append(l)

@@ -5,11 +5,19 @@ inside the aperture, Zernike coefficients N(0, 40 nm), a detector with a
 per-pixel flat field 1 + N(0, 0.02), data = a Poisson draw of the PSF scaled
 to 1e6 photons, loss = sum(m - d log m). It runs here at a reduced size
 (128^2 pupil, 64^2 detector, 4 wavelengths); tests/test_gpu_ref_golden.py runs
-the full-size configuration against dLux's own outputs. Every gradient is
-compared with the oracle's analytic reverse pass (coefficients, amplitude and
-flat field over all pixels, relative L2 <= 1e-5), and the coefficient
-gradient also with fourth-order central differences of the oracle in FP64
-(relative L2 <= 1e-5; their truncation is ~1e-9).
+the full-size configuration against dLux's own outputs.
+
+The NLL's cotangent dL/dm = 1 - d/m is a difference of nearly equal terms
+near the data (d ~ m +- sqrt(m)), so it magnifies the model image's relative
+error by up to ~sqrt(counts) (~1e2 here): an image within 1e-6 of the oracle
+gives an end-to-end gradient within ~1e-5 to 1e-4. The reverse kernels are
+therefore checked on the oracle's own cotangent: the image is backpropagated
+with dL/dimage evaluated at the FP64 oracle's image, and the coefficient,
+amplitude and flat-field gradients (all pixels) must be within 1e-5
+(relative L2) of the oracle's analytic reverse pass, the coefficient
+gradient also of fourth-order central differences of the oracle in FP64
+(truncation ~1e-9). The end-to-end autograd gradient is reported and held to
+1e-4, the conditioning bound above.
 """
 
 import numpy as np
@@ -54,52 +62,69 @@ def test_poisson_nll_gradients(cuda, variant):
     try:
         s = setup()
         dev = "cuda"
-        A = torch.as_tensor(s["A"], dtype=torch.float32, device=dev).requires_grad_(True)
-        c = torch.as_tensor(s["c"], dtype=torch.float32, device=dev).requires_grad_(True)
-        flat = torch.as_tensor(s["flat"], dtype=torch.float32, device=dev).requires_grad_(True)
-        B = torch.as_tensor(s["B"], dtype=torch.float32, device=dev)
-        optics = dl.AngularOpticalSystem(s["n"], 1.0, [dl.TransmissiveLayer(A, normalise=True),
-                                                       dl.BasisLayer(B, c)], s["m"], 0.04)
-        det = dl.LayeredDetector([dl.ApplyPixelResponse(flat)])
-        src = dl.PointSource(s["wls"])
-        img = dl.Telescope(optics, src, det).model()
-        mod = s["scale"] * img
-        d = torch.as_tensor(s["data"], dtype=torch.float32, device=dev)
-        loss = (mod - d * torch.log(mod)).sum()
-        loss.backward()
-        # value
-        assert abs(loss.item() - oracle_loss(s)) < 1e-5 * abs(oracle_loss(s)) + 1e-2
-        # analytic FP64 reverse pass: dL/dpsf = scale (1 - d / m) flat, then the chain
-        # through the amplitude normalisation A / ||A||
         wls, L, m_ = s["wls"], s["L"], s["m"]
-        opd = O.eval_basis(s["B"], s["c"])
         w = np.ones(L) / L
-        psf = O.poly_psf(s["A"], opd, wls, w, 1.0, m_, s["ps"])
-        mod_ref = s["scale"] * psf * s["flat"]
-        G = s["scale"] * (1.0 - s["data"] / mod_ref) * s["flat"]
+        opd = O.eval_basis(s["B"], s["c"])
+        psf_ref = O.poly_psf(s["A"], opd, wls, w, 1.0, m_, s["ps"])
+        mod_ref = s["scale"] * psf_ref * s["flat"]
+        # dL/dimage at the oracle's image, and the oracle's analytic reverse pass
+        g_img = s["scale"] * (1.0 - s["data"] / mod_ref)
+        G = g_img * s["flat"]                                   # dL/dpsf
         nrm = np.sqrt((s["A"] ** 2).sum())
         g = O.poly_psf_grad(s["A"] / nrm, opd, wls, w, 1.0, m_, s["ps"], G)
         gc_ref = np.tensordot(s["B"], g["g_opd"], axes=((1, 2), (0, 1)))
         gA_ref = g["g_amp"] / nrm - s["A"] * (g["g_amp"] * s["A"]).sum() / nrm ** 3
-        gF_ref = s["scale"] * (1.0 - s["data"] / mod_ref) * psf
-        gc = c.grad.cpu().numpy()
-        errs = {"coefficients": np.linalg.norm(gc - gc_ref) / np.linalg.norm(gc_ref),
-                "amplitude": np.linalg.norm(A.grad.cpu().numpy() - gA_ref) /
-                np.linalg.norm(gA_ref),
-                "flat": np.linalg.norm(flat.grad.cpu().numpy() - gF_ref) / np.linalg.norm(gF_ref)}
-        # coefficients again: fourth-order central differences of the oracle in FP64
+        gF_ref = g_img * psf_ref
+
+        def run(cotangent=None):
+            A = torch.as_tensor(s["A"], dtype=torch.float32, device=dev).requires_grad_(True)
+            c = torch.as_tensor(s["c"], dtype=torch.float32, device=dev).requires_grad_(True)
+            flat = torch.as_tensor(s["flat"], dtype=torch.float32,
+                                   device=dev).requires_grad_(True)
+            B = torch.as_tensor(s["B"], dtype=torch.float32, device=dev)
+            optics = dl.AngularOpticalSystem(s["n"], 1.0,
+                                             [dl.TransmissiveLayer(A, normalise=True),
+                                              dl.BasisLayer(B, c)], s["m"], 0.04)
+            det = dl.LayeredDetector([dl.ApplyPixelResponse(flat)])
+            img = dl.Telescope(optics, dl.PointSource(s["wls"]), det).model()
+            mod = s["scale"] * img
+            d = torch.as_tensor(s["data"], dtype=torch.float32, device=dev)
+            loss = (mod - d * torch.log(mod)).sum()
+            if cotangent is None:
+                loss.backward()
+            else:
+                img.backward(torch.as_tensor(cotangent, dtype=torch.float32, device=dev))
+            return (loss.item(), c.grad.cpu().numpy(), A.grad.cpu().numpy(),
+                    flat.grad.cpu().numpy())
+
+        def rel(a, b):
+            return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+        loss, gc_e2e, _, _ = run()
+        assert abs(loss - oracle_loss(s)) < 1e-5 * abs(oracle_loss(s))
+        _, gc, gA, gF = run(g_img)
+        errs = {"coefficients": rel(gc, gc_ref), "amplitude": rel(gA, gA_ref),
+                "flat": rel(gF, gF_ref)}
+        # coefficients again: fourth-order central differences of the oracle in FP64,
+        # with the data term's cotangent held at the oracle's image (a linear functional)
         h = 2e-10
         fd = []
         for k in range(len(s["c"])):
             e = np.zeros_like(s["c"])
             e[k] = h
-            fd.append((-oracle_loss(s, c=s["c"] + 2 * e) + 8 * oracle_loss(s, c=s["c"] + e)
-                       - 8 * oracle_loss(s, c=s["c"] - e) + oracle_loss(s, c=s["c"] - 2 * e))
-                      / (12 * h))
+
+            def lin(cc):
+                p = O.poly_psf(s["A"], O.eval_basis(s["B"], cc), wls, w, 1.0, m_, s["ps"])
+                return float((G * p).sum())
+            fd.append((-lin(s["c"] + 2 * e) + 8 * lin(s["c"] + e) - 8 * lin(s["c"] - e)
+                       + lin(s["c"] - 2 * e)) / (12 * h))
         fd = np.array(fd)
-        errs["coefficients_fd"] = np.linalg.norm(gc - fd) / np.linalg.norm(fd)
-        print(f"phase retrieval {variant}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
+        errs["coefficients_fd"] = rel(gc, fd)
+        e2e = rel(gc_e2e, gc_ref)
+        print(f"phase retrieval {variant}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items())
+              + f"; end-to-end coefficient gradient {e2e:.2e}")
         for k, v in errs.items():
             assert v < 1e-5, (k, v)
+        assert e2e < 1e-4
     finally:
         dl.set_variant(None)
