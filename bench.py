@@ -464,32 +464,47 @@ def time_e2e(args, gstep, world):
     return dt, h2d, d2h, lat
 
 
-def _serving_tuner():
+# Request streams of the serving workload: "mixed" draws every request's shape from
+# the whole grid (one bucket per (N, M, L) in it); "fixed" sends one shape (512^2
+# pupil, 256^2 PSF, 16 wavelengths), the case where batch shapes repeat and
+# captured CUDA graphs get reused.
+STREAM_SHAPES = {
+    "mixed": dict(pupils=(128, 256, 512, 1024), focals=(64, 128, 256, 512),
+                  min_wavelengths=1, max_wavelengths=64),
+    "fixed": dict(pupils=(512,), focals=(256,), min_wavelengths=16, max_wavelengths=16),
+}
+
+
+def _serving_tuner(shapes="mixed"):
     """The per-(N, M) plan autotuner, tuned once over the stream's shape grid."""
     from dlux_gb300.autotune import PlanTuner
 
     tuner = PlanTuner()
-    grid, secs = tuner.tune_grid((128, 256, 512, 1024), (64, 128, 256, 512))
+    grid, secs = tuner.tune_grid(STREAM_SHAPES[shapes]["pupils"], STREAM_SHAPES[shapes]["focals"])
     from dlux_gb300.autotune import config_label
     return tuner, {"seconds": secs, "cache": tuner.cache_path,
                    "choices": {f"{n}x{m}": config_label(c) for (n, m), c in sorted(grid.items())},
                    "timings": {k: v for k, v in tuner.timings.items()}}
 
 
-def serve_streams(args, variant, rates, n_requests, tuner=None):
+def serve_streams(args, variant, rates, n_requests, tuner=None, shapes="mixed", graphs=True):
     """One server (form `variant`, or the autotuner's per-shape choice), made
     resident for every bucket of the streams, then one seeded Poisson stream per
-    arrival rate in `rates`, timed one after the other. Returns a report per rate."""
+    arrival rate in `rates`, timed one after the other. `shapes` names the request
+    mix (STREAM_SHAPES); `graphs` False launches every batch eagerly, unpadded.
+    Returns a report per rate."""
     import torch
     from dlux_gb300 import serving
 
     srv = serving.PSFServer(max_batch=8, n_slots=args.slots, hbm_budget=150e9, k_max=36,
                             limits=(1024, 512, 64),
                             variant=None if tuner is not None else variant,
-                            tuner=tuner, timeout_s=120.0, graph_after=args.graph_after)
-    streams = [serving.poisson_stream(n_requests, rate, seed=SEED + 10 * i)
+                            tuner=tuner, timeout_s=120.0, graphs=graphs,
+                            graph_after=args.graph_after)
+    mix = STREAM_SHAPES[shapes]
+    streams = [serving.poisson_stream(n_requests, rate, seed=SEED + 10 * i, **mix)
                for i, rate in enumerate(rates)]
-    _, warm = serving.poisson_stream(max(n_requests // 4, 50), rates[0], seed=SEED + 1)
+    _, warm = serving.poisson_stream(max(n_requests // 4, 50), rates[0], seed=SEED + 1, **mix)
     keys = sorted({r.key for _, reqs in streams for r in reqs} | {r.key for r in warm})
     # the warm-up also launches every bucket of the timed streams once (a plan's first
     # launch is not what the stream measures)
@@ -523,7 +538,8 @@ def serve_streams(args, variant, rates, n_requests, tuner=None):
         rep = srv.report(reqs)
         rep.update(variant=variant if tuner is None else "autotuned", rate_hz=rate,
                    requests=n_requests, buckets=len(keys), resident_buckets=resident,
-                   prewarm_s=t_prewarm, clocks=clk)
+                   prewarm_s=t_prewarm, stream_shapes=shapes, graphs=bool(graphs),
+                   clocks=clk)
         out[rate] = rep
     srv.stop()
     srv.close()
@@ -539,7 +555,9 @@ def run_serving(args):
     each of --rates requests/s (default: --rate), one stream per rate. Plans of every
     bucket in the streams are made resident first (within the 150 GB budget); a
     warm-up stream of a different seed runs before the timed ones. Latency is
-    submit -> result on the host (pinned copies included).
+    submit -> result on the host (pinned copies included). --stream-shapes fixed
+    sends one bucket instead (N 512, M 256, L 16), and --no-graphs launches every
+    batch eagerly, so the two together measure what captured graphs are worth.
     """
     rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
     out = {}
@@ -551,9 +569,10 @@ def run_serving(args):
     for variant in variants:
         tuner = None
         if variant == "autotuned":
-            tuner, tuning = _serving_tuner()
+            tuner, tuning = _serving_tuner(args.stream_shapes)
         out[variant] = {f"{r:g}": rep for r, rep in
-                        serve_streams(args, variant, rates, args.requests, tuner).items()}
+                        serve_streams(args, variant, rates, args.requests, tuner,
+                                      args.stream_shapes, not args.no_graphs).items()}
     main_rep = out[main_leg][f"{rates[0]:g}"]
     line = {
         "metric": "served requests/sec (mixed PSF and PSF+grad stream)",
@@ -564,9 +583,11 @@ def run_serving(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16x3-split (fp32 accumulate)" if args.variant == "split_bf16" else "fp32",
         "data": "synthetic (seeded Poisson stream)",
-        "config": {"workload": f"serving: Poisson {rates[0]:g} req/s, N in 128-1024, M in "
-                               "64-512, L in 1..64, K in 4..36, 30% gradients",
+        "config": {"workload": f"serving: Poisson {rates[0]:g} req/s, " + (
+                       "N in 128-1024, M in 64-512, L in 1..64" if args.stream_shapes == "mixed"
+                       else "N 512, M 256, L 16") + ", K in 4..36, 30% gradients",
                    "requests": args.requests, "rates_hz": rates, "max_batch": 8,
+                   "stream_shapes": args.stream_shapes, "graphs": not args.no_graphs,
                    "slots": args.slots, "graph_after": args.graph_after, "hbm_budget_gb": 150},
         "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
         "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
@@ -1022,6 +1043,10 @@ def main():
     ap.add_argument("--fft-n", type=int, default=1024, help="fft: pupil side (pad 2)")
     ap.add_argument("--scene-sources", type=int, default=1024,
                     help="cfg4: point sources (1024 is the measured configuration)")
+    ap.add_argument("--stream-shapes", default="mixed", choices=sorted(STREAM_SHAPES),
+                    help="serving: request shapes (mixed grid, or one fixed bucket)")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="serving: launch every batch eagerly (no CUDA graphs, no padding)")
     ap.add_argument("--graph-after", type=int, default=8,
                     help="serving: capture a batch shape as a CUDA graph after this many uses")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,

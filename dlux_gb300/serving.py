@@ -717,12 +717,14 @@ class CudaExecutor:
 
 def poisson_stream(n_requests, rate_hz, seed, pupils=(128, 256, 512, 1024),
                    focals=(64, 128, 256, 512), max_wavelengths=64, k_range=(4, 36),
-                   grad_fraction=0.3, coeff_sigma=50e-9):
+                   grad_fraction=0.3, coeff_sigma=50e-9, min_wavelengths=1):
     """Seeded request stream: arrival offsets (s) of a Poisson process and the requests.
 
-    Shapes are drawn uniformly from ``pupils`` x ``focals`` x 1..max_wavelengths, the
-    coefficient count uniformly from ``k_range``, coefficients from N(0, coeff_sigma) m;
-    a fraction ``grad_fraction`` asks for gradients with an N(0, 1) cotangent image.
+    Shapes are drawn uniformly from ``pupils`` x ``focals`` x
+    min_wavelengths..max_wavelengths, the coefficient count uniformly from
+    ``k_range``, coefficients from N(0, coeff_sigma) m; a fraction ``grad_fraction``
+    asks for gradients with an N(0, 1) cotangent image. One pupil, one focal side
+    and min_wavelengths == max_wavelengths give a stream of a single bucket.
     """
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate_hz, n_requests)
@@ -731,7 +733,7 @@ def poisson_stream(n_requests, rate_hz, seed, pupils=(128, 256, 512, 1024),
     for _ in range(n_requests):
         n = int(rng.choice(pupils))
         m = int(rng.choice(focals))
-        L = int(rng.integers(1, max_wavelengths + 1))
+        L = int(rng.integers(min_wavelengths, max_wavelengths + 1))
         k = int(rng.integers(k_range[0], k_range[1] + 1))
         grad = bool(rng.random() < grad_fraction)
         g = rng.standard_normal((m, m), dtype=np.float32) if grad else None

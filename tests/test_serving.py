@@ -354,6 +354,13 @@ def test_poisson_stream_is_seeded():
     assert set(ks) <= {128, 256, 512, 1024}
 
 
+def test_fixed_shape_stream_has_one_bucket():
+    _, reqs = poisson_stream(40, 2000.0, seed=5, pupils=(512,), focals=(256,),
+                             min_wavelengths=16, max_wavelengths=16)
+    assert {r.key for r in reqs} == {(512, 256, 16)}
+    assert any(r.want_grad for r in reqs) and not all(r.want_grad for r in reqs)
+
+
 def test_bucket_goes_to_its_home_slot_when_free():
     ex = FakeExecutor(n_slots=3, auto_complete=False)
     srv = PSFServer(executor=ex, max_batch=4, hbm_budget=1e9)
