@@ -229,6 +229,167 @@ class CpuStep:
                 "is not installable here)")
 
 
+def _cpu_block(job):
+    """One block of the other configurations' CPU restatement (complex64 port):
+    the PSF of a block of wavelengths, or with a cotangent its reverse pass."""
+    from oracle import dlux_oracle as O
+    T, opd, wls, weights, m, ps_out, G, offset = job
+    if G is None:
+        return O.poly_psf(T, opd, wls, weights, 1.0, m, ps_out, offset=offset,
+                          precision="c64").astype(np.float32)
+    g = O.poly_psf_grad(T, opd, wls, weights, 1.0, m, ps_out, G, offset=offset,
+                        precision="c64")
+    return {k: np.asarray(v, np.float32) for k, v in g.items()}
+
+
+def cpu_config_baseline(name, workers=None):
+    """cpu_baseline of configurations 1, 3 and 4: the oracle's complex64 port of
+    dLux's op order, timed on the host cores on a bounded sample of the workload.
+
+    cfg1: whole evaluations (1 wavelength, 256^2 -> 128^2, PSF + coefficient
+          gradient) on one core; value in ms per evaluation.
+    cfg3: whole evaluations: forward PSF of all 32 wavelengths, flat field, Poisson
+          NLL and its cotangent, reverse pass of all 32 wavelengths (coefficient,
+          amplitude with the power normalisation's chain rule, and flat-field
+          gradients), wavelength blocks over a spawn pool of single-threaded
+          workers; evals/s.
+    cfg4: the forward and reverse pass of `workers` of the 1024 sources (all 16
+          wavelengths each, one source per worker), scaled to the scene: each
+          source costs the same; evals/s.
+    """
+    import multiprocessing as mp
+    from oracle import dlux_oracle as O
+
+    workers = int(workers or os.cpu_count() or 1)
+    ps = float(O.arcsec2rad(0.02))
+    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS",
+                                            "MKL_NUM_THREADS")}
+    for k in saved:
+        os.environ[k] = "1"
+    try:
+        pool = None if name == "cfg1" else mp.get_context("spawn").Pool(workers)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    try:
+        if name == "cfg1":
+            rng = np.random.default_rng(1)
+            T, B = O.circular_aperture(256, 1.0, oversample=1, secondary_diameter=0.1,
+                                       zernike_nolls=list(range(4, 14)))
+            Teff = (T / np.sqrt((T ** 2).sum())).astype(np.float32)
+            B = B.astype(np.float32)
+            c = rng.normal(0, 50e-9, 10).astype(np.float32)
+            R = rng.normal(size=(128, 128)).astype(np.float32)
+
+            def one():
+                opd = np.tensordot(B, c, axes=(0, 0))
+                psf = _cpu_block((T, opd, [1e-6], [1.0], 128, ps, None, (0.0, 0.0)))
+                g = _cpu_block((Teff, opd, [1e-6], [1.0], 128, ps, R, (0.0, 0.0)))
+                return float((psf * R).sum()), np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+            one()
+            t = []
+            for _ in range(20):
+                t0 = time.perf_counter()
+                one()
+                t.append(time.perf_counter() - t0)
+            return {"value": 1e3 * float(np.median(t)), "unit": "ms", "cores": 1, "kind": "port",
+                    "sample": "20 whole evaluations (median) after one warm-up, one thread; "
+                              "NumPy complex64 restatement of dLux's op order"}
+        if name == "cfg3":
+            rng = np.random.default_rng(3)
+            T, B = O.circular_aperture(512, 1.0, oversample=1, secondary_diameter=0.1,
+                                       zernike_nolls=list(range(4, 40)))
+            A = (T * (1 + rng.normal(0, 0.01, T.shape))).astype(np.float32)
+            B = B.astype(np.float32)
+            c = rng.normal(0, 40e-9, 36).astype(np.float32)
+            flat = (1 + rng.normal(0, 0.02, (256, 256))).astype(np.float32)
+            wls = np.linspace(0.9e-6, 1.1e-6, 32)
+            w = np.full(32, 1.0 / 32)
+            blocks = [b for b in np.array_split(np.arange(32), workers) if len(b)]
+            data = None
+
+            def one():
+                nonlocal data
+                opd = np.tensordot(B, c, axes=(0, 0))
+                s = 1.0 / np.sqrt((A.astype(np.float64) ** 2).sum())
+                Aeff = (A * s).astype(np.float32)
+                psf = np.sum(pool.map(_cpu_block, [(Aeff, opd, wls[b], w[b], 256, ps, None,
+                                                    (0.0, 0.0)) for b in blocks]), axis=0)
+                img = psf * flat * 1e6
+                if data is None:
+                    data = rng.poisson(img).astype(np.float32)
+                loss = float((img - data * np.log(img)).sum())
+                g_img = (1.0 - data / img).astype(np.float32)
+                g_flat = g_img * psf * 1e6
+                G = (g_img * flat * 1e6).astype(np.float32)
+                parts = pool.map(_cpu_block, [(Aeff, opd, wls[b], w[b], 256, ps, G, (0.0, 0.0))
+                                              for b in blocks])
+                g_opd = np.sum([q["g_opd"] for q in parts], axis=0)
+                g_eff = np.sum([q["g_amp"] for q in parts], axis=0)
+                g_A = s * g_eff - s ** 3 * A * float((A * g_eff).sum())
+                g_c = np.tensordot(B, g_opd, axes=((1, 2), (0, 1)))
+                return loss, g_c, g_A, g_flat
+            one()
+            t = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                one()
+                t.append(time.perf_counter() - t0)
+            return {"value": 1.0 / float(np.median(t)), "unit": "evals/s", "cores": workers,
+                    "kind": "port",
+                    "sample": f"3 whole evaluations (median) after one warm-up: 32 wavelengths "
+                              f"in {len(blocks)} blocks over {workers} single-threaded worker "
+                              "processes; NumPy complex64 restatement of dLux's op order"}
+        if name == "cfg4":
+            rng = np.random.default_rng(4)
+            T, B = O.circular_aperture(1024, 1.0, oversample=1, secondary_diameter=0.1,
+                                       zernike_nolls=list(range(4, 25)))
+            Teff = (T / np.sqrt((T ** 2).sum())).astype(np.float32)
+            B = B.astype(np.float32)
+            c = rng.normal(0, 30e-9, 21).astype(np.float32)
+            S = 1024
+            pos = rng.uniform(-2, 2, (S, 2)) * np.pi / 180 / 3600
+            flux = 10 ** rng.uniform(2, 6, S)
+            R = rng.normal(size=(128, 128)).astype(np.float32)
+            wls = np.linspace(0.8e-6, 1.2e-6, 16)
+            w = np.full(16, 1.0 / 16)
+            opd = np.tensordot(B, c, axes=(0, 0))
+            xs = O.coord_xs(1024, 1.0 / 1024)
+            X, Y = np.meshgrid(xs, xs, indexing="xy")
+
+            def sample(srcs):
+                # forward PSF and reverse pass (flux-weighted cotangent) per source
+                fwd = pool.map(_cpu_block, [(T, opd, wls, w, 128, ps, None, tuple(pos[i]))
+                                            for i in srcs])
+                rev = pool.map(_cpu_block, [(Teff, opd, wls, w, 128, ps,
+                                             (flux[i] * R).astype(np.float32), tuple(pos[i]))
+                                            for i in srcs])
+                img = np.sum([flux[i] * f for i, f in zip(srcs, fwd)], axis=0)
+                g_flux = [float((f * R).sum()) for f in fwd]
+                g_pos = [(float((q["g_opd"] * X).sum()), float((q["g_opd"] * Y).sum()))
+                         for q in rev]
+                return img, g_flux, g_pos
+            srcs = list(range(workers))
+            sample(srcs)
+            t0 = time.perf_counter()
+            sample(srcs)
+            dt = time.perf_counter() - t0
+            return {"value": 1.0 / (dt * S / len(srcs)), "unit": "evals/s", "cores": workers,
+                    "kind": "port",
+                    "sample": f"{len(srcs)} of the {S} sources (all 16 wavelengths each, forward "
+                              f"and reverse pass, one source per single-threaded worker "
+                              f"process) after one warm-up, scaled by {S}/{len(srcs)}; NumPy "
+                              "complex64 restatement of dLux's op order"}
+        raise ValueError(name)
+    finally:
+        if pool is not None:
+            pool.close()
+            pool.join()
+
+
 def parity_sample(variant, n_lambda_sample=2):
     """Part of the CPU-baseline leg: the FP64 oracle (the checker) on the same
     wavelength sample at full size, against the public-API step on the GPU for
@@ -525,7 +686,9 @@ def serve_streams(args, variant, rates, n_requests, tuner=None, shapes="mixed", 
         srv.completed.clear()
         srv.stats.clear()
         srv.max_queue = 0
-        srv.ex.counts.clear()
+        srv.loop_gap_max_s = 0.0
+        srv.events.clear()
+        srv.ex.clear_stats()
         clocks = ClockSampler(torch.cuda.current_device())
         clocks.start()
         gc.collect()
@@ -604,8 +767,8 @@ def serving_leg(args):
     --rate) through the autotuned server and the FP32 server; throughput, p50/p99,
     mean batch and CUDA-graph hit rate of each."""
     keys = ("throughput_rps", "p50_ms", "p99_ms", "p99_ms_by_pupil", "p99_queue_ms",
-            "p99_service_ms", "mean_batch", "graph_hit_rate", "graph_captures", "completed",
-            "failed", "slowest")
+            "p99_service_ms", "mean_batch", "graph_hit_rate", "graph_captures",
+            "capture_ms_max", "loop_gap_max_ms", "completed", "failed", "slowest")
     tuner, _ = _serving_tuner()
     out = {"rate_hz": args.rate, "requests": args.serving_requests}
     for name, variant, t in (("split_bf16_autotuned", None, tuner), ("fp32", "fp32", None)):
@@ -1004,7 +1167,8 @@ def run_config(args):
             "data": "synthetic (seeded PCG64)",
             "config": {"workload": f"{args.workload}: {desc}"}, "execution": execution,
             "e2e": e2e, "p50_ms": p50, "p99_ms": p99, "eager_ms_p50": main["ms_p50"],
-            "clocks": main["clocks"], "variants": out}
+            "clocks": main["clocks"], "variants": out,
+            "cpu_baseline": None if args.no_cpu else cpu_config_baseline(args.workload)}
     print(json.dumps(line))
     return 0
 
@@ -1048,7 +1212,8 @@ def main():
     ap.add_argument("--no-graphs", action="store_true",
                     help="serving: launch every batch eagerly (no CUDA graphs, no padding)")
     ap.add_argument("--graph-after", type=int, default=8,
-                    help="serving: capture a batch shape as a CUDA graph after this many uses")
+                    help="serving: a bucket's batches are padded to power-of-two shapes and "
+                         "captured as CUDA graphs after this many launches of the bucket")
     ap.add_argument("--wavelengths", type=int, default=N_WAVELENGTHS,
                     help="wavelength count (64 is the benchmark workload; smaller values "
                          "make the bounded cases used for profiling captures)")

@@ -30,13 +30,16 @@ Execution (``CudaExecutor``):
   pinned staging buffers.
 - A batch is one ``dlx_serve_run`` call: H2D copies, Zernike OPDs, fused
   PSF, reverse pass, coefficient gradient, D2H copies.
-- With graphs on, a batch of R requests (n_grad of them with gradients) is
-  padded to R' = the next power of two and n_grad to the next power of two
-  (at most R'), with zero-weight, zero-cotangent filler objects whose results
-  are dropped. After ``graph_after`` launches of the same (slot, bucket, R',
-  n_grad'), that call is captured as a CUDA graph and replayed from then on.
-  Each bucket has a home slot (a hash of its shape), used whenever it is
-  free, so that a bucket's graphs are found again.
+- With graphs on, a bucket becomes hot after ``graph_after`` launches. A batch
+  of a hot bucket with R requests (n_grad of them with gradients) is padded
+  to R' = the next power of two and n_grad to the next power of two (at most
+  R'), with zero-weight, zero-cotangent filler objects whose results are
+  dropped; the first launch of each (slot, R', n_grad') of the bucket is
+  captured as a CUDA graph, which is replayed from then on. Batches of cold
+  buckets launch directly with their exact shapes, so a stream of many rarely
+  repeated shapes pays neither for padding nor for captures. Each bucket has
+  a home slot (a hash of its shape), used whenever it is free, so that a
+  bucket's graphs are found again.
 - A request's numbers are bit-for-bit the same alone and inside any batch.
   The kernels give each object identical arithmetic and fixed-order
   reductions.
@@ -161,6 +164,11 @@ class PSFServer:
         self.completed = []
         self.stats = collections.Counter()
         self.max_queue = 0
+        # longest time between two scheduler iterations (the thread was busy in a
+        # launch or a capture, or waiting for the interpreter lock)
+        self.loop_gap_max_s = 0.0
+        # host stalls of the scheduler thread over 2 ms: (start, kind, seconds, detail)
+        self.events = collections.deque(maxlen=4096)
         if self.ex.fixed_bytes > self.hbm_budget:
             raise ValueError(f"slot workspaces ({self.ex.fixed_bytes / 1e9:.1f} GB) exceed the "
                              f"HBM budget ({self.hbm_budget / 1e9:.1f} GB)")
@@ -263,7 +271,17 @@ class PSFServer:
     # ---- scheduler loop ----
     def _loop(self):
         self.ex.bind_thread()
+        t_prev = time.perf_counter()
         while self.running:
+            t = time.perf_counter()
+            gap = t - t_prev
+            t_prev = t
+            if gap > self.loop_gap_max_s:
+                self.loop_gap_max_s = gap
+            if gap > 1e-3:
+                self.stats["loop_gaps_over_1ms"] += 1
+                if gap > 2e-3:
+                    self.events.append((t - gap, "loop_gap", gap, None))
             progressed = self._take_inbox()
             progressed |= self._retire()
             progressed |= self._dispatch()
@@ -364,6 +382,9 @@ class PSFServer:
                 r.t_launch = now
             try:
                 self.ex.launch(si, key, self.plans[key], reqs)
+                dt = time.perf_counter() - now
+                if dt > 2e-3:
+                    self.events.append((now, "launch", dt, [si, list(key), len(reqs)]))
             except Exception as e:  # noqa: BLE001 - delivered to the requests
                 for r in reqs:
                     _finish(r, e)
@@ -396,7 +417,11 @@ class PSFServer:
                 self.slots[si] = None
                 continue
             try:
+                tc = time.perf_counter()
                 self.ex.collect(si, reqs)
+                dt = time.perf_counter() - tc
+                if dt > 2e-3:
+                    self.events.append((tc, "collect", dt, [si, list(key), len(reqs)]))
                 err = None
             except Exception as e:  # noqa: BLE001
                 err = e
@@ -424,7 +449,9 @@ class PSFServer:
                "failed": self.stats["failed"] + self.stats["timed_out"],
                "cancelled": self.stats["cancelled"], "batches": self.stats["batches"],
                "plans_created": self.stats["plans_created"], "evicted": self.stats["evicted"],
-               "max_queue": self.max_queue, "resident_gb": self.resident_bytes() / 1e9}
+               "max_queue": self.max_queue, "resident_gb": self.resident_bytes() / 1e9,
+               "loop_gap_max_ms": 1e3 * self.loop_gap_max_s,
+               "loop_gaps_over_1ms": self.stats["loop_gaps_over_1ms"]}
         out.update(self.ex.stats())
         if not done:
             return out
@@ -447,6 +474,12 @@ class PSFServer:
                            "service_ms": round(float(service[i]), 3),
                            "key": list(done[i].key), "grad": done[i].want_grad}
                           for i in worst]
+        # scheduler stalls and graph captures inside the stream (ms after its start)
+        evs = [e for e in list(self.events) + list(getattr(self.ex, "events", []))
+               if t0 <= e[0] <= t1]
+        evs.sort(key=lambda e: -e[2])
+        out["stalls"] = [{"at_ms": round((e[0] - t0) * 1e3, 3), "kind": e[1],
+                          "ms": round(e[2] * 1e3, 3), "detail": e[3]} for e in evs[:40]]
         by_n = collections.defaultdict(list)
         for r, l in zip(done, lat):
             by_n[r.n_pupil].append(l)
@@ -524,8 +557,11 @@ class CudaExecutor:
         self.fixed_bytes = self.n_slots * (self.plan_ws_bytes + self.serve_ws_bytes)
         self.models = {}
         self.graphs = collections.OrderedDict()   # (slot, key, R, G) -> CUDAGraph
-        self.seen = collections.Counter()
+        self.bucket_launches = collections.Counter()
         self.counts = collections.Counter()
+        self.capture_s = 0.0
+        self.capture_max_s = 0.0
+        self.events = collections.deque(maxlen=4096)   # (start, "capture", seconds, detail)
 
     # ---- sizes ----
     def wavelengths(self, L):
@@ -633,7 +669,9 @@ class CudaExecutor:
         slot = self.slots[si]
         n, m, L = key
         G_req = sum(1 for r in reqs if r.want_grad)
-        R, G = self.padded_shape(len(reqs), G_req)
+        self.bucket_launches[key] += 1
+        hot = self.graphs_on and self.bucket_launches[key] >= self.graph_after
+        R, G = self.padded_shape(len(reqs), G_req) if hot else (len(reqs), G_req)
         K = self.k_max
         c = slot.coeffs[:R * K].reshape(R, K)
         c[:] = 0.0
@@ -652,17 +690,17 @@ class CudaExecutor:
         self.counts["padded_objects"] += R - len(reqs)
         gk = (si, key, R, G)
         stream = slot.stream
-        graph = self.graphs.get(gk)
+        graph = self.graphs.get(gk) if hot else None
         with torch.cuda.stream(stream):
             if graph is not None:
                 self.graphs.move_to_end(gk)
                 graph.replay()
                 self.counts["graph_replays"] += 1
             else:
-                self.seen[gk] += 1
                 b = self._batch_struct(slot, key, R, G)
                 plan.attach_workspace(slot.plan_ws)
-                if self.graphs_on and self.seen[gk] >= self.graph_after:
+                if hot:
+                    t0 = time.perf_counter()
                     graph = torch.cuda.CUDAGraph()
                     graph.capture_begin(capture_error_mode="thread_local")
                     try:
@@ -675,6 +713,12 @@ class CudaExecutor:
                         self.graphs.popitem(last=False)
                     self.counts["graph_captures"] += 1
                     graph.replay()
+                    # host time of capture, instantiation and first replay: the
+                    # scheduler thread is busy for this long
+                    dt = time.perf_counter() - t0
+                    self.capture_s += dt
+                    self.capture_max_s = max(self.capture_max_s, dt)
+                    self.events.append((t0, "capture", dt, [si, list(key), R, G]))
                 else:
                     _lib.call("dlx_serve_run", plan.handle, ctypes.byref(b), stream.cuda_stream)
                     self.counts["direct_launches"] += 1
@@ -701,9 +745,17 @@ class CudaExecutor:
     def stats(self):
         total = self.counts["graph_replays"] + self.counts["direct_launches"] + \
             self.counts["graph_captures"]
+        caps = self.counts["graph_captures"]
         return {"graph_hit_rate": self.counts["graph_replays"] / max(total, 1),
-                "graphs": len(self.graphs), "graph_captures": self.counts["graph_captures"],
+                "graphs": len(self.graphs), "graph_captures": caps,
+                "capture_ms_mean": 1e3 * self.capture_s / caps if caps else None,
+                "capture_ms_max": 1e3 * self.capture_max_s if caps else None,
                 "padded_objects": self.counts["padded_objects"]}
+
+    def clear_stats(self):
+        self.counts.clear()
+        self.events.clear()
+        self.capture_s = self.capture_max_s = 0.0
 
     def close(self):
         self.synchronize()

@@ -145,11 +145,24 @@ def test_fft_propagator_is_the_lct_on_the_fft_grid(cuda):
                                rtol=0, atol=1e-6 * np.abs(ref).max())
 
 
-def test_gradient_through_the_propagators(cuda):
+@pytest.mark.parametrize("variant", ["fp32", "split_bf16"])
+def test_gradient_through_the_propagators(cuda, variant):
     """Reverse pass through MFTPropagator and ASMPropagator (the plans'
     adjoints) against central differences of the FP64 oracle, for the
     derivative of sum |out|^2 R along a random phase direction: |d - d_ref| <=
-    1e-5 (|d_ref| + ||g * v||_2), i.e. relative to the size of the sum's terms."""
+    tol (|d_ref| + ||g * v||_2), i.e. relative to the size of the sum's terms.
+    tol is 1e-5, and 3e-5 for the split-BF16 form on this 32-pixel grid, where
+    a transform sums too few terms (K = 32) for the operand splits' rounding to
+    average out (the same bound as the MFT fixtures at K = 32)."""
+    import dlux_gb300 as dl
+    dl.set_variant(variant)
+    try:
+        _gradient_through_the_propagators(1e-5 if variant == "fp32" else 3e-5)
+    finally:
+        dl.set_variant(None)
+
+
+def _gradient_through_the_propagators(tol):
     import dlux_gb300 as dl
     from dlux_gb300.coordinates import CoordSpec, PadSpec
     from dlux_gb300.layers import abcd_propagators as ap
@@ -192,4 +205,4 @@ def test_gradient_through_the_propagators(cuda):
         scale = abs(fd) + float(np.linalg.norm(terms))
         print(f"{type(prop).__name__}: derivative {d:.6e} vs {fd:.6e}, "
               f"{abs(d - fd) / scale:.2e} of scale")
-        assert abs(d - fd) <= 1e-5 * scale, (d, fd)
+        assert abs(d - fd) <= tol * scale, (d, fd)
