@@ -648,11 +648,12 @@ def _serving_tuner(shapes="mixed"):
                    "timings": {k: v for k, v in tuner.timings.items()}}
 
 
-def serve_streams(args, variant, rates, n_requests, tuner=None, shapes="mixed", graphs=True):
+def serve_streams(args, variant, rates, n_requests, tuner=None, shapes="mixed", graphs=False):
     """One server (form `variant`, or the autotuner's per-shape choice), made
     resident for every bucket of the streams, then one seeded Poisson stream per
     arrival rate in `rates`, timed one after the other. `shapes` names the request
-    mix (STREAM_SHAPES); `graphs` False launches every batch eagerly, unpadded.
+    mix (STREAM_SHAPES); `graphs` pads the batches of hot buckets to power-of-two
+    shapes and replays them as CUDA graphs (off: every batch launches directly).
     Returns a report per rate."""
     import torch
     from dlux_gb300 import serving
@@ -719,8 +720,9 @@ def run_serving(args):
     bucket in the streams are made resident first (within the 150 GB budget); a
     warm-up stream of a different seed runs before the timed ones. Latency is
     submit -> result on the host (pinned copies included). --stream-shapes fixed
-    sends one bucket instead (N 512, M 256, L 16), and --no-graphs launches every
-    batch eagerly, so the two together measure what captured graphs are worth.
+    sends one bucket instead (N 512, M 256, L 16), and --graphs replays the
+    batches of hot buckets as CUDA graphs, so the two together measure what
+    captured graphs are worth.
     """
     rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
     out = {}
@@ -735,7 +737,7 @@ def run_serving(args):
             tuner, tuning = _serving_tuner(args.stream_shapes)
         out[variant] = {f"{r:g}": rep for r, rep in
                         serve_streams(args, variant, rates, args.requests, tuner,
-                                      args.stream_shapes, not args.no_graphs).items()}
+                                      args.stream_shapes, args.graphs).items()}
     main_rep = out[main_leg][f"{rates[0]:g}"]
     line = {
         "metric": "served requests/sec (mixed PSF and PSF+grad stream)",
@@ -750,7 +752,7 @@ def run_serving(args):
                        "N in 128-1024, M in 64-512, L in 1..64" if args.stream_shapes == "mixed"
                        else "N 512, M 256, L 16") + ", K in 4..36, 30% gradients",
                    "requests": args.requests, "rates_hz": rates, "max_batch": 8,
-                   "stream_shapes": args.stream_shapes, "graphs": not args.no_graphs,
+                   "stream_shapes": args.stream_shapes, "graphs": args.graphs,
                    "slots": args.slots, "graph_after": args.graph_after, "hbm_budget_gb": 150},
         "p50_ms": main_rep.get("p50_ms"), "p99_ms": main_rep.get("p99_ms"),
         "p99_ms_by_pupil": main_rep.get("p99_ms_by_pupil"),
@@ -1209,8 +1211,9 @@ def main():
                     help="cfg4: point sources (1024 is the measured configuration)")
     ap.add_argument("--stream-shapes", default="mixed", choices=sorted(STREAM_SHAPES),
                     help="serving: request shapes (mixed grid, or one fixed bucket)")
-    ap.add_argument("--no-graphs", action="store_true",
-                    help="serving: launch every batch eagerly (no CUDA graphs, no padding)")
+    ap.add_argument("--graphs", action="store_true",
+                    help="serving: pad the batches of hot buckets to power-of-two shapes and "
+                         "replay them as CUDA graphs (default: every batch launches directly)")
     ap.add_argument("--graph-after", type=int, default=8,
                     help="serving: a bucket's batches are padded to power-of-two shapes and "
                          "captured as CUDA graphs after this many launches of the bucket")

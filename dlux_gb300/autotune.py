@@ -17,6 +17,12 @@ its GEMMs run:
 - ``split_k`` (plans with their own workspace only): whether GEMMs whose
   tiles leave most SMs idle split K, at the count fixed at plan creation.
 
+The tile shapes searched are therefore 128 x 128 on one CTA and 256 x 128 on
+a CTA pair. Narrower tiles are not candidates: on GB300 a tcgen05 MMA with
+N = 64 (or 32) columns takes 50.8 cycles where the full rate would be 32, so
+a 128 x 64 tile spends 1.59x the MMA time per flop; wider tiles do not fit
+the main and cross accumulators in tensor memory.
+
 ``PlanTuner.choose(n, m)`` times each candidate on a probe batch (the
 one-sweep PSF + gradient of ``probe_objects`` objects at ``probe_wavelengths``
 wavelengths) with CUDA events, keeps the fastest, and caches the choice in
@@ -45,7 +51,7 @@ def _tiles(side):
 def candidate_configs(n, m, tensor_cores=True, own_workspace=False):
     """Configurations worth timing for an (n_in, n_out) plan."""
     fp32 = {"variant": "fp32", "operand_mode": 0, "pair": 0, "split_k": 1}
-    if not (tensor_cores and n % 8 == 0 and m % 8 == 0):
+    if not tensor_cores:
         return [fp32]
     out = [{"variant": "split_bf16", "operand_mode": 0, "pair": 0, "split_k": 1}]
     if _tiles(n) % 2 == 0 or _tiles(m) % 2 == 0:

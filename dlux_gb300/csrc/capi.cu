@@ -180,8 +180,13 @@ struct TwoStep {
   DevBuf inv_lambda_ff;        // float2 [b]: 1/lambda as a (hi, lo) pair
   std::vector<double> wl;
 
-  size_t elem_bytes() const { return variant == DLX_VARIANT_SPLIT_BF16 ? 8 : 8; }
-  size_t mat_bytes() const { return (size_t)batch * n_in * n_out * elem_bytes(); }
+  // T layout (rows n_out, cols n_in) or N layout (rows n_in, cols n_out); split
+  // matrices have padded rows (split_ld).
+  size_t mat_bytes(bool t_layout) const {
+    const int rows = t_layout ? n_out : n_in, cols = t_layout ? n_in : n_out;
+    if (variant == DLX_VARIANT_SPLIT_BF16) return split_bytes(batch, rows, cols);
+    return (size_t)batch * rows * cols * sizeof(float2);
+  }
 
   // The tensor-core form streams cached split DFT matrices through TMA, or
   // (operand_mode 1) builds the DFT operand inside the GEMM from `axes`: no
@@ -219,11 +224,11 @@ struct TwoStep {
                        cudaMemcpyHostToDevice);
       if (e != cudaSuccess) { st = check_cuda(e, "cudaMemcpy(axes)"); break; }
       if (!gen_a) {
-        if ((st = atx.alloc(mat_bytes())) != DLX_OK) break;
-        if ((st = anx.alloc(mat_bytes())) != DLX_OK) break;
+        if ((st = atx.alloc(mat_bytes(true))) != DLX_OK) break;
+        if ((st = anx.alloc(mat_bytes(false))) != DLX_OK) break;
         if (!shared_xy) {
-          if ((st = aty.alloc(mat_bytes())) != DLX_OK) break;
-          if ((st = any.alloc(mat_bytes())) != DLX_OK) break;
+          if ((st = aty.alloc(mat_bytes(true))) != DLX_OK) break;
+          if ((st = any.alloc(mat_bytes(false))) != DLX_OK) break;
         }
         const bool split = variant == DLX_VARIANT_SPLIT_BF16;
         auto gen = [&](DevBuf& buf, const DftAxis* ax, bool t_layout) {
@@ -289,14 +294,6 @@ int validate_variant(int variant) {
     return DLX_OK;
   }
   return fail(DLX_ERR_ARG, "variant must be DLX_VARIANT_FP32 or DLX_VARIANT_SPLIT_BF16");
-}
-
-int check_split_shape(int variant, int n_in, int n_out) {
-  if (variant == DLX_VARIANT_SPLIT_BF16 && (n_in % 8 != 0 || n_out % 8 != 0))
-    return fail(DLX_ERR_SHAPE,
-                "the split-BF16 form needs input and output sides that are multiples of 8 "
-                "(TMA row pitch); use DLX_VARIANT_FP32 for other sizes");
-  return DLX_OK;
 }
 
 // Optional CUDA-event timing of every GEMM launch (dlx_gemm_timing_*), used
@@ -404,10 +401,14 @@ struct TwoStepPlan {
 
   int alloc_buffers() {
     const size_t b = ts.batch, ni = ts.n_in, no = ts.n_out;
-    DLX_TRY(mid.alloc(b * ni * no * 8));
     if (ts.variant == DLX_VARIANT_SPLIT_BF16) {
-      DLX_TRY(in_split.alloc(b * ni * ni * 8));
-      DLX_TRY(gout_split.alloc(b * no * no * 8));
+      // split planes with padded rows: D1 [b][4][n_out][n_in], Xt [b][4][n_in][n_out]
+      const size_t m1 = split_bytes(b, ts.n_out, ts.n_in), m2 = split_bytes(b, ts.n_in, ts.n_out);
+      DLX_TRY(mid.alloc(m1 > m2 ? m1 : m2));
+      DLX_TRY(in_split.alloc(split_bytes(b, ts.n_in, ts.n_in)));
+      DLX_TRY(gout_split.alloc(split_bytes(b, ts.n_out, ts.n_out)));
+    } else {
+      DLX_TRY(mid.alloc(b * ni * no * 8));
     }
     return DLX_OK;
   }
@@ -415,8 +416,8 @@ struct TwoStepPlan {
     const int B = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     const void* field = in;
     if (v == DLX_VARIANT_SPLIT_BF16) {
-      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(in), (long long)N * N,
-                                          B, in_split.as<__nv_bfloat16>(), s));
+      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(in), N, N, B,
+                                          in_split.as<__nv_bfloat16>(), s));
       field = in_split.p;
     }
     // D1[u][y] = sum_x AxT[u][x] E[y][x]
@@ -431,9 +432,8 @@ struct TwoStepPlan {
     const int B = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     const void* g = gout;
     if (v == DLX_VARIANT_SPLIT_BF16) {
-      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(gout),
-                                          (long long)M * M, B, gout_split.as<__nv_bfloat16>(),
-                                          s));
+      DLX_TRY(launch_c64_to_split_batched(reinterpret_cast<const float2*>(gout), M, M, B,
+                                          gout_split.as<__nv_bfloat16>(), s));
       g = gout_split.p;
     }
     // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
@@ -543,7 +543,6 @@ int dlx_mft_plan_create(const dlx_mft_desc* d, const double* wl, dlx_mft_plan* p
     return fail(DLX_ERR_ARG, "mft_plan_create: pixel scales must be positive");
   DLX_TRY(check_focal(d->focal_length, "mft_plan_create"));
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
   auto* p = new (std::nothrow) dlx_mft_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   TwoStep& ts = p->p.ts;
@@ -630,7 +629,6 @@ int dlx_fft_plan_create(const dlx_fft_desc* d, const double* wl, dlx_fft_plan* p
     return DLX_OK;
   }
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, d->n_in, fft_out_side(d->n_in, d->pad)));
   auto* p = new (std::nothrow) dlx_fft_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   TwoStep& ts = p->p.ts;
@@ -1080,9 +1078,12 @@ constexpr int kPolyBuffers = 7;
 static void poly_ws_sizes(int L, int N, int M, int R, int nparts, bool split_on,
                           size_t sz[kPolyBuffers]) {
   const size_t lr = (size_t)L * R, n = N, m = M;
-  sz[0] = lr * n * n * 8;
-  sz[1] = lr * n * m * 8;
-  sz[2] = lr * m * m * 8;
+  // complex64 planes, or split planes with padded rows (split_ld), whichever
+  // is larger: E [N][N], D1 [M][N] or Xt [N][M], F-bar [M][M]
+  sz[0] = split_bytes(lr, N, N);
+  const size_t d1 = split_bytes(lr, M, N), xt = split_bytes(lr, N, M);
+  sz[1] = d1 > xt ? d1 : xt;
+  sz[2] = split_bytes(lr, M, M);
   const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
   sz[3] = a > b ? a : b;
   sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
@@ -1119,7 +1120,6 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
     return fail(DLX_ERR_ARG, "poly_plan_create: pixel scales must be positive");
   DLX_TRY(check_focal(d->focal_length, "poly_plan_create"));
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
   auto* p = new (std::nothrow) dlx_poly_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   const int L = d->n_wavelengths, N = d->n_in, M = d->n_out;
@@ -1406,7 +1406,6 @@ int dlx_xform_plan_create(const dlx_xform_desc* d, const dlx_xform_axis* ax_x,
   if (d->batch <= 0 || d->n_in <= 0 || d->n_out <= 0)
     return fail(DLX_ERR_SHAPE, "xform_plan_create: batch, n_in and n_out must be positive");
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, d->n_in, d->n_out));
   auto* p = new (std::nothrow) dlx_xform_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   std::vector<DftAxis> ax(d->batch), ay(d->batch);
@@ -1454,7 +1453,6 @@ int dlx_asm_plan_create(const dlx_asm_desc* d, const double* wavelengths_host,
     if (!(wavelengths_host[b] > 0))
       return fail(DLX_ERR_ARG, "asm_plan_create: wavelengths must be positive");
   DLX_TRY(validate_variant(d->variant));
-  DLX_TRY(check_split_shape(d->variant, N, P));
   auto* p = new (std::nothrow) dlx_asm_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");
   p->P = P;

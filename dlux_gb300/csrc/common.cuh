@@ -171,12 +171,19 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 
 inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
-// Split operand layout: [batch][4][rows][cols] bf16, planes = re_hi, re_lo, im_hi, im_lo.
-struct SplitView {
-  __nv_bfloat16* p;
-  int rows, cols;
-  __host__ __device__ long long plane() const { return (long long)rows * cols; }
-  __host__ __device__ long long batch_stride() const { return 4LL * rows * cols; }
-};
+// Split operand layout: [batch][4][rows][split_ld(cols)] bf16, planes = re_hi,
+// re_lo, im_hi, im_lo. TMA needs row pitches that are multiples of 16 bytes,
+// so a row of `cols` elements is padded to a multiple of 8. The padding is
+// never written and never read: the tensor maps declare `cols` as the extent
+// along K and fill the columns past it with zeros. For sides that are
+// multiples of 8 the layout is dense.
+__host__ __device__ __forceinline__ int split_ld(int cols) { return (cols + 7) & ~7; }
+__host__ __device__ __forceinline__ long long split_plane(int rows, int cols) {
+  return (long long)rows * split_ld(cols);
+}
+// Bytes of `batch` split operands of rows x cols.
+inline size_t split_bytes(long long batch, int rows, int cols) {
+  return (size_t)batch * 4 * (size_t)split_plane(rows, cols) * 2;
+}
 
 }  // namespace dlx

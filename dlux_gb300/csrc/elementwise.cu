@@ -35,8 +35,8 @@ __global__ void dft_gen_kernel(const DftAxis* __restrict__ axes, int rows, int c
   const long long idx = (long long)r * cols + c;
   if (out_c64) out_c64[(long long)b * out_bs + idx] = v;
   if (out_split) {
-    const long long plane = (long long)rows * cols;
-    __nv_bfloat16* base = out_split + (long long)b * 4 * plane + idx;
+    const long long plane = split_plane(rows, cols);
+    __nv_bfloat16* base = out_split + (long long)b * 4 * plane + (long long)r * split_ld(cols) + c;
     __nv_bfloat16 h, l;
     split_bf16(v.x, h, l);
     base[0] = h;
@@ -124,14 +124,17 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
       if (a.in) v = cmul(a.in[o], v);
       if (a.out_c64) a.out_c64[o] = v;
       if (a.out_split) {
-        __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p;
+        // padded rows (split_ld)
+        const long long splane = split_plane(a.n, a.n);
+        __nv_bfloat16* base =
+            a.out_split + (long long)b * 4 * splane + (long long)y * split_ld(a.n) + x;
         __nv_bfloat16 h, lo;
         split_bf16(v.x, h, lo);
         base[0] = h;
-        base[npix] = lo;
+        base[splane] = lo;
         split_bf16(v.y, h, lo);
-        base[2 * npix] = h;
-        base[3 * npix] = lo;
+        base[2 * splane] = h;
+        base[3 * splane] = lo;
       }
     }
   }
@@ -143,7 +146,8 @@ struct alignas(2 * V) Bf16Vec {
 };
 
 // Split-BF16 output only, V adjacent pixels of one row per thread (n % V ==
-// 0): each of the four planes gets one 2V-byte store per thread and
+// 0, so that with rows padded to split_ld(n) every store is aligned): each of
+// the four planes gets one 2V-byte store per thread and
 // wavelength, and the per-pixel FP64 path set-up is amortised over a
 // wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg)). Same
 // arithmetic per pixel as phasor_kernel.
@@ -213,9 +217,11 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
         split_bf16(u.x * sc, q[0].v[k], q[1].v[k]);
         split_bf16(u.y * sc, q[2].v[k], q[3].v[k]);
       }
-      __nv_bfloat16* base = a.out_split + (long long)b * 4 * npix + p0;
+      const long long splane = split_plane(a.n, a.n);
+      __nv_bfloat16* base =
+          a.out_split + (long long)b * 4 * splane + (long long)y * split_ld(a.n) + x0;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Vec<V>*>(base + c * npix) = q[c];
+      for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Vec<V>*>(base + c * splane) = q[c];
     }
   }
 }
@@ -253,29 +259,34 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
   return DLX_OK;
 }
 
-// c64 [b][plane] -> split [b][4][plane]: the batch is folded into the
-// element count because the split planes of batch b start at 4 * b * plane.
-__global__ void c64_to_split_kernel(const float2* __restrict__ in, long long plane, int batch,
+// c64 [b][rows][cols] -> split [b][4][rows][split_ld(cols)], one element
+// per thread over a plane, the batch looped inside the thread.
+__global__ void c64_to_split_kernel(const float2* __restrict__ in, int rows, int cols, int batch,
                                     __nv_bfloat16* __restrict__ out) {
+  const long long plane = (long long)rows * cols;
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= plane) return;
+  const long long splane = split_plane(rows, cols);
+  const int r = (int)(p / cols);
+  const long long sp = (long long)r * split_ld(cols) + (p - (long long)r * cols);
   for (int b = 0; b < batch; ++b) {
-    __nv_bfloat16* base = out + (long long)b * 4 * plane;
+    __nv_bfloat16* base = out + (long long)b * 4 * splane;
     float2 v = in[(long long)b * plane + p];
     __nv_bfloat16 h, l;
     split_bf16(v.x, h, l);
-    base[p] = h;
-    base[plane + p] = l;
+    base[sp] = h;
+    base[splane + sp] = l;
     split_bf16(v.y, h, l);
-    base[2 * plane + p] = h;
-    base[3 * plane + p] = l;
+    base[2 * splane + sp] = h;
+    base[3 * splane + sp] = l;
   }
 }
 
-int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
+int launch_c64_to_split_batched(const float2* in, int rows, int cols, int batch,
                                 __nv_bfloat16* out_split, cudaStream_t s) {
+  const long long plane = (long long)rows * cols;
   if (plane == 0 || batch == 0) return DLX_OK;
-  c64_to_split_kernel<<<ceil_div(plane, 256), 256, 0, s>>>(in, plane, batch, out_split);
+  c64_to_split_kernel<<<ceil_div(plane, 256), 256, 0, s>>>(in, rows, cols, batch, out_split);
   DLX_LAUNCH_CHECK("c64_to_split_kernel");
   return DLX_OK;
 }

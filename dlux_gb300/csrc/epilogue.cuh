@@ -53,13 +53,14 @@ __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int l, int
   return cis_ff(path, FF{il.x, il.y}, ph);
 }
 
-// F-bar input of EPI_DOT: split planes (hi + lo) or complex64.
+// F-bar input of EPI_DOT: split planes (hi + lo) at split index sidx of planes
+// of splane elements, or complex64 at dense index idx of planes of plane elements.
 __device__ __forceinline__ float2 epi_read_in(const EpiArgs& e, int b, long long plane,
-                                              long long idx) {
+                                              long long idx, long long splane, long long sidx) {
   if (e.in_split) {
-    const __nv_bfloat16* p = e.in_split + (long long)b * 4 * plane + idx;
-    return make_float2(__bfloat162float(p[0]) + __bfloat162float(p[plane]),
-                       __bfloat162float(p[2 * plane]) + __bfloat162float(p[3 * plane]));
+    const __nv_bfloat16* p = e.in_split + (long long)b * 4 * splane + sidx;
+    return make_float2(__bfloat162float(p[0]) + __bfloat162float(p[splane]),
+                       __bfloat162float(p[2 * splane]) + __bfloat162float(p[3 * splane]));
   }
   return e.in_c64[(long long)b * plane + idx];
 }
@@ -102,6 +103,9 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
   const float a = e.alpha ? e.alpha[l] : 1.0f;
   const long long plane = (long long)M * N;
   const long long idx = (long long)m * N + n;
+  // split outputs and inputs have padded rows (split_ld)
+  const long long splane = split_plane(M, N);
+  const long long sidx = (long long)m * split_ld(N) + n;
   if (e.coltilt && (e.kind == EPI_C64 || e.kind == EPI_SPLIT || e.kind == EPI_SPLIT2)) {
     v = ctilt(e.coltilt[(long long)b * N + n], v.x, v.y);
   }
@@ -111,7 +115,8 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       break;
     }
     case EPI_SPLIT: {
-      store_split(e.out_split + (long long)b * 4 * plane, plane, idx, make_float2(a * v.x, a * v.y));
+      store_split(e.out_split + (long long)b * 4 * splane, splane, sidx,
+                  make_float2(a * v.x, a * v.y));
       break;
     }
     case EPI_INTENSITY: {
@@ -124,7 +129,7 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
         e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
       epi_gradf_value(e, b, r, a, idx, v);
       if (e.out_split)
-        store_split(e.out_split + (long long)b * 4 * plane, plane, idx, v);
+        store_split(e.out_split + (long long)b * 4 * splane, splane, sidx, v);
       else
         e.out_c64[(long long)b * plane + idx] = v;
       break;
@@ -137,8 +142,8 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       const float2 av = make_float2(a * v.x, a * v.y);
       const float w = e.colw[n];
       if (e.out_split) {
-        store_split(e.out_split + (long long)b * 4 * plane, plane, idx, av);
-        store_split(e.out_split2 + (long long)b * 4 * plane, plane, idx,
+        store_split(e.out_split + (long long)b * 4 * splane, splane, sidx, av);
+        store_split(e.out_split2 + (long long)b * 4 * splane, splane, sidx,
                     make_float2(w * av.x, w * av.y));
       } else {
         e.out_c64[(long long)b * plane + idx] = av;
@@ -147,7 +152,7 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       break;
     }
     case EPI_DOT: {
-      const float2 fb = epi_read_in(e, b, plane, idx);
+      const float2 fb = epi_read_in(e, b, plane, idx, splane, sidx);
       e.out_f32[(long long)b * plane + idx] = e.kf[l] * a * (fb.y * v.x - fb.x * v.y);
       break;
     }
@@ -174,6 +179,10 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
   const long long plane = (long long)M * N;
   const int mc = M - m0 < 32 ? M - m0 : 32;
   const long long idx0 = (long long)m0 * N + n;
+  // split outputs and inputs have padded rows (split_ld)
+  const int ld = split_ld(N);
+  const long long splane = (long long)M * ld;
+  const long long sidx0 = (long long)m0 * ld + n;
   switch (KIND >= 0 ? KIND : e.kind) {
     case EPI_C64:
     case EPI_SPLIT: {
@@ -189,10 +198,10 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
         for (int j = 0; j < 32; ++j)
           if (j < mc) o[(long long)j * N] = ctilt(t, re[j], im[j]);
       } else {
-        __nv_bfloat16* o = e.out_split + (long long)b * 4 * plane + idx0;
+        __nv_bfloat16* o = e.out_split + (long long)b * 4 * splane + sidx0;
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          if (j < mc) store_split(o, plane, (long long)j * N, ctilt(t, re[j], im[j]));
+          if (j < mc) store_split(o, splane, (long long)j * ld, ctilt(t, re[j], im[j]));
       }
       break;
     }
@@ -228,8 +237,8 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
             const float gj = s * g[j];
             const float2 v = make_float2(gj * re[h + j], gj * im[h + j]);
             if (e.out_split)
-              store_split(e.out_split + (long long)b * 4 * plane + idx0, plane,
-                          (long long)(h + j) * N, v);
+              store_split(e.out_split + (long long)b * 4 * splane + sidx0, splane,
+                          (long long)(h + j) * ld, v);
             else
               e.out_c64[(long long)b * plane + idx0 + (long long)(h + j) * N] = v;
           }
@@ -246,8 +255,9 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
           const float2 av = ctilt(t, a * re[j], a * im[j]);
           const long long o = idx0 + (long long)j * N;
           if (e.out_split) {
-            store_split(e.out_split + (long long)b * 4 * plane, plane, o, av);
-            store_split(e.out_split2 + (long long)b * 4 * plane, plane, o,
+            const long long so = sidx0 + (long long)j * ld;
+            store_split(e.out_split + (long long)b * 4 * splane, splane, so, av);
+            store_split(e.out_split2 + (long long)b * 4 * splane, splane, so,
                         make_float2(w * av.x, w * av.y));
           } else {
             e.out_c64[(long long)b * plane + o] = av;
@@ -265,7 +275,8 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
         float2 fb[8];
 #pragma unroll
         for (int t = 0; t < 8; ++t)
-          fb[t] = j0 + t < mc ? epi_read_in(e, b, plane, idx0 + (long long)(j0 + t) * N)
+          fb[t] = j0 + t < mc ? epi_read_in(e, b, plane, idx0 + (long long)(j0 + t) * N, splane,
+                                            sidx0 + (long long)(j0 + t) * ld)
                               : make_float2(0.f, 0.f);
 #pragma unroll
         for (int t = 0; t < 8; ++t)

@@ -1161,10 +1161,13 @@ TcDevice* tc_device() {
 
 // Operand tiles are 64-byte rows (32 K elements); L2 promotion of 128 bytes
 // measured 1.9% faster per GEMM launch than 256 bytes at 512 x 512 x 512 x 64.
+// Split operand [nbatch][4][rows][split_ld(K)]: the extent along K is K, so
+// TMA fills the padded columns (and a last K block past K) with zeros.
 int encode_split(CUtensorMap* map, const __nv_bfloat16* base, int rows, int K, int nbatch,
                  int box_rows) {
+  const cuuint64_t ld = (cuuint64_t)split_ld(K);
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)nbatch * 4};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)rows * K * 2};
+  cuuint64_t strides[2] = {ld * 2, (cuuint64_t)rows * ld * 2};
   cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<__nv_bfloat16*>(base),
@@ -1222,8 +1225,7 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   const int num_sms = dev->num_sms;
   const unsigned long long wait_ns = g_wait_ns.load();
   if (g.batch <= 0 || g.M <= 0 || g.N <= 0) return DLX_OK;
-  if (g.K % 8 != 0 || g.N % 8 != 0)
-    return fail(DLX_ERR_SHAPE, "split-BF16 GEMM needs K and N to be multiples of 8");
+  if (g.K <= 0) return fail(DLX_ERR_SHAPE, "split-BF16 GEMM: inner size must be positive");
   const int div = g.a_batch_div > 0 ? g.a_batch_div : 1;
   const int bdiv = g.b_batch_div > 0 ? g.b_batch_div : 1;
   const int nB = (g.batch + bdiv - 1) / bdiv;

@@ -81,7 +81,7 @@ struct PhasorArgs {
 };
 int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream_t s);
 
-int launch_c64_to_split_batched(const float2* in, long long plane, int batch,
+int launch_c64_to_split_batched(const float2* in, int rows, int cols, int batch,
                                 __nv_bfloat16* out_split, cudaStream_t s);
 int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cudaStream_t s);
 int launch_power_scale(const float2* in, int batch, long long npix, double value, float* out,

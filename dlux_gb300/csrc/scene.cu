@@ -44,7 +44,7 @@ __global__ void scene_xtable_kernel(int n, double a, double b, float2* out) {
 // A0[l][j][i] = exp(-2 pi i x_i u_lj), u_lj = a_out[l] j + b_out[l]: the untilted
 // DFT matrix of every wavelength (the same for both axes), reduced exactly in
 // FP32 pairs (cis_ff). Written as c64 and, for the tensor-core form, as split
-// planes [l][4][j][i].
+// planes [l][4][j][split_ld(N)].
 __global__ void scene_a0_kernel(int M, int N, const float2* __restrict__ xin,
                                 const double* __restrict__ a_out,
                                 const double* __restrict__ b_out, float2* __restrict__ a0,
@@ -61,14 +61,15 @@ __global__ void scene_a0_kernel(int M, int N, const float2* __restrict__ xin,
   const float2 v = make_float2(c.x, -c.y);  // forward transform: exp(-2 pi i t)
   a0[(long long)l * mn + p] = v;
   if (a0s) {
-    __nv_bfloat16* base = a0s + (long long)l * 4 * mn + p;
+    const long long smn = split_plane(M, N);
+    __nv_bfloat16* base = a0s + (long long)l * 4 * smn + (long long)j * split_ld(N) + i;
     __nv_bfloat16 h, lo;
     split_bf16(v.x, h, lo);
     base[0] = h;
-    base[mn] = lo;
+    base[smn] = lo;
     split_bf16(v.y, h, lo);
-    base[2 * mn] = h;
-    base[3 * mn] = lo;
+    base[2 * smn] = h;
+    base[3 * smn] = lo;
   }
 }
 
@@ -99,7 +100,8 @@ struct alignas(8) Bf16x4 {
 // A'x[b][j][i] = A0[l][j][i] tx[b][i] for the sources r0 .. r0 + rg - 1 of
 // wavelength l = blockIdx.y (r0 = blockIdx.z rg): a store-bound pass, each
 // thread holding V consecutive elements of one matrix row (V = 4 needs N % 4 == 0)
-// and reusing its A0 values for every source of the group.
+// and reusing its A0 values for every source of the group. Split rows are
+// padded to split_ld(N).
 template <int V>
 __global__ void scene_ax_kernel(int M, int N, int Rc, int rg, const float2* __restrict__ a0,
                                 const float2* __restrict__ tx, __nv_bfloat16* __restrict__ ax_s,
@@ -109,7 +111,9 @@ __global__ void scene_ax_kernel(int M, int N, int Rc, int rg, const float2* __re
   const int l = blockIdx.y;
   const int r0 = blockIdx.z * rg;
   if (p0 >= mn) return;
-  const int i0 = (int)(p0 % N);
+  const int j0 = (int)(p0 / N);
+  const int i0 = (int)(p0 - (long long)j0 * N);
+  const long long smn = split_plane(M, N);
   float2 a[V];
 #pragma unroll
   for (int k = 0; k < V; ++k) a[k] = a0[(long long)l * mn + p0 + k];
@@ -126,15 +130,15 @@ __global__ void scene_ax_kernel(int M, int N, int Rc, int rg, const float2* __re
         split_bf16(v[k].x, q[0].v[k], q[1].v[k]);
         split_bf16(v[k].y, q[2].v[k], q[3].v[k]);
       }
-      __nv_bfloat16* base = ax_s + b * 4 * mn + p0;
+      __nv_bfloat16* base = ax_s + b * 4 * smn + (long long)j0 * split_ld(N) + i0;
       if (V == 4) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16x4*>(base + c * mn) = q[c];
+        for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16x4*>(base + c * smn) = q[c];
       } else {
 #pragma unroll
         for (int c = 0; c < 4; ++c)
 #pragma unroll
-          for (int k = 0; k < V; ++k) base[c * mn + k] = q[c].v[k];
+          for (int k = 0; k < V; ++k) base[c * smn + k] = q[c].v[k];
       }
     } else {
 #pragma unroll
@@ -168,13 +172,16 @@ __global__ void scene_field_kernel(int n, int L, double pixel_scale, const float
     const float2 v = make_float2(u.x * a, u.y * a);
     const float2 w = make_float2(v.x * X, v.y * X);
     if (e_s) {
-      __nv_bfloat16* b0 = e_s + (long long)l * 4 * npix + p;
-      __nv_bfloat16* b1 = ex_s + (long long)l * 4 * npix + p;
+      // split rows padded to split_ld(n)
+      const long long sp = split_plane(n, n);
+      const long long o = (long long)l * 4 * sp + (long long)y * split_ld(n) + x;
+      __nv_bfloat16* b0 = e_s + o;
+      __nv_bfloat16* b1 = ex_s + o;
       __nv_bfloat16 h, lo;
-      split_bf16(v.x, h, lo); b0[0] = h; b0[npix] = lo;
-      split_bf16(v.y, h, lo); b0[2 * npix] = h; b0[3 * npix] = lo;
-      split_bf16(w.x, h, lo); b1[0] = h; b1[npix] = lo;
-      split_bf16(w.y, h, lo); b1[2 * npix] = h; b1[3 * npix] = lo;
+      split_bf16(v.x, h, lo); b0[0] = h; b0[sp] = lo;
+      split_bf16(v.y, h, lo); b0[2 * sp] = h; b0[3 * sp] = lo;
+      split_bf16(w.x, h, lo); b1[0] = h; b1[sp] = lo;
+      split_bf16(w.y, h, lo); b1[2 * sp] = h; b1[3 * sp] = lo;
     } else {
       e_c[(long long)l * npix + p] = v;
       ex_c[(long long)l * npix + p] = w;
@@ -290,14 +297,13 @@ struct dlx_scene_plan_s {
   // half-transformed fields, M x N per source and wavelength), so that the
   // backward starts from them instead of repeating the first GEMM; it still
   // recomputes the focal field from D1.
-  Buf retain;  // per chunk: D1 [R L][M][N] then Y.D1, complex (elem() bytes each)
+  Buf retain;  // per chunk: D1 [R L][M][N] then Y.D1 (chunk_bytes())
   size_t retain_limit = (size_t)48 << 30;
   unsigned long long epoch = 0, fwd_token = 0, reuse_req = 0;
   const void* fwd_in[6] = {};
   int fwd_S = 0;
 
   bool split() const { return variant == DLX_VARIANT_SPLIT_BF16; }
-  size_t elem() const { return 8; }  // bytes per complex element (split planes or c64)
 
   void release() {
     for (Buf* b : {&alpha, &kf, &a_out, &b_out, &inv_fringe, &inv_lambda_ff, &xin, &yw, &a0,
@@ -385,7 +391,8 @@ struct dlx_scene_plan_s {
   // The shared y-axis matrix of every wavelength (A operand, batch divisor Rc).
   const void* ay0() const { return split() ? a0s.p : a0.p; }
 
-  size_t chunk_bytes() const { return 2 * (size_t)R * L * M * N * elem(); }
+  // one chunk of retained D1 and Y.D1 ([R L][M][N] each, split rows padded)
+  size_t chunk_bytes() const { return 2 * split_bytes((long long)R * L, M, N); }
   void* keep_d1(int c) const { return retain.as<char>() + (size_t)c * chunk_bytes(); }
   void* keep_d1y(int c) const { return static_cast<char*>(keep_d1(c)) + chunk_bytes() / 2; }
 
@@ -578,17 +585,18 @@ int scene_create(const dlx_scene_desc* d, const double* wl, dlx_scene_plan_s* p)
   DLX_LAUNCH_CHECK("scene_xtable_kernel");
   const size_t B = (size_t)R * L, nn = (size_t)N * N, mn = (size_t)M * N, mm = (size_t)M * M;
   DLX_TRY(p->a0.alloc(L * mn * sizeof(float2)));
-  if (p->split()) DLX_TRY(p->a0s.alloc(L * mn * 4 * sizeof(__nv_bfloat16)));
+  if (p->split()) DLX_TRY(p->a0s.alloc(split_bytes(L, M, N)));
   scene_a0_kernel<<<dim3(ceil_div((long long)mn, 256), L), 256>>>(
       M, N, p->xin.as<float2>(), p->a_out.as<double>(), p->b_out.as<double>(),
       p->a0.as<float2>(), p->split() ? p->a0s.as<__nv_bfloat16>() : nullptr);
   DLX_LAUNCH_CHECK("scene_a0_kernel");
-  DLX_TRY(p->e.alloc(L * nn * p->elem()));
-  DLX_TRY(p->ex.alloc(L * nn * p->elem()));
-  DLX_TRY(p->ax.alloc(B * mn * p->elem()));
-  DLX_TRY(p->d1.alloc(B * mn * p->elem()));
-  DLX_TRY(p->d1y.alloc(B * mn * p->elem()));
-  DLX_TRY(p->fbar.alloc(B * mm * p->elem()));
+  // complex64, or split planes with padded rows (at least as large)
+  DLX_TRY(p->e.alloc(split_bytes(L, N, N)));
+  DLX_TRY(p->ex.alloc(split_bytes(L, N, N)));
+  DLX_TRY(p->ax.alloc(split_bytes(B, M, N)));
+  DLX_TRY(p->d1.alloc(split_bytes(B, M, N)));
+  DLX_TRY(p->d1y.alloc(split_bytes(B, M, N)));
+  DLX_TRY(p->fbar.alloc(split_bytes(B, M, M)));
   DLX_TRY(p->planes.alloc(B * mm * sizeof(float)));
   DLX_TRY(p->tx.alloc(B * N * sizeof(float2)));
   DLX_TRY(p->ty.alloc(B * N * sizeof(float2)));
@@ -619,8 +627,6 @@ int dlx_scene_plan_create(const dlx_scene_desc* d, const double* wavelengths,
   if (d->variant == DLX_VARIANT_SPLIT_BF16) {
     if (!tc_supported())
       return fail(DLX_ERR_UNSUPPORTED, "the split-BF16 form needs an sm_103a (GB300) device");
-    if (d->n_in % 8 != 0 || d->n_out % 8 != 0)
-      return fail(DLX_ERR_SHAPE, "scene_plan_create: the split-BF16 form needs sides divisible by 8");
   }
   auto* p = new (std::nothrow) dlx_scene_plan_s();
   if (!p) return fail(DLX_ERR_NOMEM, "host allocation failed");

@@ -50,8 +50,9 @@ def fft_out_side(n_in: int, pad: int) -> int:
 def resolve_variant(n_in: int, n_out: int, variant: str | None = None) -> int:
     """Integer variant for a transform of the given sides.
 
-    Automatic choice: the split-BF16 tensor-core form on sm_103a when both sides
-    are multiples of 8 (the TMA row-pitch rule), the FP32 form otherwise.
+    Automatic choice: the split-BF16 tensor-core form on sm_103a (split operands
+    pad their rows to a multiple of 8 elements, so every side runs on the tensor
+    cores), the FP32 form otherwise.
     """
     v = variant if variant is not None else _default_variant
     if isinstance(v, int) and v in (_lib.VARIANT_FP32, _lib.VARIANT_SPLIT_BF16):
@@ -60,7 +61,7 @@ def resolve_variant(n_in: int, n_out: int, variant: str | None = None) -> int:
         return _lib.VARIANT_FP32
     if v == "split_bf16":
         return _lib.VARIANT_SPLIT_BF16
-    if tensor_core_available() and n_in % 8 == 0 and n_out % 8 == 0:
+    if tensor_core_available():
         return _lib.VARIANT_SPLIT_BF16
     return _lib.VARIANT_FP32
 

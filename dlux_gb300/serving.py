@@ -34,12 +34,15 @@ Execution (``CudaExecutor``):
   of a hot bucket with R requests (n_grad of them with gradients) is padded
   to R' = the next power of two and n_grad to the next power of two (at most
   R'), with zero-weight, zero-cotangent filler objects whose results are
-  dropped; the first launch of each (slot, R', n_grad') of the bucket is
-  captured as a CUDA graph, which is replayed from then on. Batches of cold
-  buckets launch directly with their exact shapes, so a stream of many rarely
-  repeated shapes pays neither for padding nor for captures. Each bucket has
-  a home slot (a hash of its shape), used whenever it is free, so that a
-  bucket's graphs are found again.
+  dropped; after ``graph_after`` launches of the same (slot, bucket, R',
+  n_grad') that call is captured as a CUDA graph and replayed from then on.
+  Batches of cold buckets launch directly with their exact shapes, so a
+  stream of many rarely repeated shapes pays neither for padding nor for
+  captures. Each bucket has a home slot (a hash of its shape), used whenever
+  it is free, so that a bucket's graphs are found again. Graphs are off by
+  default: the batches are long enough (a few hundred microseconds of GPU
+  work and more) that the launch overhead a graph saves is smaller than what
+  padding and captures cost under load.
 - A request's numbers are bit-for-bit the same alone and inside any batch.
   The kernels give each object identical arithmetic and fixed-order
   reductions.
@@ -526,7 +529,7 @@ class CudaExecutor:
 
     def __init__(self, max_batch=8, k_max=36, limits=(1024, 512, 64), n_slots=4,
                  diameter=1.0, psf_pixel_scale=0.02, band=DEFAULT_BAND, variant=None,
-                 operand_mode=0, graphs=True, graph_after=2, max_graphs=512, device=None,
+                 operand_mode=0, graphs=False, graph_after=2, max_graphs=512, device=None,
                  tuner=None, pad_batches=None):
         _lib.require_cuda()
         self.device = torch.device(device) if device is not None else \
@@ -558,6 +561,7 @@ class CudaExecutor:
         self.models = {}
         self.graphs = collections.OrderedDict()   # (slot, key, R, G) -> CUDAGraph
         self.bucket_launches = collections.Counter()
+        self.seen = collections.Counter()         # direct launches of a hot (slot, key, R, G)
         self.counts = collections.Counter()
         self.capture_s = 0.0
         self.capture_max_s = 0.0
@@ -697,9 +701,11 @@ class CudaExecutor:
                 graph.replay()
                 self.counts["graph_replays"] += 1
             else:
+                if hot:
+                    self.seen[gk] += 1
                 b = self._batch_struct(slot, key, R, G)
                 plan.attach_workspace(slot.plan_ws)
-                if hot:
+                if hot and self.seen[gk] >= self.graph_after:
                     t0 = time.perf_counter()
                     graph = torch.cuda.CUDAGraph()
                     graph.capture_begin(capture_error_mode="thread_local")

@@ -15,8 +15,9 @@ def test_candidates():
     # plans with their own workspace also try keeping every GEMM whole (no K split)
     assert "split_bf16/op0/nosplit" in [config_label(c) for c in
                                          candidate_configs(512, 512, own_workspace=True)]
-    # the split form needs sides divisible by 8; no tensor cores: FP32 only
-    assert [config_label(c) for c in candidate_configs(100, 64)] == ["fp32/op0"]
+    # every side has the split form (rows padded to 8); no tensor cores: FP32 only
+    assert [config_label(c) for c in candidate_configs(100, 64)] == \
+        ["split_bf16/op0", "split_bf16/op1", "fp32/op0"]
     assert [config_label(c) for c in candidate_configs(256, 128, tensor_cores=False)] == \
         ["fp32/op0"]
 

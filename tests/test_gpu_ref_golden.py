@@ -65,8 +65,6 @@ def variant(request):
 def test_mft_matches_dlux(cuda, variant, case):
     import dlux_gb300.utils as dlu
     name, n_in, n_out, ps_in, ps_out, fl, shift, pixel, inv, wl = case
-    if variant == "split_bf16" and (n_in % 8 or n_out % 8):
-        pytest.skip("sides that are not multiples of 8 run the FP32 form")
     ref = load("utils")
     E = torch.as_tensor(RI.case_field(name, n_in), dtype=torch.complex64, device="cuda")
     got = dlu.MFT(E, wl, ps_in, n_out, ps_out, focal_length=fl, shift=shift, pixel=pixel,
@@ -85,9 +83,6 @@ def test_mft_matches_dlux(cuda, variant, case):
 def test_fft_matches_dlux(cuda, variant, case):
     import dlux_gb300.utils as dlu
     name, n, ps, wl, fl, pad, inv = case
-    from dlux_gb300.kernels import fft_out_side
-    if variant == "split_bf16" and (n % 8 or fft_out_side(n, pad) % 8):
-        pytest.skip("sides that are not multiples of 8 run the FP32 form")
     ref = load("utils")
     E = torch.as_tensor(RI.case_field(name, n, salt=7), dtype=torch.complex64, device="cuda")
     got, ps_out = dlu.FFT(E, wl, ps, focal_length=fl, pad=pad, inverse=inv)

@@ -37,8 +37,11 @@ def scene(n, m, L, S, seed, span=0.3):
 
 
 @pytest.mark.parametrize("variant", ["fp32", "split_bf16"])
-@pytest.mark.parametrize("n,m,L,S", [(64, 32, 2, 5), (256, 64, 3, 40)])
+@pytest.mark.parametrize("n,m,L,S", [(64, 32, 2, 5), (256, 64, 3, 40), (100, 36, 2, 9),
+                                     (90, 45, 2, 6)])
 def test_scene_image_matches_oracle_and_per_source_path(cuda, variant, n, m, L, S):
+    """Sides 100 / 36 and 90 / 45 are not multiples of 8: split rows padded (the
+    tilted-matrix kernel's four-element path at 100, its scalar path at 90)."""
     from dlux_gb300 import kernels
     T, opd, wls, pos, w = scene(n, m, L, S, 3)
     ps = float(O.arcsec2rad(0.02))
