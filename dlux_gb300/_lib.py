@@ -177,6 +177,7 @@ _SIGNATURES = {
     "dlx_poly_forward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp, _c_int, _c_vp]),
     "dlx_poly_backward": (_c_int, [_c_vp, _c_vp, _c_int, _c_vp]),
     "dlx_poly_forward_token": (_c_int, [_c_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
+    "dlx_poly_keep_focal": (_c_int, [_c_vp, _c_int]),
     "dlx_poly_reuse_forward": (_c_int, [_c_vp, ctypes.c_ulonglong]),
     "dlx_set_split_k": (_c_int, [_c_int]),
     "dlx_set_gemm_pair": (_c_int, [_c_int]),

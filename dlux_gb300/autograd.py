@@ -1,8 +1,10 @@
 """torch.autograd.Function wrappers over the C ABI.
 
 Each Function's forward and backward call the library's kernels; the
-backward passes are the hand-written adjoints (the polychromatic PSF
-backward recomputes every focal field rather than storing it).
+backward passes are the hand-written adjoints. The polychromatic PSF's
+forward keeps its focal fields in the plan's workspace when a gradient is
+needed, and its backward starts from them when nothing used the plan in
+between (otherwise it recomputes them).
 """
 
 from __future__ import annotations
@@ -50,7 +52,10 @@ class PolyPSF(torch.autograd.Function):
         ctx.plan, ctx.normalise, ctx.tilt = plan, normalise, t
         ctx.tilt_device = tilt.device
         ctx.save_for_backward(amp, opd, phase, weights, amp_scale)
-        psf = plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t)
+        # with a reverse pass ahead, the forward keeps its focal fields as well
+        keep = any(ctx.needs_input_grad[2:7])
+        psf = plan.psf(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(), t,
+                       keep=keep)
         # the backward may start from this forward's workspace if nothing used the plan since
         ctx.token = plan.forward_token()
         return psf

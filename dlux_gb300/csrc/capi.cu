@@ -843,6 +843,12 @@ struct dlx_poly_plan_s {
   unsigned long long epoch = 0;      // counts single-chunk forwards
   unsigned long long fwd_token = 0;  // token of the intact forward state, 0 if none
   unsigned long long reuse_req = 0;  // token the next backward may start from
+  // Focal fields kept by the forward (dlx_poly_keep_focal): the y-contraction
+  // also writes F = alpha D (complex64, into `fbar`), so that a backward that
+  // reuses this forward forms F-bar = 2 G F elementwise instead of repeating
+  // the y-contraction GEMM.
+  bool keep_req = false;             // the next single-chunk forward keeps F
+  bool fwd_focal = false;            // the intact forward state includes F
   std::vector<dlx_poly_object> fwd_objs;
 
   static bool same_inputs(const dlx_poly_object& a, const dlx_poly_object& b) {
@@ -912,8 +918,9 @@ struct dlx_poly_plan_s {
     return g;
   }
 
+  // keep: also write the focal fields F = alpha D (complex64) into `fbar`.
   int forward_chunk(const dlx_poly_object* objs, int R, float* psf_sum, int accumulate,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool keep = false) {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
@@ -931,6 +938,13 @@ struct dlx_poly_plan_s {
     e.objs = t;
     e.alpha = ts.alpha.as<float>();
     e.out_f32 = planes.as<float>();
+    if (keep) {
+      // intensity planes and F = alpha D: the PSF + cotangent epilogue with no
+      // cotangent
+      e.kind = EPI_PSF_GRADF;
+      for (int r = 0; r < R; ++r) e.objs.o[r].G = nullptr;
+      e.out_c64 = fbar.as<float2>();
+    }
     DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, e), s));
     ObjReduceArgs ra{};
     ra.objs = t;
@@ -944,10 +958,14 @@ struct dlx_poly_plan_s {
   }
 
   // reuse: `mid` and `pathff` still hold the forward state of these objects
-  // (checked by the caller), so the pupil field and D1 are not rebuilt.
+  // (checked by the caller), so the pupil field and D1 are not rebuilt; with
+  // `focal`, `fbar` holds that forward's focal fields F as well, and F-bar =
+  // 2 G F is formed elementwise (into `planes` in the split form, in place in
+  // the FP32 form) instead of by the y-contraction GEMM.
   int backward_chunk(const dlx_poly_object* objs, int R, cudaStream_t s, float* sum_amp = nullptr,
                      float* sum_opd = nullptr, float* sum_phase = nullptr,
-                     bool sum_pixels = false, bool accumulate_sum = false, bool reuse = false) {
+                     bool sum_pixels = false, bool accumulate_sum = false, bool reuse = false,
+                     bool focal = false) {
     const int N = ts.n_in, M = ts.n_out, v = ts.variant;
     if (!field.p)
       return fail(DLX_ERR_ARG, "poly plan: no workspace (dlx_poly_attach_workspace first)");
@@ -957,6 +975,14 @@ struct dlx_poly_plan_s {
     tables(objs, R, &t, &o);
     for (int r = 0; r < R; ++r)
       if (!t.o[r].G) return fail(DLX_ERR_ARG, "poly backward: every object needs g_psf");
+    if (reuse && focal) {
+      const bool split = v == DLX_VARIANT_SPLIT_BF16;
+      DLX_TRY(launch_focal_gradf(fbar.as<float2>(), t, ts.batch * R, M,
+                                 split ? planes.as<__nv_bfloat16>() : nullptr,
+                                 split ? nullptr : fbar.as<float2>(), s));
+      return reverse_from_fbar(t, o, R, s, sum_amp, sum_opd, sum_phase, sum_pixels,
+                               accumulate_sum, split ? planes.p : fbar.p);
+    }
     if (!reuse) {
       // Recompute the forward fields.
       DLX_TRY(build_field(t, s, pathff.as<float4>()));
@@ -974,7 +1000,7 @@ struct dlx_poly_plan_s {
     else eg.out_c64 = fbar.as<float2>();
     DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, eg), s));
     return reverse_from_fbar(t, o, R, s, sum_amp, sum_opd, sum_phase, sum_pixels,
-                             accumulate_sum);
+                             accumulate_sum, fbar.p);
   }
 
   // PSF and reverse pass in one sweep, for objects whose cotangent g_psf is
@@ -1010,18 +1036,19 @@ struct dlx_poly_plan_s {
     rp.npix = (long long)M * M;
     rp.planes = planes.as<float>();
     DLX_TRY(launch_obj_psf_reduce(rp, s));
-    return reverse_from_fbar(t, o, R, s, nullptr, nullptr, nullptr, false, false);
+    return reverse_from_fbar(t, o, R, s, nullptr, nullptr, nullptr, false, false, fbar.p);
   }
 
-  // Adjoint GEMMs from F̄ (in `fbar`) and the pupil reductions.
+  // Adjoint GEMMs from F̄ (at `fb`: `fbar`, or `planes` after kept focal
+  // fields) and the pupil reductions.
   int reverse_from_fbar(const ObjTable& t, const OutTable& o, int R, cudaStream_t s,
                         float* sum_amp, float* sum_opd, float* sum_phase, bool sum_pixels,
-                        bool accumulate_sum) {
+                        bool accumulate_sum, const void* fb) {
     const int L = ts.batch, N = ts.n_in, M = ts.n_out, v = ts.variant;
     // Xt[x][v] = sum_u conj(Ax[x][u]) Fbar[v][u]
     EpiArgs e3 = epi_store(v, mid.p, nullptr);
     e3.objs = t;
-    DLX_TRY(run_gemm(v, gemm(ts.opANx(), R, N, M, M, true, fbar.p, e3), s));
+    DLX_TRY(run_gemm(v, gemm(ts.opANx(), R, N, M, M, true, fb, e3), s));
     ObjReduceArgs ra{};
     ra.objs = t;
     ra.outs = o;
@@ -1084,8 +1111,10 @@ static void poly_ws_sizes(int L, int N, int M, int R, int nparts, bool split_on,
   const size_t d1 = split_bytes(lr, M, N), xt = split_bytes(lr, N, M);
   sz[1] = d1 > xt ? d1 : xt;
   sz[2] = split_bytes(lr, M, M);
-  const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4;
-  sz[3] = a > b ? a : b;
+  // intensity [M][M] f32, pupil planes 2 x [N][N] f32, or Ē [N][N] complex64;
+  // and, after kept focal fields, F-bar as split planes [M][M]
+  const size_t a = lr * m * m * 4, b = 2 * lr * n * n * 4, c = split_bytes(lr, M, M);
+  sz[3] = std::max(a, std::max(b, c));
   sz[4] = sizeof(double) * (size_t)nparts * R * (L + 2);
   sz[5] = (sizeof(float4) + 3 * sizeof(float)) * (size_t)R * n * n;  // (path, phase) + pixel sums
   sz[6] = 0;
@@ -1261,13 +1290,17 @@ int dlx_poly_forward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obje
   if (!plan || (n_objects > 0 && !objs)) return fail(DLX_ERR_ARG, "poly_forward: null pointer");
   if (n_objects < 0) return fail(DLX_ERR_ARG, "poly_forward: negative object count");
   cudaStream_t s = as_stream(stream);
+  // focal fields are kept only by a single-chunk forward (a reusable state)
+  const bool keep = plan->keep_req && n_objects >= 1 && n_objects <= plan->max_obj;
+  plan->keep_req = false;  // a request applies to one forward call
   for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
     const int R = std::min(plan->max_obj, n_objects - o0);
-    DLX_TRY(plan->forward_chunk(objs + o0, R, psf_sum, (o0 > 0) ? 1 : accumulate, s));
+    DLX_TRY(plan->forward_chunk(objs + o0, R, psf_sum, (o0 > 0) ? 1 : accumulate, s, keep));
   }
   if (n_objects >= 1 && n_objects <= plan->max_obj) {
     plan->fwd_token = ++plan->epoch;
     plan->fwd_objs.assign(objs, objs + n_objects);
+    plan->fwd_focal = keep;
   }
   return DLX_OK;
 }
@@ -1280,10 +1313,11 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
   const unsigned long long req = plan->reuse_req;
   plan->reuse_req = 0;  // a request applies to one backward call
   const bool reuse = plan->can_reuse(req, objs, n_objects);
+  const bool focal = reuse && plan->fwd_focal;
   for (int o0 = 0; o0 < n_objects; o0 += plan->max_obj) {
     const int R = std::min(plan->max_obj, n_objects - o0);
     DLX_TRY(plan->backward_chunk(objs + o0, R, s, nullptr, nullptr, nullptr, false, false,
-                                 reuse));
+                                 reuse, focal));
   }
   return DLX_OK;
 }
@@ -1297,6 +1331,12 @@ int dlx_poly_forward_token(dlx_poly_plan plan, unsigned long long* token) {
 int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token) {
   if (!plan) return fail(DLX_ERR_ARG, "poly_reuse_forward: null plan");
   plan->reuse_req = token;
+  return DLX_OK;
+}
+
+int dlx_poly_keep_focal(dlx_poly_plan plan, int keep) {
+  if (!plan) return fail(DLX_ERR_ARG, "poly_keep_focal: null plan");
+  plan->keep_req = keep != 0;
   return DLX_OK;
 }
 

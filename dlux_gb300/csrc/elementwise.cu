@@ -291,6 +291,68 @@ int launch_c64_to_split_batched(const float2* in, int rows, int cols, int batch,
   return DLX_OK;
 }
 
+// F-bar of the poly reverse pass from the focal fields a forward kept (the
+// cotangent of sum G |F|^2 is 2 G F): V adjacent pixels of one row per thread
+// (M % V == 0, so that with rows padded to split_ld(M) each split plane gets
+// one 2V-byte store), the objects and their wavelengths looped inside, so
+// each G value is read once. out_c64 may be f itself (every element is read
+// and written by the same thread).
+template <int V>
+__global__ void focal_gradf_kernel(const float2* f, ObjTable objs, int batch, int M,
+                                   __nv_bfloat16* __restrict__ out_split, float2* out_c64) {
+  pdl_enter();
+  const long long npix = (long long)M * M;
+  const long long p0 = V * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
+  if (p0 >= npix) return;
+  const int R = objs.n > 0 ? objs.n : 1;
+  const int y = (int)(p0 / M);
+  const long long splane = split_plane(M, M);
+  const long long sp = (long long)y * split_ld(M) + (p0 - (long long)y * M);
+  for (int r = 0; r < R; ++r) {
+    float g[V];
+#pragma unroll
+    for (int k = 0; k < V; ++k) g[k] = 2.0f * objs.o[r].G[p0 + k];
+    for (int l = 0; l < batch / R; ++l) {
+      const long long b = (long long)l * R + r;
+      float2 o[V];
+#pragma unroll
+      for (int k = 0; k < V; ++k) {
+        const float2 v = f[b * npix + p0 + k];
+        o[k] = make_float2(g[k] * v.x, g[k] * v.y);
+      }
+      if (out_split) {
+        Bf16Vec<V> q[4];
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+          split_bf16(o[k].x, q[0].v[k], q[1].v[k]);
+          split_bf16(o[k].y, q[2].v[k], q[3].v[k]);
+        }
+        __nv_bfloat16* base = out_split + b * 4 * splane + sp;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) *reinterpret_cast<Bf16Vec<V>*>(base + c * splane) = q[c];
+      } else {
+#pragma unroll
+        for (int k = 0; k < V; ++k) out_c64[b * npix + p0 + k] = o[k];
+      }
+    }
+  }
+}
+
+int launch_focal_gradf(const float2* f, const ObjTable& objs, int batch, int M,
+                       __nv_bfloat16* out_split, float2* out_c64, cudaStream_t s) {
+  const long long npix = (long long)M * M;
+  if (npix == 0 || batch == 0) return DLX_OK;
+  for (int r = 0; r < (objs.n > 0 ? objs.n : 1); ++r)
+    if (!objs.o[r].G) return fail(DLX_ERR_ARG, "focal_gradf: every object needs g_psf");
+  if (M % 4 == 0)
+    DLX_PDL_LAUNCH("focal_gradf_kernel", focal_gradf_kernel<4>, dim3(ceil_div(npix / 4, 256)),
+                   dim3(256), 0, s, f, objs, batch, M, out_split, out_c64);
+  else
+    DLX_PDL_LAUNCH("focal_gradf_kernel", focal_gradf_kernel<1>, dim3(ceil_div(npix, 256)),
+                   dim3(256), 0, s, f, objs, batch, M, out_split, out_c64);
+  return DLX_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Block-level double reduction helper (fixed order -> deterministic).
 // ---------------------------------------------------------------------------

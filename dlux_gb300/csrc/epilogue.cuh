@@ -68,10 +68,15 @@ __device__ __forceinline__ float2 epi_read_in(const EpiArgs& e, int b, long long
 // ---- per-element epilogues; l = wavelength, r = object, a = alpha_l ----
 __device__ __forceinline__ void epi_gradf_value(const EpiArgs& e, int b, int r, float a,
                                                 long long idx, float2& v) {
-  // cotangent of F = alpha * D for <G, |F|^2>: 2 G F = 2 alpha G D
+  // cotangent of F = alpha * D for <G, |F|^2>: 2 G F = 2 alpha G D; with no
+  // cotangent (G null) the focal field F = alpha D itself, kept for a later
+  // reverse pass
   const float* G = e.objs.n > 0 ? e.objs.o[r].G : e.G;
-  float g = 2.0f * a * G[idx];
-  if (e.bweight) g *= e.bweight[b];
+  float g = a;
+  if (G) {
+    g = 2.0f * a * G[idx];
+    if (e.bweight) g *= e.bweight[b];
+  }
   v = make_float2(g * v.x, g * v.y);
 }
 
@@ -222,15 +227,17 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
         for (int j = 0; j < 32; ++j)
           if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
       }
-      // 16 loads at a time, so that their latencies overlap
-      const float* G = (e.objs.n > 0 ? e.objs.o[r].G : e.G) + idx0;
-      const float s = 2.0f * a * (e.bweight ? e.bweight[b] : 1.0f);
+      // 16 loads at a time, so that their latencies overlap. No cotangent (G
+      // null, warp-uniform): the focal field F = alpha D itself is stored.
+      const float* G0 = e.objs.n > 0 ? e.objs.o[r].G : e.G;
+      const float* G = G0 ? G0 + idx0 : nullptr;
+      const float s = G0 ? 2.0f * a * (e.bweight ? e.bweight[b] : 1.0f) : a;
 #pragma unroll
       for (int h = 0; h < 32; h += 16) {
         float g[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j)
-          g[j] = h + j < mc ? __ldg(G + (long long)(h + j) * N) : 0.0f;
+          g[j] = h + j < mc ? (G ? __ldg(G + (long long)(h + j) * N) : 1.0f) : 0.0f;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           if (h + j < mc) {

@@ -83,6 +83,11 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
 
 int launch_c64_to_split_batched(const float2* in, int rows, int cols, int batch,
                                 __nv_bfloat16* out_split, cudaStream_t s);
+// F-bar = 2 G_r F from kept focal fields F [batch][M][M] (complex64, b = l R +
+// r): split planes [batch][4][M][split_ld(M)] into out_split, or complex64
+// into out_c64 (which may be f itself).
+int launch_focal_gradf(const float2* f, const ObjTable& objs, int batch, int M,
+                       __nv_bfloat16* out_split, float2* out_c64, cudaStream_t s);
 int launch_psf_sum(const float2* in, int batch, long long npix, float* psf, cudaStream_t s);
 int launch_power_scale(const float2* in, int batch, long long npix, double value, float* out,
                        cudaStream_t s);
@@ -196,7 +201,8 @@ enum EpiKind {
   EPI_INTENSITY = 2, // out_f32[b][m][n] = alpha_b^2 |D|^2
   EPI_GRADF = 3,     // out[b][m][n] = 2 alpha_b G[m][n] D    (c64 or split)
   EPI_PUPIL = 4,     // pupil-gradient planes from D = Ebar_unscaled[b][y=m][x=n]
-  EPI_PSF_GRADF = 5, // both EPI_INTENSITY (out_f32) and EPI_GRADF (out_split / out_c64)
+  EPI_PSF_GRADF = 5, // both EPI_INTENSITY (out_f32) and EPI_GRADF (out_split / out_c64);
+                     // with no cotangent (G null) the second output is F = alpha D
   EPI_SPLIT2 = 6,    // EPI_SPLIT / EPI_C64, plus the same values times colw[n] into out_*2
   EPI_DOT = 7,       // out_f32 = k_l alpha_l (Fb.im D.re - Fb.re D.im), Fb read from in_*
   EPI_PARTIAL = 8,   // split K: raw FP32 partial sums [split][b][m][n] (tensor-core form,
@@ -211,7 +217,7 @@ struct EpiArgs {
   __nv_bfloat16* out_split;
   float* out_f32;            // intensity planes, or pre planes for EPI_PUPIL
   float* out_f32b;           // pim planes for EPI_PUPIL
-  const float* G;            // [m][n] for EPI_GRADF
+  const float* G;            // [m][n] for EPI_GRADF (null: store F = alpha D instead)
   // EPI_PUPIL recompute of the unit phasor
   const float* amp;          // nullable
   const float* amp_scale;    // nullable device scalar multiplying amp

@@ -433,11 +433,16 @@ class PolyPlan(_Plan):
             self._tilt_basis = tb
         return tb
 
-    def psf(self, amp, amp_scale, opd, phase, weights, tilt=(0.0, 0.0), out=None):
+    def psf(self, amp, amp_scale, opd, phase, weights, tilt=(0.0, 0.0), out=None, keep=False):
+        """PSF of one object. ``keep``: also keep the focal fields, so that a
+        reverse pass reusing this forward (grad with its forward_token()) skips
+        recomputing them."""
         amp, amp_scale, opd, phase, weights = map(_contig, (amp, amp_scale, opd, phase, weights))
         dev = weights.device
         if out is None:
             out = torch.empty((self.n_out, self.n_out), dtype=torch.float32, device=dev)
+        if keep:
+            call("dlx_poly_keep_focal", self.handle, 1)
         call("dlx_poly_psf", self.handle, ptr(amp), ptr(amp_scale), ptr(opd), ptr(phase),
              ptr(weights), float(tilt[0]), float(tilt[1]), ptr(out), _stream())
         return out

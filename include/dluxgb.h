@@ -326,7 +326,8 @@ int dlx_poly_backward(dlx_poly_plan plan, const dlx_poly_object* objs, int n_obj
  * dlx_poly_forward_token returns a token for that state (0 if none is intact).
  * dlx_poly_reuse_forward(token) lets the next dlx_poly_backward /
  * dlx_poly_psf_grad start from it: it skips the phasor rebuild and the first
- * MFT stage, and still recomputes the per-wavelength focal field from D1.
+ * MFT stage, and recomputes the per-wavelength focal field from D1 unless
+ * that forward kept it (dlx_poly_keep_focal).
  * The request covers one backward call. It is ignored, and the backward
  * recomputes everything, if another call used the plan in between or the
  * objects' inputs (amp, amp_scale, opd, phase, weights, tilt pointers and
@@ -360,6 +361,17 @@ int dlx_gemm_pair_clusters(int* clusters);
  * object's result stays the same alone and in a batch. No dLux counterpart. */
 int dlx_poly_plan_set_gemm_form(dlx_poly_plan plan, int pair_mode, int split_k);
 int dlx_poly_reuse_forward(dlx_poly_plan plan, unsigned long long token);
+/* Focal fields kept for the reverse pass, the residual a jax.custom_vjp
+ * forward of MFT -> |.|^2 would save (JAX keeps the focal field F for the
+ * backward of optical_systems.py:211-223). With keep != 0 the next
+ * dlx_poly_forward (or dlx_poly_psf) of at most max_objects objects also
+ * writes F = alpha D of every wavelength into the plan's workspace (8 bytes
+ * per focal pixel and wavelength, already part of the workspace size). A
+ * backward that reuses that forward (dlx_poly_reuse_forward) then forms
+ * F-bar = 2 G F elementwise instead of repeating the y-contraction GEMM. The
+ * request covers one forward call; without a reusing backward the kept fields
+ * are simply overwritten later. */
+int dlx_poly_keep_focal(dlx_poly_plan plan, int keep);
 /* PSF and reverse pass in one sweep for objects whose cotangent objs[r].g_psf
  * is known before the forward pass (a serving request, a linear functional):
  * writes objs[r].psf (optional) and the gradient outputs like

@@ -119,3 +119,62 @@ def test_split_form_meets_1e5_at_config2_size(cuda):
     print(f"config-2 size split_bf16: psf rel L2 {err:.2e}, g_opd rel L2 {gerr:.2e}")
     assert err < 1e-5
     assert gerr < 1e-5
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+@pytest.mark.parametrize("n,m", [(128, 64), (128, 96)])
+def test_kept_focal_fields_give_the_same_gradient(cuda, variant, n, m):
+    """A forward that keeps its focal fields F lets the reusing backward form
+    F-bar = 2 G F elementwise instead of repeating the y-contraction GEMM. Both
+    backwards match the FP64 oracle (relative L2 <= 1e-5) and each other:
+    within 1e-6 in the FP32 form (rounding order), within 3e-6 in the split
+    form, where F-bar's hi/lo split quantises the two paths' (equally accurate)
+    values differently. A backward whose inputs differ from the kept forward's
+    recomputes everything (bitwise equal to a backward without reuse).
+
+    The cotangent has mean 1 (as a likelihood's typically has): with a
+    zero-mean one, the wavelength-weight gradient <G, |F_l|^2> / w_l is a sum
+    over the focal plane that cancels to a small fraction of its terms, and
+    its relative error grows by that ratio in either backward."""
+    from dlux_gb300 import kernels
+    L = 3
+    T, B, c, wls, w = make_case(n, m, 10, L, 11)
+    rng = np.random.default_rng(12)
+    opd = O.eval_basis(B, c)
+    phase = rng.normal(0, 0.1, (n, n)) * (T > 0)
+    tilt = (0.04e-6, -0.02e-6)
+    ps_out = float(O.arcsec2rad(0.02))
+    G = 1.0 + 0.5 * rng.normal(size=(m, m))
+    Teff = T / np.sqrt((T ** 2).sum())
+    ref = O.poly_psf_grad(Teff, opd, wls, w, 1.0, m, ps_out, G, phase=phase, offset=tilt)
+    plan = kernels.PolyPlan(wls, n, 1.0 / n, m, ps_out, variant=variant)
+    amp = to_dev(T)
+    scale = kernels.amp_norm(amp)
+    args = (amp, scale, to_dev(opd), to_dev(phase), to_dev(w))
+    keys = {"amp": "g_amp", "opd": "g_opd", "phase": "g_phase", "w": "g_w"}
+    out = {}
+    for keep in (False, True):
+        p0 = plan.psf(*args, tilt=tilt, keep=keep).clone()
+        tok = plan.forward_token()
+        assert tok != 0
+        gr = plan.grad(*args, to_dev(G), tilt, reuse_token=tok)
+        out[keep] = (p0.cpu().numpy(), {k: v.cpu().numpy() for k, v in gr.items()})
+    assert np.array_equal(out[False][0], out[True][0])   # the PSF is the same launch
+    tol_same = 1e-6 if variant == "fp32" else 3e-6
+    for k, kr in keys.items():
+        e_same = rel(out[True][1][k], out[False][1][k])
+        e_keep = rel(out[True][1][k], ref[kr])
+        e_recompute = rel(out[False][1][k], ref[kr])
+        print(f"kept focal fields {variant} {n}->{m} {k}: vs recompute {e_same:.2e}, "
+              f"vs oracle {e_keep:.2e} (recomputing backward {e_recompute:.2e})")
+        assert e_same < tol_same and e_keep < 1e-5 and e_recompute < 1e-5
+    # kept fields of another forward are not used
+    opd2 = to_dev(opd * 1.1)
+    args2 = (amp, scale, opd2, to_dev(phase), to_dev(w))
+    plan.psf(*args, tilt=tilt, keep=True)
+    tok = plan.forward_token()
+    g_reuse = plan.grad(*args2, to_dev(G), tilt, reuse_token=tok)
+    g_fresh = plan.grad(*args2, to_dev(G), tilt)
+    for k in keys:
+        assert torch.equal(g_reuse[k], g_fresh[k]), k
+    plan.close()
