@@ -55,10 +55,10 @@ LATENCY_SAMPLES = 200
 # Whole steps of the CPU restatement timed for the GPU line's cpu_baseline.
 CPU_BASELINE_STEPS = 3
 # DRAM bytes (read + write) of one tensor-core GEMM launch per wavelength, from an ncu
-# capture of a 16-wavelength launch of this workload (71.0 MB / 16). Traffic grows in
-# proportion to the wavelength count (each wavelength is an independent GEMM on its own
-# operands).
-GEMM_DRAM_BYTES_PER_WAVELENGTH = (67.35e6 + 3.57e6) / 16
+# capture of the four GEMM launches of a 16-wavelength step of this workload (71.2 MB
+# per launch on average, / 16). Traffic grows in proportion to the wavelength count
+# (each wavelength is an independent GEMM on its own operands).
+GEMM_DRAM_BYTES_PER_WAVELENGTH = 71.2e6 / 16
 
 
 def config_dict(extra=None):
@@ -1276,8 +1276,9 @@ def main():
         roofline = {"bound": "tensor", "achieved": achieved, "peak": tflops, "unit": "TFLOP/s",
                     "frac": achieved / tflops,
                     "traffic": GEMM_DRAM_BYTES_PER_WAVELENGTH * N_WAVELENGTHS,
-                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                      "16-wavelength launch, scaled to the launch's wavelengths",
+                    "traffic_source": "ncu DRAM bytes of the step's GEMM launches at 16 "
+                                      "wavelengths (average per launch), scaled to the "
+                                      "launch's wavelengths",
                     "peak_source": f"{src} bf16 dense (burst)",
                     "kernel": "tc_cgemm_kernel" if args.variant == "split_bf16" else
                               "cgemm_fp32_kernel",
