@@ -770,7 +770,7 @@ def serving_leg(args):
     mean batch and CUDA-graph hit rate of each."""
     keys = ("throughput_rps", "p50_ms", "p99_ms", "p99_ms_by_pupil", "p99_queue_ms",
             "p99_service_ms", "mean_batch", "graph_hit_rate", "graph_captures",
-            "capture_ms_max", "loop_gap_max_ms", "completed", "failed", "slowest")
+            "capture_ms_max", "loop_gap_max_ms", "completed", "failed", "slowest", "stalls")
     tuner, _ = _serving_tuner()
     out = {"rate_hz": args.rate, "requests": args.serving_requests}
     for name, variant, t in (("split_bf16_autotuned", None, tuner), ("fp32", "fp32", None)):

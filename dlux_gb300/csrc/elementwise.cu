@@ -151,37 +151,8 @@ struct alignas(2 * V) Bf16Vec {
 // wavelength, and the per-pixel FP64 path set-up is amortised over a
 // wavelength group (blockIdx.y: wavelengths [y * lg, (y + 1) * lg)). Same
 // arithmetic per pixel as phasor_kernel.
-// The (path, phase) float pairs of every pixel and object, formed once in
-// FP64 (the per-pixel set-up of the phasor kernels): written to a.out_path,
-// from which phasor_splitv_kernel reads them when its wavelengths are spread
-// over several blocks, so that no group repeats the FP64 work.
-__global__ void phasor_path_kernel(PhasorArgs a) {
-  pdl_enter();
-  const long long npix = (long long)a.n * a.n;
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npix) return;
-  const int R = a.objs.n > 0 ? a.objs.n : 1;
-  const int y = (int)(p / a.n);
-  const int x = (int)(p - (long long)y * a.n);
-  const double half = 0.5 * (a.n - 1);
-  const double X = ((double)x - half) * a.pixel_scale;
-  const double Y = ((double)y - half) * a.pixel_scale;
-  for (int r = 0; r < R; ++r) {
-    const bool obj = a.objs.n > 0;
-    const float* o_opd = obj ? a.objs.o[r].opd : a.opd;
-    const float* o_phase = obj ? a.objs.o[r].phase : a.phase;
-    const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
-    const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
-    const FF path = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
-    const FF ph = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
-    a.out_path[(long long)r * npix + p] = make_float4(path.hi, path.lo, ph.hi, ph.lo);
-  }
-}
-
-// path_in: the pairs of phasor_path_kernel (read instead of formed here).
 template <int V>
-__global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg,
-                                     const float4* __restrict__ path_in) {
+__global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
   pdl_enter();
   extern __shared__ float psm[];
   const long long npix = (long long)a.n * a.n;
@@ -220,18 +191,12 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
 #pragma unroll
     for (int k = 0; k < V; ++k) {
       const long long p = p0 + k;
-      if (path_in) {
-        const float4 q = path_in[(long long)r * npix + p];
-        path[k] = FF{q.x, q.y};
-        ph[k] = FF{q.z, q.w};
-      } else {
-        const double X = ((double)(x0 + k) - half) * a.pixel_scale;
-        path[k] = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
-        ph[k] = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
-        if (a.out_path && blockIdx.y == 0)
-          a.out_path[(long long)r * npix + p] =
-              make_float4(path[k].hi, path[k].lo, ph[k].hi, ph[k].lo);
-      }
+      const double X = ((double)(x0 + k) - half) * a.pixel_scale;
+      path[k] = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
+      ph[k] = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+      if (a.out_path && blockIdx.y == 0)
+        a.out_path[(long long)r * npix + p] =
+            make_float4(path[k].hi, path[k].lo, ph[k].hi, ph[k].lo);
       float am = o_amp ? o_amp[p] : 1.0f;
       if (o_scale) am *= scale;
       amp[k] = am * (float)a.const_scale;
@@ -275,27 +240,16 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
   const size_t smem = sizeof(float) * (size_t)(2 * L + R * L);
   const int cached = smem <= 32 * 1024 ? 1 : 0;
   if (a.out_split && !a.out_c64 && !a.in && a.n % 4 == 0) {
-    // 4 pixels per thread (2 measured the same at 512^2 x 64). With the
-    // (path, phase) pairs wanted and at least 16 wavelengths, the pairs are
-    // formed once by phasor_path_kernel and the wavelengths spread over up to
-    // 8 blocks per pixel group, for more threads in flight; otherwise one
-    // wavelength group forms the pairs itself (spreading the wavelengths with
-    // the FP64 set-up repeated per group measured slower: 42.9 vs 38.3 us at
-    // 512^2 x 64).
+    // One wavelength group: spreading the wavelengths over more blocks
+    // measured slower at 512^2 x 64 (42.9 vs 38.3 us) with the FP64 path
+    // set-up repeated per group, and no faster (35.9 us plus 12.9 us for a
+    // separate FP64 pass over the pixels) with the set-up done once: the
+    // per-element phase reduction and sincos bound the kernel.
+    // 4 pixels per thread (2 measured the same at 512^2 x 64)
     constexpr int V = 4;
-    if (a.out_path && L >= 16) {
-      DLX_PDL_LAUNCH("phasor_path_kernel", phasor_path_kernel, dim3(ceil_div(npix, 256)),
-                     dim3(256), 0, s, a);
-      const int lg = (L + 7) / 8;
-      DLX_PDL_LAUNCH("phasor_splitv_kernel", phasor_splitv_kernel<V>,
-                     dim3(ceil_div(npix / V, 256), (L + lg - 1) / lg), dim3(256),
-                     cached ? smem : 0, s, a, *inv_lambda_arg, cached, lg,
-                     (const float4*)a.out_path);
-      return DLX_OK;
-    }
     DLX_PDL_LAUNCH("phasor_splitv_kernel", phasor_splitv_kernel<V>,
                    dim3(ceil_div(npix / V, 256), 1), dim3(256), cached ? smem : 0, s, a,
-                   *inv_lambda_arg, cached, L, (const float4*)nullptr);
+                   *inv_lambda_arg, cached, L);
     return DLX_OK;
   } else if (a.out_split && !a.out_c64 && !a.in)
     phasor_kernel<true><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
