@@ -59,3 +59,14 @@ def test_argument_errors_are_reported_without_a_gpu():
     d = L.MftDesc(0, 16, 8, 0.1, 0.05, 0.0, 0.0, 0.0, 0, 0)
     st = lib.dlx_mft_plan_create(ctypes.byref(d), L.dbl_array([1.0]), ctypes.byref(plan))
     assert st == L.DLX_ERR_SHAPE
+
+
+def test_plan_state_calls_refuse_a_null_plan():
+    """The forward-state calls of poly plans check their plan before any device work."""
+    import dlux_gb300._lib as L
+    lib = L.load()
+    assert lib.dlx_poly_keep_focal(None, 1) == L.DLX_ERR_ARG
+    assert b"null plan" in lib.dlx_last_error()
+    assert lib.dlx_poly_reuse_forward(None, 1) == L.DLX_ERR_ARG
+    tok = ctypes.c_ulonglong(0)
+    assert lib.dlx_poly_forward_token(None, ctypes.byref(tok)) == L.DLX_ERR_ARG
