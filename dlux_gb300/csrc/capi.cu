@@ -811,7 +811,8 @@ int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k
 // object r, so the per-wavelength DFT operands are shared (A index = b / R).
 // Larger object counts run in chunks of max_objects.
 // ---------------------------------------------------------------------------
-// Pixel chunks of the reverse-pass reductions (enough blocks to fill the GPU).
+// Pixel chunks of the reverse-pass reductions (enough blocks to fill the GPU):
+// the most a plan uses; small pupils use fewer, of at least 256 pixels each.
 constexpr int kPolyParts = 1024;
 
 struct dlx_poly_plan_s {
@@ -1157,6 +1158,10 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
   ts.wl.assign(wl, wl + L);
   p->pixel_scale_in = d->pixel_scale_in;
   p->max_obj = max_objects;
+  // pixel chunks of the reverse-pass reductions: 256 pupil pixels or more each
+  // (one per thread of a block), at most kPolyParts
+  p->nparts = (int)std::max(1LL, std::min((long long)kPolyParts,
+                                          ((long long)d->n_in * d->n_in + 255) / 256));
   std::vector<DftAxis> ax(L);
   std::vector<float> alphas(L);
   for (int b = 0; b < L; ++b) {

@@ -239,7 +239,10 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
   // stage the per-wavelength factors in shared memory when they fit in 32 KB
   const size_t smem = sizeof(float) * (size_t)(2 * L + R * L);
   const int cached = smem <= 32 * 1024 ? 1 : 0;
-  if (a.out_split && !a.out_c64 && !a.in && a.n % 4 == 0) {
+  // Four pixels per thread pays with many wavelengths; with a few, one pixel
+  // per thread gives four times the threads and a quarter of the per-thread
+  // FP64 set-up.
+  if (a.out_split && !a.out_c64 && !a.in && a.n % 4 == 0 && L >= 8) {
     // One wavelength group: spreading the wavelengths over more blocks
     // measured slower at 512^2 x 64 (42.9 vs 38.3 us) with the FP64 path
     // set-up repeated per group, and no faster (35.9 us plus 12.9 us for a

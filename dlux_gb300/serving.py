@@ -93,6 +93,17 @@ class PSFRequest:
         self.t_done = None
         self.psf = None
         self.grad = None
+        # Result buffers, allocated (and their pages touched) here in the
+        # caller's thread rather than by the scheduler when the batch retires.
+        # Fresh allocations there cost the scheduler up to ~10 ms in page
+        # faults and memory-map locking at times, which showed in p99.
+        self._psf_out = None
+        self._grad_out = None
+        if 0 < self.n_focal <= 8192:
+            self._psf_out = np.empty((self.n_focal, self.n_focal), np.float32)
+            self._psf_out.fill(0.0)   # writes every page now
+            if self.want_grad:
+                self._grad_out = np.zeros(self.coefficients.size, np.float32)
         self.error = None
         self.cancelled = False
         self.done = threading.Event()
@@ -740,9 +751,17 @@ class CudaExecutor:
         psf = slot.psf[:R * m * m].reshape(R, m, m)
         grad = slot.grad[:G * self.k_max].reshape(G, self.k_max)
         for i, r in enumerate(reqs):
-            r.psf = psf[i].copy()
+            if r._psf_out is not None and r._psf_out.shape == psf[i].shape:
+                np.copyto(r._psf_out, psf[i])
+                r.psf = r._psf_out
+            else:
+                r.psf = psf[i].copy()
             if i < G:
-                r.grad = grad[i, :r.coefficients.size].copy()
+                if r._grad_out is not None:
+                    np.copyto(r._grad_out, grad[i, :r.coefficients.size])
+                    r.grad = r._grad_out
+                else:
+                    r.grad = grad[i, :r.coefficients.size].copy()
         slot.current = None
 
     def synchronize(self):
