@@ -14,6 +14,8 @@ saves its outputs on the seeded inputs of ref_inputs.py:
   ref_cfg1.npz   config 1 through AngularOpticalSystem.propagate
                  (optical_systems.py:147-223): PSF and the gradient of
                  sum(R * PSF) with respect to the coefficients;
+  ref_unaligned.npz a system with sides that are not multiples of 8 (100^2
+                 pupil, 67^2 PSF, 4 wavelengths): PSF and coefficient gradient;
   ref_cfg2.npz   config 2 (the benchmark workload) through
                  AngularOpticalSystem + LayeredDetector([Downsample(4)]):
                  image and coefficient gradient of sum(R * image);
@@ -42,7 +44,7 @@ float64 (step h: truncation ~h^4, far below the 1e-5 tolerance of the tests).
 The script also checks the oracle (oracle/dlux_oracle.py, FP64) against every
 fixture before saving and prints the differences.
 
-    python tests/golden/make_ref_golden.py <dLux src dir> [utils cfg1 cfg2 cfg3 cfg4]
+    python tests/golden/make_ref_golden.py <dLux src dir> [utils cfg1 unaligned cfg2 ...]
 """
 
 from __future__ import annotations
@@ -171,6 +173,31 @@ def make_cfg1(dl, O):
                         128, 0.02 * RI.ARCSEC, inp["R"])
     gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
     print(f"cfg1: PSF oracle vs dLux {rel(ora, psf):.2e}, gradient oracle vs dLux FD "
+          f"{rel(gc, grad):.2e}")
+    return {"psf": psf, "loss": loss(inp["coeffs"]), "grad": grad}
+
+
+def make_unaligned(dl, O):
+    inp = RI.unaligned()
+    L = dl.layers
+    T, B = dl.utils.circular_aperture(100, 1.0, oversample=1, secondary_diameter=0.1,
+                                      zernike_nolls=inp["nolls"])
+    wls, w = inp["wavelengths"], inp["weights"]
+
+    def psf_of(c):
+        return dl.optical_systems.AngularOpticalSystem(
+            100, 1.0, [L.TransmissiveLayer(T, normalise=True), L.BasisLayer(B, c)], 67,
+            0.03, 1).propagate(wls, weights=w)
+
+    psf = psf_of(inp["coeffs"])
+    loss = lambda c: float((psf_of(c) * inp["R"]).sum())  # noqa: E731
+    grad = fd4_grad(loss, inp["coeffs"], 2e-10)
+    opd = np.tensordot(B, inp["coeffs"], axes=(0, 0))
+    ora = O.poly_psf(T, opd, wls, w, 1.0, 67, 0.03 * RI.ARCSEC)
+    Teff = T / np.sqrt((T ** 2).sum())
+    g = O.poly_psf_grad(Teff, opd, wls, w, 1.0, 67, 0.03 * RI.ARCSEC, inp["R"])
+    gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+    print(f"unaligned: PSF oracle vs dLux {rel(ora, psf):.2e}, gradient oracle vs dLux FD "
           f"{rel(gc, grad):.2e}")
     return {"psf": psf, "loss": loss(inp["coeffs"]), "grad": grad}
 
@@ -389,10 +416,12 @@ def make_apertures(dl, O):
 
 def main():
     src = sys.argv[1]
-    which = sys.argv[2:] or ["utils", "cfg1", "cfg2", "cfg3", "cfg4", "layers", "apertures"]
+    which = sys.argv[2:] or ["utils", "cfg1", "unaligned", "cfg2", "cfg3", "cfg4", "layers",
+                             "apertures"]
     dl = ref_standin.load_dlux(src)
     from oracle import dlux_oracle as O
-    makers = {"utils": make_utils, "cfg1": make_cfg1, "cfg2": make_cfg2, "cfg3": make_cfg3,
+    makers = {"utils": make_utils, "cfg1": make_cfg1, "unaligned": make_unaligned,
+              "cfg2": make_cfg2, "cfg3": make_cfg3,
               "cfg4": make_cfg4, "layers": make_layers, "apertures": make_apertures}
     for name in which:
         t0 = time.time()

@@ -79,6 +79,17 @@ def cfg1():
             "wavelengths": np.array([1.0e-6]), "nolls": list(range(4, 14))}
 
 
+def unaligned():
+    """A system whose sides are not multiples of 8: 100^2 pupil (10% obscuration),
+    Noll 4-9 ~ N(0, 50 nm), 4 wavelengths 0.9-1.1 um with Dirichlet(1) weights,
+    67^2 PSF at 0.03", loss sum(R * PSF). (An odd pupil side is avoided: dLux's
+    Zernike basis is NaN at the centre pixel of an odd grid.)"""
+    rng = np.random.default_rng(107)
+    return {"coeffs": 50e-9 * normal(rng, 6), "weights": dirichlet_ones(rng, 4),
+            "R": normal(rng, (67, 67)), "wavelengths": np.linspace(0.9e-6, 1.1e-6, 4),
+            "nolls": list(range(4, 10))}
+
+
 def cfg2():
     """Config 2 (the benchmark): 512^2 pupil with spiders, Noll 4-24 ~ N(0, 30 nm),
     64 wavelengths 0.8-1.2 um with Dirichlet(1) weights, 512^2 focal at 4x

@@ -129,6 +129,22 @@ def test_oracle_cfg1_psf_and_gradient_match_dlux():
     assert rel(gc, r["grad"]) < 1e-7
 
 
+def test_oracle_unaligned_system_matches_dlux():
+    """100^2 pupil -> 67^2 PSF, 4 wavelengths: sides that are not multiples of 8."""
+    r = _load("unaligned")
+    inp = RI.unaligned()
+    T, B = O.circular_aperture(100, 1.0, oversample=1, secondary_diameter=0.1,
+                               zernike_nolls=inp["nolls"])
+    opd = O.eval_basis(B, inp["coeffs"])
+    wls, w = inp["wavelengths"], inp["weights"]
+    psf = O.poly_psf(T, opd, wls, w, 1.0, 67, 0.03 * RI.ARCSEC)
+    assert rel(psf, r["psf"]) < 1e-9
+    Teff = T / np.sqrt((T ** 2).sum())
+    g = O.poly_psf_grad(Teff, opd, wls, w, 1.0, 67, 0.03 * RI.ARCSEC, inp["R"])
+    gc = np.tensordot(B, g["g_opd"], axes=((1, 2), (0, 1)))
+    assert rel(gc, r["grad"]) < 1e-7
+
+
 def test_oracle_cfg2_image_and_gradient_match_dlux():
     r = _load("cfg2")
     inp = RI.cfg2()
