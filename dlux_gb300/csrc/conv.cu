@@ -43,36 +43,75 @@ __global__ void conv2d_same_kernel(const float* __restrict__ in, int H, int W,
   }
   for (int t = threadIdx.x; t < K0 * K1; t += blockDim.x) ks[t] = k[t];
   __syncthreads();
-  for (int t = threadIdx.x; t < CT * CT; t += blockDim.x) {
-    const int ti = t / CT, tj = t % CT;
-    const int i = i0 + ti, j = j0 + tj;
-    if (i >= H || j >= W) continue;
-    float acc = 0.0f;
-    for (int a = 0; a < K0; ++a) {
-      // tile row of input index (convolution) i + s0 - a, (correlation) i - s0 + a
-      const int tr = flip ? ti + a : ti + K0 - 1 - a;
-      const float* row = tile + tr * TW;
-      const float* krow = ks + a * K1;
+  // Each thread computes four adjacent outputs of one tile row (CT x CT / 4 =
+  // 256 groups, one per thread), with a four-value window of the tile row that
+  // slides by one element per kernel column: one shared-memory load for the
+  // tile and one for the kernel per four FMAs. Every output keeps the term
+  // order (kernel rows, then columns) of a one-output-per-thread loop.
+  const int ti = threadIdx.x >> 3, tj0 = (threadIdx.x & 7) * 4;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int a = 0; a < K0; ++a) {
+    // tile row of input index (convolution) i + s0 - a, (correlation) i - s0 + a
+    const int tr = flip ? ti + a : ti + K0 - 1 - a;
+    const float* row = tile + tr * TW;
+    const float* krow = ks + a * K1;
+    if (flip) {
+      // output u, kernel column bb: tile column tj0 + u + bb
+      float w0 = row[tj0], w1 = row[tj0 + 1], w2 = row[tj0 + 2], w3 = row[tj0 + 3];
       for (int bb = 0; bb < K1; ++bb) {
-        const int tc = flip ? tj + bb : tj + K1 - 1 - bb;
-        acc = fmaf(row[tc], krow[bb], acc);
+        const float k = krow[bb];
+        acc[0] = fmaf(w0, k, acc[0]);
+        acc[1] = fmaf(w1, k, acc[1]);
+        acc[2] = fmaf(w2, k, acc[2]);
+        acc[3] = fmaf(w3, k, acc[3]);
+        if (bb + 1 < K1) {
+          w0 = w1; w1 = w2; w2 = w3;
+          w3 = row[tj0 + bb + 4];
+        }
+      }
+    } else {
+      // output u, kernel column bb: tile column tj0 + u + K1 - 1 - bb
+      float w0 = row[tj0 + K1 - 1], w1 = row[tj0 + K1], w2 = row[tj0 + K1 + 1],
+            w3 = row[tj0 + K1 + 2];
+      for (int bb = 0; bb < K1; ++bb) {
+        const float k = krow[bb];
+        acc[0] = fmaf(w0, k, acc[0]);
+        acc[1] = fmaf(w1, k, acc[1]);
+        acc[2] = fmaf(w2, k, acc[2]);
+        acc[3] = fmaf(w3, k, acc[3]);
+        if (bb + 1 < K1) {
+          w3 = w2; w2 = w1; w1 = w0;
+          w0 = row[tj0 + K1 - 2 - bb];
+        }
       }
     }
-    out[(long long)b * H * W + (long long)i * W + j] = acc;
+  }
+  const int i = i0 + ti;
+  if (i < H) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = j0 + tj0 + u;
+      if (j < W) out[(long long)b * H * W + (long long)i * W + j] = acc[u];
+    }
   }
 }
 
 // g_k[a][c] = sum_{i,j} g_out[i][j] in[i + s0 - a][j + s1 - c] over every batch
 // element (kernel row a, kernel column c), in two stages.
 // Stage 1: a block takes kernel row a, a chunk of KC kernel columns and a band
-// of image rows, over every batch element. Each thread keeps KC float-pair
-// sums: one g_out value meets the KC shifted input values of its row, which
-// are read through L1. The block's sums go to part[band][a][c] in double.
-// Compared with one block per kernel element, g_out and the input are read
-// from L2 once per chunk instead of once per kernel element.
+// of image rows, over every batch element. One g_out value meets the KC shifted
+// input values of its row, which are read through L1. Each thread sums its
+// products in FP32 kFold at a time and folds those partial sums into KC float
+// pairs (Knuth's TwoSum), so the per-product cost is one FMA: a partial of 16
+// products loses ~1e-6 of its own size at most, far below the tolerance, and
+// the float pairs keep the long sum over the band exact to that order. The block's sums go to part[band][a][c] in double. Compared with
+// one block per kernel element, g_out and the input are read from L2 once per
+// chunk instead of once per kernel element. KC is chosen per kernel width so
+// that the chunks divide it with the least padding.
 // Stage 2: g_k[a][c] sums the bands in order, so the result is deterministic.
-constexpr int KC = 16;
+constexpr int kFold = 16;
 
+template <int KC>
 __global__ void __launch_bounds__(256) conv2d_kgrad_rows_kernel(
     const float* __restrict__ in, const float* __restrict__ g, int H, int W, int batch, int K0,
     int K1, int rows_per_band, double* __restrict__ part) {
@@ -84,10 +123,21 @@ __global__ void __launch_bounds__(256) conv2d_kgrad_rows_kernel(
   // rows i of the band with i + s0 - a in [0, H)
   const int i0 = max(band * rows_per_band, max(0, a - s0));
   const int i1 = min(min(H, (band + 1) * rows_per_band), H + a - s0);
-  float hi[KC], lo[KC];
+  float hi[KC], lo[KC], acc[KC];
 #pragma unroll
-  for (int q = 0; q < KC; ++q) hi[q] = lo[q] = 0.f;
+  for (int q = 0; q < KC; ++q) hi[q] = lo[q] = acc[q] = 0.f;
+  auto fold = [&]() {
+#pragma unroll
+    for (int q = 0; q < KC; ++q) {
+      const float t = hi[q] + acc[q];
+      const float bv = t - hi[q];
+      lo[q] += (hi[q] - (t - bv)) + (acc[q] - bv);
+      hi[q] = t;
+      acc[q] = 0.f;
+    }
+  };
   const long long npix = (long long)H * W;
+  int terms = 0;
   for (int b = 0; b < batch; ++b) {
     for (int i = i0; i < i1; ++i) {
       const float* grow = g + b * npix + (long long)i * W;
@@ -97,19 +147,16 @@ __global__ void __launch_bounds__(256) conv2d_kgrad_rows_kernel(
 #pragma unroll
         for (int q = 0; q < KC; ++q) {
           const int c = j + s1 - (c0 + q);  // input column of kernel column c0 + q
-          if (c0 + q < K1 && c >= 0 && c < W) {
-            const float y = __ldg(xrow + c);
-            const float pr = x * y;
-            const float pe = fmaf(x, y, -pr);
-            const float t = hi[q] + pr;
-            const float bv = t - hi[q];
-            lo[q] += ((hi[q] - (t - bv)) + (pr - bv)) + pe;
-            hi[q] = t;
-          }
+          if (c0 + q < K1 && c >= 0 && c < W) acc[q] = fmaf(x, __ldg(xrow + c), acc[q]);
+        }
+        if (++terms == kFold) {
+          fold();
+          terms = 0;
         }
       }
     }
   }
+  fold();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int q = 0; q < KC; ++q) {
@@ -137,7 +184,11 @@ __global__ void conv2d_kgrad_sum_kernel(const double* __restrict__ part, int nba
 
 int launch_conv_kgrad(const float* in, const float* g, int H, int W, int batch, int K0, int K1,
                       float* g_k, cudaStream_t s) {
-  const int nchunk = (K1 + KC - 1) / KC;
+  // the chunk width with the least padding of K1 (ties to the wider chunk)
+  int kc = 16;
+  for (int c : {16, 12, 11, 8, 4})
+    if (((K1 + c - 1) / c) * c < ((K1 + kc - 1) / kc) * kc) kc = c;
+  const int nchunk = (K1 + kc - 1) / kc;
   // about two blocks per SM in all
   int sms = 0;
   DLX_TRY(device_sm_count(&sms));
@@ -149,8 +200,14 @@ int launch_conv_kgrad(const float* in, const float* g, int H, int W, int batch, 
   const int nk = K0 * K1;
   double* part = nullptr;
   DLX_TRY_CUDA(cudaMallocAsync((void**)&part, sizeof(double) * (size_t)nband * nk, s));
-  conv2d_kgrad_rows_kernel<<<dim3(K0, nchunk, nband), 256, 0, s>>>(in, g, H, W, batch, K0, K1,
-                                                                    rows, part);
+  const dim3 grid(K0, nchunk, nband);
+  switch (kc) {
+    case 4: conv2d_kgrad_rows_kernel<4><<<grid, 256, 0, s>>>(in, g, H, W, batch, K0, K1, rows, part); break;
+    case 8: conv2d_kgrad_rows_kernel<8><<<grid, 256, 0, s>>>(in, g, H, W, batch, K0, K1, rows, part); break;
+    case 11: conv2d_kgrad_rows_kernel<11><<<grid, 256, 0, s>>>(in, g, H, W, batch, K0, K1, rows, part); break;
+    case 12: conv2d_kgrad_rows_kernel<12><<<grid, 256, 0, s>>>(in, g, H, W, batch, K0, K1, rows, part); break;
+    default: conv2d_kgrad_rows_kernel<16><<<grid, 256, 0, s>>>(in, g, H, W, batch, K0, K1, rows, part); break;
+  }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
     conv2d_kgrad_sum_kernel<<<(nk + 255) / 256, 256, 0, s>>>(part, nband, nk, g_k);
@@ -178,6 +235,8 @@ int launch_conv(const float* in, int batch, int H, int W, const float* k, int K0
     DLX_TRY_CUDA(cudaFuncSetAttribute(conv2d_same_kernel,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((W + CT - 1) / CT, (H + CT - 1) / CT, batch);
+  // 256 threads: one group of four outputs of a CT x CT tile each
+  static_assert(CT * CT / 4 == 256, "one output group per thread");
   conv2d_same_kernel<<<grid, 256, smem, s>>>(in, H, W, k, K0, K1, flip, out);
   DLX_LAUNCH_CHECK("conv2d_same_kernel");
   return DLX_OK;
