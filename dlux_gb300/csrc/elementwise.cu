@@ -248,7 +248,8 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     // set-up repeated per group, and no faster (35.9 us plus 12.9 us for a
     // separate FP64 pass over the pixels) with the set-up done once: the
     // per-element phase reduction and sincos bound the kernel.
-    // 4 pixels per thread (2 measured the same at 512^2 x 64)
+    // 4 pixels per thread (2 measured the same at 512^2 x 64, 8 slower: 42.0
+    // vs 37.0 us)
     constexpr int V = 4;
     DLX_PDL_LAUNCH("phasor_splitv_kernel", phasor_splitv_kernel<V>,
                    dim3(ceil_div(npix / V, 256), 1), dim3(256), cached ? smem : 0, s, a,
@@ -548,7 +549,17 @@ __global__ void basis_eval_kernel(const float* __restrict__ basis,
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
   float acc = base ? base[p] : 0.f;
-  for (int k = 0; k < nterms; ++k) acc = fmaf(sc[k], __ldg(basis + (long long)k * npix + p), acc);
+  // eight terms' loads issued before their FMAs (which keep the term order),
+  // so that the loads' latencies overlap
+  int k = 0;
+  for (; k + 8 <= nterms; k += 8) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(basis + (long long)(k + u) * npix + p);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc = fmaf(sc[k + u], v[u], acc);
+  }
+  for (; k < nterms; ++k) acc = fmaf(sc[k], __ldg(basis + (long long)k * npix + p), acc);
   out[p] = acc;
 }
 
