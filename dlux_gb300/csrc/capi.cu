@@ -815,6 +815,12 @@ int dlx_downsample_backward(const float* in, const float* g_out, int n_in, int k
 // the most a plan uses; small pupils use fewer, of at least 256 pixels each.
 constexpr int kPolyParts = 1024;
 
+// Pixel chunks of a plan's reductions: 256 pupil pixels or more each (one per
+// thread of a block), at most kPolyParts. The workspace size depends on it.
+static int poly_nparts(int n_in) {
+  return (int)std::max(1LL, std::min((long long)kPolyParts, ((long long)n_in * n_in + 255) / 256));
+}
+
 struct dlx_poly_plan_s {
   TwoStep ts;
   double pixel_scale_in = 0;
@@ -1158,10 +1164,7 @@ static int poly_create(const dlx_poly_desc* d, const double* wl, int max_objects
   ts.wl.assign(wl, wl + L);
   p->pixel_scale_in = d->pixel_scale_in;
   p->max_obj = max_objects;
-  // pixel chunks of the reverse-pass reductions: 256 pupil pixels or more each
-  // (one per thread of a block), at most kPolyParts
-  p->nparts = (int)std::max(1LL, std::min((long long)kPolyParts,
-                                          ((long long)d->n_in * d->n_in + 255) / 256));
+  p->nparts = poly_nparts(d->n_in);
   std::vector<DftAxis> ax(L);
   std::vector<float> alphas(L);
   for (int b = 0; b < L; ++b) {
@@ -1230,7 +1233,8 @@ int dlx_poly_workspace_bytes(const dlx_poly_desc* d, int max_objects, size_t* by
   if (d->n_wavelengths <= 0 || d->n_in <= 0 || d->n_out <= 0 || max_objects <= 0)
     return fail(DLX_ERR_SHAPE, "poly_workspace_bytes: sizes must be positive");
   size_t sz[kPolyBuffers];
-  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, kPolyParts, false, sz);
+  poly_ws_sizes(d->n_wavelengths, d->n_in, d->n_out, max_objects, poly_nparts(d->n_in), false,
+                sz);
   *bytes = 0;
   for (int i = 0; i < kPolyBuffers; ++i) *bytes += sz[i];
   return DLX_OK;

@@ -442,7 +442,17 @@ __global__ void sumsq_partial_kernel(const float* __restrict__ x, long long npix
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(npix, lo + chunk);
   double acc = 0.0;
-  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+  const long long step = blockDim.x;
+  long long p = lo + threadIdx.x;
+  // eight loads in flight before the adds, which keep the element order
+  for (; p + 7 * step < hi; p += 8 * step) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldg(x + p + u * step);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc += (double)v[u] * (double)v[u];
+  }
+  for (; p < hi; p += step) {
     double v = x[p];
     acc += v * v;
   }
@@ -550,7 +560,8 @@ __global__ void basis_eval_kernel(const float* __restrict__ basis,
   if (p >= npix) return;
   float acc = base ? base[p] : 0.f;
   // eight terms' loads issued before their FMAs (which keep the term order),
-  // so that the loads' latencies overlap
+  // so that the loads' latencies overlap (4 and 6 at a time measured the
+  // same; sixteen with the last group masked 2.7x slower: 24.8 against 9.1 us)
   int k = 0;
   for (; k + 8 <= nterms; k += 8) {
     float v[8];
@@ -586,8 +597,7 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
   // product is split exactly into p + e (fmaf), the running sum is kept as a
   // float pair with Knuth's TwoSum, and only the per-thread pair is widened.
   float hi_s = 0.f, lo_s = 0.f;
-  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-    const float x = __ldg(row + p), y = __ldg(g + p);
+  auto add = [&](float x, float y) {
     const float pr = x * y;
     const float pe = fmaf(x, y, -pr);
     const float t = hi_s + pr;
@@ -595,7 +605,21 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
     const float err = (hi_s - (t - bv)) + (pr - bv);
     hi_s = t;
     lo_s += err + pe;
+  };
+  const long long step = blockDim.x;
+  long long p = lo + threadIdx.x;
+  // eight pixels' loads in flight before the (ordered) float-pair sums
+  for (; p + 7 * step < hi; p += 8 * step) {
+    float xv[8], yv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      xv[u] = __ldg(row + p + u * step);
+      yv[u] = __ldg(g + p + u * step);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) add(xv[u], yv[u]);
   }
+  for (; p < hi; p += step) add(__ldg(row + p), __ldg(g + p));
   double t = block_sum<256>((double)hi_s + (double)lo_s, smem);
   if (threadIdx.x == 0) partial[(long long)k * nparts + blockIdx.x] = t;
 }
@@ -626,19 +650,40 @@ int launch_basis_grad(const float* basis, const float* g, int nterms, long long 
 // Detector: k x k block sum (utils/array_ops.py:124-162) x pixel response
 // (layers/detector_layers.py:100-131), and the reverse.
 // ---------------------------------------------------------------------------
+// KC > 0: the block side known at compile time, so that all KC * KC loads of
+// a thread are issued before its adds; KC = 0 reads k at run time. The sums
+// run row by row in the same order either way.
+template <int KC>
 __global__ void downsample_kernel(const float* __restrict__ in, int n_in, int k, int mean,
                                   const float* __restrict__ flat, float* __restrict__ out) {
   pdl_enter();
+  if (KC > 0) k = KC;
   const int n_out = n_in / k;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const int a = blockIdx.y * blockDim.y + threadIdx.y;
   if (a >= n_out || c >= n_out) return;
   float acc = 0.f;
-  for (int i = 0; i < k; ++i) {
-    const float* row = in + (long long)(a * k + i) * n_in + (long long)c * k;
-    float r = 0.f;
-    for (int j = 0; j < k; ++j) r += row[j];
-    acc += r;
+  if (KC > 0) {
+    constexpr int K = KC > 0 ? KC : 1;
+    float v[K][K];
+#pragma unroll
+    for (int i = 0; i < K; ++i)
+#pragma unroll
+      for (int j = 0; j < K; ++j) v[i][j] = __ldg(in + (long long)(a * K + i) * n_in + c * K + j);
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      float r = 0.f;
+#pragma unroll
+      for (int j = 0; j < K; ++j) r += v[i][j];
+      acc += r;
+    }
+  } else {
+    for (int i = 0; i < k; ++i) {
+      const float* row = in + (long long)(a * k + i) * n_in + (long long)c * k;
+      float r = 0.f;
+      for (int j = 0; j < k; ++j) r += row[j];
+      acc += r;
+    }
   }
   if (mean) acc /= (float)(k * k);
   if (flat) acc *= flat[(long long)a * n_out + c];
@@ -651,8 +696,23 @@ int launch_downsample(const float* in, int n_in, int k, int mean, const float* f
   if (n_out == 0) return DLX_OK;
   dim3 block(32, 8);
   dim3 grid(ceil_div(n_out, 32), ceil_div(n_out, 8));
-  DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel, grid, block, 0, s, in, n_in, k, mean,
-                 flat, out);
+  switch (k) {
+    case 2:
+      DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel<2>, grid, block, 0, s, in, n_in, k,
+                     mean, flat, out);
+      break;
+    case 3:
+      DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel<3>, grid, block, 0, s, in, n_in, k,
+                     mean, flat, out);
+      break;
+    case 4:
+      DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel<4>, grid, block, 0, s, in, n_in, k,
+                     mean, flat, out);
+      break;
+    default:
+      DLX_PDL_LAUNCH("downsample_kernel", downsample_kernel<0>, grid, block, 0, s, in, n_in, k,
+                     mean, flat, out);
+  }
   return DLX_OK;
 }
 
@@ -701,7 +761,10 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
   float total = 0.f;
   for (int r = 0; r < R; ++r) {
     float s = 0.f;
-    // unrolled so that eight planes' loads are in flight; the sum keeps its order
+    // unrolled so that eight planes' loads are in flight; the sum keeps its
+    // order. Measured at 512^2 x 64 planes: 15.0 us; 16 or 32 in flight 19.8
+    // and 31.9 us; 16-byte loads of 4 pixels with 2, 4 or 8 in flight 21.8,
+    // 15.5 and 22.2 us.
 #pragma unroll 8
     for (int l = 0; l < a.L; ++l) s += a.planes[((long long)l * R + r) * a.npix + p];
     if (a.outs.o[r].psf) a.outs.o[r].psf[p] = s;
