@@ -131,6 +131,53 @@ __host__ __device__ __forceinline__ FF ff_from_double(double v) {
   return r;
 }
 
+// Float-pair arithmetic in FP32 alone (FP64 issues at a small fraction of
+// the FP32 rate on this GPU): TwoSum (Knuth), Fast2Sum (Dekker, |a| >= |b|)
+// and Dekker's product through one FMA. Results are normalised pairs within a
+// few units of 2^-46 of the exact value, relative.
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bv = s - a;
+  return FF{s, (a - (s - bv)) + (b - bv)};
+}
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return FF{s, b - (s - a)};
+}
+// v * c for a float v and a float pair c
+__device__ __forceinline__ FF ff_mul(float v, FF c) {
+  const float p = v * c.hi;
+  const float e = fmaf(v, c.hi, -p);
+  return ff_fast_two_sum(p, fmaf(v, c.lo, e));
+}
+// a + b for float pairs
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_two_sum(s.hi, s.lo + (a.lo + b.lo));
+}
+// 1 / (2 pi) as a float pair
+__device__ __forceinline__ FF ff_inv_two_pi() { return FF{0x1.45f306p-3f, 0x1.b93910p-28f}; }
+
+// Per-pixel inputs of cis_ff, formed once per pixel and object: the optical
+// path opd + tx X + ty Y (m) with X = (x - c) dx, Y = (y - c) dx and
+// c = (n - 1) / 2, from the float pairs t = (tx dx, ty dx); and the phase
+// (radians) in cycles. xc = x - c and yc = y - c are exact in FP32. With no
+// tilt the path is (opd, 0) exactly.
+__device__ __forceinline__ FF pupil_path(float opd, float xc, float yc, float4 t) {
+  FF path{opd, 0.f};
+  if (t.x != 0.f || t.z != 0.f) {
+    path = ff_add(path, ff_mul(xc, FF{t.x, t.y}));
+    path = ff_add(path, ff_mul(yc, FF{t.z, t.w}));
+  }
+  return path;
+}
+__device__ __forceinline__ FF phase_cycles(float phase) { return ff_mul(phase, ff_inv_two_pi()); }
+// (tx dx, ty dx) as float pairs; FP64 once per object
+__host__ __device__ __forceinline__ float4 tilt_pairs(double tx, double ty, double dx) {
+  const FF a = ff_from_double(tx * dx), b = ff_from_double(ty * dx);
+  return make_float4(a.hi, a.lo, b.hi, b.lo);
+}
+
 __device__ __forceinline__ float2 cis_ff(FF path, FF inv_lambda, FF phase_cycles) {
   const float p = path.hi * inv_lambda.hi;
   const float e = fmaf(path.hi, inv_lambda.hi, -p);  // exact residual of the product
@@ -167,6 +214,21 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
   hi = __float2bfloat16_rn(x);
   lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// split_bf16 of two values with one packed conversion (cvt.rn.bf16x2.f32)
+// for both hi parts and one for both lo parts: the same bits as two
+// split_bf16 calls, half the conversion instructions.
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, __nv_bfloat16& h0,
+                                             __nv_bfloat16& h1, __nv_bfloat16& l0,
+                                             __nv_bfloat16& l1) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+  const float2 hf = __bfloat1622float2(h);
+  const __nv_bfloat162 l = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+  h0 = h.x;
+  h1 = h.y;
+  l0 = l.x;
+  l1 = l.y;
 }
 
 inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }

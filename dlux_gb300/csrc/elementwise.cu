@@ -70,6 +70,7 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
   // cached: per-wavelength 1/lambda pairs and per-(object, wavelength)
   // sqrt(weight) staged once per block in shared memory
   extern __shared__ float psm[];
+  __shared__ float4 s_tilt[kMaxObj];
   const long long npix = (long long)a.n * a.n;
   const int R = a.objs.n > 0 ? a.objs.n : 1;
   const int L = a.batch / R;
@@ -83,15 +84,18 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
       const float* o_w = a.objs.n > 0 ? a.objs.o[r].weights : a.weights;
       c_sw[i] = o_w ? sqrtf(o_w[wl]) : 1.0f;
     }
-    __syncthreads();
   }
+  for (int r = threadIdx.x; r < R; r += blockDim.x)
+    s_tilt[r] = a.objs.n > 0 ? tilt_pairs(a.objs.o[r].tilt_x, a.objs.o[r].tilt_y, a.pixel_scale)
+                             : tilt_pairs(a.tilt_x, a.tilt_y, a.pixel_scale);
+  __syncthreads();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
   const int y = (int)(p / a.n);
   const int x = (int)(p - (long long)y * a.n);
-  const double half = 0.5 * (a.n - 1);
-  const double X = ((double)x - half) * a.pixel_scale;
-  const double Y = ((double)y - half) * a.pixel_scale;
+  const float half = 0.5f * (float)(a.n - 1);
+  const float xc = (float)x - half, yc = (float)y - half;
+  const float cs = (float)a.const_scale;
   // Objects r of a batched plan (b = l * R + r), or one object described by
   // the plain fields of PhasorArgs.
   for (int r = 0; r < R; ++r) {
@@ -101,15 +105,13 @@ __global__ void phasor_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached) 
     const float* o_opd = obj ? a.objs.o[r].opd : a.opd;
     const float* o_phase = obj ? a.objs.o[r].phase : a.phase;
     const float* o_w = obj ? a.objs.o[r].weights : a.weights;
-    const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
-    const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
-    // Per pixel and object, once: optical path (m) and phase (cycles) in FP64, as float pairs.
-    const FF path = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
-    const FF ph_cyc = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+    // Per pixel and object, once: optical path (m) and phase (cycles) as float pairs.
+    const FF path = pupil_path(o_opd ? o_opd[p] : 0.f, xc, yc, s_tilt[r]);
+    const FF ph_cyc = o_phase ? phase_cycles(o_phase[p]) : FF{0.f, 0.f};
     if (a.out_path) a.out_path[(long long)r * npix + p] = make_float4(path.hi, path.lo, ph_cyc.hi, ph_cyc.lo);
     float amp = o_amp ? o_amp[p] : 1.0f;
     if (o_scale) amp *= *o_scale;
-    amp *= (float)a.const_scale;
+    amp *= cs;
     for (int wl = 0; wl < L; ++wl) {
       const int b = wl * R + r;
       const float2 il2 = cached ? c_il[wl]
@@ -155,6 +157,7 @@ template <int V>
 __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int cached, int lg) {
   pdl_enter();
   extern __shared__ float psm[];
+  __shared__ float4 s_tilt[kMaxObj];
   const long long npix = (long long)a.n * a.n;
   const int R = a.objs.n > 0 ? a.objs.n : 1;
   const int L = a.batch / R;
@@ -168,14 +171,18 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
       const float* o_w = a.objs.n > 0 ? a.objs.o[r].weights : a.weights;
       c_sw[i] = o_w ? sqrtf(o_w[wl]) : 1.0f;
     }
-    __syncthreads();
   }
+  for (int r = threadIdx.x; r < R; r += blockDim.x)
+    s_tilt[r] = a.objs.n > 0 ? tilt_pairs(a.objs.o[r].tilt_x, a.objs.o[r].tilt_y, a.pixel_scale)
+                             : tilt_pairs(a.tilt_x, a.tilt_y, a.pixel_scale);
+  __syncthreads();
   const long long p0 = V * ((long long)blockIdx.x * blockDim.x + threadIdx.x);
   if (p0 >= npix) return;
   const int y = (int)(p0 / a.n);
   const int x0 = (int)(p0 - (long long)y * a.n);
-  const double half = 0.5 * (a.n - 1);
-  const double Y = ((double)y - half) * a.pixel_scale;
+  const float half = 0.5f * (float)(a.n - 1);
+  const float yc = (float)y - half;
+  const float cs = (float)a.const_scale;
   for (int r = 0; r < R; ++r) {
     const bool obj = a.objs.n > 0;
     const float* o_amp = obj ? a.objs.o[r].amp : a.amp;
@@ -183,23 +190,21 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
     const float* o_opd = obj ? a.objs.o[r].opd : a.opd;
     const float* o_phase = obj ? a.objs.o[r].phase : a.phase;
     const float* o_w = obj ? a.objs.o[r].weights : a.weights;
-    const double tx = obj ? a.objs.o[r].tilt_x : a.tilt_x;
-    const double ty = obj ? a.objs.o[r].tilt_y : a.tilt_y;
     const float scale = (o_scale ? *o_scale : 1.0f);
+    const float4 t = s_tilt[r];
     FF path[V], ph[V];
     float amp[V];
 #pragma unroll
     for (int k = 0; k < V; ++k) {
       const long long p = p0 + k;
-      const double X = ((double)(x0 + k) - half) * a.pixel_scale;
-      path[k] = ff_from_double((o_opd ? (double)o_opd[p] : 0.0) + tx * X + ty * Y);
-      ph[k] = ff_from_double(o_phase ? (double)o_phase[p] * (0.5 / CUDART_PI) : 0.0);
+      path[k] = pupil_path(o_opd ? o_opd[p] : 0.f, (float)(x0 + k) - half, yc, t);
+      ph[k] = o_phase ? phase_cycles(o_phase[p]) : FF{0.f, 0.f};
       if (a.out_path && blockIdx.y == 0)
         a.out_path[(long long)r * npix + p] =
             make_float4(path[k].hi, path[k].lo, ph[k].hi, ph[k].lo);
       float am = o_amp ? o_amp[p] : 1.0f;
       if (o_scale) am *= scale;
-      amp[k] = am * (float)a.const_scale;
+      amp[k] = am * cs;
     }
     const int wl1 = min(L, (int)(blockIdx.y + 1) * lg);
     for (int wl = blockIdx.y * lg; wl < wl1; ++wl) {
@@ -210,12 +215,20 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
       if (cached) sw = c_sw[r * L + wl];
       else if (o_w) sw = sqrtf(o_w[wl]);
       Bf16Vec<V> q[4];
+      float re[V], im[V];
 #pragma unroll
       for (int k = 0; k < V; ++k) {
         const float2 u = cis_ff_split(path[k], FF{il2.x, il2.y}, ph[k]);
         const float sc = amp[k] * sw;
-        split_bf16(u.x * sc, q[0].v[k], q[1].v[k]);
-        split_bf16(u.y * sc, q[2].v[k], q[3].v[k]);
+        re[k] = u.x * sc;
+        im[k] = u.y * sc;
+      }
+      // adjacent pixels' splits share packed conversions
+      static_assert(V % 2 == 0, "pixels are split in pairs");
+#pragma unroll
+      for (int k = 0; k < V; k += 2) {
+        split_bf16x2(re[k], re[k + 1], q[0].v[k], q[0].v[k + 1], q[1].v[k], q[1].v[k + 1]);
+        split_bf16x2(im[k], im[k + 1], q[2].v[k], q[2].v[k + 1], q[3].v[k], q[3].v[k + 1]);
       }
       const long long splane = split_plane(a.n, a.n);
       __nv_bfloat16* base =
@@ -250,10 +263,15 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     // per-element phase reduction and sincos bound the kernel.
     // 4 pixels per thread (2 measured the same at 512^2 x 64, 8 slower: 42.0
     // vs 37.0 us)
+    // With the path set-up in FP32 float pairs, 2 and 4 wavelength groups
+    // measured 30.5 and 30.3 us against 30.7 us for one.
     constexpr int V = 4;
+    constexpr int kPhasorGroups = 1;
+    const int lg = (L + kPhasorGroups - 1) / kPhasorGroups;
+    const int gy = (L + lg - 1) / lg;
     DLX_PDL_LAUNCH("phasor_splitv_kernel", phasor_splitv_kernel<V>,
-                   dim3(ceil_div(npix / V, 256), 1), dim3(256), cached ? smem : 0, s, a,
-                   *inv_lambda_arg, cached, L);
+                   dim3(ceil_div(npix / V, 256), gy), dim3(256), cached ? smem : 0, s, a,
+                   *inv_lambda_arg, cached, lg);
     return DLX_OK;
   } else if (a.out_split && !a.out_c64 && !a.in)
     phasor_kernel<true><<<ceil_div(npix, 256), 256, cached ? smem : 0, s>>>(a, *inv_lambda_arg,
@@ -333,10 +351,18 @@ __global__ void focal_gradf_kernel(const float2* f, ObjTable objs, int batch, in
       }
       if (out_split) {
         Bf16Vec<V> q[4];
+        if constexpr (V % 2 == 0) {
 #pragma unroll
-        for (int k = 0; k < V; ++k) {
-          split_bf16(o[k].x, q[0].v[k], q[1].v[k]);
-          split_bf16(o[k].y, q[2].v[k], q[3].v[k]);
+          for (int k = 0; k < V; k += 2) {
+            split_bf16x2(o[k].x, o[k + 1].x, q[0].v[k], q[0].v[k + 1], q[1].v[k], q[1].v[k + 1]);
+            split_bf16x2(o[k].y, o[k + 1].y, q[2].v[k], q[2].v[k + 1], q[3].v[k], q[3].v[k + 1]);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < V; ++k) {
+            split_bf16(o[k].x, q[0].v[k], q[1].v[k]);
+            split_bf16(o[k].y, q[2].v[k], q[3].v[k]);
+          }
         }
         __nv_bfloat16* base = out_split + b * 4 * splane + sp;
 #pragma unroll
@@ -823,10 +849,12 @@ __global__ void obj_pupil_pix_kernel(ObjReduceArgs a) {
     if (out.g_amp) out.g_amp[p] = sre;
     if (out.g_phase) out.g_phase[p] = sim;
     if (out.g_opd) out.g_opd[p] = sk;
-    const int y = (int)(p / a.n_side);
-    const int x = (int)(p - (long long)y * a.n_side);
-    tx += ((double)x - half) * a.pixel_scale * (double)sk;
-    ty += ((double)y - half) * a.pixel_scale * (double)sk;
+    if (out.g_tilt) {  // FP64 partials only when a tilt gradient is wanted
+      const int y = (int)(p / a.n_side);
+      const int x = (int)(p - (long long)y * a.n_side);
+      tx += ((double)x - half) * a.pixel_scale * (double)sk;
+      ty += ((double)y - half) * a.pixel_scale * (double)sk;
+    }
   }
   if (out.g_tilt) {
     const double sx = block_sum<256>(tx, smem);
@@ -994,10 +1022,12 @@ __global__ void __launch_bounds__(256, 4) obj_pupil_fused_kernel(ObjReduceArgs a
         sc[a.npix + p] = sim;
         sc[2 * a.npix + p] = sk;
       }
-      const int y = (int)(p / a.n_side);
-      const int x = (int)(p - (long long)y * a.n_side);
-      tx += ((double)x - half) * a.pixel_scale * (double)sk;
-      ty += ((double)y - half) * a.pixel_scale * (double)sk;
+      if (out.g_tilt) {  // FP64 partials only when a tilt gradient is wanted
+        const int y = (int)(p / a.n_side);
+        const int x = (int)(p - (long long)y * a.n_side);
+        tx += ((double)x - half) * a.pixel_scale * (double)sk;
+        ty += ((double)y - half) * a.pixel_scale * (double)sk;
+      }
     }
   }
   if (out.g_tilt) {
