@@ -207,6 +207,7 @@ __global__ void phasor_splitv_kernel(PhasorArgs a, BatchFF inv_lambda_arg, int c
       amp[k] = am * cs;
     }
     const int wl1 = min(L, (int)(blockIdx.y + 1) * lg);
+    // (unrolling this loop by 2 or 4 measured 31.5 / 31.7 against 30.9 us)
     for (int wl = blockIdx.y * lg; wl < wl1; ++wl) {
       const int b = wl * R + r;
       const float2 il2 = cached ? c_il[wl]
@@ -977,7 +978,38 @@ __global__ void __launch_bounds__(256, 4) obj_pupil_fused_kernel(ObjReduceArgs a
     // The Ebar loads of eight wavelengths are issued before their arithmetic,
     // so that their latencies overlap.
     constexpr int kPre = 8;  // measured: 8 beats 4 (-6.5 us per 64-wavelength step) and 2
-    for (int l0 = 0; l0 < a.L; l0 += kPre) {
+    // Whole live warps take the wavelengths in groups of kPreFast with no
+    // per-element masks, then the rest in the masked loop below: the same
+    // arithmetic in the same order. Measured at 512^2 x 64: 29.6 us with
+    // groups of 16, 37.4 with 8, 43.9 with 4 (40.0 us with masks throughout).
+    constexpr int kPreFast = 16;
+    const bool fast = __all_sync(0xffffffffu, live) && !w_out;
+    const int l_fast = fast ? a.L - a.L % kPreFast : 0;
+    {
+      const float2* ep = a.ebar + (long long)r * a.npix + p;
+      const long long estride = (long long)R * a.npix;
+      for (int l0 = 0; l0 < l_fast; l0 += kPreFast) {
+        float2 ebq[kPreFast];
+#pragma unroll
+        for (int j = 0; j < kPreFast; ++j) ebq[j] = __ldg(ep + (long long)(l0 + j) * estride);
+#pragma unroll
+        for (int j = 0; j < kPreFast; ++j) {
+          const float2 eb = ebq[j];
+          const float4 c = lam[l0 + j];
+          const float2 u = kSplit ? cis_ff_split(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w})
+                                  : cis_ff(FF{q.x, q.y}, FF{c.x, c.y}, FF{q.z, q.w});
+          const float sw = c.z;
+          const float pr = u.x * eb.x + u.y * eb.y;
+          const float pi = u.x * eb.y - u.y * eb.x;
+          const float pre = sw * pr;
+          const float pim = amp * sw * pi;
+          sre += pre;
+          sim += pim;
+          sk += c.w * pim;
+        }
+      }
+    }
+    for (int l0 = l_fast; l0 < a.L; l0 += kPre) {
       float2 ebq[kPre];
 #pragma unroll
       for (int j = 0; j < kPre; ++j)
@@ -986,7 +1018,7 @@ __global__ void __launch_bounds__(256, 4) obj_pupil_fused_kernel(ObjReduceArgs a
 #pragma unroll
       for (int j = 0; j < kPre; ++j) {
         const int l = l0 + j;
-        if (l >= a.L) break;  // block-uniform
+        if (l >= a.L) break;  // warp-uniform (l_fast is)
         float pre = 0.f;
         if (live) {
           const float2 eb = ebq[j];
