@@ -575,6 +575,31 @@ int launch_amp_norm_backward(const float* amp, const float* g_eff, long long npi
 // ---------------------------------------------------------------------------
 // Basis contraction (utils/math.py:177-196) and its reverse.
 // ---------------------------------------------------------------------------
+// acc + sum_{u < C} c[k + u] B[k + u][p] in term order, the C loads issued first
+template <int C>
+__device__ __forceinline__ float basis_terms(const float* __restrict__ basis, const float* sc,
+                                             int k, long long npix, long long p, float acc) {
+  float v[C];
+#pragma unroll
+  for (int u = 0; u < C; ++u) v[u] = __ldg(basis + (long long)(k + u) * npix + p);
+#pragma unroll
+  for (int u = 0; u < C; ++u) acc = fmaf(sc[k + u], v[u], acc);
+  return acc;
+}
+
+// basis_terms<rem> for a run-time rem in [0, C]
+template <int C>
+__device__ __forceinline__ float basis_tail(const float* __restrict__ basis, const float* sc,
+                                            int k, int rem, long long npix, long long p,
+                                            float acc) {
+  if constexpr (C == 0) {
+    return acc;
+  } else {
+    if (rem == C) return basis_terms<C>(basis, sc, k, npix, p, acc);
+    return basis_tail<C - 1>(basis, sc, k, rem, npix, p, acc);
+  }
+}
+
 __global__ void basis_eval_kernel(const float* __restrict__ basis,
                                   const float* __restrict__ coeffs,
                                   const float* __restrict__ base, int nterms, long long npix,
@@ -586,18 +611,16 @@ __global__ void basis_eval_kernel(const float* __restrict__ basis,
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
   float acc = base ? base[p] : 0.f;
-  // eight terms' loads issued before their FMAs (which keep the term order),
-  // so that the loads' latencies overlap (4 and 6 at a time measured the
-  // same; sixteen with the last group masked 2.7x slower: 24.8 against 9.1 us)
+  // kEvalBatch terms' loads issued before their FMAs (which keep the term
+  // order), so that the loads' latencies overlap; the remainder is one batch
+  // too: 8.8 us at 512^2 x 21 terms (8.6 with 16, 9.0 with 4; a serial
+  // remainder 9.4; sixteen with the last group masked 24.8).
+  constexpr int kEvalBatch = 8;
   int k = 0;
-  for (; k + 8 <= nterms; k += 8) {
-    float v[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) v[u] = __ldg(basis + (long long)(k + u) * npix + p);
-#pragma unroll
-    for (int u = 0; u < 8; ++u) acc = fmaf(sc[k + u], v[u], acc);
-  }
-  for (; k < nterms; ++k) acc = fmaf(sc[k], __ldg(basis + (long long)k * npix + p), acc);
+  for (; k + kEvalBatch <= nterms; k += kEvalBatch)
+    acc = basis_terms<kEvalBatch>(basis, sc, k, npix, p, acc);
+  // the last nterms % kEvalBatch terms as one batch as well
+  acc = basis_tail<kEvalBatch - 1>(basis, sc, k, nterms - k, npix, p, acc);
   out[p] = acc;
 }
 
@@ -635,16 +658,18 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
   };
   const long long step = blockDim.x;
   long long p = lo + threadIdx.x;
-  // eight pixels' loads in flight before the (ordered) float-pair sums
-  for (; p + 7 * step < hi; p += 8 * step) {
-    float xv[8], yv[8];
+  // kGradBatch pixels' loads in flight before the (ordered) float-pair sums
+  // (12.3-12.5 us at 512^2 x 21 terms with 8, 13.8 with 16 or 32)
+  constexpr int kGradBatch = 8;
+  for (; p + (kGradBatch - 1) * step < hi; p += kGradBatch * step) {
+    float xv[kGradBatch], yv[kGradBatch];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < kGradBatch; ++u) {
       xv[u] = __ldg(row + p + u * step);
       yv[u] = __ldg(g + p + u * step);
     }
 #pragma unroll
-    for (int u = 0; u < 8; ++u) add(xv[u], yv[u]);
+    for (int u = 0; u < kGradBatch; ++u) add(xv[u], yv[u]);
   }
   for (; p < hi; p += step) add(__ldg(row + p), __ldg(g + p));
   double t = block_sum<256>((double)hi_s + (double)lo_s, smem);
@@ -788,12 +813,22 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
   float total = 0.f;
   for (int r = 0; r < R; ++r) {
     float s = 0.f;
-    // unrolled so that eight planes' loads are in flight; the sum keeps its
-    // order. Measured at 512^2 x 64 planes: 15.0 us; 16 or 32 in flight 19.8
-    // and 31.9 us; 16-byte loads of 4 pixels with 2, 4 or 8 in flight 21.8,
-    // 15.5 and 22.2 us.
-#pragma unroll 8
-    for (int l = 0; l < a.L; ++l) s += a.planes[((long long)l * R + r) * a.npix + p];
+    // kPsfBatch planes' loads in flight (unmasked), then the rest one by
+    // one; the sum keeps the wavelength order. Measured at 512^2 x 64 planes:
+    // 13.2 us with 16 or 32, 13.9 with 8, 15.0-15.4 with an unrolled loop of
+    // 8 (16 and 32: 19.8 and 31.9 us).
+    constexpr int kPsfBatch = 16;
+    const float* src = a.planes + (long long)r * a.npix + p;
+    const long long stride = (long long)R * a.npix;
+    int l = 0;
+    for (; l + kPsfBatch <= a.L; l += kPsfBatch) {
+      float v[kPsfBatch];
+#pragma unroll
+      for (int u = 0; u < kPsfBatch; ++u) v[u] = __ldg(src + (long long)(l + u) * stride);
+#pragma unroll
+      for (int u = 0; u < kPsfBatch; ++u) s += v[u];
+    }
+    for (; l < a.L; ++l) s += __ldg(src + (long long)l * stride);
     if (a.outs.o[r].psf) a.outs.o[r].psf[p] = s;
     total += s;
   }
