@@ -767,7 +767,9 @@ int dlx_basis_grad(const float* basis, const float* g, int nterms, long long npi
   if (nterms == 0) return DLX_OK;
   if (!basis || !g || !g_coeffs) return fail(DLX_ERR_ARG, "basis_grad: null pointer");
   cudaStream_t s = as_stream(stream);
-  const int nparts = 64;
+  int sms = 0;
+  DLX_TRY(device_sm_count(&sms));
+  const int nparts = basis_grad_parts(nterms, npix, sms);
   double* ws = nullptr;
   DLX_TRY(with_partials((size_t)nparts * nterms, s, &ws));
   int st = launch_basis_grad(basis, g, nterms, npix, g_coeffs, ws, nparts, s);

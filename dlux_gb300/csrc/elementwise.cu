@@ -3,6 +3,7 @@
 // each is written for coalesced access with one pixel per thread and a
 // wavelength loop inside the thread where the inputs are shared across the
 // batch.
+#include <algorithm>
 #include <atomic>
 
 #include "kernels.h"
@@ -687,6 +688,18 @@ __global__ void basis_grad_finish_kernel(const double* __restrict__ partial, int
   if (threadIdx.x == 0) g_coeffs[k] = (float)t;
 }
 
+// Pixel chunks of the coefficient-gradient partials: nterms x nparts blocks of
+// 256 threads, kBlocksPerSM per SM when there are enough pixels, with chunks
+// of at least 2048 pixels (8 per thread). At 512^2 x 21 terms: 11.2 us with
+// 4 per SM, 11.7 with 3, 12.9 with 2, 13.0 with 8 and 15.9 with 16 (12.3 with
+// the earlier fixed 64 chunks).
+int basis_grad_parts(int nterms, long long npix, int sms) {
+  constexpr int kBlocksPerSM = 4;
+  const long long wave = (long long)kBlocksPerSM * sms / std::max(1, nterms);
+  const long long by_pixels = (npix + 2047) / 2048;
+  return (int)std::max(1LL, std::min(wave, by_pixels));
+}
+
 int launch_basis_grad(const float* basis, const float* g, int nterms, long long npix,
                       float* g_coeffs, double* partial_ws, int nparts, cudaStream_t s) {
   if (nterms == 0) return DLX_OK;
@@ -816,7 +829,7 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
     // kPsfBatch planes' loads in flight (unmasked), then the rest one by
     // one; the sum keeps the wavelength order. Measured at 512^2 x 64 planes:
     // 13.2 us with 16 or 32, 13.9 with 8, 15.0-15.4 with an unrolled loop of
-    // 8 (16 and 32: 19.8 and 31.9 us).
+    // 8 (unrolled by 16 or 32: 19.8 and 31.9 us).
     constexpr int kPsfBatch = 16;
     const float* src = a.planes + (long long)r * a.npix + p;
     const long long stride = (long long)R * a.npix;

@@ -1015,17 +1015,34 @@ cudaError_t launch_pair(void (*kernel)(KArgs...), int clusters, cudaStream_t s, 
 }
 // Split-K reduction: D = sum of the partials in split order, then the GEMM's
 // own epilogue element by element (the FP32 form's epilogue code).
+// The splits' partial sums per element, added in split order. S > 0: the
+// count known at compile time, all S loads issued before the adds (one memory
+// round trip instead of S); S = 0: `splits` read at run time.
+template <int S>
 __global__ void splitk_reduce_kernel(const float2* __restrict__ part, int splits, int batch,
                                      int M, int N, const EpiArgs e) {
   pdl_enter();
   const long long total = (long long)batch * M * N;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= total) return;
-  float2 v = part[i];
-  for (int s = 1; s < splits; ++s) {
-    const float2 q = part[(long long)s * total + i];
-    v.x += q.x;
-    v.y += q.y;
+  float2 v;
+  if constexpr (S > 0) {
+    float2 q[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) q[s] = __ldg(part + (long long)s * total + i);
+    v = q[0];
+#pragma unroll
+    for (int s = 1; s < S; ++s) {
+      v.x += q[s].x;
+      v.y += q[s].y;
+    }
+  } else {
+    v = part[i];
+    for (int s = 1; s < splits; ++s) {
+      const float2 q = part[(long long)s * total + i];
+      v.x += q.x;
+      v.y += q.y;
+    }
   }
   const long long mn = (long long)M * N;
   const int b = (int)(i / mn);
@@ -1302,8 +1319,21 @@ int launch_gemm_tc(const GemmArgs& g, cudaStream_t s) {
   DLX_PDL_LAUNCH("tc_cgemm_kernel", kern, dim3(grid), dim3(TC_THREADS), SMEM_BYTES, s, ta, tb, p);
   if (split) {
     const long long n = (long long)g.batch * g.M * g.N;
-    DLX_PDL_LAUNCH("splitk_reduce_kernel", splitk_reduce_kernel, dim3(ceil_div(n, 256)),
-                   dim3(256), 0, s, g.split_ws, p.splits, g.batch, g.M, g.N, g.epi);
+    const dim3 rgrid(ceil_div(n, 256));
+    switch (p.splits) {
+#define DLX_SPLITK_REDUCE(S, C)                                                             \
+  case C:                                                                                   \
+    DLX_PDL_LAUNCH("splitk_reduce_kernel", splitk_reduce_kernel<S>, rgrid, dim3(256), 0, s, \
+                   g.split_ws, p.splits, g.batch, g.M, g.N, g.epi);                         \
+    break;
+      DLX_SPLITK_REDUCE(2, 2) DLX_SPLITK_REDUCE(3, 3) DLX_SPLITK_REDUCE(4, 4)
+      DLX_SPLITK_REDUCE(5, 5) DLX_SPLITK_REDUCE(6, 6) DLX_SPLITK_REDUCE(7, 7)
+      DLX_SPLITK_REDUCE(8, 8)
+#undef DLX_SPLITK_REDUCE
+      default:
+        DLX_PDL_LAUNCH("splitk_reduce_kernel", splitk_reduce_kernel<0>, rgrid, dim3(256), 0, s,
+                       g.split_ws, p.splits, g.batch, g.M, g.N, g.epi);
+    }
   }
   return DLX_OK;
 }

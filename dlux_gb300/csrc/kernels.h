@@ -97,6 +97,7 @@ int launch_amp_norm_backward(const float* amp, const float* g_eff, long long npi
                              float* g_amp, double* partial_ws, int nparts, cudaStream_t s);
 int launch_basis_eval(const float* basis, const float* coeffs, const float* base, int nterms,
                       long long npix, float* out, cudaStream_t s);
+int basis_grad_parts(int nterms, long long npix, int sms);
 int launch_basis_grad(const float* basis, const float* g, int nterms, long long npix,
                       float* g_coeffs, double* partial_ws, int nparts, cudaStream_t s);
 int launch_downsample(const float* in, int n_in, int k, int mean, const float* flat, float* out,
