@@ -46,8 +46,12 @@ class PolyPSF(torch.autograd.Function):
     """
 
     @staticmethod
-    def forward(ctx, plan, normalise, amp, opd, phase, weights, tilt):
-        amp_scale = kernels.amp_norm(amp.detach()) if (normalise and amp is not None) else None
+    def forward(ctx, plan, normalise, amp, opd, phase, weights, tilt, amp_scale=None):
+        # amp_scale: the normalisation of amp, when the caller computed it already
+        if not (normalise and amp is not None):
+            amp_scale = None
+        elif amp_scale is None:
+            amp_scale = kernels.amp_norm(amp.detach())
         t = (float(tilt[0]), float(tilt[1]))
         ctx.plan, ctx.normalise, ctx.tilt = plan, normalise, t
         ctx.tilt_device = tilt.device
@@ -74,7 +78,7 @@ class PolyPSF(torch.autograd.Function):
         if ctx.needs_input_grad[5]:
             want.append("w")
         if not want:
-            return (None,) * 7
+            return (None,) * 8
         gr = plan.grad(_d(amp), amp_scale, _d(opd), _d(phase), weights.detach().contiguous(),
                        g_psf.contiguous(), ctx.tilt, tuple(want), reuse_token=ctx.token)
         g_amp = gr["amp"]
@@ -86,19 +90,20 @@ class PolyPSF(torch.autograd.Function):
             g_tilt = kernels.basis_grad(plan.tilt_basis(), gr["opd"], (2,)).to(
                 device=ctx.tilt_device, dtype=torch.float64)
         g_opd = gr["opd"] if (ctx.needs_input_grad[3] and opd is not None) else None
-        return None, None, g_amp, g_opd, gr["phase"], gr["w"], g_tilt
+        return None, None, g_amp, g_opd, gr["phase"], gr["w"], g_tilt, None
 
 
 def _d(t):
     return None if t is None else t.detach().contiguous()
 
 
-def poly_psf(plan, amp, opd, phase, weights, normalise=False, tilt=None):
-    """Fused polychromatic PSF; ``tilt`` is a float64 tensor [2] (radians), may require grad."""
+def poly_psf(plan, amp, opd, phase, weights, normalise=False, tilt=None, amp_scale=None):
+    """Fused polychromatic PSF; ``tilt`` is a float64 tensor [2] (radians), may require grad.
+    ``amp_scale``: sqrt(1 / sum amp^2) computed by the caller (else here, when normalising)."""
     if tilt is None:
         tilt = torch.zeros(2, dtype=torch.float64)
     tilt = torch.as_tensor(tilt, dtype=torch.float64)
-    return PolyPSF.apply(plan, bool(normalise), amp, opd, phase, weights, tilt)
+    return PolyPSF.apply(plan, bool(normalise), amp, opd, phase, weights, tilt, amp_scale)
 
 
 class PolySources(torch.autograd.Function):

@@ -693,10 +693,43 @@ def power_scale(field, value=1.0):
     return out
 
 
-def amp_norm(amp, value=1.0):
-    out = torch.empty((), dtype=torch.float32, device=amp.device)
+def amp_norm(amp, value=1.0, out=None):
+    if out is None:
+        out = torch.empty((), dtype=torch.float32, device=amp.device)
     call("dlx_amp_norm", ptr(amp.contiguous()), amp.shape[-1], float(value), ptr(out), _stream())
     return out
+
+
+_side_streams = {}
+
+
+def _side_stream(device):
+    s = _side_streams.get(device)
+    if s is None:
+        s = _side_streams[device] = torch.cuda.Stream(device=device)
+    return s
+
+
+class AmpNormFork:
+    """amp_norm on a side stream forked from the current one, so that it runs
+    beside the work issued next on the current stream; ``join()`` makes the
+    current stream wait for it and returns the scale. The scale tensor is
+    allocated on the current stream and the amplitude stays referenced, so
+    neither memory is reused before the join (under CUDA-graph capture the
+    fork and the join become a branch of the graph)."""
+
+    def __init__(self, amp, value=1.0):
+        self.amp = amp.contiguous()
+        self.cur = torch.cuda.current_stream(amp.device)
+        self.side = _side_stream(amp.device)
+        self.scale = torch.empty((), dtype=torch.float32, device=amp.device)
+        self.side.wait_stream(self.cur)
+        with torch.cuda.stream(self.side):
+            amp_norm(self.amp, value, out=self.scale)
+
+    def join(self):
+        self.cur.wait_stream(self.side)
+        return self.scale
 
 
 def amp_norm_backward(amp, g_eff, value=1.0):

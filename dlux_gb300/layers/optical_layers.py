@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import torch
 
-from .. import autograd
+from .. import autograd, kernels
 from ..base import Base
 
 __all__ = ["BaseLayer", "OpticalLayer", "TransmissiveLayer", "AberratedLayer", "BasisLayer",
@@ -54,6 +54,7 @@ class PupilAccumulator:
         self.opd_static = []
         self.phase_static = []
         self.tilt = torch.zeros(2, dtype=torch.float64)  # radians; may carry a gradient
+        self.amp_scale = None  # set by fields() when it computed the normalisation
 
     def amplitude(self, t):
         if t is None:
@@ -124,8 +125,14 @@ class PupilAccumulator:
         else:
             amp = (torch.full((self.n, self.n), 1.0 / self.n ** 2, device=_dev())
                    if amp is None else amp * (1.0 / self.n ** 2))
+        # The normalisation depends on the amplitude alone: on the GPU it runs on
+        # a side stream while the OPD and phase are evaluated.
+        fork = (kernels.AmpNormFork(amp.detach())
+                if flag and amp.is_cuda and (self.opd is not None or self.phase is not None)
+                else None)
         opd = self._chain(self.opd, self.opd_static)
         phase = self._chain(self.phase, self.phase_static)
+        self.amp_scale = fork.join() if fork is not None else None
         return amp, flag, opd, phase
 
 

@@ -203,7 +203,8 @@ class ParametricLayeredOpticalSystem(ParametricOpticalSystem, LayeredOpticalSyst
         return wf, outputs
 
     def fused_pupil(self):
-        """(amp, normalise, opd, phase, tilt) if every layer folds into one pupil, else None."""
+        """(amp, normalise, opd, phase, tilt, amp_scale) if every layer folds into one pupil,
+        else None; amp_scale is the normalisation when it was computed alongside the OPD."""
         acc = PupilAccumulator(self.wf_npixels, pixel_scale=self.diameter / self.wf_npixels)
         try:
             for layer in self.layers.values():
@@ -211,7 +212,7 @@ class ParametricLayeredOpticalSystem(ParametricOpticalSystem, LayeredOpticalSyst
         except NotFusable:
             return None
         amp, flag, opd, phase = acc.fields()
-        return amp, flag, opd, phase, acc.tilt
+        return amp, flag, opd, phase, acc.tilt, acc.amp_scale
 
     def fused_plan(self, wavelengths, variant=None):
         npix, ps = self._focal_sampling()
@@ -222,10 +223,10 @@ class ParametricLayeredOpticalSystem(ParametricOpticalSystem, LayeredOpticalSyst
         fused = self.fused_pupil()
         if fused is None:
             return OpticalSystem._propagate_psf(self, wl, offset, weights)
-        amp, flag, opd, phase, tilt = fused
+        amp, flag, opd, phase, tilt, amp_scale = fused
         plan = self.fused_plan(wl)
         tilt_t = offset.to(dtype=torch.float64, device=tilt.device) + tilt
-        return autograd.poly_psf(plan, amp, opd, phase, weights, flag, tilt_t)
+        return autograd.poly_psf(plan, amp, opd, phase, weights, flag, tilt_t, amp_scale)
 
 
 class AngularOpticalSystem(ParametricLayeredOpticalSystem):

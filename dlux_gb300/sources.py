@@ -120,7 +120,7 @@ class PointSources(Source):
         fused = optics.fused_pupil()
         if fused is None:
             return None
-        amp, flag, opd, phase, tilt = fused
+        amp, flag, opd, phase, tilt, _ = fused
         tilt = (float(tilt[0]), float(tilt[1]))
         wl = [float(v) for v in torch.as_tensor(src.spectrum.wavelengths,
                                                dtype=torch.float64).reshape(-1)]
