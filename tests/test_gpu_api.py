@@ -82,6 +82,25 @@ def test_transmission_gradient_through_normalise(cuda):
     assert e < 1e-5
 
 
+def test_normalisation_beside_the_opd_matches_serial(cuda):
+    """A fused pupil with a normalising transmission computes the normalisation on a
+    side stream while the OPD is evaluated; the scale is the serial kernel's bits, and
+    the PSF equals the one computed with the scale taken on the current stream."""
+    from dlux_gb300 import autograd, kernels
+    T, B, c, _ = config1(6)
+    optics = build_system(T, B, c, psf_npixels=64, pixel_scale=0.04)
+    amp, flag, opd, phase, tilt, scale = optics.fused_pupil()
+    assert flag and scale is not None
+    serial = kernels.amp_norm(amp)
+    torch.cuda.synchronize()
+    assert torch.equal(scale, serial)
+    plan = optics.fused_plan([1e-6])
+    w = torch.ones(1, device="cuda")
+    a = autograd.poly_psf(plan, amp, opd, phase, w, True, tilt, scale)
+    b = autograd.poly_psf(plan, amp, opd, phase, w, True, tilt)
+    assert torch.equal(a, b)
+
+
 def test_telescope_with_detector(cuda):
     import dlux_gb300 as dl
     T, B, c, R = config1(6)
