@@ -130,9 +130,13 @@ class PupilAccumulator:
         fork = (kernels.AmpNormFork(amp.detach())
                 if flag and amp.is_cuda and (self.opd is not None or self.phase is not None)
                 else None)
-        opd = self._chain(self.opd, self.opd_static)
-        phase = self._chain(self.phase, self.phase_static)
-        self.amp_scale = fork.join() if fork is not None else None
+        try:
+            opd = self._chain(self.opd, self.opd_static)
+            phase = self._chain(self.phase, self.phase_static)
+        finally:
+            # joined on every path, so the side stream's write to the scale
+            # is ordered before anything that reuses its memory
+            self.amp_scale = fork.join() if fork is not None else None
         return amp, flag, opd, phase
 
 
