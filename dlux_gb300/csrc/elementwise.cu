@@ -265,8 +265,9 @@ int launch_phasor(const PhasorArgs& a, const BatchFF* inv_lambda_arg, cudaStream
     // per-element phase reduction and sincos bound the kernel.
     // 4 pixels per thread (2 measured the same at 512^2 x 64, 8 slower: 42.0
     // vs 37.0 us)
-    // With the path set-up in FP32 float pairs, 2 and 4 wavelength groups
-    // measured 30.5 and 30.3 us against 30.7 us for one.
+    // With the path set-up in FP32 float pairs, 2, 4, 8, 16 and 32 wavelength
+    // groups measured 30.5, 30.3, 30.5, 35.7 and 47.7 us against 30.7 us for
+    // one.
     constexpr int V = 4;
     constexpr int kPhasorGroups = 1;
     const int lg = (L + kPhasorGroups - 1) / kPhasorGroups;
