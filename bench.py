@@ -1048,7 +1048,30 @@ def run_ops(args):
     ms, _ = timed(lambda: (kernels.aberrated_aperture(desc, noll, coeffs),
                            kernels.aberrated_aperture_grad(desc, noll, g_opd)))
     items["aperture_1024_21z"] = {"ms_per_step": ms, "pixels_per_s": na * na / (ms * 1e-3)}
-    total = sum(v["ms_per_step"] for v in items.values() if v is not items["lct_fp32"])
+    # the layer-by-layer path (a layer list with an explicit MFT layer does not fold into
+    # one pupil): phasor, normalisation, MFT and weighted intensity kernels, their reverse
+    # kernels; 512^2 pupil, Noll 4-24, 16 wavelengths, 128^2 PSF, PSF + coefficient gradient
+    import dlux_gb300 as dl
+    import dlux_gb300.utils as dlu
+    Tl, Bl = dlu.circular_aperture(n, 1.0, oversample=1, secondary_diameter=0.1,
+                                   zernike_nolls=list(range(4, 25)))
+    cl = torch.as_tensor(rng.normal(0, 30e-9, 21), dtype=torch.float32, **dev)
+    Rl = torch.as_tensor(rng.normal(size=(128, 128)), dtype=torch.float32, **dev)
+    layered = dl.LayeredOpticalSystem(n, 1.0, [dl.TransmissiveLayer(Tl, normalise=True),
+                                               dl.BasisLayer(Bl, cl),
+                                               dl.MFT(128, 1e-6 / 1.0 / 4)])
+
+    def layered_step():
+        c = cl.detach().requires_grad_(True)
+        psf = layered.set("layers.BasisLayer.coefficients", c).propagate(wls)
+        (psf * Rl).sum().backward()
+        return c.grad
+
+    ms, gemm = timed(layered_step)
+    items["layered_512_16l"] = {"ms_per_step": ms, "gemm": gemm,
+                                "note": "not in the line's value (path operations only)"}
+    total = sum(v["ms_per_step"] for k, v in items.items()
+                if k not in ("lct_fp32", "layered_512_16l"))
     lct = items["lct_split_bf16"]["gemm"] or {}
     line = {"metric": "path operations (LCT, ASM, convolution, aperture) ms per step",
             "value": total, "unit": "ms", "n_gpus": 1, "steps": args.steps,

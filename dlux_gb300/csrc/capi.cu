@@ -747,7 +747,8 @@ int dlx_amp_norm_backward(const float* amp, const float* g_eff, int n, double va
   cudaStream_t s = as_stream(stream);
   const int nparts = 128;
   double* ws = nullptr;
-  DLX_TRY(with_partials(2 * nparts, s, &ws));
+  // partials, then (n, c) as float pairs (16 bytes)
+  DLX_TRY(with_partials(2 * nparts + 2, s, &ws));
   int st = launch_amp_norm_backward(amp, g_eff, (long long)n * n, value, g_amp, ws, nparts, s);
   cudaFreeAsync(ws, s);
   return st;

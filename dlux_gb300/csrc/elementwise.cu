@@ -510,67 +510,104 @@ int launch_amp_norm(const float* amp, long long npix, double value, float* out_s
 
 // Reverse of a_eff = a * n, n = sqrt(value / S), S = sum a^2:
 // g_a[j] = n g_eff[j] - a_j n^3 / value * sum_i a_i g_eff[i].
+// Three launches: per-chunk partials of S and D = sum a g (float-pair sums,
+// as in the coefficient gradient), one warp that reduces them in a fixed
+// order and forms n and c = n^3 D / value once in FP64, and the per-pixel
+// n g - a c in FP32 float pairs. (Every block forming n and c for itself in
+// FP64 made the last kernel 20 us at 512^2: FP64 division and square root run
+// at a small fraction of the FP32 rate on this GPU.)
 __global__ void dot_sumsq_partial_kernel(const float* __restrict__ a, const float* __restrict__ g,
                                          long long npix, int nparts,
                                          double* __restrict__ partial) {
+  pdl_enter();
   __shared__ double smem[32];
   const long long chunk = (npix + nparts - 1) / nparts;
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(npix, lo + chunk);
-  double s2 = 0.0, sg = 0.0;
-  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-    double v = a[p];
-    s2 += v * v;
-    sg += v * (double)g[p];
+  // exact products (FMA) summed in float pairs (Knuth's TwoSum), widened once
+  float s2h = 0.f, s2l = 0.f, sgh = 0.f, sgl = 0.f;
+  auto add = [](float x, float y, float& h, float& l) {
+    const float pr = x * y;
+    const float pe = fmaf(x, y, -pr);
+    const float t = h + pr;
+    const float bv = t - h;
+    l += ((h - (t - bv)) + (pr - bv)) + pe;
+    h = t;
+  };
+  const long long step = blockDim.x;
+  long long p = lo + threadIdx.x;
+  for (; p + 7 * step < hi; p += 8 * step) {
+    float av[8], gv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      av[u] = __ldg(a + p + u * step);
+      gv[u] = __ldg(g + p + u * step);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      add(av[u], av[u], s2h, s2l);
+      add(av[u], gv[u], sgh, sgl);
+    }
   }
-  double t2 = block_sum<256>(s2, smem);
-  double tg = block_sum<256>(sg, smem);
+  for (; p < hi; p += step) {
+    const float av = __ldg(a + p), gv = __ldg(g + p);
+    add(av, av, s2h, s2l);
+    add(av, gv, sgh, sgl);
+  }
+  const double t2 = block_sum<256>((double)s2h + (double)s2l, smem);
+  const double tg = block_sum<256>((double)sgh + (double)sgl, smem);
   if (threadIdx.x == 0) {
     partial[2 * blockIdx.x] = t2;
     partial[2 * blockIdx.x + 1] = tg;
   }
 }
 
-__global__ void amp_norm_bwd_kernel(const float* __restrict__ a, const float* __restrict__ g,
-                                    long long npix, double value,
-                                    const double* __restrict__ partial, int nparts,
-                                    float* __restrict__ g_a) {
-  // Every block re-reduces the (few) partials in the same fixed order: the 32
-  // lanes of warp 0 take every 32nd partial, then a shuffle tree. (One thread
-  // walking them serially made the kernel 34 us at 512^2.)
-  __shared__ double sh[2];
-  if (threadIdx.x < 32) {
-    double s2 = 0.0, sg = 0.0;
-    for (int i = threadIdx.x; i < nparts; i += 32) {
-      s2 += partial[2 * i];
-      sg += partial[2 * i + 1];
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      s2 += __shfl_down_sync(0xffffffffu, s2, o);
-      sg += __shfl_down_sync(0xffffffffu, sg, o);
-    }
-    if (threadIdx.x == 0) {
-      sh[0] = s2;
-      sh[1] = sg;
-    }
+// One warp: lanes take every 32nd partial, then a shuffle tree (fixed order).
+// nc = (n, c) as float pairs.
+__global__ void amp_norm_bwd_finish_kernel(const double* __restrict__ partial, int nparts,
+                                           double value, float4* __restrict__ nc) {
+  pdl_enter();
+  double s2 = 0.0, sg = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += 32) {
+    s2 += partial[2 * i];
+    sg += partial[2 * i + 1];
   }
-  __syncthreads();
-  const double S = sh[0], D = sh[1];
-  const double n = sqrt(value / S);
-  const double c = n * n * n / value * D;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    sg += __shfl_down_sync(0xffffffffu, sg, o);
+  }
+  if (threadIdx.x == 0) {
+    const double n = sqrt(value / s2);
+    const double c = n * n * n / value * sg;
+    const FF nf = ff_from_double(n), cf = ff_from_double(c);
+    *nc = make_float4(nf.hi, nf.lo, cf.hi, cf.lo);
+  }
+}
+
+__global__ void amp_norm_bwd_kernel(const float* __restrict__ a, const float* __restrict__ g,
+                                    long long npix, const float4* __restrict__ nc,
+                                    float* __restrict__ g_a) {
+  pdl_enter();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npix) return;
-  g_a[p] = (float)(n * (double)g[p] - (double)a[p] * c);
+  const float4 q = *nc;
+  const FF t1 = ff_mul(__ldg(g + p), FF{q.x, q.y});
+  const FF t2 = ff_mul(__ldg(a + p), FF{q.z, q.w});
+  const FF d = ff_add(t1, FF{-t2.hi, -t2.lo});
+  g_a[p] = d.hi;
 }
 
 int launch_amp_norm_backward(const float* amp, const float* g_eff, long long npix, double value,
                              float* g_amp, double* partial_ws, int nparts, cudaStream_t s) {
-  dot_sumsq_partial_kernel<<<nparts, 256, 0, s>>>(amp, g_eff, npix, nparts, partial_ws);
-  DLX_LAUNCH_CHECK("dot_sumsq_partial_kernel");
-  amp_norm_bwd_kernel<<<ceil_div(npix, 256), 256, 0, s>>>(amp, g_eff, npix, value, partial_ws,
-                                                          nparts, g_amp);
-  DLX_LAUNCH_CHECK("amp_norm_bwd_kernel");
+  // partial_ws: 2 * nparts doubles of partials, then (n, c) as float pairs
+  float4* nc = reinterpret_cast<float4*>(partial_ws + 2 * (size_t)nparts);
+  DLX_PDL_LAUNCH("dot_sumsq_partial_kernel", dot_sumsq_partial_kernel, dim3(nparts), dim3(256),
+                 0, s, amp, g_eff, npix, nparts, partial_ws);
+  DLX_PDL_LAUNCH("amp_norm_bwd_finish_kernel", amp_norm_bwd_finish_kernel, dim3(1), dim3(32), 0,
+                 s, partial_ws, nparts, value, nc);
+  DLX_PDL_LAUNCH("amp_norm_bwd_kernel", amp_norm_bwd_kernel, dim3(ceil_div(npix, 256)),
+                 dim3(256), 0, s, amp, g_eff, npix, nc, g_amp);
   return DLX_OK;
 }
 
