@@ -43,13 +43,11 @@ __device__ __forceinline__ float2 pupil_unit_phasor(const EpiArgs& e, int l, int
   const bool obj = e.objs.n > 0;
   const float* opd = obj ? e.objs.o[r].opd : e.opd;
   const float* phase = obj ? e.objs.o[r].phase : e.phase;
-  const double tx = obj ? e.objs.o[r].tilt_x : e.tilt_x;
-  const double ty = obj ? e.objs.o[r].tilt_y : e.tilt_y;
-  const double half = 0.5 * (n - 1);
-  const double X = ((double)x - half) * e.pixel_scale;
-  const double Y = ((double)y - half) * e.pixel_scale;
-  const FF path = ff_from_double((opd ? (double)opd[p] : 0.0) + tx * X + ty * Y);
-  const FF ph = ff_from_double(phase ? (double)phase[p] * (0.5 / CUDART_PI) : 0.0);
+  const float4 t = obj ? tilt_pairs(e.objs.o[r].tilt_x, e.objs.o[r].tilt_y, e.pixel_scale)
+                       : tilt_pairs(e.tilt_x, e.tilt_y, e.pixel_scale);
+  const float half = 0.5f * (float)(n - 1);
+  const FF path = pupil_path(opd ? opd[p] : 0.f, (float)x - half, (float)y - half, t);
+  const FF ph = phase ? phase_cycles(phase[p]) : FF{0.f, 0.f};
   return cis_ff(path, FF{il.x, il.y}, ph);
 }
 

@@ -162,8 +162,8 @@ __global__ void scene_field_kernel(int n, int L, double pixel_scale, const float
   const int y = (int)(p / n);
   const int x = (int)(p - (long long)y * n);
   const float X = (float)(((double)x - 0.5 * (n - 1)) * pixel_scale);
-  const FF path = ff_from_double(opd ? (double)opd[p] : 0.0);
-  const FF ph = ff_from_double(phase ? (double)phase[p] * (0.5 / CUDART_PI) : 0.0);
+  const FF path{opd ? opd[p] : 0.f, 0.f};
+  const FF ph = phase ? phase_cycles(phase[p]) : FF{0.f, 0.f};
   float a = amp ? amp[p] : 1.0f;
   if (amp_scale) a *= *amp_scale;
   for (int l = 0; l < L; ++l) {
