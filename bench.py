@@ -1061,15 +1061,19 @@ def run_ops(args):
                                                dl.BasisLayer(Bl, cl),
                                                dl.MFT(128, 1e-6 / 1.0 / 4)])
 
-    def layered_step():
-        c = cl.detach().requires_grad_(True)
+    def layered_step(c_in):
+        c = c_in.detach().requires_grad_(True)
         psf = layered.set("layers.BasisLayer.coefficients", c).propagate(wls)
         (psf * Rl).sum().backward()
-        return c.grad
+        return (c.grad,)
 
-    ms, gemm = timed(layered_step)
-    items["layered_512_16l"] = {"ms_per_step": ms, "gemm": gemm,
-                                "note": "not in the line's value (path operations only)"}
+    from dlux_gb300.graphs import GraphedStep
+    eager_ms, _ = timed(lambda: layered_step(cl))
+    graphed = GraphedStep(layered_step, cl)
+    ms, gemm = timed(lambda: graphed(cl))
+    items["layered_512_16l"] = {"ms_per_step": ms, "gemm": gemm, "eager_ms_per_step": eager_ms,
+                                "note": "one CUDA graph per step; not in the line's value "
+                                        "(path operations only)"}
     total = sum(v["ms_per_step"] for k, v in items.items()
                 if k not in ("lct_fp32", "layered_512_16l"))
     lct = items["lct_split_bf16"]["gemm"] or {}

@@ -169,8 +169,13 @@ class Wavefront(Base):
         if a.shape != (2,):
             raise ValueError("angles must be a 1d array of shape (2,).")
         f = unit_factor_to_rad(unit)
+        differentiable = isinstance(angles, torch.Tensor) and angles.requires_grad
+        if not differentiable and float(a[0]) == 0.0 and float(a[1]) == 0.0:
+            # exp(i 0) = 1 exactly: the field is unchanged (and no coordinate
+            # grid is built, so the step stays capturable as a CUDA graph)
+            return self
         coords = self.coordinates()
-        if isinstance(angles, torch.Tensor) and angles.requires_grad:
+        if differentiable:
             at = (angles.to(torch.float64) * f).to(device=coords.device, dtype=torch.float32)
             opd = at[0] * coords[0] + at[1] * coords[1]
         else:
