@@ -964,10 +964,17 @@ __global__ void obj_w_partial_kernel(ObjReduceArgs a) {
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(a.npix, lo + chunk);
   const float* pre = a.pre + ((long long)l * R + r) * a.npix;
-  double acc = 0.0;
-  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x)
-    acc += (double)pre[p] * (od.amp ? (double)od.amp[p] : 1.0);
-  const double t = block_sum<256>(acc, smem);
+  // exact products (FMA) summed in float pairs, widened once per thread
+  float h = 0.f, lo_s = 0.f;
+  for (long long p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    const float x = pre[p], y = od.amp ? od.amp[p] : 1.0f;
+    const float pr = x * y;
+    const float t = h + pr;
+    const float bv = t - h;
+    lo_s += ((h - (t - bv)) + (pr - bv)) + fmaf(x, y, -pr);
+    h = t;
+  }
+  const double t = block_sum<256>((double)h + (double)lo_s, smem);
   if (threadIdx.x == 0) {
     double* part = a.partial_ws + (long long)R * a.nparts * 2;
     part[((long long)r * a.L + l) * a.nparts + blockIdx.x] = t;

@@ -84,13 +84,20 @@ __global__ void scene_tilt_kernel(int N, int Rc, const float2* __restrict__ xin,
                                   float2* __restrict__ ty) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
-  if (i >= N) return;
   const int l = b / Rc, r = b - (b / Rc) * Rc;
+  // theta / fringe of this (source, wavelength) as float pairs, formed once
+  // per block in FP64
+  __shared__ float4 st;
+  if (threadIdx.x == 0) {
+    const FF sx = ff_from_double(pos[2 * r] * inv_fringe[l]);
+    const FF sy = ff_from_double(pos[2 * r + 1] * inv_fringe[l]);
+    st = make_float4(sx.hi, sx.lo, sy.hi, sy.lo);
+  }
+  __syncthreads();
+  if (i >= N) return;
   const float2 x = xin[i];
-  const FF sx = ff_from_double(pos[2 * r] * inv_fringe[l]);
-  const FF sy = ff_from_double(pos[2 * r + 1] * inv_fringe[l]);
-  tx[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, sx, FF{0.f, 0.f});
-  ty[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, sy, FF{0.f, 0.f});
+  tx[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, FF{st.x, st.y}, FF{0.f, 0.f});
+  ty[(long long)b * N + i] = cis_ff(FF{x.x, x.y}, FF{st.z, st.w}, FF{0.f, 0.f});
 }
 
 struct alignas(8) Bf16x4 {
