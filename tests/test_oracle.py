@@ -212,3 +212,29 @@ def test_split_emulator_meets_1e5():
     Fs = S.split_mft(E[0].astype(np.complex64), A.astype(np.complex64), A.astype(np.complex64), s)
     P, P64 = np.abs(Fs.astype(complex)) ** 2, np.abs(F[0]) ** 2
     assert np.linalg.norm(P - P64) / np.linalg.norm(P64) < 1e-5
+
+
+def test_split_emulator_gauss_product_error():
+    """Gauss's three-product complex multiply (9 split products per complex
+    multiply-add instead of 12), emulated: its PSF error stays within the bar
+    and within 1.5x of the four-product form's at the same field; the field
+    error (P3 - P1 - P2 cancels) is below 2.5x."""
+    T, B = O.circular_aperture(128, 1.0, oversample=3, secondary_diameter=0.1,
+                               spider_width=0.01, spider_angles=(0, 90, 180, 270),
+                               zernike_nolls=list(range(4, 25)))
+    opd = O.eval_basis(B, np.random.default_rng(5).normal(0, 30e-9, 21))
+    ps = float(O.arcsec2rad(0.01))
+    F, E = O.poly_psf_fields(T, opd, [1e-6], [1.0], 1.0, 128, ps)
+    A = O.transfer_matrix(1e-6, 128, 1 / 128, 128, ps).astype(np.complex64)
+    s = O.calc_nfringes(1e-6, 128, 1 / 128, 128, ps) / (128 * 128)
+    P64 = np.abs(F[0]) ** 2
+    err = {}
+    for prod in ("four", "gauss"):
+        Fs = S.split_mft(E[0].astype(np.complex64), A, A, s, product=prod).astype(complex)
+        err[prod] = (np.linalg.norm(np.abs(Fs) ** 2 - P64) / np.linalg.norm(P64),
+                     np.linalg.norm(Fs - F[0]) / np.linalg.norm(F[0]))
+    print(f"emulated PSF / field error: four products {err['four'][0]:.2e} / "
+          f"{err['four'][1]:.2e}, Gauss {err['gauss'][0]:.2e} / {err['gauss'][1]:.2e}")
+    assert err["gauss"][0] < 1e-5
+    assert err["gauss"][0] < 1.5 * err["four"][0]
+    assert err["gauss"][1] < 2.5 * err["four"][1]
