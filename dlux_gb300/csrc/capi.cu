@@ -949,11 +949,12 @@ struct dlx_poly_plan_s {
     e.alpha = ts.alpha.as<float>();
     e.out_f32 = planes.as<float>();
     if (keep) {
-      // intensity planes and F = alpha D: the PSF + cotangent epilogue with no
-      // cotangent
+      // F = alpha D only (the PSF + cotangent epilogue with no cotangent and
+      // no intensity planes): the wavelength sum forms |F|^2 from F
       e.kind = EPI_PSF_GRADF;
       for (int r = 0; r < R; ++r) e.objs.o[r].G = nullptr;
       e.out_c64 = fbar.as<float2>();
+      e.out_f32 = nullptr;
     }
     DLX_TRY(run_gemm(v, gemm(ts.opATy(), R, M, M, N, false, mid.p, e), s));
     ObjReduceArgs ra{};
@@ -962,6 +963,7 @@ struct dlx_poly_plan_s {
     ra.L = L;
     ra.npix = (long long)M * M;
     ra.planes = planes.as<float>();
+    if (keep) ra.fields = fbar.as<float2>();
     ra.psf_sum = psf_sum;
     ra.accumulate = accumulate;
     return launch_obj_psf_reduce(ra, s);

@@ -206,6 +206,13 @@ __device__ __forceinline__ float2 cis_ff_split(FF path, FF inv_lambda, FF phase_
   return make_float2(c, s);
 }
 
+// |F|^2 of F = (fx, fy), with no FMA contraction: the same bits wherever it
+// is formed (the GEMM epilogues from alpha D, and the wavelength sum over kept
+// focal fields F = alpha D stored by a forward).
+__device__ __forceinline__ float intensity_rn(float fx, float fy) {
+  return __fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy));
+}
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }

@@ -856,6 +856,10 @@ int launch_downsample_backward(const float* in, const float* g_out, int n_in, in
 // weight and tilt gradients. Fixed summation order, so results are
 // reproducible and independent of which other objects share the batch.
 // ---------------------------------------------------------------------------
+// kField: the planes are kept focal fields F (complex64), and each term is
+// |F|^2 with the GEMM epilogues' own rounding (intensity_rn), so the sum is
+// bitwise the one over intensity planes.
+template <bool kField>
 __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
   pdl_enter();
   const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -869,17 +873,25 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
     // 13.2 us with 16 or 32, 13.9 with 8, 15.0-15.4 with an unrolled loop of
     // 8 (unrolled by 16 or 32: 19.8 and 31.9 us).
     constexpr int kPsfBatch = 16;
-    const float* src = a.planes + (long long)r * a.npix + p;
     const long long stride = (long long)R * a.npix;
+    const long long off = (long long)r * a.npix + p;
+    auto term = [&](int l) -> float {
+      if constexpr (kField) {
+        const float2 f = __ldg(a.fields + off + (long long)l * stride);
+        return intensity_rn(f.x, f.y);
+      } else {
+        return __ldg(a.planes + off + (long long)l * stride);
+      }
+    };
     int l = 0;
     for (; l + kPsfBatch <= a.L; l += kPsfBatch) {
       float v[kPsfBatch];
 #pragma unroll
-      for (int u = 0; u < kPsfBatch; ++u) v[u] = __ldg(src + (long long)(l + u) * stride);
+      for (int u = 0; u < kPsfBatch; ++u) v[u] = term(l + u);
 #pragma unroll
       for (int u = 0; u < kPsfBatch; ++u) s += v[u];
     }
-    for (; l < a.L; ++l) s += __ldg(src + (long long)l * stride);
+    for (; l < a.L; ++l) s += term(l);
     if (a.outs.o[r].psf) a.outs.o[r].psf[p] = s;
     total += s;
   }
@@ -888,8 +900,12 @@ __global__ void obj_psf_reduce_kernel(ObjReduceArgs a) {
 
 int launch_obj_psf_reduce(const ObjReduceArgs& a, cudaStream_t s) {
   if (a.npix == 0 || a.objs.n == 0) return DLX_OK;
-  DLX_PDL_LAUNCH("obj_psf_reduce_kernel", obj_psf_reduce_kernel, dim3(ceil_div(a.npix, 256)),
-                 dim3(256), 0, s, a);
+  if (a.fields)
+    DLX_PDL_LAUNCH("obj_psf_reduce_kernel", obj_psf_reduce_kernel<true>,
+                   dim3(ceil_div(a.npix, 256)), dim3(256), 0, s, a);
+  else
+    DLX_PDL_LAUNCH("obj_psf_reduce_kernel", obj_psf_reduce_kernel<false>,
+                   dim3(ceil_div(a.npix, 256)), dim3(256), 0, s, a);
   return DLX_OK;
 }
 

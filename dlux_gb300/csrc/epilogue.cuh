@@ -123,13 +123,14 @@ __device__ __forceinline__ void epi_apply(const EpiArgs& e, int b, int m, int n,
       break;
     }
     case EPI_INTENSITY: {
-      e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
+      e.out_f32[(long long)b * plane + idx] = intensity_rn(__fmul_rn(a, v.x), __fmul_rn(a, v.y));
       break;
     }
     case EPI_GRADF:
     case EPI_PSF_GRADF: {
-      if (e.kind == EPI_PSF_GRADF)
-        e.out_f32[(long long)b * plane + idx] = a * a * (v.x * v.x + v.y * v.y);
+      if (e.kind == EPI_PSF_GRADF && e.out_f32)
+        e.out_f32[(long long)b * plane + idx] =
+            intensity_rn(__fmul_rn(a, v.x), __fmul_rn(a, v.y));
       epi_gradf_value(e, b, r, a, idx, v);
       if (e.out_split)
         store_split(e.out_split + (long long)b * 4 * splane, splane, sidx, v);
@@ -210,20 +211,22 @@ __device__ __forceinline__ void epi_col32(const EpiArgs& e, int b, int n, int m0
     }
     case EPI_INTENSITY: {
       float* o = e.out_f32 + (long long)b * plane + idx0;
-      const float a2 = a * a;
 #pragma unroll
       for (int j = 0; j < 32; ++j)
-        if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
+        if (j < mc)
+          o[(long long)j * N] = intensity_rn(__fmul_rn(a, re[j]), __fmul_rn(a, im[j]));
       break;
     }
     case EPI_GRADF:
     case EPI_PSF_GRADF: {
-      if ((KIND >= 0 ? KIND : e.kind) == EPI_PSF_GRADF) {
+      // no intensity planes when a forward keeps F (out_f32 null): the
+      // wavelength sum then reads F itself
+      if ((KIND >= 0 ? KIND : e.kind) == EPI_PSF_GRADF && e.out_f32) {
         float* o = e.out_f32 + (long long)b * plane + idx0;
-        const float a2 = a * a;
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          if (j < mc) o[(long long)j * N] = a2 * (re[j] * re[j] + im[j] * im[j]);
+          if (j < mc)
+            o[(long long)j * N] = intensity_rn(__fmul_rn(a, re[j]), __fmul_rn(a, im[j]));
       }
       // 16 loads at a time, so that their latencies overlap. No cotangent (G
       // null, warp-uniform): the focal field F = alpha D itself is stored.

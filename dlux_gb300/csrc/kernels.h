@@ -112,6 +112,8 @@ struct ObjReduceArgs {
   int L;                     // wavelengths
   long long npix;            // pixels per plane
   const float* planes;       // intensity planes [L*R][npix]
+  const float2* fields;      // or (when set) kept focal fields F = alpha D [L*R][npix]:
+                             // the wavelength sum forms |F|^2 itself
   float* psf_sum;            // nullable: sum over objects (and wavelengths)
   int accumulate;            // add into psf_sum instead of overwriting it
   const float* pre;          // pupil planes [L*R][npix]
