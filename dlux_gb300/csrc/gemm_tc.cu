@@ -151,7 +151,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volati
   }
 }
 
-// Warp-uniform bounded wait: lane 0 polls, the verdict is broadcast, so the
+// Warp-uniform bounded wait: lane 0 polls, the outcome is broadcast, so the
 // whole warp leaves together (required before .sync.aligned tcgen05 ops).
 __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity,
                                           volatile int* abort_flag, int* status,
