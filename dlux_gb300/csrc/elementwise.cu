@@ -420,6 +420,35 @@ __device__ __forceinline__ double block_sum(double v, double* smem) {
   return t;  // valid in thread 0
 }
 
+// Block sum of per-thread float pairs (hi, lo): the warps reduce in FP32
+// float pairs (TwoSum at each shuffle level), and only the BLOCK / 32 warp
+// totals are added in FP64, by warp 0. A fixed order, like block_sum, at a
+// fraction of its FP64 work (FP64 issues at a small fraction of the FP32 rate
+// on this GPU). Valid in thread 0.
+template <int BLOCK>
+__device__ __forceinline__ double block_sum_ff(float hi, float lo, double* smem) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+    const float t = hi + oh;
+    const float bv = t - hi;
+    lo += ((hi - (t - bv)) + (oh - bv)) + ol;
+    hi = t;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = (double)hi + (double)lo;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = (lane < BLOCK / 32) ? smem[lane] : 0.0;
+#pragma unroll
+    for (int o = (BLOCK / 32) / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;
+}
+
 // psf[p] = sum_b |in[b][p]|^2 (wavefronts.py:279 summed as optical_systems.py:223)
 __global__ void psf_sum_kernel(const float2* __restrict__ in, int batch, long long npix,
                                float* __restrict__ psf) {
@@ -471,22 +500,27 @@ __global__ void sumsq_partial_kernel(const float* __restrict__ x, long long npix
   const long long chunk = (npix + nparts - 1) / nparts;
   const long long lo = (long long)blockIdx.x * chunk;
   const long long hi = min(npix, lo + chunk);
-  double acc = 0.0;
+  // exact squares (FMA) summed in float pairs, eight loads in flight before
+  // the adds, which keep the element order
+  float h = 0.f, l = 0.f;
+  auto add = [&](float v) {
+    const float pr = v * v;
+    const float t = h + pr;
+    const float bv = t - h;
+    l += ((h - (t - bv)) + (pr - bv)) + fmaf(v, v, -pr);
+    h = t;
+  };
   const long long step = blockDim.x;
   long long p = lo + threadIdx.x;
-  // eight loads in flight before the adds, which keep the element order
   for (; p + 7 * step < hi; p += 8 * step) {
     float v[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) v[u] = __ldg(x + p + u * step);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) acc += (double)v[u] * (double)v[u];
+    for (int u = 0; u < 8; ++u) add(v[u]);
   }
-  for (; p < hi; p += step) {
-    double v = x[p];
-    acc += v * v;
-  }
-  double t = block_sum<256>(acc, smem);
+  for (; p < hi; p += step) add(__ldg(x + p));
+  const double t = block_sum_ff<256>(h, l, smem);
   if (threadIdx.x == 0) partial[blockIdx.x] = t;
 }
 
@@ -555,8 +589,8 @@ __global__ void dot_sumsq_partial_kernel(const float* __restrict__ a, const floa
     add(av, av, s2h, s2l);
     add(av, gv, sgh, sgl);
   }
-  const double t2 = block_sum<256>((double)s2h + (double)s2l, smem);
-  const double tg = block_sum<256>((double)sgh + (double)sgl, smem);
+  const double t2 = block_sum_ff<256>(s2h, s2l, smem);
+  const double tg = block_sum_ff<256>(sgh, sgl, smem);
   if (threadIdx.x == 0) {
     partial[2 * blockIdx.x] = t2;
     partial[2 * blockIdx.x + 1] = tg;
@@ -712,7 +746,7 @@ __global__ void basis_grad_partial_kernel(const float* __restrict__ basis,
     for (int u = 0; u < kGradBatch; ++u) add(xv[u], yv[u]);
   }
   for (; p < hi; p += step) add(__ldg(row + p), __ldg(g + p));
-  double t = block_sum<256>((double)hi_s + (double)lo_s, smem);
+  const double t = block_sum_ff<256>(hi_s, lo_s, smem);
   if (threadIdx.x == 0) partial[(long long)k * nparts + blockIdx.x] = t;
 }
 
@@ -991,7 +1025,7 @@ __global__ void obj_w_partial_kernel(ObjReduceArgs a) {
     lo_s += ((h - (t - bv)) + (pr - bv)) + fmaf(x, y, -pr);
     h = t;
   }
-  const double t = block_sum<256>((double)h + (double)lo_s, smem);
+  const double t = block_sum_ff<256>(h, lo_s, smem);
   if (threadIdx.x == 0) {
     double* part = a.partial_ws + (long long)R * a.nparts * 2;
     part[((long long)r * a.L + l) * a.nparts + blockIdx.x] = t;
