@@ -238,6 +238,35 @@ __device__ __forceinline__ void split_bf16x2(float x0, float x1, __nv_bfloat16& 
   l1 = l.y;
 }
 
+// Block sum of per-thread float pairs (hi, lo): the warps reduce in FP32
+// float pairs (TwoSum at each shuffle level), and only the BLOCK / 32 warp
+// totals are added in FP64, by warp 0. A fixed order, like block_sum, at a
+// fraction of its FP64 work (FP64 issues at a small fraction of the FP32 rate
+// on this GPU). Valid in thread 0.
+template <int BLOCK>
+__device__ __forceinline__ double block_sum_ff(float hi, float lo, double* smem) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_down_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_down_sync(0xffffffffu, lo, o);
+    const float t = hi + oh;
+    const float bv = t - hi;
+    lo += ((hi - (t - bv)) + (oh - bv)) + ol;
+    hi = t;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = (double)hi + (double)lo;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0) {
+    t = (lane < BLOCK / 32) ? smem[lane] : 0.0;
+#pragma unroll
+    for (int o = (BLOCK / 32) / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+  }
+  __syncthreads();
+  return t;
+}
+
 inline unsigned ceil_div(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 // Split operand layout: [batch][4][rows][split_ld(cols)] bf16, planes = re_hi,

@@ -420,35 +420,6 @@ __device__ __forceinline__ double block_sum(double v, double* smem) {
   return t;  // valid in thread 0
 }
 
-// Block sum of per-thread float pairs (hi, lo): the warps reduce in FP32
-// float pairs (TwoSum at each shuffle level), and only the BLOCK / 32 warp
-// totals are added in FP64, by warp 0. A fixed order, like block_sum, at a
-// fraction of its FP64 work (FP64 issues at a small fraction of the FP32 rate
-// on this GPU). Valid in thread 0.
-template <int BLOCK>
-__device__ __forceinline__ double block_sum_ff(float hi, float lo, double* smem) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const float oh = __shfl_down_sync(0xffffffffu, hi, o);
-    const float ol = __shfl_down_sync(0xffffffffu, lo, o);
-    const float t = hi + oh;
-    const float bv = t - hi;
-    lo += ((hi - (t - bv)) + (oh - bv)) + ol;
-    hi = t;
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0) smem[warp] = (double)hi + (double)lo;
-  __syncthreads();
-  double t = 0.0;
-  if (warp == 0) {
-    t = (lane < BLOCK / 32) ? smem[lane] : 0.0;
-#pragma unroll
-    for (int o = (BLOCK / 32) / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-  }
-  __syncthreads();
-  return t;
-}
-
 // psf[p] = sum_b |in[b][p]|^2 (wavefronts.py:279 summed as optical_systems.py:223)
 __global__ void psf_sum_kernel(const float2* __restrict__ in, int batch, long long npix,
                                float* __restrict__ psf) {

@@ -231,7 +231,7 @@ __global__ void psf_wsum_bwd_weight_partial_kernel(const float2* __restrict__ in
     // the squares' own rounding errors, weighted
     acc.lo += gp * (fmaf(v.x, v.x, -__fmul_rn(v.x, v.x)) + fmaf(v.y, v.y, -__fmul_rn(v.y, v.y)));
   }
-  const double t = block_sum_d<kBlock>(acc.value(), smem);
+  const double t = block_sum_ff<kBlock>(acc.hi, acc.lo, smem);
   if (threadIdx.x == 0) parts[(long long)b * nparts + blockIdx.x] = t;
 }
 
@@ -272,8 +272,8 @@ __global__ void stats_partial_kernel(const float2* __restrict__ in, long long np
       dd.add_prod(q.y, v.y);
     }
   }
-  const double tp = block_sum_d<kBlock>(pw.value(), dsm);
-  const double td = block_sum_d<kBlock>(dd.value(), dsm);
+  const double tp = block_sum_ff<kBlock>(pw.hi, pw.lo, dsm);
+  const double td = block_sum_ff<kBlock>(dd.hi, dd.lo, dsm);
   const float tm = block_max_f<kBlock>(mx, fsm);
   if (threadIdx.x == 0) {
     double* o = parts + ((long long)b * nparts + blockIdx.x) * 3;
